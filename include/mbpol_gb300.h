@@ -1,0 +1,152 @@
+/*
+ * mbpol_gb300.h -- C ABI of the GB300-native MB-pol force/energy library.
+ *
+ * This is the drop-in boundary for the MB-pol OpenMM plugin's compute path.
+ * In the reference, each force's computation sits behind an OpenMM kernel
+ * (openmmapi/include/openmm/mbpolKernels.h:49-207):
+ *     CalcMBPol{OneBody,TwoBody,ThreeBody,Electrostatics}ForceKernel
+ *         ::initialize(const System&, const MBPol*Force&)
+ *         ::execute(ContextImpl&, bool includeForces, bool includeEnergy)
+ *         ::copyParametersToContext(ContextImpl&, const MBPol*Force&)
+ * plus dispersion, which python/mbpol.xml:37-108 builds as an OpenMM
+ * CustomNonbondedForce, and the M-site virtual site (python/mbpol.xml:14).
+ * OpenMM is not part of this library, so the context (positions, box,
+ * forces, virtual sites) is owned by an mbpol_context; the Force-class
+ * layers (include/mbpol_gb300.hpp for C++, the mbpol_openmm_plugin_gb300
+ * Python package) sit on top of these calls.
+ *
+ * Conventions (same as the reference): nm, kJ/mol, kJ/mol/nm; forces are
+ * ACCUMULATED (+=) into caller-owned arrays; energies are doubles.  Host
+ * pointers are borrowed for the duration of a call.  No C++ exception crosses
+ * this boundary: every call returns an mbpol_status; mbpol_last_error() gives
+ * the message for the calling thread.  One CUDA stream per context.  There is
+ * no CPU fallback: without a usable CUDA device mbpol_context_create fails.
+ */
+#ifndef MBPOL_GB300_H
+#define MBPOL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int mbpol_status;
+enum {
+    MBPOL_OK = 0,
+    MBPOL_ERR_INVALID_ARGUMENT = 1,  /* bad index, size or parameter        */
+    MBPOL_ERR_CUDA = 2,              /* a CUDA runtime / cuFFT call failed   */
+    MBPOL_ERR_NOT_CONVERGED = 3,     /* induced dipoles did not converge     */
+    MBPOL_ERR_BOX_TOO_SMALL = 4,     /* box < 2 * cutoff                     */
+    MBPOL_ERR_CAPACITY = 5,          /* neighbour capacity could not be met  */
+    MBPOL_ERR_STATE = 6,             /* call order (e.g. no positions yet)   */
+    MBPOL_ERR_NO_DEVICE = 7          /* no CUDA device                       */
+};
+
+/* Nonbonded methods, numbered as in the reference's Force classes. */
+enum { MBPOL_ONEBODY_NONPERIODIC = 0, MBPOL_ONEBODY_PERIODIC = 1 };              /* MBPolOneBodyForce.h */
+enum { MBPOL_NOCUTOFF = 0, MBPOL_CUTOFF_NONPERIODIC = 1, MBPOL_CUTOFF_PERIODIC = 2 }; /* MBPolTwoBodyForce.h, MBPolThreeBodyForce.h */
+enum { MBPOL_ELEC_NOCUTOFF = 0, MBPOL_ELEC_PME = 1 };                             /* MBPolElectrostaticsForce.h */
+/* Trimer enumeration: the reference's rule, or every trimer with a nonzero switch. */
+enum { MBPOL_TRIMER_REFERENCE = 0, MBPOL_TRIMER_COMPLETE = 1 };
+
+/* Energy slots returned by mbpol_compute (kJ/mol). */
+enum {
+    MBPOL_TERM_ONEBODY = 0,
+    MBPOL_TERM_TWOBODY = 1,
+    MBPOL_TERM_THREEBODY = 2,
+    MBPOL_TERM_ELECTROSTATICS = 3,
+    MBPOL_TERM_DISPERSION = 4,
+    MBPOL_NUM_TERMS = 5
+};
+#define MBPOL_TERM_BIT(t) (1u << (t))
+#define MBPOL_ALL_TERMS 0x1Fu
+
+typedef struct mbpol_context mbpol_context;
+
+/* Parameters of MBPolElectrostaticsForce (openmmapi/include/openmm/MBPolElectrostaticsForce.h:66-260;
+ * defaults at openmmapi/src/MBPolElectrostaticsForce.cpp:43-48). */
+typedef struct {
+    int nonbonded_method;        /* MBPOL_ELEC_NOCUTOFF or MBPOL_ELEC_PME                      */
+    double cutoff;               /* real-space cutoff (nm), PME only; default 0.9               */
+    double ewald_alpha;          /* nm^-1; 0 = choose from ewald_error_tolerance               */
+    int pme_grid[3];             /* 0 = choose from ewald_error_tolerance                       */
+    double ewald_error_tolerance;/* default 1e-4                                                */
+    int max_iterations;          /* mutual induced max iterations; default 200                  */
+    double target_epsilon;       /* Debye; default 1e-7                                         */
+    double thole[5];             /* TCC, TCD, TDD, TDDOH, TDDHH; default {0.4,0.4,0.055,0.626,0.055} */
+    int include_charge_redistribution; /* default 1                                              */
+    int guess;                   /* initial dipole guess: 0 direct (alpha*E_fixed, as the reference),
+                                    1 previous call's dipoles, 2 learned (MLP) with direct fallback */
+} mbpol_electrostatics_params;
+
+/* Fill p with the reference's defaults. */
+void mbpol_electrostatics_params_default(mbpol_electrostatics_params* p);
+
+/* Create / destroy a context for num_particles particles on CUDA device `device`.
+ * Replaces the OpenMM Context + Platform::createKernel plumbing
+ * (openmmapi/src/MBPolTwoBodyForceImpl.cpp:55-76). */
+mbpol_status mbpol_context_create(int num_particles, int device, mbpol_context** out);
+mbpol_status mbpol_context_destroy(mbpol_context* ctx);
+
+/* Virtual site: particle `site` = w1*p1 + w2*p2 + w3*p3; its force is spread
+ * back with the same weights (OpenMM ThreeParticleAverageSite, used for the
+ * M site at python/mbpol.xml:14). */
+mbpol_status mbpol_add_average3_site(mbpol_context* ctx, int site, int p1, int p2, int p3, double w1, double w2,
+                                     double w3);
+
+/* Force set-up.  `waters` holds num_waters x {O, H1, H2} particle indices
+ * (the vector<int> passed to addOneBody/addParticle, python/mbpol.py:65-76).
+ *   one-body:   CalcMBPolOneBodyForceKernel::initialize   (platforms/reference/src/MBPolReferenceKernels.cpp:77-101)
+ *   two-body:   CalcMBPolTwoBodyForceKernel::initialize   (MBPolReferenceKernels.cpp:330-360)
+ *   three-body: CalcMBPolThreeBodyForceKernel::initialize (MBPolReferenceKernels.cpp:420-449) */
+mbpol_status mbpol_add_onebody_force(mbpol_context* ctx, int num_waters, const int* waters, int method);
+mbpol_status mbpol_add_twobody_force(mbpol_context* ctx, int num_waters, const int* waters, int method,
+                                     double cutoff);
+mbpol_status mbpol_add_threebody_force(mbpol_context* ctx, int num_waters, const int* waters, int method,
+                                       double cutoff, int trimer_rule);
+
+/* Electrostatics over all num_particles particles (the reference requires one
+ * entry per particle, openmmapi/src/MBPolElectrostaticsForceImpl.cpp:53-54),
+ * with per-particle charge, molecule index, atom type (O=0, H=1, M=2),
+ * damping factor and polarizability as in addElectrostatics
+ * (MBPolElectrostaticsForce.h:153).  Waters must be laid out as consecutive
+ * O, H1, H2, M particles, as the reference assumes
+ * (platforms/reference/src/MBPolReferenceElectrostaticsForce.cpp:879-884).
+ * Replaces CalcMBPolElectrostaticsForceKernel::initialize (MBPolReferenceKernels.cpp:127-207). */
+mbpol_status mbpol_add_electrostatics_force(mbpol_context* ctx, const mbpol_electrostatics_params* params,
+                                            const double* charge, const int* molecule, const int* atom_type,
+                                            const double* damping, const double* polarity);
+
+/* Dispersion over the O/H sites of `num_waters` waters ({O,H1,H2} each);
+ * c6 and d6 are 4x4 class tables (O=0, H=1, M=2, Cl=3) as in python/mbpol.xml:52-83.
+ * method: MBPOL_NOCUTOFF or MBPOL_CUTOFF_PERIODIC / MBPOL_CUTOFF_NONPERIODIC. */
+mbpol_status mbpol_add_dispersion_force(mbpol_context* ctx, int num_waters, const int* waters, int method,
+                                        double cutoff, const double* c6, const double* d6);
+
+/* Positions (3*num_particles, nm) and the rectangular box (3 lengths, nm),
+ * or box = NULL for a non-periodic system.  Virtual sites are placed from
+ * their parents on the device before each evaluation. */
+mbpol_status mbpol_set_positions(mbpol_context* ctx, const double* xyz, const double* box);
+
+/* Evaluate the terms in term_mask (MBPOL_TERM_BIT(...)), i.e. ::execute of each
+ * kernel (MBPolReferenceKernels.cpp:120-125, 246-259, 362-399, 451-483).
+ * energies (optional, MBPOL_NUM_TERMS doubles) receives each term's energy;
+ * forces (optional, 3*num_particles) is ACCUMULATED into.  Returns
+ * MBPOL_ERR_NOT_CONVERGED if the induced dipoles did not reach the target, as
+ * the reference throws (MBPolReferenceElectrostaticsForce.cpp:888-894). */
+mbpol_status mbpol_compute(mbpol_context* ctx, unsigned term_mask, double* energies, double* forces);
+
+/* Induced dipoles (3*num_particles, e*nm) of the last electrostatics
+ * evaluation, with its solver iteration count and final epsilon (Debye). */
+mbpol_status mbpol_get_induced_dipoles(mbpol_context* ctx, double* dipoles, int* iterations, double* epsilon);
+
+/* Counts from the last evaluation: [0] two-body pairs, [1] trimers,
+ * [2] electrostatics site pairs within the cutoff, [3] solver iterations. */
+mbpol_status mbpol_get_counts(mbpol_context* ctx, long* counts4);
+
+const char* mbpol_status_string(mbpol_status s);
+const char* mbpol_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MBPOL_GB300_H */

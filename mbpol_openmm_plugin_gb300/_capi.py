@@ -1,0 +1,103 @@
+"""ctypes binding to the C ABI in include/mbpol_gb300.h.
+
+The shared library is built in-tree (``python -m mbpol_openmm_plugin_gb300.build``
+or ``__graft_entry__.build()``).  There is no CPU fallback: if the library or
+a CUDA device is missing, the calls raise."""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libmbpol_gb300.so")
+
+MBPOL_OK = 0
+STATUS_NAMES = {
+    0: "OK", 1: "INVALID_ARGUMENT", 2: "CUDA", 3: "NOT_CONVERGED", 4: "BOX_TOO_SMALL",
+    5: "CAPACITY", 6: "STATE", 7: "NO_DEVICE",
+}
+TERM_ONEBODY, TERM_TWOBODY, TERM_THREEBODY, TERM_ELECTROSTATICS, TERM_DISPERSION = range(5)
+NUM_TERMS = 5
+ALL_TERMS = 0x1F
+
+EXPORTED = [
+    "mbpol_electrostatics_params_default", "mbpol_context_create", "mbpol_context_destroy",
+    "mbpol_add_average3_site", "mbpol_add_onebody_force", "mbpol_add_twobody_force",
+    "mbpol_add_threebody_force", "mbpol_add_electrostatics_force", "mbpol_add_dispersion_force",
+    "mbpol_set_positions", "mbpol_compute", "mbpol_get_induced_dipoles", "mbpol_get_counts",
+    "mbpol_status_string", "mbpol_last_error",
+]
+
+
+class MBPolError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+class ElectrostaticsParams(ctypes.Structure):
+    _fields_ = [
+        ("nonbonded_method", ctypes.c_int),
+        ("cutoff", ctypes.c_double),
+        ("ewald_alpha", ctypes.c_double),
+        ("pme_grid", ctypes.c_int * 3),
+        ("ewald_error_tolerance", ctypes.c_double),
+        ("max_iterations", ctypes.c_int),
+        ("target_epsilon", ctypes.c_double),
+        ("thole", ctypes.c_double * 5),
+        ("include_charge_redistribution", ctypes.c_int),
+        ("guess", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load (once) and return the library; raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise MBPolError(7, "CUDA library %s is not built (run __graft_entry__.build())" % path)
+    lib = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    I, D = ctypes.c_int, ctypes.c_double
+    sig = {
+        "mbpol_electrostatics_params_default": (None, [ctypes.POINTER(ElectrostaticsParams)]),
+        "mbpol_context_create": (I, [I, I, ctypes.POINTER(P)]),
+        "mbpol_context_destroy": (I, [P]),
+        "mbpol_add_average3_site": (I, [P, I, I, I, I, D, D, D]),
+        "mbpol_add_onebody_force": (I, [P, I, P, I]),
+        "mbpol_add_twobody_force": (I, [P, I, P, I, D]),
+        "mbpol_add_threebody_force": (I, [P, I, P, I, D, I]),
+        "mbpol_add_electrostatics_force": (I, [P, ctypes.POINTER(ElectrostaticsParams), P, P, P, P, P]),
+        "mbpol_add_dispersion_force": (I, [P, I, P, I, D, P, P]),
+        "mbpol_set_positions": (I, [P, P, P]),
+        "mbpol_compute": (I, [P, ctypes.c_uint, P, P]),
+        "mbpol_get_induced_dipoles": (I, [P, P, ctypes.POINTER(I), ctypes.POINTER(D)]),
+        "mbpol_get_counts": (I, [P, P]),
+        "mbpol_status_string": (ctypes.c_char_p, [I]),
+        "mbpol_last_error": (ctypes.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status):
+    if status != MBPOL_OK:
+        msg = load().mbpol_last_error().decode(errors="replace")
+        raise MBPolError(status, msg)
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def as_c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)

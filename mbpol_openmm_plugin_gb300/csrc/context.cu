@@ -1,0 +1,494 @@
+// C-ABI implementation: context, buffers, orchestration of the MB-pol
+// kernels on one CUDA stream.  See include/mbpol_gb300.h for the contract.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mbpol_gb300.h"
+#include "elec.h"
+#include "mbpol_kernels.h"
+
+// Generated at build time: one-body tables.
+#include "gen/model_tables.inc"
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+mbpol_status mbpol_fail(mbpol_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+mbpol_status mbpol_fail_cuda(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return MBPOL_ERR_CUDA;
+}
+
+namespace mbpol {
+
+// Grow-only device buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        size_t nb = n + n / 4 + 256;
+        cudaError_t e = cudaMalloc(&p, nb);
+        if (e == cudaSuccess) bytes = nb;
+        return e;
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+struct WaterTerm {
+    bool on = false;
+    int method = 0;
+    double cutoff = 0.0;
+    int rule = 0;
+    std::vector<int4> waters;
+    DevBuf d_waters;
+};
+
+}  // namespace mbpol
+
+using namespace mbpol;
+
+struct mbpol_context {
+    int N = 0;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    DevBuf d_pos, d_force, d_energy, d_counters;
+    std::vector<double> h_force;
+    bool have_pos = false;
+    Box box{};
+    // virtual sites
+    std::vector<int4> vs_idx;
+    std::vector<double> vs_w;
+    DevBuf d_vs_idx, d_vs_w;
+    bool vs_dirty = false;
+    WaterTerm t1, t2, t3, tdisp;
+    // two-body buffers
+    DevBuf p2, x2, g2, e2;
+    int cap2 = 0;
+    // three-body buffers
+    DevBuf lower3, nlower3, count3, offs3, trips3, x3, g3, e3, full3, nfull3;
+    int cap_lower3 = 48, cap3 = 0, cap_full3 = 96;
+    // dispersion buffers
+    DevBuf full_d, nfull_d, lower_d, nlower_d;
+    int cap_full_d = 0;
+    double disp_c6[16], disp_d6[16];
+    // electrostatics
+    std::unique_ptr<ElecEngine> elec;
+    int num_sms = 0;
+    long counts[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+mbpol_status check_waters(mbpol_context* ctx, int nw, const int* w) {
+    if (nw < 0 || (nw > 0 && !w)) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad water list");
+    for (int i = 0; i < 3 * nw; ++i)
+        if (w[i] < 0 || w[i] >= ctx->N) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "particle index out of range");
+    return MBPOL_OK;
+}
+
+mbpol_status set_term(mbpol_context* ctx, WaterTerm& t, int nw, const int* w, int method, double cutoff, int rule) {
+    mbpol_status s = check_waters(ctx, nw, w);
+    if (s) return s;
+    t.on = true;
+    t.method = method;
+    t.cutoff = cutoff;
+    t.rule = rule;
+    t.waters.resize((size_t)nw);
+    for (int i = 0; i < nw; ++i) t.waters[(size_t)i] = make_int4(w[3 * i], w[3 * i + 1], w[3 * i + 2], -1);
+    MBPOL_CUDA_OK(t.d_waters.ensure(sizeof(int4) * (size_t)(nw > 0 ? nw : 1)));
+    if (nw > 0)
+        MBPOL_CUDA_OK(cudaMemcpy(t.d_waters.p, t.waters.data(), sizeof(int4) * (size_t)nw, cudaMemcpyHostToDevice));
+    return MBPOL_OK;
+}
+
+Box term_box(const mbpol_context* ctx, bool periodic) {
+    Box b = ctx->box;
+    b.periodic = periodic && ctx->box.periodic;
+    return b;
+}
+
+mbpol_status check_box(const mbpol_context* ctx, double cutoff) {
+    if (!ctx->box.periodic) return mbpol_fail(MBPOL_ERR_STATE, "periodic method requires a box");
+    for (int k = 0; k < 3; ++k)
+        if (ctx->box.L[k] < 1.999999 * cutoff)
+            return mbpol_fail(MBPOL_ERR_BOX_TOO_SMALL, "The periodic box size has decreased to less than twice the cutoff.");
+    return MBPOL_OK;
+}
+
+mbpol_status run_twobody(mbpol_context* ctx, double* energy) {
+    WaterTerm& t = ctx->t2;
+    const int nw = (int)t.waters.size();
+    if (nw < 2) return MBPOL_OK;
+    const bool periodic = t.method == MBPOL_CUTOFF_PERIODIC;
+    if (periodic) {
+        mbpol_status s = check_box(ctx, t.cutoff);
+        if (s) return s;
+    }
+    const Box box = term_box(ctx, periodic);
+    const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
+    int* cnt = ctx->d_counters.as<int>();
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (ctx->cap2 == 0) ctx->cap2 = nw * 24 + 64;
+        MBPOL_CUDA_OK(ctx->p2.ensure(sizeof(int2) * (size_t)ctx->cap2));
+        MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
+        launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, -1.0, -1.0, rc, 0, 0,
+                             nullptr, nullptr, nullptr, nullptr, ctx->p2.as<int2>(),
+                             ctx->cap2, cnt, cnt + 1, nullptr);
+        int h[2];
+        MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+        if (h[0] > ctx->cap2) {
+            ctx->cap2 = h[0] + h[0] / 4 + 64;
+            continue;
+        }
+        const int np = h[0];
+        ctx->counts[0] = np;
+        const int stride = ctx->cap2;
+        MBPOL_CUDA_OK(ctx->x2.ensure(sizeof(float) * 31 * (size_t)stride));
+        MBPOL_CUDA_OK(ctx->g2.ensure(sizeof(float) * 31 * (size_t)stride));
+        MBPOL_CUDA_OK(ctx->e2.ensure(sizeof(float) * (size_t)stride));
+        launch_twobody_vars(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
+                            ctx->x2.as<float>(), stride);
+        launch_poly2b(ctx->st, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride,
+                      ctx->num_sms);
+        launch_twobody_forces(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
+                              ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy);
+        return MBPOL_OK;
+    }
+    return mbpol_fail(MBPOL_ERR_CAPACITY, "two-body pair list capacity");
+}
+
+mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
+    WaterTerm& t = ctx->t3;
+    const int nw = (int)t.waters.size();
+    if (nw < 3) return MBPOL_OK;
+    const bool periodic = t.method == MBPOL_CUTOFF_PERIODIC;
+    if (periodic) {
+        mbpol_status s = check_box(ctx, t.cutoff);
+        if (s) return s;
+    }
+    const Box box = term_box(ctx, periodic);
+    const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
+    int* cnt = ctx->d_counters.as<int>();
+    const bool complete = t.rule == MBPOL_TRIMER_COMPLETE;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        MBPOL_CUDA_OK(ctx->nlower3.ensure(sizeof(int) * (size_t)nw));
+        MBPOL_CUDA_OK(ctx->count3.ensure(sizeof(int) * (size_t)nw));
+        MBPOL_CUDA_OK(ctx->offs3.ensure(sizeof(int) * (size_t)(nw + 1)));
+        MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
+        if (!complete) {
+            MBPOL_CUDA_OK(ctx->lower3.ensure(sizeof(int) * (size_t)nw * ctx->cap_lower3));
+            launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, -1.0, rc, -1.0, 0,
+                                 ctx->cap_lower3, nullptr, nullptr, ctx->lower3.as<int>(),
+                                 ctx->nlower3.as<int>(), nullptr, 0, cnt, cnt + 1, nullptr);
+            launch_trimer_count(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
+                                ctx->count3.as<int>(), ctx->offs3.as<int>());
+        } else {
+            MBPOL_CUDA_OK(ctx->full3.ensure(sizeof(int) * (size_t)nw * ctx->cap_full3));
+            MBPOL_CUDA_OK(ctx->nfull3.ensure(sizeof(int) * (size_t)nw));
+            launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc, -1.0, -1.0,
+                                 ctx->cap_full3, 0, ctx->full3.as<int>(), ctx->nfull3.as<int>(), nullptr,
+                                 nullptr, nullptr, 0, cnt, cnt + 1, nullptr);
+            launch_trimer_complete(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
+                                   ctx->full3.as<int>(), ctx->nfull3.as<int>(), ctx->cap_full3,
+                                   ctx->count3.as<int>(), ctx->offs3.as<int>(), 0, nullptr, false);
+        }
+        int h[3];
+        MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(h + 2, ctx->offs3.as<int>() + nw, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+        if (h[1]) {  // neighbour capacity overflow: grow and redo
+            if (complete) ctx->cap_full3 *= 2;
+            else ctx->cap_lower3 *= 2;
+            continue;
+        }
+        const int ntrip = h[2];
+        ctx->counts[1] = ntrip;
+        if (ntrip > ctx->cap3) ctx->cap3 = ntrip + ntrip / 4 + 64;
+        const int stride = ctx->cap3;
+        MBPOL_CUDA_OK(ctx->trips3.ensure(sizeof(int4) * (size_t)stride));
+        MBPOL_CUDA_OK(ctx->x3.ensure(sizeof(float) * 36 * (size_t)stride));
+        MBPOL_CUDA_OK(ctx->g3.ensure(sizeof(float) * 36 * (size_t)stride));
+        MBPOL_CUDA_OK(ctx->e3.ensure(sizeof(float) * (size_t)stride));
+        if (!complete)
+            launch_trimer_fill(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
+                               ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>());
+        else
+            launch_trimer_complete(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
+                                   ctx->full3.as<int>(), ctx->nfull3.as<int>(), ctx->cap_full3, nullptr,
+                                   ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>(), true);
+        launch_threebody_vars(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+                              box, ctx->x3.as<float>(), stride);
+        launch_poly3b(ctx->st, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
+                      ctx->num_sms);
+        launch_threebody_forces(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(),
+                                ctx->d_pos.as<double>(), box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride,
+                                ctx->d_force.as<double>(), energy);
+        return MBPOL_OK;
+    }
+    return mbpol_fail(MBPOL_ERR_CAPACITY, "three-body neighbour capacity");
+}
+
+mbpol_status run_dispersion(mbpol_context* ctx, double* energy) {
+    WaterTerm& t = ctx->tdisp;
+    const int nw = (int)t.waters.size();
+    if (nw < 2) return MBPOL_OK;
+    const bool periodic = t.method == MBPOL_CUTOFF_PERIODIC;
+    if (periodic) {
+        mbpol_status s = check_box(ctx, t.cutoff);
+        if (s) return s;
+    }
+    const Box box = term_box(ctx, periodic);
+    const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
+    // molecule list radius: site cutoff plus twice the largest O-H extent
+    const double rlist = t.method == MBPOL_NOCUTOFF ? 1e30 : rc + 0.25;
+    int* cnt = ctx->d_counters.as<int>();
+    if (ctx->cap_full_d == 0) ctx->cap_full_d = t.method == MBPOL_NOCUTOFF ? ((nw + 31) / 32) * 32 : 256;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        MBPOL_CUDA_OK(ctx->full_d.ensure(sizeof(int) * (size_t)nw * ctx->cap_full_d));
+        MBPOL_CUDA_OK(ctx->nfull_d.ensure(sizeof(int) * (size_t)nw));
+        MBPOL_CUDA_OK(ctx->nlower_d.ensure(sizeof(int) * (size_t)nw));
+        MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
+        launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rlist, -1.0, -1.0,
+                             ctx->cap_full_d, 0, ctx->full_d.as<int>(), ctx->nfull_d.as<int>(), nullptr,
+                             nullptr, nullptr, 0, cnt, cnt + 1, nullptr);
+        int h[2];
+        MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+        if (h[1]) {
+            ctx->cap_full_d *= 2;
+            continue;
+        }
+        launch_dispersion(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, ctx->full_d.as<int>(),
+                          ctx->nfull_d.as<int>(), ctx->cap_full_d, rc, ctx->d_force.as<double>(), energy);
+        return MBPOL_OK;
+    }
+    return mbpol_fail(MBPOL_ERR_CAPACITY, "dispersion neighbour capacity");
+}
+
+}  // namespace
+
+extern "C" {
+
+void mbpol_electrostatics_params_default(mbpol_electrostatics_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->nonbonded_method = MBPOL_ELEC_NOCUTOFF;
+    p->cutoff = 0.9;
+    p->ewald_alpha = 0.0;
+    p->ewald_error_tolerance = 1e-4;
+    p->max_iterations = 200;
+    p->target_epsilon = 1e-7;
+    const double th[5] = {0.4, 0.4, 0.055, 0.626, 0.055};
+    for (int k = 0; k < 5; ++k) p->thole[k] = th[k];
+    p->include_charge_redistribution = 1;
+    p->guess = 0;
+}
+
+mbpol_status mbpol_context_create(int num_particles, int device, mbpol_context** out) {
+    if (!out || num_particles <= 0) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad context arguments");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return mbpol_fail(MBPOL_ERR_NO_DEVICE, "no CUDA device is available; this library has no CPU fallback");
+    if (device < 0 || device >= ndev) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad device index");
+    MBPOL_CUDA_OK(cudaSetDevice(device));
+    std::unique_ptr<mbpol_context> ctx(new mbpol_context());
+    ctx->N = num_particles;
+    ctx->device = device;
+    MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+    MBPOL_CUDA_OK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+    MBPOL_CUDA_OK(ctx->d_pos.ensure(sizeof(double) * 3 * (size_t)num_particles));
+    MBPOL_CUDA_OK(ctx->d_force.ensure(sizeof(double) * 3 * (size_t)num_particles));
+    MBPOL_CUDA_OK(ctx->d_energy.ensure(sizeof(double) * MBPOL_NUM_TERMS));
+    MBPOL_CUDA_OK(ctx->d_counters.ensure(sizeof(int) * 16));
+    ctx->h_force.resize(3 * (size_t)num_particles);
+    upload_polyterm_constants(kOneBodyCoef, &kOneBodyIdx[0][0]);
+    MBPOL_CUDA_OK(cudaGetLastError());
+    MBPOL_CUDA_OK(poly_tables_upload(device));
+    *out = ctx.release();
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_context_destroy(mbpol_context* ctx) {
+    if (!ctx) return MBPOL_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->st);
+    ctx->elec.reset();
+    cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_add_average3_site(mbpol_context* ctx, int site, int p1, int p2, int p3, double w1, double w2,
+                                     double w3) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    const int idx[4] = {site, p1, p2, p3};
+    for (int k = 0; k < 4; ++k)
+        if (idx[k] < 0 || idx[k] >= ctx->N) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "virtual site index out of range");
+    ctx->vs_idx.push_back(make_int4(site, p1, p2, p3));
+    ctx->vs_w.push_back(w1);
+    ctx->vs_w.push_back(w2);
+    ctx->vs_w.push_back(w3);
+    ctx->vs_dirty = true;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_add_onebody_force(mbpol_context* ctx, int nw, const int* w, int method) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    return set_term(ctx, ctx->t1, nw, w, method, 0.0, 0);
+}
+
+mbpol_status mbpol_add_twobody_force(mbpol_context* ctx, int nw, const int* w, int method, double cutoff) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (method != MBPOL_NOCUTOFF && !(cutoff > 0)) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad cutoff");
+    return set_term(ctx, ctx->t2, nw, w, method, cutoff, 0);
+}
+
+mbpol_status mbpol_add_threebody_force(mbpol_context* ctx, int nw, const int* w, int method, double cutoff,
+                                       int rule) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (method != MBPOL_NOCUTOFF && !(cutoff > 0)) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad cutoff");
+    return set_term(ctx, ctx->t3, nw, w, method, cutoff, rule);
+}
+
+mbpol_status mbpol_add_dispersion_force(mbpol_context* ctx, int nw, const int* w, int method, double cutoff,
+                                        const double* c6, const double* d6) {
+    if (!ctx || !c6 || !d6) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    if (method != MBPOL_NOCUTOFF && !(cutoff > 0)) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad cutoff");
+    std::memcpy(ctx->disp_c6, c6, sizeof(ctx->disp_c6));
+    std::memcpy(ctx->disp_d6, d6, sizeof(ctx->disp_d6));
+    upload_dispersion_tables(c6, d6);
+    return set_term(ctx, ctx->tdisp, nw, w, method, cutoff, 0);
+}
+
+mbpol_status mbpol_add_electrostatics_force(mbpol_context* ctx, const mbpol_electrostatics_params* p,
+                                            const double* charge, const int* molecule, const int* atom_type,
+                                            const double* damping, const double* polarity) {
+    if (!ctx || !p || !charge || !molecule || !atom_type || !damping || !polarity)
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    ctx->elec.reset(new ElecEngine());
+    return ctx->elec->init(ctx->N, *p, charge, molecule, atom_type, damping, polarity);
+}
+
+mbpol_status mbpol_set_positions(mbpol_context* ctx, const double* xyz, const double* box) {
+    if (!ctx || !xyz) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    for (size_t i = 0; i < 3 * (size_t)ctx->N; ++i)
+        if (!std::isfinite(xyz[i])) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "non-finite position");
+    if (box) {
+        for (int k = 0; k < 3; ++k) {
+            if (!(box[k] > 0) || !std::isfinite(box[k]))
+                return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "Box size of zero is invalid.");
+            ctx->box.L[k] = box[k];
+            ctx->box.inv[k] = 1.0 / box[k];
+        }
+        ctx->box.periodic = 1;
+    } else {
+        ctx->box.periodic = 0;
+    }
+    MBPOL_CUDA_OK(cudaMemcpyAsync(ctx->d_pos.p, xyz, sizeof(double) * 3 * ctx->N, cudaMemcpyHostToDevice, ctx->st));
+    ctx->have_pos = true;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_compute(mbpol_context* ctx, unsigned mask, double* energies, double* forces) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (!ctx->have_pos) return mbpol_fail(MBPOL_ERR_STATE, "positions have not been set");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    if (ctx->vs_dirty) {
+        MBPOL_CUDA_OK(ctx->d_vs_idx.ensure(sizeof(int4) * ctx->vs_idx.size()));
+        MBPOL_CUDA_OK(ctx->d_vs_w.ensure(sizeof(double) * ctx->vs_w.size()));
+        MBPOL_CUDA_OK(cudaMemcpy(ctx->d_vs_idx.p, ctx->vs_idx.data(), sizeof(int4) * ctx->vs_idx.size(), cudaMemcpyHostToDevice));
+        MBPOL_CUDA_OK(cudaMemcpy(ctx->d_vs_w.p, ctx->vs_w.data(), sizeof(double) * ctx->vs_w.size(), cudaMemcpyHostToDevice));
+        ctx->vs_dirty = false;
+    }
+    const int nvs = (int)ctx->vs_idx.size();
+    launch_place_vsites(ctx->st, nvs, ctx->d_vs_idx.as<int4>(), ctx->d_vs_w.as<double>(), ctx->d_pos.as<double>());
+    MBPOL_CUDA_OK(cudaMemsetAsync(ctx->d_force.p, 0, sizeof(double) * 3 * ctx->N, ctx->st));
+    MBPOL_CUDA_OK(cudaMemsetAsync(ctx->d_energy.p, 0, sizeof(double) * MBPOL_NUM_TERMS, ctx->st));
+    double* e = ctx->d_energy.as<double>();
+    mbpol_status s = MBPOL_OK;
+    if ((mask & MBPOL_TERM_BIT(MBPOL_TERM_ONEBODY)) && ctx->t1.on) {
+        const bool periodic = ctx->t1.method == MBPOL_ONEBODY_PERIODIC && ctx->box.periodic;
+        launch_onebody(ctx->st, (int)ctx->t1.waters.size(), ctx->t1.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+                       term_box(ctx, periodic), ctx->d_force.as<double>(), e + MBPOL_TERM_ONEBODY);
+    }
+    if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_TWOBODY)) && ctx->t2.on) s = run_twobody(ctx, e + MBPOL_TERM_TWOBODY);
+    if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_THREEBODY)) && ctx->t3.on)
+        s = run_threebody(ctx, e + MBPOL_TERM_THREEBODY);
+    if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_DISPERSION)) && ctx->tdisp.on)
+        s = run_dispersion(ctx, e + MBPOL_TERM_DISPERSION);
+    if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS)) && ctx->elec) {
+        s = ctx->elec->compute(ctx->st, ctx->d_pos.as<double>(), ctx->box, ctx->d_force.as<double>(),
+                               e + MBPOL_TERM_ELECTROSTATICS);
+        ctx->counts[2] = ctx->elec->num_site_pairs();
+        ctx->counts[3] = ctx->elec->iterations();
+    }
+    if (s) {
+        cudaStreamSynchronize(ctx->st);
+        return s;
+    }
+    launch_spread_vsites(ctx->st, nvs, ctx->d_vs_idx.as<int4>(), ctx->d_vs_w.as<double>(), ctx->d_force.as<double>());
+    double h_e[MBPOL_NUM_TERMS];
+    MBPOL_CUDA_OK(cudaMemcpyAsync(h_e, e, sizeof(h_e), cudaMemcpyDeviceToHost, ctx->st));
+    if (forces)
+        MBPOL_CUDA_OK(cudaMemcpyAsync(ctx->h_force.data(), ctx->d_force.p, sizeof(double) * 3 * ctx->N,
+                                      cudaMemcpyDeviceToHost, ctx->st));
+    MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+    MBPOL_CUDA_OK(cudaGetLastError());
+    if (energies)
+        for (int k = 0; k < MBPOL_NUM_TERMS; ++k) energies[k] = h_e[k];
+    if (forces)
+        for (size_t i = 0; i < 3 * (size_t)ctx->N; ++i) forces[i] += ctx->h_force[i];
+    if (ctx->elec && (mask & MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS)) && !ctx->elec->converged())
+        return mbpol_fail(MBPOL_ERR_NOT_CONVERGED, ctx->elec->convergence_message());
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_get_induced_dipoles(mbpol_context* ctx, double* dipoles, int* iterations, double* epsilon) {
+    if (!ctx || !ctx->elec) return mbpol_fail(MBPOL_ERR_STATE, "no electrostatics force");
+    return ctx->elec->get_dipoles(ctx->st, dipoles, iterations, epsilon);
+}
+
+mbpol_status mbpol_get_counts(mbpol_context* ctx, long* c) {
+    if (!ctx || !c) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    for (int k = 0; k < 4; ++k) c[k] = ctx->counts[k];
+    return MBPOL_OK;
+}
+
+const char* mbpol_status_string(mbpol_status s) {
+    switch (s) {
+        case MBPOL_OK: return "ok";
+        case MBPOL_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case MBPOL_ERR_CUDA: return "CUDA error";
+        case MBPOL_ERR_NOT_CONVERGED: return "induced dipoles did not converge";
+        case MBPOL_ERR_BOX_TOO_SMALL: return "periodic box smaller than twice the cutoff";
+        case MBPOL_ERR_CAPACITY: return "neighbour capacity exceeded";
+        case MBPOL_ERR_STATE: return "invalid call order";
+        case MBPOL_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* mbpol_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,1416 @@
+// MB-pol electrostatics on the GPU: geometry-dependent charges, Thole-damped
+// permanent and induced fields, the induced-dipole solver, smooth PME
+// (order 5, hand-written spread/gather, cuFFT for the 3D FFT only) and the
+// energy/forces including the charge-derivative terms.
+//
+// Restates platforms/reference/src/MBPolReferenceElectrostaticsForce.cpp:
+//   charges + dq/dr         computeWaterCharge                 :2793-3096
+//   Thole scale factors     getAndScaleInverseRs(13justScaleTCC) :261-359, gammq.cpp:133-178
+//   fixed field             NoCutoff :361-420, PME :1342-1439
+//   induced field / solver  :438-647 (NoCutoff), :2280-2470 (PME), update :516-531,
+//                           convergence :557-616
+//   energy / forces         NoCutoff :649-836, PME :2510-2777, recip :2113-2265, self :2472-2508
+//   PME grids               B-spline moduli :1248-1340, splines :1446-1554, spread :1610-1674,1823-1908,
+//                           convolution :1676-1713, potentials :1715-1821,1910-2111
+// The reference keeps two identical dipole sets ("d" and "p"); one set is
+// solved here and every formula is reduced accordingly (d = p).
+//
+// Layout: molecules of K consecutive sites (K = 4: O, H1, H2, M; or K = 3
+// without M).  Per evaluation a full molecule neighbour list (j != i,
+// O-O distance <= cutoff + 0.24 nm; all molecules for NoCutoff) stores j and
+// the FP64 minimum-image O-O vector rounded to FP32; site-site vectors are
+// that vector plus FP32 intramolecular offsets, so no FP64 arithmetic is
+// needed in the pair loops.  Pair kernels run one warp per molecule over its
+// full list, so each molecule's sites are written by exactly one warp.
+#include <cufft.h>
+
+#include <cmath>
+#include <cstring>
+#include <sstream>
+#include <vector>
+
+#include "elec.h"
+
+namespace mbpol {
+
+namespace {
+
+constexpr int kMaxK = 4;
+constexpr float kSqrtPiF = 1.77245385091f;  // reference SQRT_PI (MBPolReferenceElectrostaticsForce.cpp:1097)
+constexpr double kSqrtPi = 1.77245385091;
+constexpr double kElectric = 138.9354558456;  // reference _electric (:52)
+constexpr double kDebye = 48.033324;          // reference _debye (:60)
+constexpr double kSOR = 0.55;                 // reference _polarSOR (:59)
+
+struct ElecConst {
+    float thole[5];       // TCC, TCD, TDD, TDDOH, TDDHH
+    float alpha;          // Ewald alpha (nm^-1), 0 for NoCutoff
+    float rc2;            // real-space cutoff^2 (nm^2); huge for NoCutoff
+    float self_term;      // 4 alpha^3 / (3 sqrt(pi))
+    int K;                // sites per molecule
+    int grid[3];
+    float scale[3];       // grid / box
+    double box[3], inv[3];
+};
+__constant__ ElecConst c_el;
+
+// ------------------------------------------------------------ Thole scales
+// u = r / (alpha_i alpha_j)^(1/6); x = gamma u^4.  Orders as
+// getAndScaleInverseRs (justScale): 1 (charge-charge, incomplete gamma),
+// 3, 5, 7.  Returns 1 when undamped (damp == 0).
+
+// Regularized upper incomplete gamma Q(3/4, x): series for x < a+1, Lentz
+// continued fraction otherwise (Numerical Recipes, "Incomplete Gamma
+// Function"; the same method as the reference's gammq.cpp).
+__device__ float gammq34(float x) {
+    const float a = 0.75f;
+    const float gln = 0.203280951431295f;  // ln Gamma(3/4)
+    if (x <= 0.f) return 1.f;
+    if (x > 88.f) return 0.f;
+    if (x < a + 1.f) {
+        float ap = a, sum = 1.f / a, del = sum;
+        for (int n = 0; n < 64; ++n) {
+            ap += 1.f;
+            del *= x / ap;
+            sum += del;
+            if (fabsf(del) < fabsf(sum) * 1e-8f) break;
+        }
+        return 1.f - sum * expf(-x + a * logf(x) - gln);
+    }
+    const float FPMIN = 1e-30f;
+    float b = x + 1.f - a, c = 1.f / FPMIN, d = 1.f / b, h = d;
+    for (int i = 1; i < 64; ++i) {
+        const float an = -i * (i - a);
+        b += 2.f;
+        d = an * d + b;
+        if (fabsf(d) < FPMIN) d = FPMIN;
+        c = b + an / c;
+        if (fabsf(c) < FPMIN) c = FPMIN;
+        d = 1.f / d;
+        const float del = d * c;
+        h *= del;
+        if (fabsf(del - 1.f) <= 1e-7f) break;
+    }
+    return expf(-x + a * logf(x) - gln) * h;
+}
+
+struct Thole {
+    float e, u4g, u;  // exp(-gamma u^4), gamma u^4, u
+    bool damped;
+};
+
+__device__ __forceinline__ Thole thole(float r, float dampprod, float gamma) {
+    Thole t;
+    t.damped = dampprod != 0.f;
+    if (!t.damped) {
+        t.e = 0.f; t.u4g = 0.f; t.u = 0.f;
+        return t;
+    }
+    const float damp = powf(dampprod, 1.f / 6.f);
+    t.u = r / damp;
+    const float u2 = t.u * t.u;
+    t.u4g = gamma * u2 * u2;
+    t.e = expf(-t.u4g);
+    return t;
+}
+__device__ __forceinline__ float s3_of(const Thole& t) { return t.damped ? 1.f - t.e : 1.f; }
+__device__ __forceinline__ float s5_of(const Thole& t) {
+    return t.damped ? (1.f - t.e) - (4.f / 3.f) * t.u4g * t.e : 1.f;
+}
+__device__ __forceinline__ float s7_of(const Thole& t, float gamma) {
+    // ((1-e) - 4/3 g e u^4) - 4/15 g (4 g u^4 - 1) e u^4
+    return t.damped ? s5_of(t) - (4.f / 15.f) * t.u4g * (4.f * t.u4g - 1.f) * t.e : 1.f;
+}
+__device__ __forceinline__ float s1_of(const Thole& t, float gamma) {
+    if (!t.damped) return 1.f;
+    const float GAMMA34 = 1.2254167024651776f;  // Gamma(3/4)
+    return (1.f - t.e) + powf(gamma, 0.25f) * t.u * GAMMA34 * gammq34(t.u4g);
+}
+
+// dipole-dipole Thole parameter for a site pair (reference :294-310)
+__device__ __forceinline__ float tdd_gamma(bool same, int ti, int tj) {
+    if (!same) return c_el.thole[2];
+    return (ti == 0 || tj == 0) ? c_el.thole[3] : c_el.thole[4];
+}
+
+// Ewald real-space radial functions bn0..bn3 (reference :2538-2560).
+struct Bn {
+    float b0, b1, b2, b3;
+};
+__device__ __forceinline__ Bn ewald_bn(float r, float r2) {
+    Bn b;
+    const float al = c_el.alpha;
+    const float ra = al * r;
+    b.b0 = erfcf(ra) / r;
+    const float alsq2 = 2.f * al * al;
+    float alsq2n = al > 0.f ? 1.f / (kSqrtPiF * al) : 0.f;
+    const float exp2a = expf(-(ra * ra));
+    alsq2n *= alsq2;
+    b.b1 = (b.b0 + alsq2n * exp2a) / r2;
+    alsq2n *= alsq2;
+    b.b2 = (3.f * b.b1 + alsq2n * exp2a) / r2;
+    alsq2n *= alsq2;
+    b.b3 = (5.f * b.b2 + alsq2n * exp2a) / r2;
+    return b;
+}
+
+__device__ __forceinline__ f3 ld3(const float* p, int i) { return mk(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+
+// ------------------------------------------------------ per-molecule prep
+// Charges and their derivatives (reference computeWaterCharge :2793-3096;
+// dipole-moment-surface coefficients at :2823-2870), FP64 per water.
+__constant__ double c_dms[84];
+__constant__ unsigned char c_dms_idx[3][84];
+
+__device__ void water_charges(const double3 O, const double3 H1, const double3 H2, double q[4], double dq[4][3][3]) {
+    const double Bohr_A = 0.52917721092;
+    const double gammaM = 0.426706882, gamma1 = 1.0 - gammaM, gamma2 = gammaM / 2;
+    const double costhe = -0.24780227221366464506, reoh = 0.958649, b1D = 1.0;
+    const double a = 0.2999e0, b = -0.6932e0, c0 = 1.0099e0, c1 = -0.1801e0, c2 = 0.0892e0;
+    double R1[3] = {(H1.x - O.x) * 10.0, (H1.y - O.y) * 10.0, (H1.z - O.z) * 10.0};
+    double R2[3] = {(H2.x - O.x) * 10.0, (H2.y - O.y) * 10.0, (H2.z - O.z) * 10.0};
+    const double d1 = sqrt(R1[0] * R1[0] + R1[1] * R1[1] + R1[2] * R1[2]);
+    const double d2 = sqrt(R2[0] * R2[0] + R2[1] * R2[1] + R2[2] * R2[2]);
+    const double costh = (R1[0] * R2[0] + R1[1] * R2[1] + R1[2] * R2[2]) / (d1 * d2);
+    const double efac = exp(-b1D * ((d1 - reoh) * (d1 - reoh) + (d2 - reoh) * (d2 - reoh)));
+    const double x1 = (d1 - reoh) / reoh, x2 = (d2 - reoh) / reoh, x3 = costh - costhe;
+    double p1f[8], p2f[8], p3f[8];  // x^n, n = 0..7
+    p1f[0] = p2f[0] = p3f[0] = 1.0;
+    for (int n = 1; n < 8; ++n) {
+        p1f[n] = p1f[n - 1] * x1;
+        p2f[n] = p2f[n - 1] * x2;
+        p3f[n] = p3f[n - 1] * x3;
+    }
+    double p1 = 0, p2 = 0, dp1dr1 = 0, dp1dr2 = 0, dp1dc = 0, dp2dr1 = 0, dp2dr2 = 0, dp2dc = 0;
+    for (int j = 1; j < 84; ++j) {
+        const int i0 = c_dms_idx[0][j] - 1, i1 = c_dms_idx[1][j] - 1, i2 = c_dms_idx[2][j] - 1;
+        const double cj = c_dms[j];
+        p1 += cj * p1f[i0] * p2f[i1] * p3f[i2];
+        p2 += cj * p1f[i1] * p2f[i0] * p3f[i2];
+        if (i0 > 0) dp1dr1 += cj * i0 * p1f[i0 - 1] * p2f[i1] * p3f[i2];
+        if (i1 > 0) dp1dr2 += cj * i1 * p1f[i0] * p2f[i1 - 1] * p3f[i2];
+        if (i2 > 0) dp1dc += cj * i2 * p1f[i0] * p2f[i1] * p3f[i2 - 1];
+        if (i1 > 0) dp2dr1 += cj * i1 * p1f[i1 - 1] * p2f[i0] * p3f[i2];
+        if (i0 > 0) dp2dr2 += cj * i0 * p1f[i1] * p2f[i0 - 1] * p3f[i2];
+        if (i2 > 0) dp2dc += cj * i2 * p1f[i1] * p2f[i0] * p3f[i2 - 1];
+    }
+    const double xx = Bohr_A, xx2 = xx * xx;
+    dp1dr1 /= reoh / xx;
+    dp1dr2 /= reoh / xx;
+    dp2dr1 /= reoh / xx;
+    dp2dr2 /= reoh / xx;
+    const double pl1 = costh, pl2 = 0.5 * (3 * pl1 * pl1 - 1.0);
+    const double pc0 = a * (pow(d1, b) + pow(d2, b)) * (c0 + pl1 * c1 + pl2 * c2);
+    const double dpc0dr1 = a * b * pow(d1, b - 1) * (c0 + pl1 * c1 + pl2 * c2) * xx2;
+    const double dpc0dr2 = a * b * pow(d2, b - 1) * (c0 + pl1 * c1 + pl2 * c2) * xx2;
+    const double dpc0dc = a * (pow(d1, b) + pow(d2, b)) * (c1 + 0.5 * (6.0 * pl1) * c2) * xx;
+    const double defacdr1 = -2.0 * b1D * (d1 - reoh) * efac * xx;
+    const double defacdr2 = -2.0 * b1D * (d2 - reoh) * efac * xx;
+    dp1dr1 = dp1dr1 * efac + p1 * defacdr1 + dpc0dr1;
+    dp1dr2 = dp1dr2 * efac + p1 * defacdr2 + dpc0dr2;
+    dp1dc = dp1dc * efac + dpc0dc;
+    dp2dr1 = dp2dr1 * efac + p2 * defacdr1 + dpc0dr1;
+    dp2dr2 = dp2dr2 * efac + p2 * defacdr2 + dpc0dr2;
+    dp2dc = dp2dc * efac + dpc0dc;
+    p1 = c_dms[0] + p1 * efac + pc0 * xx;
+    p2 = c_dms[0] + p2 * efac + pc0 * xx;
+    const double qO = -(p1 + p2), qH1 = p1, qH2 = p2;
+    const double g21 = gamma2 / gamma1;
+    q[0] = 0.0;
+    q[1] = qH1 + g21 * (qH1 + qH2);
+    q[2] = qH2 + g21 * (qH1 + qH2);
+    q[3] = qO / gamma1;
+    dp1dr1 /= xx;
+    dp1dr2 /= xx;
+    dp2dr1 /= xx;
+    dp2dr2 /= xx;
+    const double f1q1r13 = (dp1dr1 - (dp1dc * costh / d1)) / d1;
+    const double f1q1r23 = dp1dc / (d1 * d2);
+    const double f2q1r23 = (dp1dr2 - (dp1dc * costh / d2)) / d2;
+    const double f2q1r13 = dp1dc / (d2 * d1);
+    const double f1q2r13 = (dp2dr1 - (dp2dc * costh / d1)) / d1;
+    const double f1q2r23 = dp2dc / (d1 * d2);
+    const double f2q2r23 = (dp2dr2 - (dp2dc * costh / d2)) / d2;
+    const double f2q2r13 = dp2dc / (d2 * d1);
+    // dq[site][s][xyz]: derivative of the charge of other-site s (H1, H2, M)
+    // w.r.t. the position of `site` (O=0, H1=1, H2=2, M=3), per nm
+    for (int k = 0; k < 3; ++k) {
+        const double qh1_h1 = f1q1r13 * R1[k] + f1q1r23 * R2[k];
+        const double qh1_h2 = f2q1r13 * R1[k] + f2q1r23 * R2[k];
+        const double qh1_o = -(qh1_h1 + qh1_h2);
+        const double qh2_h1 = f1q2r13 * R1[k] + f1q2r23 * R2[k];
+        const double qh2_h2 = f2q2r13 * R1[k] + f2q2r23 * R2[k];
+        const double qh2_o = -(qh2_h1 + qh2_h2);
+        const double qo_h1 = -(qh1_h1 + qh2_h1), qo_h2 = -(qh1_h2 + qh2_h2), qo_o = -(qh1_o + qh2_o);
+        const double sH1 = g21 * (qh1_h1 + qh2_h1), sH2 = g21 * (qh1_h2 + qh2_h2), sO = g21 * (qh1_o + qh2_o);
+        dq[1][0][k] = (qh1_h1 + sH1) * 10.0;
+        dq[2][0][k] = (qh1_h2 + sH2) * 10.0;
+        dq[0][0][k] = (qh1_o + sO) * 10.0;
+        dq[1][1][k] = (qh2_h1 + sH1) * 10.0;
+        dq[2][1][k] = (qh2_h2 + sH2) * 10.0;
+        dq[0][1][k] = (qh2_o + sO) * 10.0;
+        dq[1][2][k] = (qo_h1 - 2 * sH1) * 10.0;
+        dq[2][2][k] = (qo_h2 - 2 * sH2) * 10.0;
+        dq[0][2][k] = (qo_o - 2 * sO) * 10.0;
+        dq[3][0][k] = dq[3][1][k] = dq[3][2][k] = 0.0;
+    }
+}
+
+// Per molecule: site offsets from the first site (FP64 -> FP32, minimum
+// image), charges (static or redistributed), charge derivatives, and the PME
+// grid coordinates of every site.
+__global__ void elec_prepare_kernel(int nmol, const double* __restrict__ pos, int periodic, int redist,
+                                    const float* __restrict__ q_static, float* __restrict__ off,
+                                    float* __restrict__ q, float* __restrict__ dq, int pme,
+                                    int* __restrict__ gidx, float* __restrict__ gfrac) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmol) return;
+    const int K = c_el.K, s0 = K * m;
+    const double3 O = load_pos(pos, s0);
+    double3 S[kMaxK];
+    for (int s = 0; s < K; ++s) {
+        double3 p = load_pos(pos, s0 + s);
+        if (periodic) {
+            p.x = O.x + min_image(p.x - O.x, c_el.box[0], c_el.inv[0]);
+            p.y = O.y + min_image(p.y - O.y, c_el.box[1], c_el.inv[1]);
+            p.z = O.z + min_image(p.z - O.z, c_el.box[2], c_el.inv[2]);
+        }
+        S[s] = p;
+        off[3 * (s0 + s)] = (float)(p.x - O.x);
+        off[3 * (s0 + s) + 1] = (float)(p.y - O.y);
+        off[3 * (s0 + s) + 2] = (float)(p.z - O.z);
+    }
+    if (redist) {
+        double qq[4], dd[4][3][3];
+        water_charges(S[0], S[1], S[2], qq, dd);
+        for (int s = 0; s < 4; ++s) {
+            q[s0 + s] = (float)qq[s];
+            for (int o = 0; o < 3; ++o)
+                for (int k = 0; k < 3; ++k) dq[9 * (s0 + s) + 3 * o + k] = (float)dd[s][o][k];
+        }
+    } else {
+        for (int s = 0; s < K; ++s) {
+            q[s0 + s] = q_static[s0 + s];
+            for (int o = 0; o < 9; ++o) dq[9 * (s0 + s) + o] = 0.f;
+        }
+    }
+    if (pme) {
+        // reference computeMBPolBsplines (:1522-1554): wrap into [-L/2, L/2),
+        // fr = N (w - (int)(w + 0.5) + 0.5), base index ifr - 4 (mod N)
+        for (int s = 0; s < K; ++s) {
+            const double pp[3] = {S[s].x, S[s].y, S[s].z};
+            for (int d = 0; d < 3; ++d) {
+                double x = pp[d] - floor(pp[d] * c_el.inv[d] + 0.5) * c_el.box[d];
+                double w = x * c_el.inv[d];
+                double fr = c_el.grid[d] * (w - (int)(w + 0.5) + 0.5);
+                int ifr = (int)fr;
+                float frac = (float)(fr - ifr);
+                int ig = ifr - 5 + 1;
+                if (ig < 0) ig += c_el.grid[d];
+                gidx[3 * (s0 + s) + d] = ig;
+                gfrac[3 * (s0 + s) + d] = frac;
+            }
+        }
+    }
+}
+
+// Molecule neighbour list: j != i, O-O <= rlist (cluster-restricted when
+// cluster ids are given), with the FP64 minimum-image O-O vector in FP32.
+__global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, int periodic, double rlist2,
+                                      int cap, int* __restrict__ nb, float* __restrict__ nbd,
+                                      int* __restrict__ nnb, int* __restrict__ overflow,
+                                      const int* __restrict__ cluster) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= nmol) return;
+    const int K = c_el.K;
+    const double3 oi = load_pos(pos, K * i);
+    const int ci = cluster ? cluster[i] : 0;
+    int n = 0;
+    for (int base = 0; base < nmol; base += 32) {
+        const int j = base + lane;
+        bool in = false;
+        double dx = 0, dy = 0, dz = 0;
+        if (j < nmol && j != i && (!cluster || cluster[j] == ci)) {
+            const double3 oj = load_pos(pos, K * j);
+            dx = oj.x - oi.x;
+            dy = oj.y - oi.y;
+            dz = oj.z - oi.z;
+            if (periodic) {
+                dx = min_image(dx, c_el.box[0], c_el.inv[0]);
+                dy = min_image(dy, c_el.box[1], c_el.inv[1]);
+                dz = min_image(dz, c_el.box[2], c_el.inv[2]);
+            }
+            in = dx * dx + dy * dy + dz * dz <= rlist2;
+        }
+        const unsigned msk = __ballot_sync(0xffffffffu, in);
+        if (in) {
+            const int slot = n + __popc(msk & ((1u << lane) - 1u));
+            if (slot < cap) {
+                nb[(size_t)i * cap + slot] = j;
+                nbd[3 * ((size_t)i * cap + slot)] = (float)dx;
+                nbd[3 * ((size_t)i * cap + slot) + 1] = (float)dy;
+                nbd[3 * ((size_t)i * cap + slot) + 2] = (float)dz;
+            }
+        }
+        n += __popc(msk);
+    }
+    if (lane == 0) {
+        nnb[i] = n;
+        if (n > cap) atomicOr(overflow, 1);
+    }
+}
+
+// ---------------------------------------------------------------- B-splines
+// Order-5 cardinal B-spline weights at the 5 grid points, and their first and
+// second derivatives (Cox-de Boor recursion; derivatives by differencing the
+// order-4 and order-3 splines).
+__device__ __forceinline__ void bspline5(float w, float th[5], float d1[5], float d2[5]) {
+    float A2[2] = {1.f - w, w};
+    float A3[3];
+    A3[2] = 0.5f * w * A2[1];
+    A3[1] = 0.5f * ((1.f + w) * A2[0] + (2.f - w) * A2[1]);
+    A3[0] = 0.5f * (1.f - w) * A2[0];
+    float A4[4];
+    {
+        const float dn = 1.f / 3.f;
+        A4[3] = dn * w * A3[2];
+        A4[2] = dn * ((w + 1.f) * A3[1] + (3.f - w) * A3[2]);
+        A4[1] = dn * ((w + 2.f) * A3[0] + (2.f - w) * A3[1]);
+        A4[0] = dn * (1.f - w) * A3[0];
+    }
+    {
+        const float dn = 0.25f;
+        th[4] = dn * w * A4[3];
+        th[3] = dn * ((w + 1.f) * A4[2] + (4.f - w) * A4[3]);
+        th[2] = dn * ((w + 2.f) * A4[1] + (3.f - w) * A4[2]);
+        th[1] = dn * ((w + 3.f) * A4[0] + (2.f - w) * A4[1]);
+        th[0] = dn * (1.f - w) * A4[0];
+    }
+    // first derivative from the order-4 values
+    d1[4] = A4[3];
+    d1[3] = A4[2] - A4[3];
+    d1[2] = A4[1] - A4[2];
+    d1[1] = A4[0] - A4[1];
+    d1[0] = -A4[0];
+    // second derivative: difference the order-3 values twice
+    float E[4];
+    E[3] = A3[2];
+    E[2] = A3[1] - A3[2];
+    E[1] = A3[0] - A3[1];
+    E[0] = -A3[0];
+    d2[4] = E[3];
+    d2[3] = E[2] - E[3];
+    d2[2] = E[1] - E[2];
+    d2[1] = E[0] - E[1];
+    d2[0] = -E[0];
+}
+
+// Spread charges (mode 0) or dipoles (mode 1) of every site onto the grid.
+__global__ void pme_spread_kernel(int nsite, int mode, const float* __restrict__ q, const float* __restrict__ mu,
+                                  const int* __restrict__ gidx, const float* __restrict__ gfrac,
+                                  float* __restrict__ grid) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsite) return;
+    float tx[5], ty[5], tz[5], dx[5], dy[5], dz[5], sx[5];
+    bspline5(gfrac[3 * i], tx, dx, sx);
+    bspline5(gfrac[3 * i + 1], ty, dy, sx);
+    bspline5(gfrac[3 * i + 2], tz, dz, sx);
+    const int Nx = c_el.grid[0], Ny = c_el.grid[1], Nz = c_el.grid[2];
+    const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
+    float c0 = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+    if (mode == 0) {
+        c0 = q[i];
+        if (c0 == 0.f) return;
+    } else {
+        mx = mu[3 * i] * c_el.scale[0];
+        my = mu[3 * i + 1] * c_el.scale[1];
+        mz = mu[3 * i + 2] * c_el.scale[2];
+        if (mx == 0.f && my == 0.f && mz == 0.f) return;
+    }
+    for (int a = 0; a < 5; ++a) {
+        int x = gx + a;
+        if (x >= Nx) x -= Nx;
+        for (int b = 0; b < 5; ++b) {
+            int y = gy + b;
+            if (y >= Ny) y -= Ny;
+            const float txy = tx[a] * ty[b];
+            const float wA = mode == 0 ? c0 * txy : mx * dx[a] * ty[b];
+            const float wB = mode == 0 ? 0.f : my * tx[a] * dy[b];
+            const float wC = mode == 0 ? 0.f : mz * txy;
+            float* row = grid + ((size_t)x * Ny + y) * Nz;
+            for (int c = 0; c < 5; ++c) {
+                int z = gz + c;
+                if (z >= Nz) z -= Nz;
+                const float v = mode == 0 ? wA * tz[c] : (wA + wB) * tz[c] + wC * dz[c];
+                atomicAdd(row + z, v);
+            }
+        }
+    }
+}
+
+// Reciprocal convolution on the R2C half grid (reference :1676-1713).
+__global__ void pme_convolve_kernel(cufftComplex* __restrict__ g, const float* __restrict__ bx,
+                                    const float* __restrict__ by, const float* __restrict__ bz, float expf_,
+                                    float scalef, int nzh) {
+    const int Nx = c_el.grid[0], Ny = c_el.grid[1], Nz = c_el.grid[2];
+    const long total = (long)Nx * Ny * nzh;
+    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+        const int kz = (int)(idx % nzh);
+        const long rest = idx / nzh;
+        const int ky = (int)(rest % Ny);
+        const int kx = (int)(rest / Ny);
+        if (kx == 0 && ky == 0 && kz == 0) {
+            g[idx].x = g[idx].y = 0.f;
+            continue;
+        }
+        const int mx = kx < (Nx + 1) / 2 ? kx : kx - Nx;
+        const int my = ky < (Ny + 1) / 2 ? ky : ky - Ny;
+        const int mz = kz < (Nz + 1) / 2 ? kz : kz - Nz;
+        const float mhx = mx * (float)c_el.inv[0], mhy = my * (float)c_el.inv[1], mhz = mz * (float)c_el.inv[2];
+        const float m2 = mhx * mhx + mhy * mhy + mhz * mhz;
+        const float denom = m2 * bx[kx] * by[ky] * bz[kz];
+        const float eterm = scalef * expf(-expf_ * m2) / denom;
+        g[idx].x *= eterm;
+        g[idx].y *= eterm;
+    }
+}
+
+// Gather phi and derivatives (grid units) at every site: ncomp 4 (phi, dx,
+// dy, dz) or 10 (+ xx, yy, zz, xy, xz, yz).
+__global__ void pme_gather_kernel(int nsite, int ncomp, const float* __restrict__ grid,
+                                  const int* __restrict__ gidx, const float* __restrict__ gfrac,
+                                  float* __restrict__ phi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsite) return;
+    float tx[5], ty[5], tz[5], dx[5], dy[5], dz[5], ex[5], ey[5], ez[5];
+    bspline5(gfrac[3 * i], tx, dx, ex);
+    bspline5(gfrac[3 * i + 1], ty, dy, ey);
+    bspline5(gfrac[3 * i + 2], tz, dz, ez);
+    const int Nx = c_el.grid[0], Ny = c_el.grid[1], Nz = c_el.grid[2];
+    const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
+    float p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < 5; ++a) {
+        int x = gx + a;
+        if (x >= Nx) x -= Nx;
+        for (int b = 0; b < 5; ++b) {
+            int y = gy + b;
+            if (y >= Ny) y -= Ny;
+            const float* row = grid + ((size_t)x * Ny + y) * Nz;
+            float t0 = 0.f, t1 = 0.f, t2 = 0.f;
+            for (int c = 0; c < 5; ++c) {
+                int z = gz + c;
+                if (z >= Nz) z -= Nz;
+                const float v = row[z];
+                t0 += v * tz[c];
+                t1 += v * dz[c];
+                t2 += v * ez[c];
+            }
+            p[0] += tx[a] * ty[b] * t0;
+            p[1] += dx[a] * ty[b] * t0;
+            p[2] += tx[a] * dy[b] * t0;
+            p[3] += tx[a] * ty[b] * t1;
+            if (ncomp == 10) {
+                p[4] += ex[a] * ty[b] * t0;
+                p[5] += tx[a] * ey[b] * t0;
+                p[6] += tx[a] * ty[b] * t2;
+                p[7] += dx[a] * dy[b] * t0;
+                p[8] += dx[a] * ty[b] * t1;
+                p[9] += tx[a] * dy[b] * t1;
+            }
+        }
+    }
+    for (int k = 0; k < ncomp; ++k) phi[(size_t)ncomp * i + k] = p[k];
+}
+
+// ------------------------------------------------------------ pair kernels
+struct MolSites {
+    f3 off[kMaxK];
+    float q[kMaxK], damp[kMaxK], pol[kMaxK];
+    int type[kMaxK];
+};
+
+__device__ __forceinline__ void load_mol(int m, const float* __restrict__ off, const float* __restrict__ q,
+                                         const float* __restrict__ damp, const float* __restrict__ pol,
+                                         const int* __restrict__ type, MolSites& M) {
+    const int K = c_el.K;
+    #pragma unroll
+    for (int s = 0; s < kMaxK; ++s) {
+        if (s < K) {
+            const int i = K * m + s;
+            M.off[s] = ld3(off, i);
+            M.q[s] = q[i];
+            M.damp[s] = damp[i];
+            M.pol[s] = pol[i];
+            M.type[s] = type[i];
+        } else {
+            M.off[s] = mk(0.f, 0.f, 0.f);
+            M.q[s] = M.damp[s] = M.pol[s] = 0.f;
+            M.type[s] = -1;
+        }
+    }
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed field at the sites of molecule A (one warp).  PME adds E_rec (from
+// the gathered potential, -scale * dphi).  Writes E0 and mu0 = alpha E0.
+template <bool PME>
+__global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ q,
+                                   const float* __restrict__ damp, const float* __restrict__ pol,
+                                   const int* __restrict__ type, const int* __restrict__ nb,
+                                   const float* __restrict__ nbd, const int* __restrict__ nnb, int cap,
+                                   const float* __restrict__ phi_fix, float* __restrict__ E0,
+                                   float* __restrict__ mu_out) {
+    const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (A >= nmol) return;
+    const int K = c_el.K;
+    MolSites MA;
+    load_mol(A, off, q, damp, pol, type, MA);
+    float E[kMaxK][3];
+    #pragma unroll
+    for (int a = 0; a < kMaxK; ++a) E[a][0] = E[a][1] = E[a][2] = 0.f;
+    const int n = min(nnb[A], cap);
+    const float gcc = c_el.thole[0];
+    for (int t = lane; t < n; t += 32) {
+        const int B = nb[(size_t)A * cap + t];
+        const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
+        MolSites MB;
+        load_mol(B, off, q, damp, pol, type, MB);
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) {
+            if (a >= K) continue;
+            #pragma unroll
+            for (int b = 0; b < kMaxK; ++b) {
+                if (b >= K || MB.q[b] == 0.f) continue;
+                const f3 d = dAB + MB.off[b] - MA.off[a];  // r_b - r_a
+                const float r2 = dot(d, d);
+                if (PME && r2 > c_el.rc2) continue;
+                const float r = sqrtf(r2);
+                const Thole th = thole(r, MA.damp[a] * MB.damp[b], gcc);
+                float fac;
+                if (PME) {
+                    const Bn bn = ewald_bn(r, r2);
+                    const float rr3 = (s3_of(th) - 1.f) / (r2 * r);
+                    fac = bn.b1 - rr3;
+                } else {
+                    fac = s3_of(th) / (r2 * r);
+                }
+                const float c = -MB.q[b] * fac;
+                E[a][0] += d.x * c;
+                E[a][1] += d.y * c;
+                E[a][2] += d.z * c;
+            }
+        }
+    }
+    #pragma unroll
+    for (int a = 0; a < kMaxK; ++a) {
+        E[a][0] = warp_sum(E[a][0]);
+        E[a][1] = warp_sum(E[a][1]);
+        E[a][2] = warp_sum(E[a][2]);
+    }
+    if (lane == 0) {
+        if (PME) {
+            // intramolecular pairs: s3 = 2 (reference :1375-1377), within the cutoff
+            for (int a = 0; a < K; ++a)
+                for (int b = 0; b < K; ++b) {
+                    if (a == b || MA.q[b] == 0.f) continue;
+                    const f3 d = MA.off[b] - MA.off[a];
+                    const float r2 = dot(d, d);
+                    if (r2 > c_el.rc2) continue;
+                    const float r = sqrtf(r2);
+                    const Bn bn = ewald_bn(r, r2);
+                    const float fac = bn.b1 - 1.f / (r2 * r);
+                    const float c = -MA.q[b] * fac;
+                    E[a][0] += d.x * c;
+                    E[a][1] += d.y * c;
+                    E[a][2] += d.z * c;
+                }
+        }
+        for (int a = 0; a < K; ++a) {
+            const int i = K * A + a;
+            float ex = E[a][0], ey = E[a][1], ez = E[a][2];
+            if (PME) {
+                ex -= c_el.scale[0] * phi_fix[10 * i + 1];
+                ey -= c_el.scale[1] * phi_fix[10 * i + 2];
+                ez -= c_el.scale[2] * phi_fix[10 * i + 3];
+            }
+            E0[3 * i] = ex;
+            E0[3 * i + 1] = ey;
+            E0[3 * i + 2] = ez;
+            mu_out[3 * i] = MA.pol[a] * ex;
+            mu_out[3 * i + 1] = MA.pol[a] * ey;
+            mu_out[3 * i + 2] = MA.pol[a] * ez;
+        }
+    }
+}
+
+// Induced field from mu_in at the sites of molecule A, then the SOR update
+// mu_out = mu_in + 0.55 (alpha (E0 + E_ind) - mu_in) and sum |delta|^2.
+template <bool PME>
+__global__ void induced_update_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ damp,
+                                      const float* __restrict__ pol, const int* __restrict__ type,
+                                      const int* __restrict__ nb, const float* __restrict__ nbd,
+                                      const int* __restrict__ nnb, int cap, const float* __restrict__ E0,
+                                      const float* __restrict__ phi_mu, const float* __restrict__ mu_in,
+                                      float* __restrict__ mu_out, double* __restrict__ eps2) {
+    const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    double d2sum = 0.0;
+    if (A < nmol) {
+        const int K = c_el.K;
+        f3 offA[kMaxK];
+        float dA[kMaxK];
+        int tA[kMaxK];
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) {
+            if (a < K) {
+                offA[a] = ld3(off, K * A + a);
+                dA[a] = damp[K * A + a];
+                tA[a] = type[K * A + a];
+            }
+        }
+        float E[kMaxK][3];
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) E[a][0] = E[a][1] = E[a][2] = 0.f;
+        const int n = min(nnb[A], cap);
+        for (int t = lane; t < n; t += 32) {
+            const int B = nb[(size_t)A * cap + t];
+            const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
+            #pragma unroll
+            for (int b = 0; b < kMaxK; ++b) {
+                if (b >= K) continue;
+                const int jb = K * B + b;
+                const f3 mub = ld3(mu_in, jb);
+                if (mub.x == 0.f && mub.y == 0.f && mub.z == 0.f) continue;
+                const f3 offb = ld3(off, jb);
+                const float db = damp[jb];
+                #pragma unroll
+                for (int a = 0; a < kMaxK; ++a) {
+                    if (a >= K) continue;
+                    const f3 d = dAB + offb - offA[a];
+                    const float r2 = dot(d, d);
+                    if (PME && r2 > c_el.rc2) continue;
+                    const float r = sqrtf(r2);
+                    const Thole th = thole(r, dA[a] * db, c_el.thole[2]);
+                    float pf1, pf2;
+                    if (PME) {
+                        const Bn bn = ewald_bn(r, r2);
+                        const float rr3 = (1.f - s3_of(th)) / (r2 * r);
+                        const float rr5 = 3.f * (1.f - s5_of(th)) / (r2 * r2 * r);
+                        pf1 = rr3 - bn.b1;
+                        pf2 = bn.b2 - rr5;
+                    } else {
+                        pf1 = -s3_of(th) / (r2 * r);
+                        pf2 = 3.f * s5_of(th) / (r2 * r2 * r);
+                    }
+                    const float dur = dot(mub, d) * pf2;
+                    E[a][0] += d.x * dur + mub.x * pf1;
+                    E[a][1] += d.y * dur + mub.y * pf1;
+                    E[a][2] += d.z * dur + mub.z * pf1;
+                }
+            }
+        }
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) {
+            E[a][0] = warp_sum(E[a][0]);
+            E[a][1] = warp_sum(E[a][1]);
+            E[a][2] = warp_sum(E[a][2]);
+        }
+        if (lane == 0) {
+            // intramolecular pairs (same-water Thole parameters)
+            for (int a = 0; a < K; ++a)
+                for (int b = 0; b < K; ++b) {
+                    if (a == b) continue;
+                    const int jb = K * A + b;
+                    const f3 mub = ld3(mu_in, jb);
+                    const f3 d = offA[b] - offA[a];
+                    const float r2 = dot(d, d);
+                    if (PME && r2 > c_el.rc2) continue;
+                    const float r = sqrtf(r2);
+                    const Thole th = thole(r, dA[a] * dA[b], tdd_gamma(true, tA[a], tA[b]));
+                    float pf1, pf2;
+                    if (PME) {
+                        const Bn bn = ewald_bn(r, r2);
+                        pf1 = (1.f - s3_of(th)) / (r2 * r) - bn.b1;
+                        pf2 = bn.b2 - 3.f * (1.f - s5_of(th)) / (r2 * r2 * r);
+                    } else {
+                        pf1 = -s3_of(th) / (r2 * r);
+                        pf2 = 3.f * s5_of(th) / (r2 * r2 * r);
+                    }
+                    const float dur = dot(mub, d) * pf2;
+                    E[a][0] += d.x * dur + mub.x * pf1;
+                    E[a][1] += d.y * dur + mub.y * pf1;
+                    E[a][2] += d.z * dur + mub.z * pf1;
+                }
+            for (int a = 0; a < K; ++a) {
+                const int i = K * A + a;
+                const f3 mu = ld3(mu_in, i);
+                float ex = E[a][0], ey = E[a][1], ez = E[a][2];
+                if (PME) {
+                    ex += c_el.self_term * mu.x - c_el.scale[0] * phi_mu[4 * i + 1];
+                    ey += c_el.self_term * mu.y - c_el.scale[1] * phi_mu[4 * i + 2];
+                    ez += c_el.self_term * mu.z - c_el.scale[2] * phi_mu[4 * i + 3];
+                }
+                const float al = pol[i];
+                // reference updateInducedDipole (:516-531); E0 is unscaled here
+                const double nx = (double)al * ((double)E0[3 * i] + ex);
+                const double ny = (double)al * ((double)E0[3 * i + 1] + ey);
+                const double nz = (double)al * ((double)E0[3 * i + 2] + ez);
+                const double dx = nx - mu.x, dy = ny - mu.y, dz = nz - mu.z;
+                mu_out[3 * i] = (float)(mu.x + kSOR * dx);
+                mu_out[3 * i + 1] = (float)(mu.y + kSOR * dy);
+                mu_out[3 * i + 2] = (float)(mu.z + kSOR * dz);
+                d2sum += dx * dx + dy * dy + dz * dz;
+            }
+        }
+    }
+    block_sum_atomic<128>(d2sum, eps2);
+}
+
+// Energy and forces for molecule A (one warp): direct pairs over the full
+// list (force on A's sites, half the pair energy), intramolecular pairs, the
+// reciprocal and self parts, and the charge-derivative forces through the
+// total potential at A's H1, H2, M sites.
+template <bool PME>
+__global__ void energy_force_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ q,
+                                    const float* __restrict__ dq, const float* __restrict__ damp,
+                                    const int* __restrict__ type, const int* __restrict__ nb,
+                                    const float* __restrict__ nbd, const int* __restrict__ nnb, int cap,
+                                    const float* __restrict__ mu, const float* __restrict__ phi_fix,
+                                    const float* __restrict__ phi_mu, int redist, double* __restrict__ force,
+                                    double* __restrict__ energy) {
+    const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    double e_out = 0.0;
+    if (A < nmol) {
+        const int K = c_el.K;
+        const float f = (float)kElectric;
+        f3 offA[kMaxK], muA[kMaxK];
+        float qA[kMaxK], dA[kMaxK];
+        int tA[kMaxK];
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) {
+            if (a < K) {
+                const int i = K * A + a;
+                offA[a] = ld3(off, i);
+                muA[a] = ld3(mu, i);
+                qA[a] = q[i];
+                dA[a] = damp[i];
+                tA[a] = type[i];
+            }
+        }
+        float F[kMaxK][3], P[kMaxK];  // force on A's sites (before * f), potential (for dq terms)
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) F[a][0] = F[a][1] = F[a][2] = P[a] = 0.f;
+        float e = 0.f;
+        const int n = min(nnb[A], cap);
+        const float gcc = c_el.thole[0], gcd = c_el.thole[1], gdd = c_el.thole[2];
+        for (int t = lane; t < n; t += 32) {
+            const int B = nb[(size_t)A * cap + t];
+            const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
+            #pragma unroll
+            for (int b = 0; b < kMaxK; ++b) {
+                if (b >= K) continue;
+                const int jb = K * B + b;
+                const f3 offb = ld3(off, jb), mub = ld3(mu, jb);
+                const float qb = q[jb], db = damp[jb];
+                #pragma unroll
+                for (int a = 0; a < kMaxK; ++a) {
+                    if (a >= K) continue;
+                    const f3 d = dAB + offb - offA[a];  // r_b - r_a  (A = i, B = j)
+                    const float r2 = dot(d, d);
+                    if (PME && r2 > c_el.rc2) continue;
+                    const float r = sqrtf(r2);
+                    const float rr1 = 1.f / r, rr3 = rr1 / r2, rr5 = 3.f * rr3 / r2, rr7 = 5.f * rr5 / r2;
+                    const float dprod = dA[a] * db;
+                    const float sci3 = dot(muA[a], d), sci4 = dot(mub, d), mumu = dot(muA[a], mub);
+                    const float gl0 = qA[a] * qb;
+                    const float gli = qb * sci3 - qA[a] * sci4;
+                    const Thole tCC = thole(r, dprod, gcc), tCD = thole(r, dprod, gcd), tDD = thole(r, dprod, gdd);
+                    f3 fo;
+                    if (PME) {
+                        const Bn bn = ewald_bn(r, r2);
+                        const float s1CC = gl0 != 0.f || qb != 0.f ? s1_of(tCC, gcc) : 1.f;
+                        const float s3CD = s3_of(tCD);
+                        e += 0.5f * (bn.b0 * gl0 + 0.5f * bn.b1 * gli - rr1 * gl0 * (1.f - s1CC) -
+                                     0.5f * rr3 * gli * (1.f - s3CD));
+                        P[a] += qb * (bn.b0 - rr1 * (1.f - s1CC)) - sci4 * (bn.b1 - rr3 * (1.f - s3CD));
+                        const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
+                        const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
+                        const float gf1 = bn.b1 * gl0, gfr1 = (1.f - s3CC) * rr3 * gl0;
+                        const float gfi1 = bn.b2 * (gli + mumu) - bn.b3 * sci3 * sci4;
+                        const float gfri1 = rr5 * (gli * (1.f - s5CD) + mumu * (1.f - s5DD)) -
+                                            rr7 * sci3 * sci4 * (1.f - s7DD);
+                        const float c_d = gf1 - gfr1 + gfi1 - gfri1;
+                        const float c_i = -qb * bn.b1 - (-qb) * rr3 * (1.f - s3CD);  // mu_i coefficient
+                        const float c_j = qA[a] * bn.b1 - qA[a] * rr3 * (1.f - s3CD);
+                        const float c_dd = bn.b2 - rr5 * (1.f - s5DD);
+                        fo = d * c_d + muA[a] * (c_i + sci4 * c_dd) + mub * (c_j + sci3 * c_dd);
+                    } else {
+                        const float s1CC = s1_of(tCC, gcc), s3CD = s3_of(tCD);
+                        e += 0.5f * (rr1 * gl0 * s1CC + 0.5f * rr3 * gli * s3CD);
+                        const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
+                        const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
+                        const float gf0 = rr3 * gl0 * s3CC;
+                        const float gfi0 = rr5 * gli * s5CD + rr5 * mumu * s5DD - rr7 * sci3 * sci4 * s7DD;
+                        fo = d * (gf0 + gfi0) + (muA[a] * sci4 + mub * sci3) * (rr5 * s5DD) +
+                             (mub * qA[a] - muA[a] * qb) * (rr3 * s3CD);
+                        if (redist) {
+                            // potential at A's site from B's site, TCC scaling for both
+                            // terms (reference :808-827)
+                            const float sc3 = s3_of(tCC);
+                            const float sc1 = s1_of(tCC, gcc);
+                            P[a] += qb * sc1 * rr1 - sc3 * sci4 * rr3;
+                        }
+                    }
+                    // force on site a of A: -force(i, j)
+                    F[a][0] -= fo.x;
+                    F[a][1] -= fo.y;
+                    F[a][2] -= fo.z;
+                }
+            }
+        }
+        e = warp_sum(e);
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) {
+            F[a][0] = warp_sum(F[a][0]);
+            F[a][1] = warp_sum(F[a][1]);
+            F[a][2] = warp_sum(F[a][2]);
+            P[a] = warp_sum(P[a]);
+        }
+        if (lane == 0) {
+            // intramolecular pairs, a < b (both sites are A's)
+            for (int a = 0; a < K; ++a)
+                for (int b = a + 1; b < K; ++b) {
+                    const f3 d = offA[b] - offA[a];
+                    const float r2 = dot(d, d);
+                    if (PME && r2 > c_el.rc2) continue;
+                    const float r = sqrtf(r2);
+                    const float rr1 = 1.f / r, rr3 = rr1 / r2, rr5 = 3.f * rr3 / r2, rr7 = 5.f * rr5 / r2;
+                    const float sci3 = dot(muA[a], d), sci4 = dot(muA[b], d), mumu = dot(muA[a], muA[b]);
+                    const float gdd2 = tdd_gamma(true, tA[a], tA[b]);
+                    const Thole tDD = thole(r, dA[a] * dA[b], gdd2);
+                    const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd2);
+                    f3 fo;
+                    if (PME) {
+                        const Bn bn = ewald_bn(r, r2);
+                        const float gl0 = qA[a] * qA[b];
+                        const float gli = qA[b] * sci3 - qA[a] * sci4;
+                        // same water: s1CC = s3CD = s3CC = s5CD = 0
+                        e += bn.b0 * gl0 + 0.5f * bn.b1 * gli - rr1 * gl0 - 0.5f * rr3 * gli;
+                        P[a] += qA[b] * (bn.b0 - rr1) - sci4 * (bn.b1 - rr3);
+                        P[b] += qA[a] * (bn.b0 - rr1) + sci3 * (bn.b1 - rr3);
+                        const float gf1 = bn.b1 * gl0, gfr1 = rr3 * gl0;
+                        const float gfi1 = bn.b2 * (gli + mumu) - bn.b3 * sci3 * sci4;
+                        const float gfri1 = rr5 * (gli + mumu * (1.f - s5DD)) - rr7 * sci3 * sci4 * (1.f - s7DD);
+                        const float c_d = gf1 - gfr1 + gfi1 - gfri1;
+                        const float c_i = -qA[b] * bn.b1 + qA[b] * rr3;
+                        const float c_j = qA[a] * bn.b1 - qA[a] * rr3;
+                        const float c_dd = bn.b2 - rr5 * (1.f - s5DD);
+                        fo = d * c_d + muA[a] * (c_i + sci4 * c_dd) + muA[b] * (c_j + sci3 * c_dd);
+                    } else {
+                        // same water: no charge-charge or charge-dipole terms
+                        const float gfi0 = rr5 * mumu * s5DD - rr7 * sci3 * sci4 * s7DD;
+                        fo = d * gfi0 + (muA[a] * sci4 + muA[b] * sci3) * (rr5 * s5DD);
+                    }
+                    F[a][0] -= fo.x;
+                    F[a][1] -= fo.y;
+                    F[a][2] -= fo.z;
+                    F[b][0] += fo.x;
+                    F[b][1] += fo.y;
+                    F[b][2] += fo.z;
+                }
+            // reciprocal space and self (reference :2113-2265, :2472-2508)
+            if (PME) {
+                const float sx = c_el.scale[0], sy = c_el.scale[1], sz = c_el.scale[2];
+                const float sc[3] = {sx, sy, sz};
+                const float ak = c_el.alpha;
+                for (int a = 0; a < K; ++a) {
+                    const int i = K * A + a;
+                    const float* pf = phi_fix + 10 * i;
+                    const float* pm = phi_mu + 10 * i;
+                    // energies: fixed 0.5 q phi, induced 0.5 mu . grad phi_fixed, self -q^2 alpha/sqrt(pi)
+                    e += 0.5f * qA[a] * pf[0];
+                    e += 0.5f * (sx * muA[a].x * pf[1] + sy * muA[a].y * pf[2] + sz * muA[a].z * pf[3]);
+                    e += -qA[a] * qA[a] * ak / kSqrtPiF;
+                    P[a] += pf[0] + pm[0] - 2.f * qA[a] * ak / kSqrtPiF;
+                    // hessian index of (a, k): xx 4, yy 5, zz 6, xy 7, xz 8, yz 9
+                    const int H[3][3] = {{4, 7, 8}, {7, 5, 9}, {8, 9, 6}};
+                    const float m3[3] = {muA[a].x, muA[a].y, muA[a].z};
+                    for (int c = 0; c < 3; ++c) {
+                        float fdip = 0.f;
+                        for (int k = 0; k < 3; ++k) fdip += sc[k] * m3[k] * (pf[H[c][k]] + pm[H[c][k]]);
+                        const float fc = sc[c] * (fdip + qA[a] * (pf[1 + c] + pm[1 + c]));
+                        F[a][c] -= fc;
+                    }
+                }
+            }
+            // charge-derivative forces: F_i -= sum_s dq_i[s] * phi(other site s)
+            // (reference :2767-2773 for PME, :791-827 for NoCutoff)
+            if (redist && K == 4) {
+                for (int a = 0; a < K; ++a) {
+                    const int i = K * A + a;
+                    for (int s = 0; s < 3; ++s) {
+                        const float phis = P[s + 1];
+                        F[a][0] -= dq[9 * i + 3 * s] * phis;
+                        F[a][1] -= dq[9 * i + 3 * s + 1] * phis;
+                        F[a][2] -= dq[9 * i + 3 * s + 2] * phis;
+                    }
+                }
+            }
+            for (int a = 0; a < K; ++a) {
+                const int i = K * A + a;
+                force[3 * i] += (double)F[a][0] * f;
+                force[3 * i + 1] += (double)F[a][1] * f;
+                force[3 * i + 2] += (double)F[a][2] * f;
+            }
+            e_out = (double)e * f;
+        }
+    }
+    block_sum_atomic<128>(e_out, energy);
+}
+
+// B-spline moduli with the reference's fixes (:1248-1340), host FP64.
+void bspline_moduli(int size, std::vector<double>& mod) {
+    const int order = 5;
+    double arr[order];
+    const double x = 0.0;
+    arr[0] = 1.0 - x;
+    arr[1] = x;
+    for (int k = 2; k < order; ++k) {
+        const double dn = 1.0 / k;
+        arr[k] = x * arr[k - 1] * dn;
+        for (int i = 1; i < k; ++i) arr[k - i] = ((x + i) * arr[k - i - 1] + ((k - i + 1) - x) * arr[k - i]) * dn;
+        arr[0] = (1.0 - x) * arr[0] * dn;
+    }
+    std::vector<double> bs((size_t)size + 1 + order + 2, 0.0);
+    for (int i = 2; i <= order + 1; ++i) bs[(size_t)i] = arr[i - 2];
+    mod.assign((size_t)size, 0.0);
+    const double factor = 2.0 * M_PI / size;
+    for (int i = 0; i < size; ++i) {
+        double s1 = 0, s2 = 0;
+        for (int j = 1; j <= size; ++j) {
+            const double arg = factor * i * (j - 1);
+            const double bj = j < (int)bs.size() ? bs[(size_t)j] : 0.0;
+            s1 += bj * cos(arg);
+            s2 += bj * sin(arg);
+        }
+        mod[(size_t)i] = s1 * s1 + s2 * s2;
+    }
+    const double eps = 1.0e-7;
+    if (mod[0] < eps) mod[0] = 0.5 * mod[1];
+    for (int i = 1; i < size - 1; ++i)
+        if (mod[(size_t)i] < eps) mod[(size_t)i] = 0.5 * (mod[(size_t)i - 1] + mod[(size_t)i + 1]);
+    if (mod[(size_t)size - 1] < eps) mod[(size_t)size - 1] = 0.5 * mod[(size_t)size - 2];
+    const int jcut = 50;
+    for (int i = 1; i <= size; ++i) {
+        int k = i - 1;
+        if (i > size / 2) k = k - size;
+        double zeta;
+        if (k == 0) {
+            zeta = 1.0;
+        } else {
+            double s1 = 1.0, s2 = 1.0;
+            const double fac = M_PI * k / size;
+            for (int j = 1; j <= jcut; ++j) {
+                const double arg = fac / (fac + M_PI * j);
+                s1 += pow(arg, order);
+                s2 += pow(arg, 2 * order);
+            }
+            for (int j = 1; j <= jcut; ++j) {
+                const double arg = fac / (fac - M_PI * j);
+                s1 += pow(arg, order);
+                s2 += pow(arg, 2 * order);
+            }
+            zeta = s2 / s1;
+        }
+        mod[(size_t)i - 1] *= zeta * zeta;
+    }
+}
+
+// Dipole-moment-surface fit of the charge redistribution
+// (MBPolReferenceElectrostaticsForce.cpp:2823-2870): index triples and coefficients.
+const unsigned char kDmsIdx[3][84] = {
+    {1, 1, 1, 2, 1, 1, 1, 2, 2, 3, 1, 1, 1, 1, 2, 2, 2, 3, 3, 4, 1, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 5, 1, 1, 1,
+     1, 1, 1, 2, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 5, 5, 6, 1, 1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2, 3, 3, 3, 3, 3, 4, 4,
+     4, 4, 5, 5, 5, 6, 6, 7},
+    {1, 1, 2, 1, 1, 2, 3, 1, 2, 1, 1, 2, 3, 4, 1, 2, 3, 1, 2, 1, 1, 2, 3, 4, 5, 1, 2, 3, 4, 1, 2, 3, 1, 2, 1, 1, 2, 3,
+     4, 5, 6, 1, 2, 3, 4, 5, 1, 2, 3, 4, 1, 2, 3, 1, 2, 1, 1, 2, 3, 4, 5, 6, 7, 1, 2, 3, 4, 5, 6, 1, 2, 3, 4, 5, 1, 2,
+     3, 4, 1, 2, 3, 1, 2, 1},
+    {1, 2, 1, 1, 3, 2, 1, 2, 1, 1, 4, 3, 2, 1, 3, 2, 1, 2, 1, 1, 5, 4, 3, 2, 1, 4, 3, 2, 1, 3, 2, 1, 2, 1, 1, 6, 5, 4,
+     3, 2, 1, 5, 4, 3, 2, 1, 4, 3, 2, 1, 3, 2, 1, 2, 1, 1, 7, 6, 5, 4, 3, 2, 1, 6, 5, 4, 3, 2, 1, 5, 4, 3, 2, 1, 4, 3,
+     2, 1, 3, 2, 1, 2, 1, 1}};
+const double kDmsCoef[84] = {
+    -2.1689686086730e-03, 1.4910379754728e-02, 5.3546078430060e-02, -7.4055995388666e-02, -3.7764333017616e-03,
+    1.4089887256484e-01,  -6.2584207687264e-02, -1.1260393113022e-01, -5.7824159269319e-02, 1.4360743650655e-02,
+    -1.5469680141070e-02, -1.3036350092795e-02, 2.7515837781556e-02, 1.4098478875076e-01, -2.7663168397781e-02,
+    -5.2378176254797e-03, -1.0237198381792e-02, 8.9571999265473e-02, 7.2920263098603e-03, -2.6873260551686e-01,
+    2.0220870325864e-02,  -7.0764766270927e-02, 1.2140640273760e-01, 2.0978491966341e-02, -1.9443840512668e-01,
+    4.0826835370618e-02,  -4.5365190474650e-02, 6.2779900072132e-02, -1.3194351021000e-01, -1.4673032718563e-01,
+    1.1894031277247e-01,  -6.4952851564679e-03, 8.8503610374493e-02, 1.4899437409291e-01, 1.3962841511565e-01,
+    -2.6459446720450e-02, -5.0128914532773e-02, 1.8329676428116e-01, -1.5559089125095e-01, -4.0176879767592e-02,
+    3.6192059996636e-01,  1.0202887240343e-01, 1.9318668580051e-01, -4.3435977107932e-01, -4.2080828803311e-02,
+    1.9144626027273e-01,  -1.7851138969948e-01, 1.0524533875070e-01, -1.7954071602185e-02, 5.2022455612120e-02,
+    -2.8891891146828e-01, -4.7452036576319e-02, -1.0939400546289e-01, 3.5916564473568e-01, -2.0162789820172e-01,
+    -3.5838629543696e-01, 5.6706523551202e-03, 1.3849337488211e-01, -4.1733982195604e-01, 4.1641570764241e-01,
+    -1.2243429796296e-01, 4.7141730971228e-02, -1.8224510249551e-01, -1.8880981556620e-01, -3.1992359561800e-01,
+    -1.8567550546587e-01, 6.1850530431280e-01, -6.1142756235141e-02, -1.6996135584933e-01, 5.4252879499871e-01,
+    6.6128603899427e-01,  1.2107016404639e-02, -1.9633639729189e-01, 2.7652059420824e-03, -2.2684111109778e-01,
+    -4.7924491598635e-01, 2.4287790137314e-01, -1.4296023329441e-01, 8.9664665907006e-02, -1.4003228575602e-01,
+    -1.3321543452254e-01, -1.8340983193745e-01, 2.3426707273520e-01, 1.5141050914514e-01};
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DBuf() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t ensure(size_t m) {
+        if (m <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, sizeof(T) * (m ? m : 1));
+        if (e == cudaSuccess) n = m;
+        return e;
+    }
+};
+
+}  // namespace
+
+struct ElecImpl {
+    int N = 0, K = 4, nmol = 0;
+    mbpol_electrostatics_params prm{};
+    bool pme = false;
+    std::vector<float> q_static, damp, pol;
+    std::vector<int> type;
+    DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd, d_gfrac;
+    DBuf<int> d_type, d_nb, d_nnb, d_gidx, d_flags;
+    DBuf<double> d_eps2;
+    int cap = 0;
+    // PME
+    int grid[3] = {0, 0, 0};
+    double alpha = 0.0;
+    DBuf<float> d_grid, d_gridfix, d_bx, d_by, d_bz;
+    DBuf<cufftComplex> d_cgrid;
+    cufftHandle plan_f = 0, plan_b = 0;
+    bool plans = false;
+    double box_used[3] = {0, 0, 0};
+    // state
+    bool converged = true;
+    int iterations = 0;
+    double epsilon = 0.0;
+    long npairs = 0;
+    bool have_prev = false;
+    int mu_cur = 0;  // which buffer holds the current dipoles
+
+    ~ElecImpl() {
+        if (plans) {
+            cufftDestroy(plan_f);
+            cufftDestroy(plan_b);
+        }
+    }
+};
+
+ElecEngine::ElecEngine() : impl_(new ElecImpl()) {}
+ElecEngine::~ElecEngine() { delete impl_; }
+
+mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const double* charge, const int* molecule,
+                              const int* atom_type, const double* damping, const double* polarity) {
+    ElecImpl& I = *impl_;
+    I.N = n;
+    I.prm = p;
+    I.pme = p.nonbonded_method == MBPOL_ELEC_PME;
+    if (p.nonbonded_method != MBPOL_ELEC_PME && p.nonbonded_method != MBPOL_ELEC_NOCUTOFF)
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "unknown electrostatics nonbonded method");
+    // molecules: consecutive blocks of K sites with a common molecule index
+    int K = 1;
+    while (K < n && molecule[K] == molecule[0]) ++K;
+    if (K != 3 && K != 4)
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "electrostatics expects molecules of 3 (O,H,H) or 4 (O,H,H,M) consecutive sites");
+    if (n % K) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "particle count is not a multiple of the molecule size");
+    for (int i = 0; i < n; ++i) {
+        if (molecule[i] != molecule[(i / K) * K])
+            return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "molecule indices must be constant over consecutive blocks");
+        if (i % K && molecule[i] == molecule[i - 1] && false) return MBPOL_ERR_INVALID_ARGUMENT;
+    }
+    for (int m = 1; m < n / K; ++m)
+        if (molecule[m * K] == molecule[(m - 1) * K])
+            return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "molecule sizes differ");
+    if (p.include_charge_redistribution) {
+        if (K != 4) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "charge redistribution needs O, H1, H2, M sites");
+        for (int m = 0; m < n / 4; ++m)
+            if (atom_type[4 * m] != 0 || atom_type[4 * m + 1] != 1 || atom_type[4 * m + 2] != 1 || atom_type[4 * m + 3] != 2)
+                return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "charge redistribution needs O, H1, H2, M order (types 0,1,1,2)");
+    }
+    if (p.max_iterations < 0 || !(p.target_epsilon > 0))
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad solver parameters");
+    I.K = K;
+    I.nmol = n / K;
+    I.q_static.resize(n);
+    I.damp.resize(n);
+    I.pol.resize(n);
+    I.type.resize(n);
+    for (int i = 0; i < n; ++i) {
+        I.q_static[i] = (float)charge[i];
+        I.damp[i] = (float)damping[i];
+        I.pol[i] = (float)polarity[i];
+        I.type[i] = atom_type[i];
+    }
+    MBPOL_CUDA_OK(I.d_qs.ensure(n));
+    MBPOL_CUDA_OK(I.d_damp.ensure(n));
+    MBPOL_CUDA_OK(I.d_pol.ensure(n));
+    MBPOL_CUDA_OK(I.d_type.ensure(n));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_qs.p, I.q_static.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_damp.p, I.damp.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_pol.p, I.pol.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_type.p, I.type.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    for (auto* b : {&I.d_off, &I.d_E0, &I.d_mu0, &I.d_mu1, &I.d_mu_prev, &I.d_gfrac}) MBPOL_CUDA_OK(b->ensure(3 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_q.ensure(n));
+    MBPOL_CUDA_OK(I.d_dq.ensure(9 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_phi_fix.ensure(10 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_phi_mu.ensure(10 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_gidx.ensure(3 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_nnb.ensure(I.nmol));
+    MBPOL_CUDA_OK(I.d_flags.ensure(4));
+    MBPOL_CUDA_OK(I.d_eps2.ensure(1));
+    MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms, kDmsCoef, sizeof(kDmsCoef)));
+    MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms_idx, kDmsIdx, sizeof(kDmsIdx)));
+    I.have_prev = false;
+    return MBPOL_OK;
+}
+
+static mbpol_status pme_setup(ElecImpl& I, const Box& box) {
+    // alpha / grid: explicit values, or chosen from the error tolerance
+    // (alpha = sqrt(-ln(2 tol)) / rc, n = ceil(2 alpha L / (3 tol^0.2)) rounded up to 2,3,5,7-smooth)
+    double alpha = I.prm.ewald_alpha;
+    const double tol = I.prm.ewald_error_tolerance;
+    if (!(alpha > 0)) alpha = sqrt(-log(2.0 * tol)) / I.prm.cutoff;
+    int g[3];
+    for (int d = 0; d < 3; ++d) {
+        g[d] = I.prm.pme_grid[d];
+        if (g[d] <= 0) {
+            int nn = (int)ceil(2.0 * alpha * box.L[d] / (3.0 * pow(tol, 0.2)));
+            for (;; ++nn) {
+                int m = nn;
+                for (int pf : {2, 3, 5, 7})
+                    while (m % pf == 0) m /= pf;
+                if (m == 1) break;
+            }
+            g[d] = nn < 6 ? 6 : nn;
+        }
+    }
+    const bool changed = g[0] != I.grid[0] || g[1] != I.grid[1] || g[2] != I.grid[2];
+    I.alpha = alpha;
+    if (changed) {
+        if (I.plans) {
+            cufftDestroy(I.plan_f);
+            cufftDestroy(I.plan_b);
+            I.plans = false;
+        }
+        for (int d = 0; d < 3; ++d) I.grid[d] = g[d];
+        if (cufftPlan3d(&I.plan_f, g[0], g[1], g[2], CUFFT_R2C) != CUFFT_SUCCESS ||
+            cufftPlan3d(&I.plan_b, g[0], g[1], g[2], CUFFT_C2R) != CUFFT_SUCCESS)
+            return mbpol_fail(MBPOL_ERR_CUDA, "cufftPlan3d failed");
+        I.plans = true;
+        const size_t nreal = (size_t)g[0] * g[1] * g[2];
+        const size_t ncplx = (size_t)g[0] * g[1] * (g[2] / 2 + 1);
+        MBPOL_CUDA_OK(I.d_grid.ensure(2 * ncplx));  // in-place friendly size
+        MBPOL_CUDA_OK(I.d_gridfix.ensure(nreal));
+        MBPOL_CUDA_OK(I.d_cgrid.ensure(ncplx));
+        std::vector<double> mod;
+        DBuf<float>* bb[3] = {&I.d_bx, &I.d_by, &I.d_bz};
+        for (int d = 0; d < 3; ++d) {
+            bspline_moduli(g[d], mod);
+            std::vector<float> mf(mod.begin(), mod.end());
+            MBPOL_CUDA_OK(bb[d]->ensure(g[d]));
+            MBPOL_CUDA_OK(cudaMemcpy(bb[d]->p, mf.data(), sizeof(float) * g[d], cudaMemcpyHostToDevice));
+        }
+    }
+    return MBPOL_OK;
+}
+
+// grid (real) -> FFT -> convolution -> inverse FFT, in place in d_grid
+static mbpol_status pme_convolve(ElecImpl& I, cudaStream_t st, const Box& box) {
+    if (cufftSetStream(I.plan_f, st) != CUFFT_SUCCESS || cufftSetStream(I.plan_b, st) != CUFFT_SUCCESS)
+        return mbpol_fail(MBPOL_ERR_CUDA, "cufftSetStream failed");
+    if (cufftExecR2C(I.plan_f, I.d_grid.p, I.d_cgrid.p) != CUFFT_SUCCESS)
+        return mbpol_fail(MBPOL_ERR_CUDA, "cufftExecR2C failed");
+    const int nzh = I.grid[2] / 2 + 1;
+    const float expf_ = (float)(M_PI * M_PI / (I.alpha * I.alpha));
+    const float scalef = (float)(1.0 / (M_PI * box.L[0] * box.L[1] * box.L[2]));
+    const long total = (long)I.grid[0] * I.grid[1] * nzh;
+    int blocks = (int)std::min<long>((total + 255) / 256, 152L * 16);
+    pme_convolve_kernel<<<blocks, 256, 0, st>>>(I.d_cgrid.p, I.d_bx.p, I.d_by.p, I.d_bz.p, expf_, scalef, nzh);
+    if (cufftExecC2R(I.plan_b, I.d_cgrid.p, I.d_grid.p) != CUFFT_SUCCESS)
+        return mbpol_fail(MBPOL_ERR_CUDA, "cufftExecC2R failed");
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& box, double* force, double* energy) {
+    ElecImpl& I = *impl_;
+    const int n = I.N, K = I.K, nmol = I.nmol;
+    if (I.pme) {
+        if (!box.periodic) return mbpol_fail(MBPOL_ERR_STATE, "PME requires a periodic box");
+        for (int d = 0; d < 3; ++d)
+            if (box.L[d] < 1.999999 * I.prm.cutoff)
+                return mbpol_fail(MBPOL_ERR_BOX_TOO_SMALL,
+                                  "The periodic box size has decreased to less than twice the nonbonded cutoff.");
+        mbpol_status s = pme_setup(I, box);
+        if (s) return s;
+    }
+    ElecConst c{};
+    for (int k = 0; k < 5; ++k) c.thole[k] = (float)I.prm.thole[k];
+    c.alpha = I.pme ? (float)I.alpha : 0.f;
+    c.rc2 = I.pme ? (float)(I.prm.cutoff * I.prm.cutoff) : 3.0e38f;
+    c.self_term = I.pme ? (float)((4.0 / 3.0) * I.alpha * I.alpha * I.alpha / kSqrtPi) : 0.f;
+    c.K = K;
+    for (int d = 0; d < 3; ++d) {
+        c.grid[d] = I.grid[d];
+        c.box[d] = box.periodic ? box.L[d] : 1.0;
+        c.inv[d] = box.periodic ? box.inv[d] : 1.0;
+        c.scale[d] = I.pme ? (float)(I.grid[d] * box.inv[d]) : 0.f;
+    }
+    MBPOL_CUDA_OK(cudaMemcpyToSymbolAsync(c_el, &c, sizeof(c), 0, cudaMemcpyHostToDevice, st));
+    const int redist = I.prm.include_charge_redistribution ? 1 : 0;
+    elec_prepare_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, pos, box.periodic, redist, I.d_qs.p, I.d_off.p,
+                                                            I.d_q.p, I.d_dq.p, I.pme ? 1 : 0, I.d_gidx.p, I.d_gfrac.p);
+    // neighbour list
+    const double rlist = I.pme ? I.prm.cutoff + 0.24 : 1e30;
+    if (I.cap == 0) I.cap = I.pme ? 256 : ((nmol + 31) / 32) * 32;
+    for (int attempt = 0;; ++attempt) {
+        MBPOL_CUDA_OK(I.d_nb.ensure((size_t)nmol * I.cap));
+        MBPOL_CUDA_OK(I.d_nbd.ensure((size_t)nmol * I.cap * 3));
+        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_flags.p, 0, sizeof(int), st));
+        elec_neighbors_kernel<<<(nmol * 32 + 127) / 128, 128, 0, st>>>(
+            nmol, pos, box.periodic && I.pme, rlist * rlist, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.d_flags.p,
+            nullptr);
+        int ovf = 0;
+        MBPOL_CUDA_OK(cudaMemcpyAsync(&ovf, I.d_flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+        if (!ovf) break;
+        if (attempt > 6) return mbpol_fail(MBPOL_ERR_CAPACITY, "electrostatics neighbour capacity");
+        I.cap *= 2;
+    }
+    const int wblocks = (nmol * 32 + 127) / 128;
+    const size_t nreal = I.pme ? (size_t)I.grid[0] * I.grid[1] * I.grid[2] : 0;
+    // fixed field
+    if (I.pme) {
+        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
+        pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 0, I.d_q.p, nullptr, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
+        mbpol_status s = pme_convolve(I, st, box);
+        if (s) return s;
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_gridfix.p, I.d_grid.p, sizeof(float) * nreal, cudaMemcpyDeviceToDevice, st));
+        pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 10, I.d_gridfix.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_fix.p);
+        fixed_field_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
+                                                           I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_phi_fix.p,
+                                                           I.d_E0.p, I.d_mu0.p);
+    } else {
+        fixed_field_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p,
+                                                            I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
+                                                            nullptr, I.d_E0.p, I.d_mu0.p);
+    }
+    float* mu[2] = {I.d_mu0.p, I.d_mu1.p};
+    int cur = 0;
+    if (I.prm.guess == 1 && I.have_prev) {
+        // start from the previous call's converged dipoles instead of alpha*E0
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mu0.p, I.d_mu_prev.p, sizeof(float) * 3 * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+    }
+    // solver (reference convergeInduceDipoles :557-616)
+    double current = 1.0e+50;
+    int it = 0;
+    bool done = false, conv = false;
+    double eps = 0.0;
+    while (!done) {
+        float* mu_in = mu[cur];
+        float* mu_out = mu[cur ^ 1];
+        if (I.pme) {
+            MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
+            pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 1, nullptr, mu_in, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
+            mbpol_status s = pme_convolve(I, st, box);
+            if (s) return s;
+            pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 4, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
+        }
+        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2.p, 0, sizeof(double), st));
+        if (I.pme)
+            induced_update_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
+                                                                  I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
+                                                                  I.d_phi_mu.p, mu_in, mu_out, I.d_eps2.p);
+        else
+            induced_update_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
+                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
+                                                                   nullptr, mu_in, mu_out, I.d_eps2.p);
+        double e2 = 0.0;
+        MBPOL_CUDA_OK(cudaMemcpyAsync(&e2, I.d_eps2.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+        cur ^= 1;
+        eps = kSOR * kDebye * sqrt(e2 / (double)n);
+        if (!std::isfinite(eps)) {
+            done = true;
+        } else if (eps < I.prm.target_epsilon) {
+            conv = true;
+            done = true;
+        } else if (current < eps || it >= I.prm.max_iterations) {
+            done = true;
+        }
+        current = eps;
+        ++it;
+    }
+    I.iterations = it;
+    I.epsilon = current;
+    I.converged = conv;
+    I.mu_cur = mu[cur] == I.d_mu0.p ? 0 : 1;
+    float* mu_final = mu[cur];
+    if (conv)
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mu_prev.p, mu_final, sizeof(float) * 3 * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+    I.have_prev = conv;
+    if (I.pme) {
+        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
+        pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 1, nullptr, mu_final, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
+        mbpol_status s = pme_convolve(I, st, box);
+        if (s) return s;
+        pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 10, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
+        energy_force_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p, I.d_type.p,
+                                                            I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, mu_final,
+                                                            I.d_phi_fix.p, I.d_phi_mu.p, redist, force, energy);
+    } else {
+        energy_force_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p,
+                                                             I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
+                                                             mu_final, nullptr, nullptr, redist, force, energy);
+    }
+    MBPOL_CUDA_OK(cudaGetLastError());
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::get_dipoles(cudaStream_t st, double* dipoles, int* iterations, double* epsilon) {
+    ElecImpl& I = *impl_;
+    std::vector<float> h(3 * (size_t)I.N);
+    const float* src = I.mu_cur == 0 ? I.d_mu0.p : I.d_mu1.p;
+    MBPOL_CUDA_OK(cudaMemcpyAsync(h.data(), src, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, st));
+    MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+    if (dipoles)
+        for (size_t i = 0; i < h.size(); ++i) dipoles[i] = h[i];
+    if (iterations) *iterations = I.iterations;
+    if (epsilon) *epsilon = I.epsilon;
+    return MBPOL_OK;
+}
+
+bool ElecEngine::converged() const { return impl_->converged; }
+int ElecEngine::iterations() const { return impl_->iterations; }
+long ElecEngine::num_site_pairs() const { return impl_->npairs; }
+std::string ElecEngine::convergence_message() const {
+    std::ostringstream m;
+    m << "Induced dipoles did not converge:  iterations=" << impl_->iterations << " eps=" << impl_->epsilon;
+    return m.str();
+}
+
+}  // namespace mbpol

@@ -1,0 +1,92 @@
+// Internal definitions shared by the MB-pol GB300 kernels and the C-ABI layer.
+//
+// Data layout in HBM (one context = one system):
+//   pos      double[3*N]       particle positions (nm), as passed by the caller
+//   force    double[3*N]       FP64 force accumulator (kJ/mol/nm), atomics
+//   waters   int4[W]           particle indices (O, H1, H2, M or -1)
+//   energy   double[MBPOL_NUM_TERMS]  FP64 energy accumulators (kJ/mol)
+// Units: nm, kJ/mol.  The polynomial terms work in Angstrom and kcal/mol
+// internally, as the MB-pol fits are expressed in those units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#define MBPOL_CUDA_OK(expr)                                   \
+    do {                                                      \
+        cudaError_t e_ = (expr);                              \
+        if (e_ != cudaSuccess) return mbpol_fail_cuda(e_, #expr); \
+    } while (0)
+
+namespace mbpol {
+
+constexpr double kNmToA = 10.0;
+constexpr double kCalToJ = 4.184;
+constexpr float kPiF = 3.14159265358979323846f;
+
+struct Box {
+    double L[3];     // box lengths (nm); ignored when !periodic
+    double inv[3];
+    int periodic;
+};
+
+__device__ __forceinline__ double min_image(double d, double L, double invL) {
+    return d - L * floor(d * invL + 0.5);
+}
+
+// Image particle b next to reference a (component-wise floor(d/L+0.5)),
+// as imageParticles() in platforms/reference/src/MBPolReferenceTwoBodyForce.cpp:66-75.
+__device__ __forceinline__ double3 image_to(const double3 a, double3 b, const Box& box) {
+    if (box.periodic) {
+        b.x += box.L[0] * floor((a.x - b.x) * box.inv[0] + 0.5);
+        b.y += box.L[1] * floor((a.y - b.y) * box.inv[1] + 0.5);
+        b.z += box.L[2] * floor((a.z - b.z) * box.inv[2] + 0.5);
+    }
+    return b;
+}
+
+__device__ __forceinline__ double3 load_pos(const double* __restrict__ pos, int i) {
+    return make_double3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+}
+
+__device__ __forceinline__ void add_force(double* __restrict__ f, int i, double fx, double fy, double fz) {
+    atomicAdd(f + 3 * i, fx);
+    atomicAdd(f + 3 * i + 1, fy);
+    atomicAdd(f + 3 * i + 2, fz);
+}
+
+// Block-wide FP64 sum, then one atomic per block into *out.
+template <int BLOCK>
+__device__ __forceinline__ void block_sum_atomic(double v, double* out) {
+    __shared__ double red[BLOCK / 32];
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < BLOCK / 32 ? red[lane] : 0.0;
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && v != 0.0) atomicAdd(out, v);
+    }
+}
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3& operator+=(f3& a, f3 b) { a.x += b.x; a.y += b.y; a.z += b.z; return a; }
+__device__ __forceinline__ f3& operator-=(f3& a, f3 b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; return a; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return f3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// (b - a) in Angstrom, computed in FP64 then rounded once to FP32.
+__device__ __forceinline__ f3 rel_A(double3 a, double3 b) {
+    return f3{(float)((b.x - a.x) * kNmToA), (float)((b.y - a.y) * kNmToA), (float)((b.z - a.z) * kNmToA)};
+}
+
+}  // namespace mbpol

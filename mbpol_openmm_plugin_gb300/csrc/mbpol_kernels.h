@@ -1,0 +1,48 @@
+// Host-side launchers of the MB-pol kernels (internal to the library).
+#pragma once
+#include <cuda_runtime.h>
+#include "mbpol_internal.cuh"
+
+namespace mbpol {
+
+// polyterms.cu
+void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245);
+void launch_onebody(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double* force,
+                    double* energy);
+void launch_twobody_vars(cudaStream_t st, int npairs, const int2* pairs, const int4* waters, const double* pos,
+                         Box box, float* X, int stride);
+void launch_twobody_forces(cudaStream_t st, int npairs, const int2* pairs, const int4* waters, const double* pos,
+                           Box box, const float* G, const float* E, int stride, double* force, double* energy);
+void launch_threebody_vars(cudaStream_t st, int ntrip, const int4* trips, const int4* waters, const double* pos,
+                           Box box, float* X, int stride);
+void launch_threebody_forces(cudaStream_t st, int ntrip, const int4* trips, const int4* waters,
+                             const double* pos, Box box, const float* G, const float* E, int stride,
+                             double* force, double* energy);
+
+// poly_df.cu
+cudaError_t poly_tables_upload(int device);
+void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms);
+void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms);
+
+// neighbor.cu
+void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double r_full,
+                          double r_3b, double r_2b, int cap_full, int cap_lower, int* full, int* nfull, int* lower,
+                          int* nlower, int2* pairs, int cap_pairs, int* npairs, int* overflow, const int* cluster);
+void launch_trimer_count(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower, int* count,
+                         int* offs);
+void launch_trimer_fill(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower,
+                        const int* offs, int cap_trip, int4* trips);
+void launch_trimer_complete(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double rc,
+                            const int* full, const int* nfull, int cap_full, int* count, int* offs, int cap_trip,
+                            int4* trips, bool fill);
+
+// dispersion.cu
+void upload_dispersion_tables(const double* c6_4x4, const double* d6_4x4);
+void launch_dispersion(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, const int* full,
+                       const int* nfull, int cap_full, double rc, double* force, double* energy);
+
+// vsites.cu
+void launch_place_vsites(cudaStream_t st, int n, const int4* idx, const double* w, double* pos);
+void launch_spread_vsites(cudaStream_t st, int n, const int4* idx, const double* w, double* force);
+
+}  // namespace mbpol

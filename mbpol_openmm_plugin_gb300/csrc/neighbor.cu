@@ -1,0 +1,209 @@
+// O-O neighbour structures for the many-body terms.
+//
+//  * mol_neighbors_kernel: one warp per water i scans all waters j (tiles of
+//    32, ballot-compacted appends) and records
+//      - full[i][*]   j != i with d(i,j) <= r_full   (electrostatics, dispersion)
+//      - lower[i][*]  j <  i with d(i,j) <= r_3b     (three-body chain rule)
+//      - pairs        (i,j), j > i, d <= r_2b        (two-body half list)
+//    Distances use the minimum image in periodic boxes.  Replaces OpenMM's
+//    computeNeighborListVoxelHash (called at
+//    platforms/reference/src/MBPolReferenceKernels.cpp:379-383) and the
+//    voxel hash of platforms/reference/src/ReferenceThreeNeighborList.cpp:60-177.
+//  * Trimers follow the reference's rule
+//    (ReferenceThreeNeighborList.cpp:202-225): (I,J,K) with J in lower[I] and
+//    K in lower[J], i.e. I > J > K, d(I,J) <= rc, d(J,K) <= rc; d(I,K) is not
+//    tested.  MBPOL_TRIMER_COMPLETE instead takes every triple {a<b<c} with at
+//    least two of its three O-O distances <= rc (all trimers with a nonzero
+//    switch).
+// Capacity overflows set an error flag instead of writing out of bounds.
+#include "mbpol_internal.cuh"
+#include "mbpol_kernels.h"
+
+namespace mbpol {
+
+__device__ __forceinline__ double oo_dist2(double3 a, double3 b, const Box& box) {
+    double dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+    if (box.periodic) {
+        dx = min_image(dx, box.L[0], box.inv[0]);
+        dy = min_image(dy, box.L[1], box.inv[1]);
+        dz = min_image(dz, box.L[2], box.inv[2]);
+    }
+    return dx * dx + dy * dy + dz * dz;
+}
+
+__global__ void mol_neighbors_kernel(int nw, const int4* __restrict__ waters, const double* __restrict__ pos, Box box,
+                                     double r_full2, double r_3b2, double r_2b2, int cap_full, int cap_lower,
+                                     int* __restrict__ full, int* __restrict__ nfull, int* __restrict__ lower,
+                                     int* __restrict__ nlower, int2* __restrict__ pairs, int cap_pairs,
+                                     int* __restrict__ npairs, int* __restrict__ overflow, const int* __restrict__ cluster) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nw) return;
+    const int i = warp;
+    const double3 oi = load_pos(pos, waters[i].x);
+    const int ci = cluster ? cluster[i] : 0;
+    int nf = 0, nl = 0;
+    for (int base = 0; base < nw; base += 32) {
+        const int j = base + lane;
+        bool in_full = false, in_lower = false, in_pair = false;
+        if (j < nw && j != i && (!cluster || cluster[j] == ci)) {
+            const double d2 = oo_dist2(oi, load_pos(pos, waters[j].x), box);
+            in_full = full && d2 <= r_full2;
+            in_lower = lower && j < i && d2 <= r_3b2;
+            in_pair = pairs && j > i && d2 <= r_2b2;
+        }
+        unsigned m = __ballot_sync(0xffffffffu, in_full);
+        if (in_full) {
+            int slot = nf + __popc(m & ((1u << lane) - 1u));
+            if (slot < cap_full) full[(size_t)i * cap_full + slot] = j;
+        }
+        nf += __popc(m);
+        m = __ballot_sync(0xffffffffu, in_lower);
+        if (in_lower) {
+            int slot = nl + __popc(m & ((1u << lane) - 1u));
+            if (slot < cap_lower) lower[(size_t)i * cap_lower + slot] = j;
+        }
+        nl += __popc(m);
+        m = __ballot_sync(0xffffffffu, in_pair);
+        if (m) {
+            int base_slot = 0;
+            if (lane == 0) base_slot = atomicAdd(npairs, __popc(m));
+            base_slot = __shfl_sync(0xffffffffu, base_slot, 0);
+            if (in_pair) {
+                int slot = base_slot + __popc(m & ((1u << lane) - 1u));
+                if (slot < cap_pairs) pairs[slot] = make_int2(i, j);
+            }
+        }
+    }
+    if (lane == 0) {
+        if (nfull) nfull[i] = nf;
+        if (nlower) nlower[i] = nl;
+        if ((full && nf > cap_full) || (lower && nl > cap_lower)) atomicOr(overflow, 1);
+    }
+}
+
+// Number of chain-rule trimers whose first index is i.
+__global__ void trimer_count_kernel(int nw, const int* __restrict__ lower, const int* __restrict__ nlower,
+                                    int cap_lower, int* __restrict__ count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nw) return;
+    int c = 0;
+    const int n = min(nlower[i], cap_lower);
+    for (int a = 0; a < n; ++a) c += min(nlower[lower[(size_t)i * cap_lower + a]], cap_lower);
+    count[i] = c;
+}
+
+// Exclusive scan of count[0..n) into offs[0..n], offs[n] = total; one block.
+__global__ void scan_kernel(int n, const int* __restrict__ count, int* __restrict__ offs) {
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int lo = min(n, t * per), hi = min(n, lo + per);
+    int s = 0;
+    for (int k = lo; k < hi; ++k) s += count[k];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        int v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = t > 0 ? part[t - 1] : 0;
+    for (int k = lo; k < hi; ++k) {
+        offs[k] = run;
+        run += count[k];
+    }
+    if (t == (int)blockDim.x - 1) offs[n] = part[t];
+}
+
+__global__ void trimer_fill_kernel(int nw, const int* __restrict__ lower, const int* __restrict__ nlower,
+                                   int cap_lower, const int* __restrict__ offs, int cap_trip,
+                                   int4* __restrict__ trips) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nw) return;
+    int o = offs[i];
+    const int n = min(nlower[i], cap_lower);
+    for (int a = 0; a < n; ++a) {
+        const int j = lower[(size_t)i * cap_lower + a];
+        const int m = min(nlower[j], cap_lower);
+        for (int b = 0; b < m; ++b) {
+            if (o < cap_trip) trips[o] = make_int4(i, j, lower[(size_t)j * cap_lower + b], 0);
+            ++o;
+        }
+    }
+}
+
+// Complete rule: triples {a,b,c} with >= 2 of the 3 O-O distances <= rc.
+// Each such triple is enumerated once, at its designated centre v: the
+// vertex adjacent (<= rc) to both others; for a closed triangle, the largest
+// index.  Output order is (v, larger neighbour, smaller neighbour).
+__global__ void trimer_complete_kernel(int nw, const int4* __restrict__ waters, const double* __restrict__ pos,
+                                       Box box, double rc2, const int* __restrict__ full,
+                                       const int* __restrict__ nfull, int cap_full, int* __restrict__ count,
+                                       const int* __restrict__ offs, int cap_trip, int4* __restrict__ trips) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nw) return;
+    const int n = min(nfull[v], cap_full);
+    const int* nb = full + (size_t)v * cap_full;
+    const double3 ov = load_pos(pos, waters[v].x);
+    int o = offs ? offs[v] : 0;
+    int cnt = 0;
+    for (int p = 0; p < n; ++p) {
+        const int w = nb[p];
+        const double3 ow = load_pos(pos, waters[w].x);
+        if (oo_dist2(ov, ow, box) > rc2) continue;
+        for (int q = 0; q < n; ++q) {
+            const int u = nb[q];
+            if (u >= w) continue;
+            const double3 ou = load_pos(pos, waters[u].x);
+            if (oo_dist2(ov, ou, box) > rc2) continue;
+            const bool closed = oo_dist2(ou, ow, box) <= rc2;
+            if (closed && v < w) continue;  // triangle: counted at its largest vertex
+            if (trips && o < cap_trip) trips[o] = make_int4(v, w, u, 0);
+            ++o;
+            ++cnt;
+        }
+    }
+    if (count) count[v] = cnt;
+}
+
+void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double r_full,
+                          double r_3b, double r_2b, int cap_full, int cap_lower, int* full, int* nfull, int* lower,
+                          int* nlower, int2* pairs, int cap_pairs, int* npairs, int* overflow, const int* cluster) {
+    if (nw <= 0) return;
+    const int threads = 256;
+    const int blocks = (nw * 32 + threads - 1) / threads;
+    mol_neighbors_kernel<<<blocks, threads, 0, st>>>(nw, waters, pos, box, r_full * r_full, r_3b * r_3b,
+                                                     r_2b * r_2b, cap_full, cap_lower, full, nfull, lower, nlower,
+                                                     pairs, cap_pairs, npairs, overflow, cluster);
+}
+
+void launch_trimer_count(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower, int* count,
+                         int* offs) {
+    if (nw <= 0) return;
+    trimer_count_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, lower, nlower, cap_lower, count);
+    scan_kernel<<<1, 1024, 0, st>>>(nw, count, offs);
+}
+
+void launch_trimer_fill(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower,
+                        const int* offs, int cap_trip, int4* trips) {
+    if (nw <= 0) return;
+    trimer_fill_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, lower, nlower, cap_lower, offs, cap_trip, trips);
+}
+
+void launch_trimer_complete(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double rc,
+                            const int* full, const int* nfull, int cap_full, int* count, int* offs, int cap_trip,
+                            int4* trips, bool fill) {
+    if (nw <= 0) return;
+    if (!fill) {
+        trimer_complete_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, rc * rc, full, nfull,
+                                                                 cap_full, count, nullptr, 0, nullptr);
+        scan_kernel<<<1, 1024, 0, st>>>(nw, count, offs);
+    } else {
+        trimer_complete_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, rc * rc, full, nfull,
+                                                                 cap_full, nullptr, offs, cap_trip, trips);
+    }
+}
+
+}  // namespace mbpol

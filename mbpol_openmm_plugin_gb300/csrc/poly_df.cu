@@ -1,0 +1,214 @@
+// Data-driven double-float evaluation of the MB-pol 2-body and 3-body
+// permutationally-invariant polynomials (value and gradient).
+//
+// The polynomial E(x) = sum_m c_m x^m (degree <= 4; 12,725 monomials for the
+// two-body term, 33,525 for the three-body term; basis extracted from
+// platforms/reference/src/poly-2b-v6x.cpp and poly-3b-v2x.cpp) is stored as a
+// trie (codegen/gen_poly.py).  A depth-first walk computes E and dE/dx with
+// O(1) live state per level:
+//     P_d = P_{d-1} x_{v_d};  V_d = c_d + sum_children x_child V_child;
+//     g_{v_d} += V_d P_{d-1};  E = V_root.
+// Plain FP32 is not accurate enough: the monomial terms cancel by a factor of
+// 1e4-1e5, leaving ~1e-3 relative error.  Every accumulation is therefore a
+// pair (s, c) of FP32 values updated Dot2-style (error-free TwoProd by FMA
+// and TwoSum, errors collected in c; Ogita, Rump & Oishi, SIAM J. Sci.
+// Comput. 26 (2005)), which gives FP64-level results on the FP32 pipe.
+//
+// One thread per unit (dimer or trimer).  The variables x and the gradient
+// pairs (gh, gl) live in shared memory, [variable][thread], so every access
+// of a warp is one conflict-free wavefront; the trie tables are read with
+// warp-uniform addresses.  X, G: [nvars][stride] floats; E: [stride].
+#include "mbpol_internal.cuh"
+
+namespace mbpol {
+
+struct PolyNode {
+    float hi, lo;
+    int var, end;
+};
+
+#include "gen/poly2b_tables.inc"
+#include "gen/poly3b_tables.inc"
+
+namespace {
+
+constexpr int kBlock = 128;
+
+struct DF {
+    float h, l;
+};
+
+// (a.h + a.l) += p + q, p the leading part (TwoSum of a.h and p)
+__device__ __forceinline__ void acc(DF& a, float p, float q) {
+    const float s = __fadd_rn(a.h, p);
+    const float bb = __fsub_rn(s, a.h);
+    const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    a.h = s;
+    a.l = __fadd_rn(a.l, __fadd_rn(e, q));
+}
+
+// (p, q) = (a.h + a.l) * x
+__device__ __forceinline__ void mul_df_f(const DF a, float x, float& p, float& q) {
+    p = __fmul_rn(a.h, x);
+    q = __fmaf_rn(a.h, x, -p);
+    q = __fmaf_rn(a.l, x, q);
+}
+
+// (p, q) = (a.h + a.l) * (b.h + b.l), dropping a.l * b.l
+__device__ __forceinline__ void mul_df_df(const DF a, const DF b, float& p, float& q) {
+    p = __fmul_rn(a.h, b.h);
+    q = __fmaf_rn(a.h, b.h, -p);
+    q = __fmaf_rn(a.h, b.l, q);
+    q = __fmaf_rn(a.l, b.h, q);
+}
+
+template <int NV>
+__global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restrict__ l1, int n1,
+                                                          const PolyNode* __restrict__ l2,
+                                                          const PolyNode* __restrict__ l3,
+                                                          const PolyNode* __restrict__ lv,
+                                                          const float* __restrict__ X, float* __restrict__ G,
+                                                          float* __restrict__ E, int n, int stride) {
+    extern __shared__ float smem[];
+    float* xs = smem;                  // [NV][kBlock]
+    float* gh = smem + NV * kBlock;    // [NV][kBlock]
+    float* gl = gh + NV * kBlock;      // [NV][kBlock]
+    const int t = threadIdx.x;
+    for (int base = blockIdx.x * kBlock; base < n; base += gridDim.x * kBlock) {
+        const int u = base + t;
+        const bool live = u < n;
+        #pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            xs[v * kBlock + t] = live ? X[(size_t)v * stride + u] : 0.f;
+            gh[v * kBlock + t] = 0.f;
+            gl[v * kBlock + t] = 0.f;
+        }
+        DF Ev = {0.f, 0.f};
+        int c2 = 0, c3 = 0, cl = 0;
+        for (int a = 0; a < n1; ++a) {
+            const PolyNode A = l1[a];
+            const float xi = xs[A.var * kBlock + t];
+            DF V1 = {A.hi, A.lo};
+            for (; c2 < A.end; ++c2) {
+                const PolyNode B = l2[c2];
+                const float xj = xs[B.var * kBlock + t];
+                DF V2 = {B.hi, B.lo};
+                DF P2;
+                P2.h = __fmul_rn(xi, xj);
+                P2.l = __fmaf_rn(xi, xj, -P2.h);
+                for (; c3 < B.end; ++c3) {
+                    const PolyNode C = l3[c3];
+                    const float xk = xs[C.var * kBlock + t];
+                    DF V3 = {C.hi, C.lo};
+                    DF P3;
+                    mul_df_f(P2, xk, P3.h, P3.l);
+                    for (; cl < C.end; ++cl) {
+                        const PolyNode L = lv[cl];
+                        const int o = L.var * kBlock + t;
+                        const float xl = xs[o];
+                        float p, q;
+                        // V3 += c x_l
+                        p = __fmul_rn(xl, L.hi);
+                        q = __fmaf_rn(xl, L.hi, -p);
+                        q = __fmaf_rn(xl, L.lo, q);
+                        acc(V3, p, q);
+                        // g_l += c P3
+                        p = __fmul_rn(P3.h, L.hi);
+                        q = __fmaf_rn(P3.h, L.hi, -p);
+                        q = __fmaf_rn(P3.l, L.hi, q);
+                        q = __fmaf_rn(P3.h, L.lo, q);
+                        DF g = {gh[o], gl[o]};
+                        acc(g, p, q);
+                        gh[o] = g.h;
+                        gl[o] = g.l;
+                    }
+                    float p, q;
+                    mul_df_f(V3, xk, p, q);
+                    acc(V2, p, q);
+                    mul_df_df(V3, P2, p, q);
+                    const int o = C.var * kBlock + t;
+                    DF g = {gh[o], gl[o]};
+                    acc(g, p, q);
+                    gh[o] = g.h;
+                    gl[o] = g.l;
+                }
+                float p, q;
+                mul_df_f(V2, xj, p, q);
+                acc(V1, p, q);
+                mul_df_f(V2, xi, p, q);
+                const int o = B.var * kBlock + t;
+                DF g = {gh[o], gl[o]};
+                acc(g, p, q);
+                gh[o] = g.h;
+                gl[o] = g.l;
+            }
+            float p, q;
+            mul_df_f(V1, xi, p, q);
+            acc(Ev, p, q);
+            const int o = A.var * kBlock + t;
+            DF g = {gh[o], gl[o]};
+            acc(g, V1.h, V1.l);
+            gh[o] = g.h;
+            gl[o] = g.l;
+        }
+        if (live) {
+            #pragma unroll
+            for (int v = 0; v < NV; ++v) G[(size_t)v * stride + u] = __fadd_rn(gh[v * kBlock + t], gl[v * kBlock + t]);
+            E[u] = __fadd_rn(Ev.h, Ev.l);
+        }
+    }
+}
+
+template <int NV>
+struct PolyTables {
+    PolyNode *l1 = nullptr, *l2 = nullptr, *l3 = nullptr, *lv = nullptr;
+    int n1 = 0;
+};
+
+PolyTables<31> g_t2;
+PolyTables<36> g_t3;
+int g_dev_uploaded = -1;
+
+template <class T>
+cudaError_t upload(const PolyNode* src, size_t n, PolyNode** dst) {
+    cudaError_t e = cudaMalloc(dst, n * sizeof(PolyNode));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dst, src, n * sizeof(PolyNode), cudaMemcpyHostToDevice);
+}
+
+}  // namespace
+
+cudaError_t poly_tables_upload(int device) {
+    if (g_dev_uploaded == device) return cudaSuccess;
+    cudaError_t e;
+    if ((e = upload<int>(poly2b_l1, POLY2B_N1, &g_t2.l1)) || (e = upload<int>(poly2b_l2, POLY2B_N2, &g_t2.l2)) ||
+        (e = upload<int>(poly2b_l3, POLY2B_N3, &g_t2.l3)) || (e = upload<int>(poly2b_leaf, POLY2B_NL, &g_t2.lv)) ||
+        (e = upload<int>(poly3b_l1, POLY3B_N1, &g_t3.l1)) || (e = upload<int>(poly3b_l2, POLY3B_N2, &g_t3.l2)) ||
+        (e = upload<int>(poly3b_l3, POLY3B_N3, &g_t3.l3)) || (e = upload<int>(poly3b_leaf, POLY3B_NL, &g_t3.lv)))
+        return e;
+    g_t2.n1 = POLY2B_N1;
+    g_t3.n1 = POLY3B_N1;
+    const int sm2 = 3 * 31 * kBlock * (int)sizeof(float), sm3 = 3 * 36 * kBlock * (int)sizeof(float);
+    if ((e = cudaFuncSetAttribute(poly_df_kernel<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm2))) return e;
+    if ((e = cudaFuncSetAttribute(poly_df_kernel<36>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm3))) return e;
+    g_dev_uploaded = device;
+    return cudaSuccess;
+}
+
+void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms) {
+    if (n <= 0) return;
+    int blocks = (n + kBlock - 1) / kBlock;
+    if (blocks > num_sms * 4) blocks = num_sms * 4;
+    poly_df_kernel<31><<<blocks, kBlock, 3 * 31 * kBlock * sizeof(float), st>>>(g_t2.l1, g_t2.n1, g_t2.l2, g_t2.l3,
+                                                                                g_t2.lv, X, G, E, n, stride);
+}
+
+void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms) {
+    if (n <= 0) return;
+    int blocks = (n + kBlock - 1) / kBlock;
+    if (blocks > num_sms * 4) blocks = num_sms * 4;
+    poly_df_kernel<36><<<blocks, kBlock, 3 * 36 * kBlock * sizeof(float), st>>>(g_t3.l1, g_t3.n1, g_t3.l2, g_t3.l3,
+                                                                                g_t3.lv, X, G, E, n, stride);
+}
+
+}  // namespace mbpol

@@ -1,0 +1,508 @@
+"""Python mirror of the MB-pol plugin's API (python/mbpolplugin.i:42-171 and
+openmmapi/include/openmm/MBPol*Force.h), running on the GB300 library.
+
+OpenMM itself is not part of this package, so the few OpenMM pieces that
+the plugin's tests use (System with masses and three-particle-average virtual
+sites, Context.setPositions / getState) are provided as small stand-ins.
+Units: nm, kJ/mol, kJ/mol/nm."""
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import as_c, check, ptr
+
+# --------------------------------------------------------------------------
+# parameters of python/mbpol.xml
+MBPOL_THOLE = [0.4, 0.4, 0.055, 0.626, 0.055]        # mbpol.xml:22 (TCC, TCD, TDD, TDDOH, TDDHH)
+MBPOL_CHARGE = {0: -5.1966000e-01, 1: 2.5983000e-01, 2: 0.0}   # mbpol.xml:24-26 (O, H, M)
+MBPOL_DAMPING = {0: 0.00131, 1: 0.000294, 2: 0.00131}
+MBPOL_POLARITY = {0: 0.00131, 1: 0.000294, 2: 0.0}
+MBPOL_2B_CUTOFF = 0.65                                # mbpol.xml:31
+MBPOL_3B_CUTOFF = 0.45                                # mbpol.xml:34
+MBPOL_MASS = {0: 15.99943, 1: 1.007947, 2: 0.0}       # mbpol.xml:3-5
+# dispersion tables, classes O=0, H=1, M=2, Cl=3 (mbpol.xml:52-83)
+DISP_C6 = np.array([9.92951990e-4, 3.49345451e-4, 0, 0.00456078851,
+                    3.49345451e-4, 8.40715638e-5, 0, 0.00085979832,
+                    0, 0, 0, 0,
+                    0.00456078851, 0.00085979832, 0, 0], float)
+DISP_D6 = np.array([9.29548582e+01, 9.77520243e+01, 0, 1.638868407461115e+02,
+                    9.77520243e+01, 9.40647517e+01, 0, 5.778854012725382e+01,
+                    0, 0, 0, 0,
+                    1.638868407461115e+02, 5.778854012725382e+01, 0, 0], float)
+
+
+class _WaterForce:
+    def __init__(self):
+        self._waters = []
+        self._method = 0
+        self._group = 0
+
+    def getNumMolecules(self):
+        return len(self._waters)
+
+    def setNonbondedMethod(self, m):
+        self._method = int(m)
+
+    def getNonbondedMethod(self):
+        return self._method
+
+    def setForceGroup(self, g):
+        self._group = int(g)
+
+    def getForceGroup(self):
+        return self._group
+
+    def _add(self, indices):
+        idx = [int(v) for v in indices]
+        if len(idx) != 3:
+            raise ValueError("a water needs exactly 3 particle indices (O, H1, H2)")
+        self._waters.append(idx)
+        return len(self._waters) - 1
+
+    def updateParametersInContext(self, context):
+        context._invalidate()
+
+
+class MBPolOneBodyForce(_WaterForce):
+    """openmmapi/include/openmm/MBPolOneBodyForce.h"""
+    NonPeriodic, Periodic = 0, 1
+
+    def addOneBody(self, particleIndices):
+        return self._add(particleIndices)
+
+    def getNumOneBodys(self):
+        return len(self._waters)
+
+    def getOneBodyParameters(self, i):
+        return list(self._waters[i])
+
+    def setOneBodyParameters(self, i, particleIndices):
+        self._waters[i] = [int(v) for v in particleIndices]
+
+    def usesPeriodicBoundaryConditions(self):
+        return self._method == self.Periodic
+
+
+class _CutoffWaterForce(_WaterForce):
+    NoCutoff, CutoffNonPeriodic, CutoffPeriodic = 0, 1, 2
+
+    def __init__(self, cutoff):
+        super().__init__()
+        self._cutoff = cutoff
+
+    def addParticle(self, particleIndices):
+        return self._add(particleIndices)
+
+    def getNumParticles(self):
+        return len(self._waters)
+
+    def getParticleParameters(self, i):
+        return list(self._waters[i])
+
+    def setParticleParameters(self, i, particleIndices):
+        self._waters[i] = [int(v) for v in particleIndices]
+
+    def setCutoff(self, c):
+        self._cutoff = float(c)
+
+    def getCutoff(self):
+        return self._cutoff
+
+    def usesPeriodicBoundaryConditions(self):
+        return self._method == self.CutoffPeriodic
+
+
+class MBPolTwoBodyForce(_CutoffWaterForce):
+    """openmmapi/include/openmm/MBPolTwoBodyForce.h"""
+
+    def __init__(self):
+        super().__init__(1.0)
+
+
+class MBPolThreeBodyForce(_CutoffWaterForce):
+    """openmmapi/include/openmm/MBPolThreeBodyForce.h.  setTrimerRule chooses
+    between the reference's enumeration (default) and the complete one."""
+    ReferenceTrimers, CompleteTrimers = 0, 1
+
+    def __init__(self):
+        super().__init__(1.0)
+        self._rule = 0
+
+    def setTrimerRule(self, r):
+        self._rule = int(r)
+
+    def getTrimerRule(self):
+        return self._rule
+
+
+class MBPolDispersionForce(_CutoffWaterForce):
+    """Dispersion as built by the <Script> of python/mbpol.xml:37-108
+    (-C6 tt6/r^6 over O/H pairs of different waters)."""
+
+    def __init__(self):
+        super().__init__(0.9)
+        self.c6 = DISP_C6.copy()
+        self.d6 = DISP_D6.copy()
+
+
+class MBPolElectrostaticsForce:
+    """openmmapi/include/openmm/MBPolElectrostaticsForce.h"""
+    NoCutoff, PME = 0, 1
+    # initial guess for the induced dipoles (this library's addition)
+    DirectGuess, PreviousGuess, LearnedGuess = 0, 1, 2
+
+    def __init__(self):
+        self._particles = []
+        self._method = 0
+        self._cutoff = 0.9
+        self._alpha = 0.0
+        self._grid = [0, 0, 0]
+        self._tol = 1e-4
+        self._maxiter = 200
+        self._eps = 1e-7
+        self._thole = list(MBPOL_THOLE)
+        self._redist = True
+        self._guess = 0
+        self._group = 0
+
+    def addElectrostatics(self, charge, moleculeIndex, atomType, dampingFactor, polarity):
+        self._particles.append((float(charge), int(moleculeIndex), int(atomType), float(dampingFactor), float(polarity)))
+        return len(self._particles) - 1
+
+    def getNumElectrostatics(self):
+        return len(self._particles)
+
+    def getElectrostaticsParameters(self, i):
+        return self._particles[i]
+
+    def setElectrostaticsParameters(self, i, charge, moleculeIndex, atomType, dampingFactor, polarity):
+        self._particles[i] = (float(charge), int(moleculeIndex), int(atomType), float(dampingFactor), float(polarity))
+
+    def setNonbondedMethod(self, m):
+        self._method = int(m)
+
+    def getNonbondedMethod(self):
+        return self._method
+
+    def setCutoffDistance(self, d):
+        self._cutoff = float(d)
+
+    def getCutoffDistance(self):
+        return self._cutoff
+
+    def setAEwald(self, a):
+        self._alpha = float(a)
+
+    def getAEwald(self):
+        return self._alpha
+
+    def getPmeBSplineOrder(self):
+        return 5
+
+    def setPmeGridDimensions(self, g):
+        self._grid = [int(v) for v in g]
+
+    def getPmeGridDimensions(self):
+        return list(self._grid)
+
+    def setEwaldErrorTolerance(self, t):
+        self._tol = float(t)
+
+    def getEwaldErrorTolerance(self):
+        return self._tol
+
+    def setMutualInducedMaxIterations(self, n):
+        self._maxiter = int(n)
+
+    def getMutualInducedMaxIterations(self):
+        return self._maxiter
+
+    def setMutualInducedTargetEpsilon(self, e):
+        self._eps = float(e)
+
+    def getMutualInducedTargetEpsilon(self):
+        return self._eps
+
+    def setTholeParameters(self, t):
+        self._thole = [float(v) for v in t]
+
+    def getTholeParameters(self):
+        return list(self._thole)
+
+    def setIncludeChargeRedistribution(self, b):
+        self._redist = bool(b)
+
+    def getIncludeChargeRedistribution(self):
+        return self._redist
+
+    def setInducedDipoleGuess(self, g):
+        self._guess = int(g)
+
+    def getInducedDipoleGuess(self):
+        return self._guess
+
+    def setForceGroup(self, g):
+        self._group = int(g)
+
+    def getForceGroup(self):
+        return self._group
+
+    def updateParametersInContext(self, context):
+        context._invalidate()
+
+    def _params(self):
+        p = _capi.ElectrostaticsParams()
+        _capi.load().mbpol_electrostatics_params_default(ctypes.byref(p))
+        p.nonbonded_method = self._method
+        p.cutoff = self._cutoff
+        p.ewald_alpha = self._alpha
+        for k in range(3):
+            p.pme_grid[k] = self._grid[k]
+        p.ewald_error_tolerance = self._tol
+        p.max_iterations = self._maxiter
+        p.target_epsilon = self._eps
+        for k in range(5):
+            p.thole[k] = self._thole[k]
+        p.include_charge_redistribution = 1 if self._redist else 0
+        p.guess = self._guess
+        return p
+
+
+class ThreeParticleAverageSite:
+    def __init__(self, p1, p2, p3, w1, w2, w3):
+        self.particles = (int(p1), int(p2), int(p3))
+        self.weights = (float(w1), float(w2), float(w3))
+
+
+class System:
+    """Minimal stand-in for OpenMM's System."""
+
+    def __init__(self):
+        self.masses = []
+        self.forces = []
+        self.vsites = {}
+        self.box = None
+
+    def addParticle(self, mass):
+        self.masses.append(float(mass))
+        return len(self.masses) - 1
+
+    def getNumParticles(self):
+        return len(self.masses)
+
+    def setVirtualSite(self, index, site):
+        self.vsites[int(index)] = site
+
+    def isVirtualSite(self, index):
+        return int(index) in self.vsites
+
+    def addForce(self, f):
+        self.forces.append(f)
+        return len(self.forces) - 1
+
+    def setDefaultPeriodicBoxVectors(self, a, b, c):
+        self.box = np.array([a[0], b[1], c[2]], float)
+
+
+class State:
+    def __init__(self, energy, forces, terms):
+        self._energy = energy
+        self._forces = forces
+        self.term_energies = terms
+
+    def getPotentialEnergy(self):
+        return self._energy
+
+    def getForces(self, asNumpy=True):
+        return self._forces
+
+
+TERM_OF = {MBPolOneBodyForce: _capi.TERM_ONEBODY, MBPolTwoBodyForce: _capi.TERM_TWOBODY,
+           MBPolThreeBodyForce: _capi.TERM_THREEBODY, MBPolElectrostaticsForce: _capi.TERM_ELECTROSTATICS,
+           MBPolDispersionForce: _capi.TERM_DISPERSION}
+
+
+class Context:
+    """Stand-in for OpenMM's Context on the GB300 library (one CUDA device)."""
+
+    def __init__(self, system, device=0):
+        self.system = system
+        self.device = device
+        self._h = None
+        self._pos = None
+        self._box = None if system.box is None else np.array(system.box, float)
+
+    def _invalidate(self):
+        self._destroy()
+
+    def _destroy(self):
+        if self._h is not None:
+            _capi.load().mbpol_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self._destroy()
+        except Exception:
+            pass
+
+    def _build(self):
+        lib = _capi.load()
+        n = self.system.getNumParticles()
+        h = ctypes.c_void_p()
+        check(lib.mbpol_context_create(n, self.device, ctypes.byref(h)))
+        self._h = h
+        for idx, vs in sorted(self.system.vsites.items()):
+            check(lib.mbpol_add_average3_site(h, idx, *vs.particles, *vs.weights))
+        for f in self.system.forces:
+            if isinstance(f, MBPolElectrostaticsForce):
+                if f.getNumElectrostatics() != n:
+                    raise _capi.MBPolError(1, "MBPolElectrostaticsForce must have exactly as many particles as the System")
+                a = np.array(f._particles, dtype=object)
+                q = as_c([p[0] for p in f._particles], np.float64)
+                mol = as_c([p[1] for p in f._particles], np.int32)
+                typ = as_c([p[2] for p in f._particles], np.int32)
+                dmp = as_c([p[3] for p in f._particles], np.float64)
+                pol = as_c([p[4] for p in f._particles], np.float64)
+                prm = f._params()
+                check(lib.mbpol_add_electrostatics_force(h, ctypes.byref(prm), ptr(q), ptr(mol), ptr(typ), ptr(dmp), ptr(pol)))
+                del a
+                continue
+            w = as_c(np.array(f._waters, dtype=np.int32).reshape(-1, 3), np.int32)
+            nw = w.shape[0]
+            if isinstance(f, MBPolOneBodyForce):
+                check(lib.mbpol_add_onebody_force(h, nw, ptr(w), f._method))
+            elif isinstance(f, MBPolTwoBodyForce):
+                check(lib.mbpol_add_twobody_force(h, nw, ptr(w), f._method, f._cutoff))
+            elif isinstance(f, MBPolThreeBodyForce):
+                check(lib.mbpol_add_threebody_force(h, nw, ptr(w), f._method, f._cutoff, f._rule))
+            elif isinstance(f, MBPolDispersionForce):
+                c6 = as_c(f.c6, np.float64)
+                d6 = as_c(f.d6, np.float64)
+                check(lib.mbpol_add_dispersion_force(h, nw, ptr(w), f._method, f._cutoff, ptr(c6), ptr(d6)))
+            else:
+                raise TypeError("unsupported force %r" % (f,))
+
+    def setPositions(self, positions):
+        self._pos = as_c(np.asarray(positions, float).reshape(-1, 3), np.float64)
+
+    def setPeriodicBoxVectors(self, a, b, c):
+        self._box = np.array([a[0], b[1], c[2]], float)
+
+    def getState(self, getEnergy=True, getForces=True, groups=None):
+        if self._h is None:
+            self._build()
+        lib = _capi.load()
+        box = None if self._box is None else as_c(self._box, np.float64)
+        check(lib.mbpol_set_positions(self._h, ptr(self._pos), ptr(box)))
+        mask = 0
+        for f in self.system.forces:
+            g = f.getForceGroup()
+            if groups is None or (int(groups) >> g) & 1:
+                mask |= 1 << TERM_OF[type(f)]
+        e = np.zeros(_capi.NUM_TERMS)
+        forces = np.zeros((self.system.getNumParticles(), 3))
+        check(lib.mbpol_compute(self._h, mask, ptr(e), ptr(forces)))
+        return State(float(e.sum()), forces, e)
+
+    def getInducedDipoles(self):
+        lib = _capi.load()
+        d = np.zeros((self.system.getNumParticles(), 3))
+        it = ctypes.c_int()
+        eps = ctypes.c_double()
+        check(lib.mbpol_get_induced_dipoles(self._h, ptr(d), ctypes.byref(it), ctypes.byref(eps)))
+        return d, it.value, eps.value
+
+    def getCounts(self):
+        c = np.zeros(4, dtype=np.int64)
+        check(_capi.load().mbpol_get_counts(self._h, ptr(c)))
+        return c
+
+
+def create_mbpol_system(ws, nonbonded_method="auto", terms=("onebody", "twobody", "threebody", "electrostatics",
+                                                            "dispersion"), nonbonded_cutoff=0.9,
+                        ewald_alpha=0.0, pme_grid=None, ewald_tol=1e-5, target_epsilon=1e-8, max_iterations=200,
+                        trimer_rule=0, guess=0):
+    """Build the MB-pol System for a WaterSystem as ForceField('mbpol.xml')
+    does (python/mbpol.py:65-76, 138-150, 211-223, 288-326 and the <Script>
+    of python/mbpol.xml): per water O, H1, H2, M with the M virtual site."""
+    periodic = ws.box is not None if nonbonded_method == "auto" else nonbonded_method == "PME"
+    sys_ = System()
+    nw = ws.num_waters
+    for _ in range(nw):
+        for t in (0, 1, 1, 2):
+            sys_.addParticle(MBPOL_MASS[t])
+    for w in range(nw):
+        sys_.setVirtualSite(4 * w + 3, ThreeParticleAverageSite(4 * w, 4 * w + 1, 4 * w + 2, 0.573293118,
+                                                                0.213353441, 0.213353441))
+    if periodic:
+        sys_.setDefaultPeriodicBoxVectors((ws.box[0], 0, 0), (0, ws.box[1], 0), (0, 0, ws.box[2]))
+    waters = ws.water_indices()
+    if "onebody" in terms:
+        f = MBPolOneBodyForce()
+        f.setNonbondedMethod(MBPolOneBodyForce.Periodic if periodic else MBPolOneBodyForce.NonPeriodic)
+        for w in waters:
+            f.addOneBody(w)
+        sys_.addForce(f)
+    if "twobody" in terms:
+        f = MBPolTwoBodyForce()
+        f.setCutoff(MBPOL_2B_CUTOFF)
+        f.setNonbondedMethod(MBPolTwoBodyForce.CutoffPeriodic if periodic else MBPolTwoBodyForce.CutoffNonPeriodic)
+        for w in waters:
+            f.addParticle(w)
+        sys_.addForce(f)
+    if "threebody" in terms:
+        f = MBPolThreeBodyForce()
+        f.setCutoff(MBPOL_3B_CUTOFF)
+        f.setTrimerRule(trimer_rule)
+        f.setNonbondedMethod(MBPolThreeBodyForce.CutoffPeriodic if periodic else MBPolThreeBodyForce.CutoffNonPeriodic)
+        for w in waters:
+            f.addParticle(w)
+        sys_.addForce(f)
+    if "electrostatics" in terms:
+        f = MBPolElectrostaticsForce()
+        f.setNonbondedMethod(MBPolElectrostaticsForce.PME if periodic else MBPolElectrostaticsForce.NoCutoff)
+        f.setCutoffDistance(nonbonded_cutoff)
+        f.setTholeParameters(MBPOL_THOLE)
+        f.setMutualInducedTargetEpsilon(target_epsilon)
+        f.setMutualInducedMaxIterations(max_iterations)
+        f.setInducedDipoleGuess(guess)
+        if periodic:
+            f.setEwaldErrorTolerance(ewald_tol)
+            if ewald_alpha:
+                f.setAEwald(ewald_alpha)
+            if pme_grid is not None:
+                f.setPmeGridDimensions(pme_grid)
+        for w in range(nw):
+            for t in (0, 1, 1, 2):
+                f.addElectrostatics(MBPOL_CHARGE[t], w, t, MBPOL_DAMPING[t], MBPOL_POLARITY[t])
+        sys_.addForce(f)
+    if "dispersion" in terms:
+        f = MBPolDispersionForce()
+        f.setCutoff(nonbonded_cutoff)
+        f.setNonbondedMethod(MBPolDispersionForce.CutoffPeriodic if periodic else MBPolDispersionForce.NoCutoff)
+        for w in waters:
+            f.addParticle(w)
+        sys_.addForce(f)
+    return sys_
+
+
+def pme_parameters(box_nm, cutoff, tol):
+    """Ewald alpha and grid by OpenMM's documented rule:
+    alpha = sqrt(-ln(2 tol))/rc, n = ceil(2 alpha L / (3 tol^(1/5))) rounded up
+    to a 2,3,5,7-smooth size."""
+    alpha = np.sqrt(-np.log(2 * tol)) / cutoff
+    grid = []
+    for L in box_nm:
+        n = int(np.ceil(2 * alpha * L / (3 * tol ** 0.2)))
+        while True:
+            m = n
+            for p in (2, 3, 5, 7):
+                while m % p == 0:
+                    m //= p
+            if m == 1:
+                break
+            n += 1
+        grid.append(max(n, 6))
+    return float(alpha), grid

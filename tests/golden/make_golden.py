@@ -1,0 +1,226 @@
+"""Generate the golden fixtures under tests/golden/ (run in a checkout with the
+reference next to it; the GPU tests only read the committed outputs).
+
+Sources:
+  * the reference's own known-answer tests, read as text:
+      platforms/reference/tests/TestReferenceMBPolOneBodyForce.cpp:83-113
+      platforms/reference/tests/TestReferenceMBPolTwoBodyForce.cpp:99-127
+      platforms/reference/tests/TestReferenceMBPolThreeBodyForce.cpp:97-138
+      platforms/reference/tests/TestReferenceThreeNeighborList.cpp:42-78
+  * the reference's Reference-platform force classes, compiled unmodified by
+    oracle/build_ref.sh into oracle/_ref/libmbpol_ref.so, evaluated on seeded
+    synthetic systems (mbpol_openmm_plugin_gb300.systems).
+Dispersion has no plugin code in the reference (python/mbpol.xml:37-108 builds
+an OpenMM CustomNonbondedForce); its values come from the C oracle port.
+
+    python tests/golden/make_golden.py [/path/to/reference]
+"""
+import ctypes
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from mbpol_openmm_plugin_gb300 import systems  # noqa: E402
+
+REF = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] != "-" else "/root/reference"
+LIB = os.path.join(ROOT, "oracle", "_ref", "libmbpol_ref.so")
+
+VEC3 = r"Vec3\(\s*([-+0-9.eE]+)\s*,\s*([-+0-9.eE]+)\s*,\s*([-+0-9.eE]+)\s*\)"
+
+
+def parse_test(path, func):
+    src = open(path).read()
+    i = src.index(func)
+    ends = [k for k in (src.find("\nvoid ", i + 10), src.find("\nstatic void ", i + 10), src.find("\nint main", i + 10)) if k > 0]
+    body = src[i:min(ends) if ends else len(src)]
+    pos, exp = {}, {}
+    for m in re.finditer(r"positions\[(\d+)\]\s*=\s*" + VEC3, body):
+        pos.setdefault(int(m.group(1)), [float(m.group(k)) for k in (2, 3, 4)])
+    for m in re.finditer(r"expectedForces\[(\d+)\]\s*=\s*" + VEC3, body):
+        exp.setdefault(int(m.group(1)), [float(m.group(k)) for k in (2, 3, 4)])
+    e = re.search(r"expectedEnergy\s*=\s*([-+0-9.eE]+)\s*(\*\s*cal2joule\s*)?;", body)
+    n = len(pos)
+    return {
+        "positions_A": [pos[k] for k in range(n)],
+        "expected_gradient_kcal_A": [exp[k] for k in range(len(exp))] if sorted(exp) == list(range(len(exp)))
+        else {str(k): v for k, v in exp.items()},
+        "expected_energy_kcal": float(e.group(1)),
+    }
+
+
+def lib():
+    L = ctypes.CDLL(LIB)
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    L.ref_onebody.restype = D
+    L.ref_onebody.argtypes = [I, P, I, P, P, P]
+    L.ref_twobody.restype = D
+    L.ref_twobody.argtypes = [I, P, I, P, P, D, P, P]
+    L.ref_threebody.restype = D
+    L.ref_threebody.argtypes = [I, P, I, P, P, D, P, P, P, ctypes.c_long]
+    L.ref_electrostatics.restype = I
+    L.ref_electrostatics.argtypes = [I, P, P, P, P, P, P, P, I, D, D, P, P, D, I, I, P, P, P, P, ctypes.c_char_p, I]
+    return L
+
+
+MW = (0.573293118, 0.213353441, 0.213353441)   # python/mbpol.xml:14
+THOLE = [0.4, 0.4, 0.055, 0.626, 0.055]        # python/mbpol.xml:22
+
+
+def place_m(pos):
+    pos = pos.copy()
+    for w in range(pos.shape[0] // 4):
+        pos[4 * w + 3] = MW[0] * pos[4 * w] + MW[1] * pos[4 * w + 1] + MW[2] * pos[4 * w + 2]
+    return pos
+
+
+def electrostatics(L, pos, box, pme, alpha=0.0, grid=(0, 0, 0), cutoff=0.9, eps=1e-8, maxiter=200):
+    """Reference electrostatics for O,H1,H2,M waters with the mbpol.xml
+    parameters; M forces are spread back onto O, H1, H2 with the M weights."""
+    n = pos.shape[0]
+    typ = np.tile([0, 1, 1, 2], n // 4).astype(np.int32)
+    q = np.array([-5.1966000e-01, 2.5983000e-01, 2.5983000e-01, 0.0])[typ % 4 if False else [0, 1, 1, 2] * (n // 4)]
+    q = np.tile([-5.1966000e-01, 2.5983000e-01, 2.5983000e-01, 0.0], n // 4)
+    damp = np.tile([0.00131, 0.000294, 0.000294, 0.00131], n // 4)
+    pol = np.tile([0.00131, 0.000294, 0.000294, 0.0], n // 4)
+    mol = np.repeat(np.arange(n // 4), 4).astype(np.int32)
+    f = np.zeros((n, 3))
+    e = ctypes.c_double()
+    dip = np.zeros((n, 3))
+    it = ctypes.c_int()
+    err = ctypes.create_string_buffer(512)
+    g = np.array(grid, np.int32)
+    b = np.zeros(3) if box is None else np.asarray(box, float)
+    th = np.array(THOLE)
+    rc = L.ref_electrostatics(n, p(np.ascontiguousarray(pos)), p(q), p(mol), p(typ), p(damp), p(pol), p(th),
+                              1 if pme else 0, cutoff, alpha, p(g), p(b), eps, maxiter, 1, p(f),
+                              ctypes.byref(e), p(dip), ctypes.byref(it), err, 512)
+    if rc:
+        raise RuntimeError(err.value.decode())
+    for w in range(n // 4):
+        fm = f[4 * w + 3].copy()
+        f[4 * w + 3] = 0
+        for k in range(3):
+            f[4 * w + k] += MW[k] * fm
+    return e.value, f, dip, it.value
+
+
+def p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def run_terms(L, pos, waters, box, cut2=0.65, cut3=0.45):
+    pos = np.ascontiguousarray(pos, np.float64)
+    w = np.ascontiguousarray(waters, np.int32)
+    nw, n = w.shape[0], pos.shape[0]
+    b = None if box is None else np.ascontiguousarray(box, np.float64)
+    out = {}
+    f = np.zeros((n, 3))
+    out["e1"] = L.ref_onebody(nw, p(w), n, p(pos), p(b), p(f))
+    out["f1"] = f
+    f = np.zeros((n, 3))
+    npairs = ctypes.c_long()
+    out["e2"] = L.ref_twobody(nw, p(w), n, p(pos), p(b), cut2, p(f), ctypes.byref(npairs))
+    out["f2"] = f
+    out["npairs"] = npairs.value
+    f = np.zeros((n, 3))
+    nt = ctypes.c_long()
+    cap = 4000000
+    trips = np.zeros((cap, 3), np.int32)
+    out["e3"] = L.ref_threebody(nw, p(w), n, p(pos), p(b), cut3, p(f), ctypes.byref(nt), p(trips), cap)
+    out["f3"] = f
+    out["ntrip"] = nt.value
+    t = trips[:nt.value]
+    out["trip_hash"] = int(np.sum((t[:, 0].astype(np.int64) * 1000003 + t[:, 1]) * 1000003 + t[:, 2]) % (1 << 61))
+    return out
+
+
+def dispersion_oracle(pos, waters, box, rc):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # noqa: E402
+    return oracle.dispersion(pos, waters, box, rc)
+
+
+def main():
+    L = lib()
+    tests = os.path.join(REF, "platforms", "reference", "tests")
+    known = {
+        "onebody_water1": parse_test(os.path.join(tests, "TestReferenceMBPolOneBodyForce.cpp"), "void testOneOneBody"),
+        "twobody_water2": parse_test(os.path.join(tests, "TestReferenceMBPolTwoBodyForce.cpp"), "void testTwoBody"),
+        "threebody_water3": parse_test(os.path.join(tests, "TestReferenceMBPolThreeBodyForce.cpp"), "void testThreeBody"),
+    }
+    # trimer chain rule (TestReferenceThreeNeighborList.cpp:42-78): O positions, cutoff, expected count
+    src = open(os.path.join(tests, "TestReferenceThreeNeighborList.cpp")).read()
+    known["trimer_rule_source"] = "platforms/reference/tests/TestReferenceThreeNeighborList.cpp:42-78"
+    known["trimer_rule_excerpt"] = [ln.strip() for ln in src.splitlines()[41:78]]
+    with open(os.path.join(HERE, "reference_known_answers.json"), "w") as f:
+        json.dump(known, f, indent=1)
+
+    # the known-answer systems through the compiled reference
+    res = {}
+    for key, nwat in (("onebody_water1", 1), ("twobody_water2", 2), ("threebody_water3", 3)):
+        pos = np.array(known[key]["positions_A"]) * 0.1
+        w = np.arange(3 * nwat, dtype=np.int32).reshape(-1, 3)
+        r = run_terms(L, pos, w, None, cut2=10.0, cut3=10.0)
+        res[key] = {"e1": r["e1"], "e2": r["e2"], "e3": r["e3"],
+                    "f1": r["f1"].tolist(), "f2": r["f2"].tolist(), "f3": r["f3"].tolist()}
+    with open(os.path.join(HERE, "reference_known_answers_oracle.json"), "w") as f:
+        json.dump(res, f, indent=1)
+
+    # seeded synthetic systems: O,H1,H2,M per water (M unused by 1B/2B/3B)
+    for name, seed in (("cluster14", 0), ("cluster14", 1), ("box256", 0), ("cluster64", 2)):
+        ws = systems.cluster(64, seed, radius=8.0, dmin=2.5) if name == "cluster64" else systems.workload(name, seed)
+        waters = ws.water_indices()
+        r = run_terms(L, ws.positions, waters, ws.box)
+        ed, fd = dispersion_oracle(ws.positions, waters, ws.box, 0.9 if ws.box is not None else 1e30)
+        np.savez_compressed(os.path.join(HERE, "%s_seed%d.npz" % (name, seed)),
+                            positions=ws.positions, box=np.zeros(3) if ws.box is None else ws.box,
+                            periodic=ws.box is not None, e1=r["e1"], e2=r["e2"], e3=r["e3"], f1=r["f1"],
+                            f2=r["f2"], f3=r["f3"], npairs=r["npairs"], ntrip=r["ntrip"], trip_hash=r["trip_hash"],
+                            edisp=ed, fdisp=fd)
+        print(name, seed, "e1 %.6f e2 %.6f e3 %.6f edisp %.6f pairs %d trimers %d" % (
+            r["e1"], r["e2"], r["e3"], ed, r["npairs"], r["ntrip"]))
+
+
+def main_elec():
+    L = lib()
+    tests = os.path.join(REF, "platforms", "reference", "tests")
+    known = parse_test(os.path.join(tests, "TestReferenceMBPolElectrostaticsForce.cpp"), "static void testWater3VirtualSite()")
+    pos = place_m(np.array(known["positions_A"]) * 0.1)
+    e, f, dip, it = electrostatics(L, pos, None, False, eps=1e-7)
+    known["oracle_energy_kJ"] = e
+    known["oracle_forces_kJ_nm"] = f.tolist()
+    known["oracle_iterations"] = it
+    known["source"] = "platforms/reference/tests/TestReferenceMBPolElectrostaticsForce.cpp:419-546"
+    with open(os.path.join(HERE, "elec_water3_virtualsite.json"), "w") as fh:
+        json.dump(known, fh, indent=1)
+    print("water3 virtual site: E %.6f kcal/mol (expected %.6f), iterations %d" % (
+        e / 4.184, known["expected_energy_kcal"], it))
+    sys.path.insert(0, ROOT)
+    from mbpol_openmm_plugin_gb300.plugin import pme_parameters
+    for name, seed in (("cluster14", 0), ("cluster14", 1), ("box256", 0)):
+        ws = systems.workload(name, seed)
+        pos = place_m(ws.positions)
+        if ws.box is None:
+            e, f, dip, it = electrostatics(L, pos, None, False, eps=1e-8)
+            alpha, grid = 0.0, [0, 0, 0]
+        else:
+            alpha, grid = pme_parameters(ws.box, 0.9, 1e-5)
+            e, f, dip, it = electrostatics(L, pos, ws.box, True, alpha=alpha, grid=grid, eps=1e-8)
+        np.savez_compressed(os.path.join(HERE, "elec_%s_seed%d.npz" % (name, seed)), positions=pos,
+                            box=np.zeros(3) if ws.box is None else ws.box, periodic=ws.box is not None,
+                            alpha=alpha, grid=np.array(grid), eelec=e, felec=f, dipoles=dip, iterations=it)
+        print(name, seed, "Eelec %.6f kJ/mol  iterations %d  alpha %.4f grid %s" % (e, it, alpha, grid))
+
+
+if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "elec":
+        main_elec()
+    else:
+        main()
+        main_elec()

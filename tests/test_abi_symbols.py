@@ -1,0 +1,35 @@
+"""CPU: the C-ABI library exists (after build()), loads, and exports every
+function declared in include/mbpol_gb300.h.  No compute call is made."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+from mbpol_openmm_plugin_gb300 import _capi
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "mbpol_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mbpol_[a-z0-9_]+)\s*\(", src)) - {"mbpol_status"})
+
+
+def test_header_matches_binding_list():
+    assert set(declared_functions()) == set(_capi.EXPORTED)
+
+
+def test_library_exports_all_symbols():
+    if not os.path.exists(_capi.LIB_PATH):
+        pytest.skip("library not built")
+    lib = ctypes.CDLL(_capi.LIB_PATH)
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_status_strings_without_gpu():
+    if not os.path.exists(_capi.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _capi.load()
+    assert lib.mbpol_status_string(3) == b"induced dipoles did not converge"
