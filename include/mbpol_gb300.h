@@ -135,6 +135,21 @@ mbpol_status mbpol_set_positions(mbpol_context* ctx, const double* xyz, const do
  * the reference throws (MBPolReferenceElectrostaticsForce.cpp:888-894). */
 mbpol_status mbpol_compute(mbpol_context* ctx, unsigned term_mask, double* energies, double* forces);
 
+/* Molecular dynamics on the device (the integrator OpenMM provides for the
+ * reference, python/example_nvt_nve.py): masses (amu; 0 = virtual/massless),
+ * velocities (nm/ps).  mbpol_md_run advances nsteps of velocity Verlet with
+ * time step dt (ps); collision_rate > 0 (1/ps) adds an Andersen thermostat at
+ * `temperature` (K).  gpu_ms receives the CUDA-event time of the run on the
+ * context's stream; energies (optional, MBPOL_NUM_TERMS + 1 doubles) the
+ * last step's potential terms and kinetic energy; solver_iterations the
+ * induced-dipole iterations summed over the run. */
+mbpol_status mbpol_set_masses(mbpol_context* ctx, const double* masses);
+mbpol_status mbpol_set_velocities(mbpol_context* ctx, const double* velocities);
+mbpol_status mbpol_md_run(mbpol_context* ctx, int nsteps, double dt, double temperature, double collision_rate,
+                          unsigned long long seed, double* gpu_ms, double* energies, long* solver_iterations);
+/* Copy the device state (any pointer may be NULL). */
+mbpol_status mbpol_get_state(mbpol_context* ctx, double* positions, double* velocities, double* forces);
+
 /* Induced dipoles (3*num_particles, e*nm) of the last electrostatics
  * evaluation, with its solver iteration count and final epsilon (Debye). */
 mbpol_status mbpol_get_induced_dipoles(mbpol_context* ctx, double* dipoles, int* iterations, double* epsilon);
@@ -142,6 +157,14 @@ mbpol_status mbpol_get_induced_dipoles(mbpol_context* ctx, double* dipoles, int*
 /* Counts from the last evaluation: [0] two-body pairs, [1] trimers,
  * [2] electrostatics site pairs within the cutoff, [3] solver iterations. */
 mbpol_status mbpol_get_counts(mbpol_context* ctx, long* counts4);
+
+/* Kernel timing with CUDA events on the launching stream (process-wide).
+ * Kernel ids: 0 two-body polynomial, 1 three-body polynomial, 2 fixed field,
+ * 3 induced field + solver update, 4 PME dipole pass (spread, FFT,
+ * convolution, inverse FFT, gather), 5 electrostatic energy/forces.
+ * Enabling clears previous records; read returns the summed time and count. */
+mbpol_status mbpol_profile_enable(int on);
+mbpol_status mbpol_profile_read(int kernel, double* total_ms, long* launches);
 
 const char* mbpol_status_string(mbpol_status s);
 const char* mbpol_last_error(void);

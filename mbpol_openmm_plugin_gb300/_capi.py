@@ -24,9 +24,11 @@ EXPORTED = [
     "mbpol_electrostatics_params_default", "mbpol_context_create", "mbpol_context_destroy",
     "mbpol_add_average3_site", "mbpol_add_onebody_force", "mbpol_add_twobody_force",
     "mbpol_add_threebody_force", "mbpol_add_electrostatics_force", "mbpol_add_dispersion_force",
-    "mbpol_set_positions", "mbpol_compute", "mbpol_get_induced_dipoles", "mbpol_get_counts",
-    "mbpol_status_string", "mbpol_last_error",
+    "mbpol_set_positions", "mbpol_compute", "mbpol_set_masses", "mbpol_set_velocities", "mbpol_md_run",
+    "mbpol_get_state", "mbpol_get_induced_dipoles", "mbpol_get_counts",
+    "mbpol_profile_enable", "mbpol_profile_read", "mbpol_status_string", "mbpol_last_error",
 ]
+KERNELS = ["poly2b", "poly3b", "elec_fixed_field", "elec_induced_update", "elec_pme_dipoles", "elec_energy_forces"]
 
 
 class MBPolError(RuntimeError):
@@ -76,8 +78,14 @@ def load(path=None):
         "mbpol_add_dispersion_force": (I, [P, I, P, I, D, P, P]),
         "mbpol_set_positions": (I, [P, P, P]),
         "mbpol_compute": (I, [P, ctypes.c_uint, P, P]),
+        "mbpol_set_masses": (I, [P, P]),
+        "mbpol_set_velocities": (I, [P, P]),
+        "mbpol_md_run": (I, [P, I, D, D, D, ctypes.c_ulonglong, ctypes.POINTER(D), P, ctypes.POINTER(ctypes.c_long)]),
+        "mbpol_get_state": (I, [P, P, P, P]),
         "mbpol_get_induced_dipoles": (I, [P, P, ctypes.POINTER(I), ctypes.POINTER(D)]),
         "mbpol_get_counts": (I, [P, P]),
+        "mbpol_profile_enable": (I, [I]),
+        "mbpol_profile_read": (I, [I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_long)]),
         "mbpol_status_string": (ctypes.c_char_p, [I]),
         "mbpol_last_error": (ctypes.c_char_p, []),
     }

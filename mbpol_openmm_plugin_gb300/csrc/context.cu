@@ -29,6 +29,38 @@ mbpol_status mbpol_fail_cuda(cudaError_t e, const char* what) {
 
 namespace mbpol {
 
+// Event-pair timing of selected kernels, one global profile per process
+// (the library drives one device per context and the bench uses one).
+struct Profiler {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<std::pair<size_t, size_t>> rec[K_NUM];
+    cudaEvent_t get() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+};
+Profiler g_prof;
+size_t g_open[K_NUM];
+
+void prof_begin(cudaStream_t st, int id) {
+    if (!g_prof.on) return;
+    cudaEvent_t e = g_prof.get();
+    cudaEventRecord(e, st);
+    g_open[id] = g_prof.used - 1;
+}
+void prof_end(cudaStream_t st, int id) {
+    if (!g_prof.on) return;
+    cudaEvent_t e = g_prof.get();
+    cudaEventRecord(e, st);
+    g_prof.rec[id].push_back({g_open[id], g_prof.used - 1});
+}
+
 // Grow-only device buffer.
 struct DevBuf {
     void* p = nullptr;
@@ -93,6 +125,12 @@ struct mbpol_context {
     std::unique_ptr<ElecEngine> elec;
     int num_sms = 0;
     long counts[4] = {0, 0, 0, 0};
+    // molecular dynamics state (device resident)
+    DevBuf d_vel, d_invm, d_ekin;
+    bool have_masses = false, have_vel = false, forces_valid = false;
+    unsigned long long md_step = 0;
+    long solver_iterations_total = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
 namespace {
@@ -162,13 +200,15 @@ mbpol_status run_twobody(mbpol_context* ctx, double* energy) {
         const int np = h[0];
         ctx->counts[0] = np;
         const int stride = ctx->cap2;
-        MBPOL_CUDA_OK(ctx->x2.ensure(sizeof(float) * 31 * (size_t)stride));
+        MBPOL_CUDA_OK(ctx->x2.ensure(sizeof(float) * 2 * 31 * (size_t)stride));
         MBPOL_CUDA_OK(ctx->g2.ensure(sizeof(float) * 31 * (size_t)stride));
         MBPOL_CUDA_OK(ctx->e2.ensure(sizeof(float) * (size_t)stride));
         launch_twobody_vars(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
                             ctx->x2.as<float>(), stride);
+        prof_begin(ctx->st, K_POLY2B);
         launch_poly2b(ctx->st, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride,
                       ctx->num_sms);
+        prof_end(ctx->st, K_POLY2B);
         launch_twobody_forces(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
                               ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy);
         return MBPOL_OK;
@@ -225,7 +265,7 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
         if (ntrip > ctx->cap3) ctx->cap3 = ntrip + ntrip / 4 + 64;
         const int stride = ctx->cap3;
         MBPOL_CUDA_OK(ctx->trips3.ensure(sizeof(int4) * (size_t)stride));
-        MBPOL_CUDA_OK(ctx->x3.ensure(sizeof(float) * 36 * (size_t)stride));
+        MBPOL_CUDA_OK(ctx->x3.ensure(sizeof(float) * 2 * 36 * (size_t)stride));
         MBPOL_CUDA_OK(ctx->g3.ensure(sizeof(float) * 36 * (size_t)stride));
         MBPOL_CUDA_OK(ctx->e3.ensure(sizeof(float) * (size_t)stride));
         if (!complete)
@@ -237,8 +277,10 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
                                    ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>(), true);
         launch_threebody_vars(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                               box, ctx->x3.as<float>(), stride);
+        prof_begin(ctx->st, K_POLY3B);
         launch_poly3b(ctx->st, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
                       ctx->num_sms);
+        prof_end(ctx->st, K_POLY3B);
         launch_threebody_forces(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(),
                                 ctx->d_pos.as<double>(), box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride,
                                 ctx->d_force.as<double>(), energy);
@@ -333,6 +375,8 @@ mbpol_status mbpol_context_destroy(mbpol_context* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->st);
     ctx->elec.reset();
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     cudaStreamDestroy(ctx->st);
     delete ctx;
     return MBPOL_OK;
@@ -407,13 +451,18 @@ mbpol_status mbpol_set_positions(mbpol_context* ctx, const double* xyz, const do
     }
     MBPOL_CUDA_OK(cudaMemcpyAsync(ctx->d_pos.p, xyz, sizeof(double) * 3 * ctx->N, cudaMemcpyHostToDevice, ctx->st));
     ctx->have_pos = true;
+    ctx->forces_valid = false;
     return MBPOL_OK;
 }
 
-mbpol_status mbpol_compute(mbpol_context* ctx, unsigned mask, double* energies, double* forces) {
-    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
-    if (!ctx->have_pos) return mbpol_fail(MBPOL_ERR_STATE, "positions have not been set");
-    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+}  // extern "C"
+
+namespace {
+
+// Evaluate the requested terms; forces and energies stay on the device
+// (d_force, d_energy).  Host synchronisation happens only for list sizes and
+// the solver's convergence test.
+mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
     if (ctx->vs_dirty) {
         MBPOL_CUDA_OK(ctx->d_vs_idx.ensure(sizeof(int4) * ctx->vs_idx.size()));
         MBPOL_CUDA_OK(ctx->d_vs_w.ensure(sizeof(double) * ctx->vs_w.size()));
@@ -442,25 +491,120 @@ mbpol_status mbpol_compute(mbpol_context* ctx, unsigned mask, double* energies, 
                                e + MBPOL_TERM_ELECTROSTATICS);
         ctx->counts[2] = ctx->elec->num_site_pairs();
         ctx->counts[3] = ctx->elec->iterations();
+        ctx->solver_iterations_total += ctx->elec->iterations();
     }
     if (s) {
         cudaStreamSynchronize(ctx->st);
         return s;
     }
     launch_spread_vsites(ctx->st, nvs, ctx->d_vs_idx.as<int4>(), ctx->d_vs_w.as<double>(), ctx->d_force.as<double>());
+    MBPOL_CUDA_OK(cudaGetLastError());
+    if (ctx->elec && (mask & MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS)) && !ctx->elec->converged())
+        return mbpol_fail(MBPOL_ERR_NOT_CONVERGED, ctx->elec->convergence_message());
+    return MBPOL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mbpol_status mbpol_compute(mbpol_context* ctx, unsigned mask, double* energies, double* forces) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (!ctx->have_pos) return mbpol_fail(MBPOL_ERR_STATE, "positions have not been set");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    ctx->forces_valid = false;
+    mbpol_status s = compute_device(ctx, mask);
+    if (s && s != MBPOL_ERR_NOT_CONVERGED) return s;
     double h_e[MBPOL_NUM_TERMS];
-    MBPOL_CUDA_OK(cudaMemcpyAsync(h_e, e, sizeof(h_e), cudaMemcpyDeviceToHost, ctx->st));
+    MBPOL_CUDA_OK(cudaMemcpyAsync(h_e, ctx->d_energy.p, sizeof(h_e), cudaMemcpyDeviceToHost, ctx->st));
     if (forces)
         MBPOL_CUDA_OK(cudaMemcpyAsync(ctx->h_force.data(), ctx->d_force.p, sizeof(double) * 3 * ctx->N,
                                       cudaMemcpyDeviceToHost, ctx->st));
     MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
-    MBPOL_CUDA_OK(cudaGetLastError());
     if (energies)
         for (int k = 0; k < MBPOL_NUM_TERMS; ++k) energies[k] = h_e[k];
     if (forces)
         for (size_t i = 0; i < 3 * (size_t)ctx->N; ++i) forces[i] += ctx->h_force[i];
-    if (ctx->elec && (mask & MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS)) && !ctx->elec->converged())
-        return mbpol_fail(MBPOL_ERR_NOT_CONVERGED, ctx->elec->convergence_message());
+    if (s) return s;
+    ctx->forces_valid = mask == MBPOL_ALL_TERMS;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_set_masses(mbpol_context* ctx, const double* masses) {
+    if (!ctx || !masses) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<double> im((size_t)ctx->N);
+    for (int i = 0; i < ctx->N; ++i) {
+        if (!(masses[i] >= 0)) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "negative mass");
+        im[(size_t)i] = masses[i] > 0 ? 1.0 / masses[i] : 0.0;
+    }
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    MBPOL_CUDA_OK(ctx->d_invm.ensure(sizeof(double) * ctx->N));
+    MBPOL_CUDA_OK(cudaMemcpy(ctx->d_invm.p, im.data(), sizeof(double) * ctx->N, cudaMemcpyHostToDevice));
+    ctx->have_masses = true;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_set_velocities(mbpol_context* ctx, const double* v) {
+    if (!ctx || !v) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    MBPOL_CUDA_OK(ctx->d_vel.ensure(sizeof(double) * 3 * ctx->N));
+    MBPOL_CUDA_OK(cudaMemcpy(ctx->d_vel.p, v, sizeof(double) * 3 * ctx->N, cudaMemcpyHostToDevice));
+    ctx->have_vel = true;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_md_run(mbpol_context* ctx, int nsteps, double dt, double temperature, double collision_rate,
+                          unsigned long long seed, double* gpu_ms, double* energies, long* solver_iterations) {
+    if (!ctx || nsteps < 0 || !(dt > 0)) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad MD arguments");
+    if (!ctx->have_pos || !ctx->have_masses || !ctx->have_vel)
+        return mbpol_fail(MBPOL_ERR_STATE, "MD needs positions, masses and velocities");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    if (!ctx->ev0) {
+        MBPOL_CUDA_OK(cudaEventCreate(&ctx->ev0));
+        MBPOL_CUDA_OK(cudaEventCreate(&ctx->ev1));
+    }
+    MBPOL_CUDA_OK(ctx->d_ekin.ensure(sizeof(double)));
+    const double kT = 0.00831446261815324 * temperature;  // kJ/mol
+    ctx->solver_iterations_total = 0;
+    MBPOL_CUDA_OK(cudaEventRecord(ctx->ev0, ctx->st));
+    if (!ctx->forces_valid) {
+        mbpol_status s = compute_device(ctx, MBPOL_ALL_TERMS);
+        if (s) return s;
+        ctx->forces_valid = true;
+    }
+    for (int step = 0; step < nsteps; ++step) {
+        launch_kick_drift(ctx->st, ctx->N, ctx->d_invm.as<double>(), ctx->d_vel.as<double>(), ctx->d_pos.as<double>(),
+                          ctx->d_force.as<double>(), dt);
+        ctx->forces_valid = false;
+        mbpol_status s = compute_device(ctx, MBPOL_ALL_TERMS);
+        if (s) return s;
+        ctx->forces_valid = true;
+        MBPOL_CUDA_OK(cudaMemsetAsync(ctx->d_ekin.p, 0, sizeof(double), ctx->st));
+        launch_kick(ctx->st, ctx->N, ctx->d_invm.as<double>(), ctx->d_vel.as<double>(), ctx->d_force.as<double>(),
+                    dt, kT, collision_rate, seed, ctx->md_step++, ctx->d_ekin.as<double>());
+    }
+    MBPOL_CUDA_OK(cudaEventRecord(ctx->ev1, ctx->st));
+    double h[MBPOL_NUM_TERMS + 1];
+    MBPOL_CUDA_OK(cudaMemcpyAsync(h, ctx->d_energy.p, sizeof(double) * MBPOL_NUM_TERMS, cudaMemcpyDeviceToHost, ctx->st));
+    MBPOL_CUDA_OK(cudaMemcpyAsync(h + MBPOL_NUM_TERMS, ctx->d_ekin.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+    float ms = 0.f;
+    MBPOL_CUDA_OK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    if (gpu_ms) *gpu_ms = ms;
+    if (energies)
+        for (int k = 0; k <= MBPOL_NUM_TERMS; ++k) energies[k] = nsteps > 0 || k < MBPOL_NUM_TERMS ? h[k] : 0.0;
+    if (solver_iterations) *solver_iterations = ctx->solver_iterations_total;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_get_state(mbpol_context* ctx, double* positions, double* velocities, double* forces) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    const size_t nb = sizeof(double) * 3 * ctx->N;
+    if (positions) MBPOL_CUDA_OK(cudaMemcpyAsync(positions, ctx->d_pos.p, nb, cudaMemcpyDeviceToHost, ctx->st));
+    if (velocities && ctx->have_vel) MBPOL_CUDA_OK(cudaMemcpyAsync(velocities, ctx->d_vel.p, nb, cudaMemcpyDeviceToHost, ctx->st));
+    if (forces) MBPOL_CUDA_OK(cudaMemcpyAsync(forces, ctx->d_force.p, nb, cudaMemcpyDeviceToHost, ctx->st));
+    MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
     return MBPOL_OK;
 }
 
@@ -490,5 +634,26 @@ const char* mbpol_status_string(mbpol_status s) {
 }
 
 const char* mbpol_last_error(void) { return g_last_error.c_str(); }
+
+mbpol_status mbpol_profile_enable(int on) {
+    g_prof.on = on != 0;
+    for (auto& r : g_prof.rec) r.clear();
+    g_prof.used = 0;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_profile_read(int kernel, double* total_ms, long* launches) {
+    if (kernel < 0 || kernel >= K_NUM) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad kernel id");
+    double t = 0.0;
+    for (auto& pr : g_prof.rec[kernel]) {
+        MBPOL_CUDA_OK(cudaEventSynchronize(g_prof.pool[pr.second]));
+        float ms = 0.f;
+        MBPOL_CUDA_OK(cudaEventElapsedTime(&ms, g_prof.pool[pr.first], g_prof.pool[pr.second]));
+        t += ms;
+    }
+    if (total_ms) *total_ms = t;
+    if (launches) *launches = (long)g_prof.rec[kernel].size();
+    return MBPOL_OK;
+}
 
 }  // extern "C"

@@ -658,7 +658,8 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                                       const int* __restrict__ nb, const float* __restrict__ nbd,
                                       const int* __restrict__ nnb, int cap, const float* __restrict__ E0,
                                       const float* __restrict__ phi_mu, const float* __restrict__ mu_in,
-                                      float* __restrict__ mu_out, double* __restrict__ eps2) {
+                                      float* __restrict__ mu_out, double* __restrict__ mu_d,
+                                      double* __restrict__ eps2) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     double d2sum = 0.0;
@@ -751,6 +752,7 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
             for (int a = 0; a < K; ++a) {
                 const int i = K * A + a;
                 const f3 mu = ld3(mu_in, i);
+                const double m0 = mu_d[3 * i], m1 = mu_d[3 * i + 1], m2 = mu_d[3 * i + 2];
                 float ex = E[a][0], ey = E[a][1], ez = E[a][2];
                 if (PME) {
                     ex += c_el.self_term * mu.x - c_el.scale[0] * phi_mu[4 * i + 1];
@@ -762,10 +764,16 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                 const double nx = (double)al * ((double)E0[3 * i] + ex);
                 const double ny = (double)al * ((double)E0[3 * i + 1] + ey);
                 const double nz = (double)al * ((double)E0[3 * i + 2] + ez);
-                const double dx = nx - mu.x, dy = ny - mu.y, dz = nz - mu.z;
-                mu_out[3 * i] = (float)(mu.x + kSOR * dx);
-                mu_out[3 * i + 1] = (float)(mu.y + kSOR * dy);
-                mu_out[3 * i + 2] = (float)(mu.z + kSOR * dz);
+                // the dipole state is FP64: FP32 storage alone would put a
+                // floor of ~1e-8 D under the convergence measure
+                const double dx = nx - m0, dy = ny - m1, dz = nz - m2;
+                const double u0 = m0 + kSOR * dx, u1 = m1 + kSOR * dy, u2 = m2 + kSOR * dz;
+                mu_d[3 * i] = u0;
+                mu_d[3 * i + 1] = u1;
+                mu_d[3 * i + 2] = u2;
+                mu_out[3 * i] = (float)u0;
+                mu_out[3 * i + 1] = (float)u1;
+                mu_out[3 * i + 2] = (float)u2;
                 d2sum += dx * dx + dy * dy + dz * dz;
             }
         }
@@ -976,6 +984,11 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
     block_sum_atomic<128>(e_out, energy);
 }
 
+__global__ void widen_kernel(int n, const float* __restrict__ a, double* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = a[i];
+}
+
 // B-spline moduli with the reference's fixes (:1248-1340), host FP64.
 void bspline_moduli(int size, std::vector<double>& mod) {
     const int order = 5;
@@ -1093,7 +1106,7 @@ struct ElecImpl {
     std::vector<int> type;
     DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd, d_gfrac;
     DBuf<int> d_type, d_nb, d_nnb, d_gidx, d_flags;
-    DBuf<double> d_eps2;
+    DBuf<double> d_eps2, d_mud, d_mud_prev;
     int cap = 0;
     // PME
     int grid[3] = {0, 0, 0};
@@ -1181,6 +1194,8 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     MBPOL_CUDA_OK(I.d_nnb.ensure(I.nmol));
     MBPOL_CUDA_OK(I.d_flags.ensure(4));
     MBPOL_CUDA_OK(I.d_eps2.ensure(1));
+    MBPOL_CUDA_OK(I.d_mud.ensure(3 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_mud_prev.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms, kDmsCoef, sizeof(kDmsCoef)));
     MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms_idx, kDmsIdx, sizeof(kDmsIdx)));
     I.have_prev = false;
@@ -1309,9 +1324,11 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         if (s) return s;
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_gridfix.p, I.d_grid.p, sizeof(float) * nreal, cudaMemcpyDeviceToDevice, st));
         pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 10, I.d_gridfix.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_fix.p);
+        prof_begin(st, K_ELEC_FIXED);
         fixed_field_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                            I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_phi_fix.p,
                                                            I.d_E0.p, I.d_mu0.p);
+        prof_end(st, K_ELEC_FIXED);
     } else {
         fixed_field_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p,
                                                             I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
@@ -1323,6 +1340,10 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         // start from the previous call's converged dipoles instead of alpha*E0
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mu0.p, I.d_mu_prev.p, sizeof(float) * 3 * (size_t)n,
                                       cudaMemcpyDeviceToDevice, st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mud.p, I.d_mud_prev.p, sizeof(double) * 3 * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+    } else {
+        widen_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, I.d_mu0.p, I.d_mud.p);
     }
     // solver (reference convergeInduceDipoles :557-616)
     double current = 1.0e+50;
@@ -1333,21 +1354,25 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         float* mu_in = mu[cur];
         float* mu_out = mu[cur ^ 1];
         if (I.pme) {
+            prof_begin(st, K_ELEC_PME);
             MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
             pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 1, nullptr, mu_in, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
             mbpol_status s = pme_convolve(I, st, box);
             if (s) return s;
             pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 4, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
+            prof_end(st, K_ELEC_PME);
         }
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2.p, 0, sizeof(double), st));
+        prof_begin(st, K_ELEC_INDUCED);
         if (I.pme)
             induced_update_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
-                                                                  I.d_phi_mu.p, mu_in, mu_out, I.d_eps2.p);
+                                                                  I.d_phi_mu.p, mu_in, mu_out, I.d_mud.p, I.d_eps2.p);
         else
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                    I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
-                                                                   nullptr, mu_in, mu_out, I.d_eps2.p);
+                                                                   nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p);
+        prof_end(st, K_ELEC_INDUCED);
         double e2 = 0.0;
         MBPOL_CUDA_OK(cudaMemcpyAsync(&e2, I.d_eps2.p, sizeof(double), cudaMemcpyDeviceToHost, st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(st));
@@ -1369,9 +1394,12 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     I.converged = conv;
     I.mu_cur = mu[cur] == I.d_mu0.p ? 0 : 1;
     float* mu_final = mu[cur];
-    if (conv)
+    if (conv) {
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mu_prev.p, mu_final, sizeof(float) * 3 * (size_t)n,
                                       cudaMemcpyDeviceToDevice, st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mud_prev.p, I.d_mud.p, sizeof(double) * 3 * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+    }
     I.have_prev = conv;
     if (I.pme) {
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
@@ -1379,9 +1407,11 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         mbpol_status s = pme_convolve(I, st, box);
         if (s) return s;
         pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 10, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
+        prof_begin(st, K_ELEC_FORCES);
         energy_force_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p, I.d_type.p,
                                                             I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, mu_final,
                                                             I.d_phi_fix.p, I.d_phi_mu.p, redist, force, energy);
+        prof_end(st, K_ELEC_FORCES);
     } else {
         energy_force_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p,
                                                              I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
@@ -1393,9 +1423,8 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
 
 mbpol_status ElecEngine::get_dipoles(cudaStream_t st, double* dipoles, int* iterations, double* epsilon) {
     ElecImpl& I = *impl_;
-    std::vector<float> h(3 * (size_t)I.N);
-    const float* src = I.mu_cur == 0 ? I.d_mu0.p : I.d_mu1.p;
-    MBPOL_CUDA_OK(cudaMemcpyAsync(h.data(), src, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, st));
+    std::vector<double> h(3 * (size_t)I.N);
+    MBPOL_CUDA_OK(cudaMemcpyAsync(h.data(), I.d_mud.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
     MBPOL_CUDA_OK(cudaStreamSynchronize(st));
     if (dipoles)
         for (size_t i = 0; i < h.size(); ++i) dipoles[i] = h[i];

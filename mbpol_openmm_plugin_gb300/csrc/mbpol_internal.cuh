@@ -19,6 +19,12 @@
 
 namespace mbpol {
 
+// Per-kernel CUDA-event timing (enabled with mbpol_profile_enable): ids of
+// the timed kernels.
+enum KernelId { K_POLY2B = 0, K_POLY3B, K_ELEC_FIXED, K_ELEC_INDUCED, K_ELEC_PME, K_ELEC_FORCES, K_NUM };
+void prof_begin(cudaStream_t st, int id);
+void prof_end(cudaStream_t st, int id);
+
 constexpr double kNmToA = 10.0;
 constexpr double kCalToJ = 4.184;
 constexpr float kPiF = 3.14159265358979323846f;

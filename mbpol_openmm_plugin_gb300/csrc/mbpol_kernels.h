@@ -41,6 +41,12 @@ void upload_dispersion_tables(const double* c6_4x4, const double* d6_4x4);
 void launch_dispersion(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, const int* full,
                        const int* nfull, int cap_full, double rc, double* force, double* energy);
 
+// md.cu
+void launch_kick_drift(cudaStream_t st, int n, const double* invm, double* vel, double* pos, const double* force,
+                       double dt);
+void launch_kick(cudaStream_t st, int n, const double* invm, double* vel, const double* force, double dt, double kT,
+                 double nu, unsigned long long seed, unsigned long long step, double* ekin);
+
 // vsites.cu
 void launch_place_vsites(cudaStream_t st, int n, const int4* idx, const double* w, double* pos);
 void launch_spread_vsites(cudaStream_t st, int n, const int4* idx, const double* w, double* force);

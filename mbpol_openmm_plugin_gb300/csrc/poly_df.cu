@@ -17,7 +17,8 @@
 // One thread per unit (dimer or trimer).  The variables x and the gradient
 // pairs (gh, gl) live in shared memory, [variable][thread], so every access
 // of a warp is one conflict-free wavefront; the trie tables are read with
-// warp-uniform addresses.  X, G: [nvars][stride] floats; E: [stride].
+// warp-uniform addresses.  X: [2][nvars][stride] floats (FP64 variables as
+// hi and lo planes); G: [nvars][stride]; E: [stride].
 #include "mbpol_internal.cuh"
 
 namespace mbpol {
@@ -70,8 +71,9 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                                                           const float* __restrict__ X, float* __restrict__ G,
                                                           float* __restrict__ E, int n, int stride) {
     extern __shared__ float smem[];
-    float* xs = smem;                  // [NV][kBlock]
-    float* gh = smem + NV * kBlock;    // [NV][kBlock]
+    float* xs = smem;                  // [NV][kBlock]   variables, high part
+    float* xq = smem + NV * kBlock;    // [NV][kBlock]   variables, low part
+    float* gh = xq + NV * kBlock;      // [NV][kBlock]
     float* gl = gh + NV * kBlock;      // [NV][kBlock]
     const int t = threadIdx.x;
     for (int base = blockIdx.x * kBlock; base < n; base += gridDim.x * kBlock) {
@@ -80,6 +82,7 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
         #pragma unroll
         for (int v = 0; v < NV; ++v) {
             xs[v * kBlock + t] = live ? X[(size_t)v * stride + u] : 0.f;
+            xq[v * kBlock + t] = live ? X[(size_t)(NV + v) * stride + u] : 0.f;
             gh[v * kBlock + t] = 0.f;
             gl[v * kBlock + t] = 0.f;
         }
@@ -87,30 +90,34 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
         int c2 = 0, c3 = 0, cl = 0;
         for (int a = 0; a < n1; ++a) {
             const PolyNode A = l1[a];
-            const float xi = xs[A.var * kBlock + t];
+            const float xi = xs[A.var * kBlock + t], xil = xq[A.var * kBlock + t];
             DF V1 = {A.hi, A.lo};
             for (; c2 < A.end; ++c2) {
                 const PolyNode B = l2[c2];
-                const float xj = xs[B.var * kBlock + t];
+                const float xj = xs[B.var * kBlock + t], xjl = xq[B.var * kBlock + t];
                 DF V2 = {B.hi, B.lo};
                 DF P2;
                 P2.h = __fmul_rn(xi, xj);
                 P2.l = __fmaf_rn(xi, xj, -P2.h);
+                P2.l = __fmaf_rn(xi, xjl, P2.l);
+                P2.l = __fmaf_rn(xil, xj, P2.l);
                 for (; c3 < B.end; ++c3) {
                     const PolyNode C = l3[c3];
-                    const float xk = xs[C.var * kBlock + t];
+                    const float xk = xs[C.var * kBlock + t], xkl = xq[C.var * kBlock + t];
                     DF V3 = {C.hi, C.lo};
                     DF P3;
                     mul_df_f(P2, xk, P3.h, P3.l);
+                    P3.l = __fmaf_rn(P2.h, xkl, P3.l);
                     for (; cl < C.end; ++cl) {
                         const PolyNode L = lv[cl];
                         const int o = L.var * kBlock + t;
-                        const float xl = xs[o];
+                        const float xl = xs[o], xll = xq[o];
                         float p, q;
                         // V3 += c x_l
                         p = __fmul_rn(xl, L.hi);
                         q = __fmaf_rn(xl, L.hi, -p);
                         q = __fmaf_rn(xl, L.lo, q);
+                        q = __fmaf_rn(xll, L.hi, q);
                         acc(V3, p, q);
                         // g_l += c P3
                         p = __fmul_rn(P3.h, L.hi);
@@ -124,6 +131,7 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                     }
                     float p, q;
                     mul_df_f(V3, xk, p, q);
+                    q = __fmaf_rn(V3.h, xkl, q);
                     acc(V2, p, q);
                     mul_df_df(V3, P2, p, q);
                     const int o = C.var * kBlock + t;
@@ -134,8 +142,10 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                 }
                 float p, q;
                 mul_df_f(V2, xj, p, q);
+                q = __fmaf_rn(V2.h, xjl, q);
                 acc(V1, p, q);
                 mul_df_f(V2, xi, p, q);
+                q = __fmaf_rn(V2.h, xil, q);
                 const int o = B.var * kBlock + t;
                 DF g = {gh[o], gl[o]};
                 acc(g, p, q);
@@ -144,6 +154,7 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
             }
             float p, q;
             mul_df_f(V1, xi, p, q);
+            q = __fmaf_rn(V1.h, xil, q);
             acc(Ev, p, q);
             const int o = A.var * kBlock + t;
             DF g = {gh[o], gl[o]};
@@ -188,7 +199,7 @@ cudaError_t poly_tables_upload(int device) {
         return e;
     g_t2.n1 = POLY2B_N1;
     g_t3.n1 = POLY3B_N1;
-    const int sm2 = 3 * 31 * kBlock * (int)sizeof(float), sm3 = 3 * 36 * kBlock * (int)sizeof(float);
+    const int sm2 = 4 * 31 * kBlock * (int)sizeof(float), sm3 = 4 * 36 * kBlock * (int)sizeof(float);
     if ((e = cudaFuncSetAttribute(poly_df_kernel<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm2))) return e;
     if ((e = cudaFuncSetAttribute(poly_df_kernel<36>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm3))) return e;
     g_dev_uploaded = device;
@@ -199,7 +210,7 @@ void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, i
     if (n <= 0) return;
     int blocks = (n + kBlock - 1) / kBlock;
     if (blocks > num_sms * 4) blocks = num_sms * 4;
-    poly_df_kernel<31><<<blocks, kBlock, 3 * 31 * kBlock * sizeof(float), st>>>(g_t2.l1, g_t2.n1, g_t2.l2, g_t2.l3,
+    poly_df_kernel<31><<<blocks, kBlock, 4 * 31 * kBlock * sizeof(float), st>>>(g_t2.l1, g_t2.n1, g_t2.l2, g_t2.l3,
                                                                                 g_t2.lv, X, G, E, n, stride);
 }
 
@@ -207,7 +218,7 @@ void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, i
     if (n <= 0) return;
     int blocks = (n + kBlock - 1) / kBlock;
     if (blocks > num_sms * 4) blocks = num_sms * 4;
-    poly_df_kernel<36><<<blocks, kBlock, 3 * 36 * kBlock * sizeof(float), st>>>(g_t3.l1, g_t3.n1, g_t3.l2, g_t3.l3,
+    poly_df_kernel<36><<<blocks, kBlock, 4 * 36 * kBlock * sizeof(float), st>>>(g_t3.l1, g_t3.n1, g_t3.l2, g_t3.l3,
                                                                                 g_t3.lv, X, G, E, n, stride);
 }
 

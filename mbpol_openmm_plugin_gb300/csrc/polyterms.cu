@@ -5,13 +5,13 @@
 //    ~1% of the work).  Restates
 //    platforms/reference/src/MBPolReferenceOneBodyForce.cpp:69-201.
 //  * two-body: per O-O pair, variables (31 exp/Coulomb-like functions of
-//    site distances incl. two lone-pair X sites per water) in FP32 ->
-//    generated polynomial kernel (poly2b.ptx) -> chain rule + switch in FP32,
-//    FP64 force atomics.  Restates
+//    site distances incl. two lone-pair X sites per water) in FP64 ->
+//    double-float polynomial walk (poly_df.cu) -> chain rule + switch in
+//    FP32, FP64 force atomics.  Restates
 //    platforms/reference/src/MBPolReferenceTwoBodyForce.cpp:110-296 and
 //    mbpol_2body_constants.cpp:10-111.
-//  * three-body: per trimer, 36 exp variables -> poly3b.ptx -> chain rule
-//    and the product switch.  Restates
+//  * three-body: per trimer, 36 exp variables (FP64) -> poly_df.cu -> chain
+//    rule and the product switch in FP32.  Restates
 //    platforms/reference/src/MBPolReferenceThreeBodyForce.cpp:67-293.
 #include "mbpol_internal.cuh"
 #include "mbpol_kernels.h"
@@ -102,6 +102,7 @@ __global__ void onebody_kernel(int nw, const int4* __restrict__ waters, const do
 struct Var2 {
     unsigned char a, b, kind;
     float k, r0;
+    double kd;  // k in FP64 for the variable kernel
 };
 __constant__ Var2 c_v2[31];
 struct TwoBodyParams {
@@ -141,20 +142,54 @@ __device__ __forceinline__ void twobody_sites(const int4 wa, const int4 wb, cons
     }
 }
 
+// The polynomial inputs are computed in FP64 and handed over as FP32
+// (hi, lo) pairs: the monomial sum amplifies input rounding by its
+// cancellation factor, so FP32-rounded variables would cost ~5e-6 relative.
+__device__ __forceinline__ void store_hl(float* __restrict__ X, int idx, int plane, double v) {
+    const float h = (float)v;
+    X[idx] = h;
+    X[idx + plane] = (float)(v - (double)h);
+}
+
+struct d3v {
+    double x, y, z;
+};
+__device__ __forceinline__ d3v dsub(double3 a, double3 b) { return d3v{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ double dnorm(d3v a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
 __global__ void twobody_vars_kernel(int npairs, const int2* __restrict__ pairs, const int4* __restrict__ waters,
                                     const double* __restrict__ pos, Box box, float* __restrict__ X, int stride) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs) return;
     const int2 pr = pairs[p];
-    f3 s[10];
-    twobody_sites(waters[pr.x], waters[pr.y], pos, box, s);
-    #pragma unroll
+    const int4 wa = waters[pr.x], wb = waters[pr.y];
+    double3 S[10];
+    S[0] = load_pos(pos, wa.x);
+    S[1] = image_to(S[0], load_pos(pos, wa.y), box);
+    S[2] = image_to(S[0], load_pos(pos, wa.z), box);
+    S[3] = image_to(S[0], load_pos(pos, wb.x), box);
+    S[4] = image_to(S[3], load_pos(pos, wb.y), box);
+    S[5] = image_to(S[3], load_pos(pos, wb.z), box);
+    const double3 O0 = S[0];
+    for (int i = 0; i < 6; ++i)  // Angstrom, relative to Oa
+        S[i] = make_double3((S[i].x - O0.x) * kNmToA, (S[i].y - O0.y) * kNmToA, (S[i].z - O0.z) * kNmToA);
+    const double gi = -9.721486914088159e-02, go = 9.859272078406150e-02;
+    for (int m = 0; m < 2; ++m) {
+        const double3 O = S[3 * m], H1 = S[3 * m + 1], H2 = S[3 * m + 2];
+        const d3v a = dsub(H1, O), b = dsub(H2, O);
+        const d3v c = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+        const double3 inp = make_double3(O.x + (a.x + b.x) * 0.5 * gi, O.y + (a.y + b.y) * 0.5 * gi,
+                                         O.z + (a.z + b.z) * 0.5 * gi);
+        S[6 + 2 * m] = make_double3(inp.x + c.x * go, inp.y + c.y * go, inp.z + c.z * go);
+        S[7 + 2 * m] = make_double3(inp.x - c.x * go, inp.y - c.y * go, inp.z - c.z * go);
+    }
+    const int plane = 31 * stride;
+    #pragma unroll 1
     for (int n = 0; n < 31; ++n) {
         const Var2 v = c_v2[n];
-        f3 d = s[v.a] - s[v.b];
-        float r = sqrtf(dot(d, d));
-        float e = expf(v.k * (v.r0 - r));
-        X[n * stride + p] = v.kind ? e / r : e;
+        const double r = dnorm(dsub(S[v.a], S[v.b]));
+        const double e = exp((double)v.kd * ((double)v.r0 - r));
+        store_hl(X, n * stride + p, plane, v.kind ? e / r : e);
     }
 }
 
@@ -238,6 +273,7 @@ __global__ void twobody_forces_kernel(int npairs, const int2* __restrict__ pairs
 struct Var3 {
     unsigned char a, b;
     float k, d0;
+    double kd, dd;  // FP64 copies for the variable kernel
 };
 __constant__ Var3 c_v3[36];
 __constant__ float c_3b_rf;  // switch outer radius (A)
@@ -269,14 +305,23 @@ __global__ void threebody_vars_kernel(int ntrip, const int4* __restrict__ trips,
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntrip) return;
     const int4 tr = trips[t];
-    f3 s[9];
-    threebody_sites(waters[tr.x], waters[tr.y], waters[tr.z], pos, box, s);
-    #pragma unroll
+    const int4 wa = waters[tr.x], wb = waters[tr.y], wc = waters[tr.z];
+    double3 S[9];
+    S[0] = load_pos(pos, wa.x);
+    S[1] = image_to(S[0], load_pos(pos, wa.y), box);
+    S[2] = image_to(S[0], load_pos(pos, wa.z), box);
+    S[3] = image_to(S[0], load_pos(pos, wb.x), box);
+    S[4] = image_to(S[3], load_pos(pos, wb.y), box);
+    S[5] = image_to(S[3], load_pos(pos, wb.z), box);
+    S[6] = image_to(S[0], load_pos(pos, wc.x), box);
+    S[7] = image_to(S[6], load_pos(pos, wc.y), box);
+    S[8] = image_to(S[6], load_pos(pos, wc.z), box);
+    const int plane = 36 * stride;
+    #pragma unroll 1
     for (int n = 0; n < 36; ++n) {
         const Var3 v = c_v3[n];
-        f3 d = s[v.a] - s[v.b];
-        float r = sqrtf(dot(d, d));
-        X[n * stride + t] = expf(-v.k * (r - v.d0));
+        const double r = dnorm(dsub(S[v.a], S[v.b])) * kNmToA;
+        store_hl(X, n * stride + t, plane, exp(-v.kd * (r - v.dd)));
     }
 }
 
@@ -367,7 +412,7 @@ void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245)
     const float kHHc = 1.148231864355956e+00f, kOHc = 1.205989761123099e+00f, kOOc = 1.395357065790959e+00f;
     const float kXH = 7.347036852042255e-01f, kXO = 7.998249864422826e-01f, kXX = 7.960663960630585e-01f;
     const Var2 v2[31] = {
-        {1, 2, 0, kHHi, 1.f}, {4, 5, 0, kHHi, 1.f}, {0, 1, 0, kOHi, 1.f}, {0, 2, 0, kOHi, 1.f},
+        {1, 2, 0, kHHi, 1.f, 0.0}, {4, 5, 0, kHHi, 1.f}, {0, 1, 0, kOHi, 1.f}, {0, 2, 0, kOHi, 1.f},
         {3, 4, 0, kOHi, 1.f}, {3, 5, 0, kOHi, 1.f}, {1, 4, 1, kHHc, 4.f}, {1, 5, 1, kHHc, 4.f},
         {2, 4, 1, kHHc, 4.f}, {2, 5, 1, kHHc, 4.f}, {0, 4, 1, kOHc, 4.f}, {0, 5, 1, kOHc, 4.f},
         {3, 1, 1, kOHc, 4.f}, {3, 2, 1, kOHc, 4.f}, {0, 3, 1, kOOc, 4.f}, {6, 4, 0, kXH, 4.f},
@@ -375,7 +420,16 @@ void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245)
         {8, 2, 0, kXH, 4.f},  {9, 1, 0, kXH, 4.f},  {9, 2, 0, kXH, 4.f},  {0, 8, 0, kXO, 4.f},
         {0, 9, 0, kXO, 4.f},  {3, 6, 0, kXO, 4.f},  {3, 7, 0, kXO, 4.f},  {6, 8, 0, kXX, 4.f},
         {6, 9, 0, kXX, 4.f},  {7, 8, 0, kXX, 4.f},  {7, 9, 0, kXX, 4.f}};
-    cudaMemcpyToSymbol(c_v2, v2, sizeof(v2));
+    Var2 v2d[31];
+    const double kd2[8] = {-6.480884773303821e-01, 1.674518993682975e+00, 1.148231864355956e+00, 1.205989761123099e+00,
+                           1.395357065790959e+00, 7.347036852042255e-01, 7.998249864422826e-01, 7.960663960630585e-01};
+    const float kf2[8] = {kHHi, kOHi, kHHc, kOHc, kOOc, kXH, kXO, kXX};
+    for (int n = 0; n < 31; ++n) {
+        v2d[n] = v2[n];
+        for (int q = 0; q < 8; ++q)
+            if (v2[n].k == kf2[q]) v2d[n].kd = kd2[q];
+    }
+    cudaMemcpyToSymbol(c_v2, v2d, sizeof(v2d));
     TwoBodyParams tp = {-9.721486914088159e-02f, 9.859272078406150e-02f, 4.5f, 6.5f};
     cudaMemcpyToSymbol(c_2b, &tp, sizeof(tp));
 
@@ -393,7 +447,21 @@ void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245)
         {3, 1, kOH, dOH},    {3, 2, kOH, dOH},    {3, 7, kOH, dOH},    {3, 8, kOH, dOH},    {6, 1, kOH, dOH},
         {6, 2, kOH, dOH},    {6, 4, kOH, dOH},    {6, 5, kOH, dOH},    {0, 3, kOO, dOO},    {0, 6, kOO, dOO},
         {3, 6, kOO, dOO}};
-    cudaMemcpyToSymbol(c_v3, v3, sizeof(v3));
+    Var3 v3d[36];
+    const double kd3[5] = {-2.254303257872797e+00, -2.564771901404151e-01, 4.247920544074333e-01,
+                           8.128985941165371e-01, 3.749457984616480e-02};
+    const float kf3[5] = {kHHi3, kOHi3, kHH, kOH, kOO};
+    const double dd3[5] = {1.690594510379166e+00, -2.999999868517452e+00, 3.499031358429095e+00,
+                           4.854042963514281e+00, 4.816312044947604e-08};
+    for (int n = 0; n < 36; ++n) {
+        v3d[n] = v3[n];
+        for (int q = 0; q < 5; ++q)
+            if (v3[n].k == kf3[q]) {
+                v3d[n].kd = kd3[q];
+                v3d[n].dd = dd3[q];
+            }
+    }
+    cudaMemcpyToSymbol(c_v3, v3d, sizeof(v3d));
     const float rf = 4.5f;
     cudaMemcpyToSymbol(c_3b_rf, &rf, sizeof(rf));
 }

@@ -187,6 +187,54 @@ def main():
             r["e1"], r["e2"], r["e3"], ed, r["npairs"], r["ntrip"]))
 
 
+def read_pdb(path):
+    xyz = []
+    for ln in open(path):
+        if ln.startswith(("ATOM", "HETATM")):
+            xyz.append([float(ln[30:38]), float(ln[38:46]), float(ln[46:54])])
+    return np.array(xyz) * 0.1
+
+
+def main_pdb():
+    """Full-model energies of the reference's integration-test configurations
+    (python/tests/pdb_files, boxes and expected totals from
+    python/tests/TestReferenceMBPolIntegrationTest.py:12-64 and
+    TestReferenceMBPol14WaterTest.py:14-22).  PME alpha and grid are explicit
+    (OpenMM's rule at the force's default tolerance 1e-4), since the
+    reference takes them from OpenMM's calcPMEParameters."""
+    L = lib()
+    sys.path.insert(0, ROOT)
+    from mbpol_openmm_plugin_gb300.plugin import pme_parameters
+    pdbdir = os.path.join(REF, "python", "tests", "pdb_files")
+    cases = [("water3", "water3.pdb", None, -8.78893485, 0.1), ("water14", "water14.pdb", None, None, None),
+             ("water14_pme", "water14.pdb", 1.8, -60.0, 1.0), ("water50_pme", "water50.pdb", 1.8, -244.37507, 1.0),
+             ("water256_pme", "water256_integration_test.pdb", 1.93996888399961804, -2270.88890, 20.0)]
+    for name, fn, boxL, expected, tol in cases:
+        pos = place_m(read_pdb(os.path.join(pdbdir, fn)))
+        nw = pos.shape[0] // 4
+        waters = np.stack([4 * np.arange(nw), 4 * np.arange(nw) + 1, 4 * np.arange(nw) + 2], 1).astype(np.int32)
+        box = None if boxL is None else np.array([boxL] * 3)
+        r = run_terms(L, pos, waters, box)
+        ed, fd = dispersion_oracle(pos, waters, box, 0.9 if box is not None else 1e30)
+        if box is None:
+            ee, fe, dip, it = electrostatics(L, pos, None, False, eps=1e-8)
+            alpha, grid = 0.0, [0, 0, 0]
+        else:
+            alpha, grid = pme_parameters(box, 0.9, 1e-4)
+            ee, fe, dip, it = electrostatics(L, pos, box, True, alpha=alpha, grid=grid, eps=1e-8)
+        etot = r["e1"] + r["e2"] + r["e3"] + ed + ee
+        ftot = r["f1"] + r["f2"] + r["f3"] + fd + fe
+        np.savez_compressed(os.path.join(HERE, "pdb_%s.npz" % name), positions=pos,
+                            box=np.zeros(3) if box is None else box, periodic=box is not None, alpha=alpha,
+                            grid=np.array(grid), e1=r["e1"], e2=r["e2"], e3=r["e3"], edisp=ed, eelec=ee,
+                            etotal=etot, ftotal=ftot, f1=r["f1"], f2=r["f2"], f3=r["f3"], fdisp=fd, felec=fe,
+                            iterations=it, ntrip=r["ntrip"], npairs=r["npairs"],
+                            expected_kcal=np.nan if expected is None else expected,
+                            expected_tol_kcal=np.nan if tol is None else tol)
+        print("%-14s total %.5f kcal/mol (reference test expects %s +- %s); elec %.4f it %d" % (
+            name, etot / 4.184, expected, tol, ee / 4.184, it))
+
+
 def main_elec():
     L = lib()
     tests = os.path.join(REF, "platforms", "reference", "tests")
@@ -221,6 +269,9 @@ def main_elec():
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "elec":
         main_elec()
+    elif len(sys.argv) > 2 and sys.argv[2] == "pdb":
+        main_pdb()
     else:
         main()
         main_elec()
+        main_pdb()
