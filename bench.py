@@ -1,0 +1,283 @@
+#!/usr/bin/env python3
+"""MB-pol molecular-dynamics throughput on one GB300.
+
+Workload (default): 4096 waters in a 4.967 nm cubic box (jittered 16^3
+lattice, seeded; mbpol_openmm_plugin_gb300.systems.workload("box4096")),
+the full MB-pol model (1B, 2B, 3B, electrostatics with PME at a 0.9 nm
+real-space cutoff and Ewald tolerance 1e-5, induced dipoles converged to
+1e-8 D, dispersion), NVE velocity Verlet at 0.2 fs.  A "step" is one MD step:
+one full force/energy evaluation plus the integration.
+
+  value  ns/day with everything resident in HBM (mbpol_md_run; CUDA events
+         on the library's stream around the K timed steps)
+  e2e    ns/day through the public API with host buffers: every step copies
+         positions host->device (mbpol_set_positions), evaluates, and copies
+         forces and energies device->host (mbpol_compute); the integration is
+         done on the host, as OpenMM drives the reference plugin.
+
+Inputs (positions, velocities) are ~0.4 MB; the per-step working set is a few
+hundred MB of pair/trimer buffers and PME grids, larger than L2 only in part,
+so config["l2"] states that no flush is done between steps.
+
+--impl reference times the reference's algorithm on the host cores: the
+oracle's C port (the reference's own CPU code cannot be built on the GPU
+host) over a bounded sample of the same workload, extrapolated to one step.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DT_PS = 0.0002  # 0.2 fs
+
+
+def ns_per_day(seconds_per_step):
+    return DT_PS * 1e-3 * 86400.0 / seconds_per_step
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle reasons sampled during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(name, seed, guess):
+    import mbpol_openmm_plugin_gb300 as mb
+    from mbpol_openmm_plugin_gb300 import systems
+    ws = systems.workload(name, seed)
+    alpha, grid = mb.pme_parameters(ws.box, 0.9, 1e-5)
+    sysm = mb.create_mbpol_system(ws, ewald_alpha=alpha, pme_grid=grid, ewald_tol=1e-5, target_epsilon=1e-8,
+                                  guess=guess)
+    return ws, sysm, alpha, grid
+
+
+def maxwell_boltzmann(masses, T, seed):
+    rng = np.random.default_rng(seed + 7)
+    kT = 0.00831446261815324 * T
+    v = np.zeros((len(masses), 3))
+    for i, m in enumerate(masses):
+        if m > 0:
+            v[i] = rng.normal(0.0, np.sqrt(kT / m), 3)
+    return v
+
+
+def fp32_ops_per_unit(name):
+    """FP32 operations (add/sub/mul = 1, fma = 2) of the double-float walk per
+    dimer/trimer, counted from the trie sizes (csrc/poly_df.cu):
+    leaf 32, level-3 node 38, level-2 node 36, level-1 node 28."""
+    path = os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "csrc", "gen", "%s_tables.inc" % name)
+    sizes = {}
+    for ln in open(path):
+        if ln.startswith("#define"):
+            _, k, v = ln.split()
+            sizes[k.split("_")[-1]] = int(v)
+    return 32 * sizes["NL"] + 38 * sizes["N3"] + 36 * sizes["N2"] + 28 * sizes["N1"]
+
+
+def run_ours(args):
+    import mbpol_openmm_plugin_gb300 as mb
+    from mbpol_openmm_plugin_gb300 import _capi
+    lib = _capi.load()
+    guess = 2 if args.guess == "learned" else 1
+    ws, sysm, alpha, grid = build_workload(args.workload, args.seed, guess)
+    ctx = mb.Context(sysm)
+    ctx.setPositions(ws.positions)
+    ctx._build()
+    h = ctx._h
+    box = np.ascontiguousarray(ws.box, np.float64)
+    pos = np.ascontiguousarray(ws.positions, np.float64)
+    masses = np.array(sysm.masses)
+    vel = maxwell_boltzmann(masses, 300.0, args.seed)
+    _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), _capi.ptr(box)))
+    _capi.check(lib.mbpol_set_masses(h, _capi.ptr(np.ascontiguousarray(masses))))
+    _capi.check(lib.mbpol_set_velocities(h, _capi.ptr(np.ascontiguousarray(vel))))
+    ms = ctypes.c_double()
+    iters = ctypes.c_long()
+    en = np.zeros(6)
+    # warm-up (includes the first force evaluation and buffer growth)
+    _capi.check(lib.mbpol_md_run(h, args.warmup, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(ms), _capi.ptr(en),
+                                 ctypes.byref(iters)))
+    counts = ctx.getCounts()
+    # timed region: device resident
+    sampler = ClockSampler()
+    sampler.start()
+    lib.mbpol_profile_enable(1)
+    l0 = lib.mbpol_launch_count()
+    _capi.check(lib.mbpol_md_run(h, args.steps, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(ms), _capi.ptr(en),
+                                 ctypes.byref(iters)))
+    launches = int(lib.mbpol_launch_count() - l0)
+    clocks = sampler.stop()
+    gpu_ms = ms.value
+    kern = {}
+    for kid, kname in enumerate(_capi.KERNELS):
+        t = ctypes.c_double()
+        n = ctypes.c_long()
+        lib.mbpol_profile_read(kid, ctypes.byref(t), ctypes.byref(n))
+        kern[kname] = {"total_ms": t.value, "launches": n.value}
+    lib.mbpol_profile_enable(0)
+    step_s = gpu_ms / 1e3 / args.steps
+    value = ns_per_day(step_s)
+    solver_it = iters.value / max(args.steps, 1)
+
+    # e2e: public API with host buffers, host-side velocity Verlet
+    hpos = np.zeros_like(pos)
+    hvel = np.zeros_like(pos)
+    hf = np.zeros_like(pos)
+    _capi.check(lib.mbpol_get_state(h, _capi.ptr(hpos), _capi.ptr(hvel), _capi.ptr(hf)))
+    invm = np.where(masses > 0, 1.0 / np.where(masses > 0, masses, 1.0), 0.0)[:, None]
+    e5 = np.zeros(5)
+    forces = hf.copy()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        hvel += 0.5 * DT_PS * forces * invm
+        hpos += DT_PS * hvel * (invm > 0)
+        _capi.check(lib.mbpol_set_positions(h, _capi.ptr(hpos), _capi.ptr(box)))
+        forces[:] = 0.0
+        _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
+        hvel += 0.5 * DT_PS * forces * invm
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    n = pos.shape[0]
+
+    # roofline of the dominant kernel (by measured time)
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    roof = None
+    if dom in ("poly3b", "poly2b") and kern[dom]["launches"]:
+        units = int(counts[1] if dom == "poly3b" else counts[0])
+        ops = fp32_ops_per_unit(dom)
+        per_launch_ms = kern[dom]["total_ms"] / kern[dom]["launches"]
+        achieved = units * ops / (per_launch_ms * 1e-3) / 1e12
+        sm_mhz = clocks.get("sm_mhz") or 2070.0
+        peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "work": "%d units x %d FP32 flop (double-float walk)" % (units, ops),
+                "peak_kind": "nominal FP32 FMA rate at the median sampled SM clock (152 SM x 128 lanes x 2)",
+                "launch_ms": per_launch_ms}
+    out = {
+        "metric": "ns/day @4096 H2O PME, learned-guess vs plain GPU at <=1e-4 rel RMS force err",
+        "value": value, "unit": "ns/day", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "replicas", "vs_baseline": None,
+        "dtype": "fp32+double-float polynomials, fp64 accumulation", "data": "synthetic (seeded lattice box)",
+        "config": {"workload": args.workload, "waters": n // 4, "box_nm": float(ws.box[0]), "pme_alpha": alpha,
+                   "pme_grid": grid, "cutoff_nm": 0.9, "ewald_tol": 1e-5, "target_epsilon_D": 1e-8,
+                   "dt_fs": 0.2, "guess": args.guess, "seed": args.seed,
+                   "l2": "no flush; per-step buffers (pair/trimer variables, PME grids) exceed L2 in part"},
+        "e2e": {"value": ns_per_day(e2e_s), "unit": "ns/day", "h2d_bytes_per_step": int(pos.nbytes),
+                "d2h_bytes_per_step": int(pos.nbytes + 5 * 8)},
+        "gpu_launches": launches,
+        "solver_iterations_per_step": solver_it,
+        "counts": {"pairs_2b": int(counts[0]), "trimers": int(counts[1])},
+        "kernels_ms_per_step": {k: v["total_ms"] / args.steps for k, v in kern.items()},
+        "clocks": clocks,
+        "roofline": roof,
+        "energies_kJ_mol": {"1b": en[0], "2b": en[1], "3b": en[2], "elec": en[3], "disp": en[4], "kinetic": en[5]},
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, sample=True)
+    return out
+
+
+def cpu_baseline(args, sample=True):
+    """The oracle's C port on the host (single thread, as the reference's
+    Reference platform), on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    try:
+        import oracle
+        return oracle.time_reference_step(args.workload, args.seed, budget_s=args.cpu_budget)
+    except Exception as ex:  # the port not built / not available
+        return {"value": None, "unit": "ns/day", "cores": 1, "kind": "port", "sample": "unavailable: %s" % ex}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="box4096")
+    ap.add_argument("--guess", default="plain", choices=["plain", "learned"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(args)
+        out = {"impl": "reference", "metric": "ns/day @4096 H2O PME, learned-guess vs plain GPU at <=1e-4 rel RMS force err",
+               "value": cb.get("value"), "unit": "ns/day", "n_gpus": args.gpus, "steps": args.steps,
+               "warmup": args.warmup, "higher_is_better": True, "config": {"workload": args.workload, "seed": args.seed},
+               "cpu_baseline": cb,
+               "e2e": {"value": cb.get("value"), "unit": "ns/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if cb.get("value") is None:
+            out = {"impl": "reference", "unavailable": cb.get("sample")}
+        print(json.dumps(out))
+        return
+    # one process per GPU; this path does not shard (a single periodic box):
+    # extra ranks run independent replicas
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.gpus > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    out = run_ours(args)
+    if rank == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -164,6 +164,8 @@ mbpol_status mbpol_get_counts(mbpol_context* ctx, long* counts4);
  * convolution, inverse FFT, gather), 5 electrostatic energy/forces.
  * Enabling clears previous records; read returns the summed time and count. */
 mbpol_status mbpol_profile_enable(int on);
+/* Kernels launched by this library so far (cuFFT's internal launches excluded). */
+unsigned long long mbpol_launch_count(void);
 mbpol_status mbpol_profile_read(int kernel, double* total_ms, long* launches);
 
 const char* mbpol_status_string(mbpol_status s);

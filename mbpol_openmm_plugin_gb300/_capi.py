@@ -26,7 +26,7 @@ EXPORTED = [
     "mbpol_add_threebody_force", "mbpol_add_electrostatics_force", "mbpol_add_dispersion_force",
     "mbpol_set_positions", "mbpol_compute", "mbpol_set_masses", "mbpol_set_velocities", "mbpol_md_run",
     "mbpol_get_state", "mbpol_get_induced_dipoles", "mbpol_get_counts",
-    "mbpol_profile_enable", "mbpol_profile_read", "mbpol_status_string", "mbpol_last_error",
+    "mbpol_profile_enable", "mbpol_profile_read", "mbpol_launch_count", "mbpol_status_string", "mbpol_last_error",
 ]
 KERNELS = ["poly2b", "poly3b", "elec_fixed_field", "elec_induced_update", "elec_pme_dipoles", "elec_energy_forces"]
 
@@ -85,6 +85,7 @@ def load(path=None):
         "mbpol_get_induced_dipoles": (I, [P, P, ctypes.POINTER(I), ctypes.POINTER(D)]),
         "mbpol_get_counts": (I, [P, P]),
         "mbpol_profile_enable": (I, [I]),
+        "mbpol_launch_count": (ctypes.c_ulonglong, []),
         "mbpol_profile_read": (I, [I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_long)]),
         "mbpol_status_string": (ctypes.c_char_p, [I]),
         "mbpol_last_error": (ctypes.c_char_p, []),

@@ -46,6 +46,8 @@ struct Profiler {
     }
 };
 Profiler g_prof;
+unsigned long long g_launches = 0;
+void count_launch() { ++g_launches; }
 size_t g_open[K_NUM];
 
 void prof_begin(cudaStream_t st, int id) {
@@ -634,6 +636,8 @@ const char* mbpol_status_string(mbpol_status s) {
 }
 
 const char* mbpol_last_error(void) { return g_last_error.c_str(); }
+
+unsigned long long mbpol_launch_count(void) { return g_launches; }
 
 mbpol_status mbpol_profile_enable(int on) {
     g_prof.on = on != 0;

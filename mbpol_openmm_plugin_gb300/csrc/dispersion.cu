@@ -97,6 +97,7 @@ void launch_dispersion(cudaStream_t st, int nw, const int4* waters, const double
     if (nw <= 0 || cap_full <= 0) return;
     const long total = (long)nw * cap_full;
     const float rc2 = rc > 1e15 ? 3.0e38f : (float)(rc * rc);
+    count_launch();
     dispersion_kernel<<<(int)((total + 127) / 128), 128, 0, st>>>(nw, waters, pos, box, full, nfull, cap_full, rc2,
                                                                    force, energy);
 }

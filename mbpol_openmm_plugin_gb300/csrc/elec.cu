@@ -51,8 +51,24 @@ struct ElecConst {
     int grid[3];
     float scale[3];       // grid / box
     double box[3], inv[3];
+    float boxf[3], invf[3];
+    int periodic;         // per-site-pair minimum image (PME)
 };
 __constant__ ElecConst c_el;
+
+// Site-site vector from the molecule O-O vector and the intramolecular
+// offsets, re-imaged per site pair as the reference does
+// (getPeriodicDelta, MBPolReferenceElectrostaticsForce.cpp:1226-1231): near
+// half the box a site pair's minimum image can differ from its molecules'.
+__device__ __forceinline__ f3 site_delta(const f3 dOO, const f3 offb, const f3 offa) {
+    f3 d = dOO + offb - offa;
+    if (c_el.periodic) {
+        d.x -= c_el.boxf[0] * rintf(d.x * c_el.invf[0]);
+        d.y -= c_el.boxf[1] * rintf(d.y * c_el.invf[1]);
+        d.z -= c_el.boxf[2] * rintf(d.z * c_el.invf[2]);
+    }
+    return d;
+}
 
 // ------------------------------------------------------------ Thole scales
 // u = r / (alpha_i alpha_j)^(1/6); x = gamma u^4.  Orders as
@@ -588,7 +604,7 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
             #pragma unroll
             for (int b = 0; b < kMaxK; ++b) {
                 if (b >= K || MB.q[b] == 0.f) continue;
-                const f3 d = dAB + MB.off[b] - MA.off[a];  // r_b - r_a
+                const f3 d = site_delta(dAB, MB.off[b], MA.off[a]);  // r_b - r_a
                 const float r2 = dot(d, d);
                 if (PME && r2 > c_el.rc2) continue;
                 const float r = sqrtf(r2);
@@ -694,7 +710,7 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                 #pragma unroll
                 for (int a = 0; a < kMaxK; ++a) {
                     if (a >= K) continue;
-                    const f3 d = dAB + offb - offA[a];
+                    const f3 d = site_delta(dAB, offb, offA[a]);
                     const float r2 = dot(d, d);
                     if (PME && r2 > c_el.rc2) continue;
                     const float r = sqrtf(r2);
@@ -816,7 +832,9 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
         float F[kMaxK][3], P[kMaxK];  // force on A's sites (before * f), potential (for dq terms)
         #pragma unroll
         for (int a = 0; a < kMaxK; ++a) F[a][0] = F[a][1] = F[a][2] = P[a] = 0.f;
-        float e = 0.f;
+        // the energy is summed in FP64 from FP32 inputs (pair terms of tens of
+        // kJ/mol cancel to the total)
+        double e = 0.0;
         const int n = min(nnb[A], cap);
         const float gcc = c_el.thole[0], gcd = c_el.thole[1], gdd = c_el.thole[2];
         for (int t = lane; t < n; t += 32) {
@@ -831,7 +849,7 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                 #pragma unroll
                 for (int a = 0; a < kMaxK; ++a) {
                     if (a >= K) continue;
-                    const f3 d = dAB + offb - offA[a];  // r_b - r_a  (A = i, B = j)
+                    const f3 d = site_delta(dAB, offb, offA[a]);  // r_b - r_a  (A = i, B = j)
                     const float r2 = dot(d, d);
                     if (PME && r2 > c_el.rc2) continue;
                     const float r = sqrtf(r2);
@@ -846,8 +864,17 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                         const Bn bn = ewald_bn(r, r2);
                         const float s1CC = gl0 != 0.f || qb != 0.f ? s1_of(tCC, gcc) : 1.f;
                         const float s3CD = s3_of(tCD);
-                        e += 0.5f * (bn.b0 * gl0 + 0.5f * bn.b1 * gli - rr1 * gl0 * (1.f - s1CC) -
-                                     0.5f * rr3 * gli * (1.f - s3CD));
+                        {
+                            const double rd = sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z);
+                            const double r1d = 1.0 / rd, r3d = r1d / (rd * rd);
+                            const double gl0d = (double)qA[a] * qb;
+                            const double glid = (double)qb * ((double)muA[a].x * d.x + (double)muA[a].y * d.y +
+                                                              (double)muA[a].z * d.z) -
+                                                (double)qA[a] * ((double)mub.x * d.x + (double)mub.y * d.y +
+                                                                 (double)mub.z * d.z);
+                            e += 0.5 * ((double)bn.b0 * gl0d + 0.5 * (double)bn.b1 * glid -
+                                        r1d * gl0d * (1.0 - (double)s1CC) - 0.5 * r3d * glid * (1.0 - (double)s3CD));
+                        }
                         P[a] += qb * (bn.b0 - rr1 * (1.f - s1CC)) - sci4 * (bn.b1 - rr3 * (1.f - s3CD));
                         const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
                         const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
@@ -862,7 +889,16 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                         fo = d * c_d + muA[a] * (c_i + sci4 * c_dd) + mub * (c_j + sci3 * c_dd);
                     } else {
                         const float s1CC = s1_of(tCC, gcc), s3CD = s3_of(tCD);
-                        e += 0.5f * (rr1 * gl0 * s1CC + 0.5f * rr3 * gli * s3CD);
+                        {
+                            const double rd = sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z);
+                            const double r1d = 1.0 / rd, r3d = r1d / (rd * rd);
+                            const double gl0d = (double)qA[a] * qb;
+                            const double glid = (double)qb * ((double)muA[a].x * d.x + (double)muA[a].y * d.y +
+                                                              (double)muA[a].z * d.z) -
+                                                (double)qA[a] * ((double)mub.x * d.x + (double)mub.y * d.y +
+                                                                 (double)mub.z * d.z);
+                            e += 0.5 * (r1d * gl0d * (double)s1CC + 0.5 * r3d * glid * (double)s3CD);
+                        }
                         const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
                         const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
                         const float gf0 = rr3 * gl0 * s3CC;
@@ -884,7 +920,8 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                 }
             }
         }
-        e = warp_sum(e);
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
         #pragma unroll
         for (int a = 0; a < kMaxK; ++a) {
             F[a][0] = warp_sum(F[a][0]);
@@ -911,7 +948,16 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                         const float gl0 = qA[a] * qA[b];
                         const float gli = qA[b] * sci3 - qA[a] * sci4;
                         // same water: s1CC = s3CD = s3CC = s5CD = 0
-                        e += bn.b0 * gl0 + 0.5f * bn.b1 * gli - rr1 * gl0 - 0.5f * rr3 * gli;
+                        {
+                            const double rd = sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z);
+                            const double r1d = 1.0 / rd, r3d = r1d / (rd * rd);
+                            const double gl0d = (double)qA[a] * qA[b];
+                            const double glid = (double)qA[b] * ((double)muA[a].x * d.x + (double)muA[a].y * d.y +
+                                                                 (double)muA[a].z * d.z) -
+                                                (double)qA[a] * ((double)muA[b].x * d.x + (double)muA[b].y * d.y +
+                                                                 (double)muA[b].z * d.z);
+                            e += (double)bn.b0 * gl0d + 0.5 * (double)bn.b1 * glid - r1d * gl0d - 0.5 * r3d * glid;
+                        }
                         P[a] += qA[b] * (bn.b0 - rr1) - sci4 * (bn.b1 - rr3);
                         P[b] += qA[a] * (bn.b0 - rr1) + sci3 * (bn.b1 - rr3);
                         const float gf1 = bn.b1 * gl0, gfr1 = rr3 * gl0;
@@ -944,9 +990,10 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                     const float* pf = phi_fix + 10 * i;
                     const float* pm = phi_mu + 10 * i;
                     // energies: fixed 0.5 q phi, induced 0.5 mu . grad phi_fixed, self -q^2 alpha/sqrt(pi)
-                    e += 0.5f * qA[a] * pf[0];
-                    e += 0.5f * (sx * muA[a].x * pf[1] + sy * muA[a].y * pf[2] + sz * muA[a].z * pf[3]);
-                    e += -qA[a] * qA[a] * ak / kSqrtPiF;
+                    e += 0.5 * (double)qA[a] * pf[0];
+                    e += 0.5 * ((double)sx * muA[a].x * pf[1] + (double)sy * muA[a].y * pf[2] +
+                                (double)sz * muA[a].z * pf[3]);
+                    e += -(double)qA[a] * qA[a] * ak / kSqrtPi;
                     P[a] += pf[0] + pm[0] - 2.f * qA[a] * ak / kSqrtPiF;
                     // hessian index of (a, k): xx 4, yy 5, zz 6, xy 7, xz 8, yz 9
                     const int H[3][3] = {{4, 7, 8}, {7, 5, 9}, {8, 9, 6}};
@@ -978,7 +1025,7 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                 force[3 * i + 1] += (double)F[a][1] * f;
                 force[3 * i + 2] += (double)F[a][2] * f;
             }
-            e_out = (double)e * f;
+            e_out = e * kElectric;
         }
     }
     block_sum_atomic<128>(e_out, energy);
@@ -1263,6 +1310,7 @@ static mbpol_status pme_convolve(ElecImpl& I, cudaStream_t st, const Box& box) {
     const float scalef = (float)(1.0 / (M_PI * box.L[0] * box.L[1] * box.L[2]));
     const long total = (long)I.grid[0] * I.grid[1] * nzh;
     int blocks = (int)std::min<long>((total + 255) / 256, 152L * 16);
+    count_launch();
     pme_convolve_kernel<<<blocks, 256, 0, st>>>(I.d_cgrid.p, I.d_bx.p, I.d_by.p, I.d_bz.p, expf_, scalef, nzh);
     if (cufftExecC2R(I.plan_b, I.d_cgrid.p, I.d_grid.p) != CUFFT_SUCCESS)
         return mbpol_fail(MBPOL_ERR_CUDA, "cufftExecC2R failed");
@@ -1292,9 +1340,13 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         c.box[d] = box.periodic ? box.L[d] : 1.0;
         c.inv[d] = box.periodic ? box.inv[d] : 1.0;
         c.scale[d] = I.pme ? (float)(I.grid[d] * box.inv[d]) : 0.f;
+        c.boxf[d] = (float)c.box[d];
+        c.invf[d] = (float)c.inv[d];
     }
+    c.periodic = I.pme ? 1 : 0;
     MBPOL_CUDA_OK(cudaMemcpyToSymbolAsync(c_el, &c, sizeof(c), 0, cudaMemcpyHostToDevice, st));
     const int redist = I.prm.include_charge_redistribution ? 1 : 0;
+    count_launch();
     elec_prepare_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, pos, box.periodic, redist, I.d_qs.p, I.d_off.p,
                                                             I.d_q.p, I.d_dq.p, I.pme ? 1 : 0, I.d_gidx.p, I.d_gfrac.p);
     // neighbour list
@@ -1304,6 +1356,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         MBPOL_CUDA_OK(I.d_nb.ensure((size_t)nmol * I.cap));
         MBPOL_CUDA_OK(I.d_nbd.ensure((size_t)nmol * I.cap * 3));
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_flags.p, 0, sizeof(int), st));
+        count_launch();
         elec_neighbors_kernel<<<(nmol * 32 + 127) / 128, 128, 0, st>>>(
             nmol, pos, box.periodic && I.pme, rlist * rlist, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.d_flags.p,
             nullptr);
@@ -1319,17 +1372,21 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     // fixed field
     if (I.pme) {
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
+        count_launch();
         pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 0, I.d_q.p, nullptr, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
         mbpol_status s = pme_convolve(I, st, box);
         if (s) return s;
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_gridfix.p, I.d_grid.p, sizeof(float) * nreal, cudaMemcpyDeviceToDevice, st));
+        count_launch();
         pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 10, I.d_gridfix.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_fix.p);
         prof_begin(st, K_ELEC_FIXED);
+        count_launch();
         fixed_field_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                            I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_phi_fix.p,
                                                            I.d_E0.p, I.d_mu0.p);
         prof_end(st, K_ELEC_FIXED);
     } else {
+        count_launch();
         fixed_field_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p,
                                                             I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
                                                             nullptr, I.d_E0.p, I.d_mu0.p);
@@ -1343,6 +1400,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mud.p, I.d_mud_prev.p, sizeof(double) * 3 * (size_t)n,
                                       cudaMemcpyDeviceToDevice, st));
     } else {
+        count_launch();
         widen_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, I.d_mu0.p, I.d_mud.p);
     }
     // solver (reference convergeInduceDipoles :557-616)
@@ -1356,14 +1414,17 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         if (I.pme) {
             prof_begin(st, K_ELEC_PME);
             MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
+            count_launch();
             pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 1, nullptr, mu_in, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
             mbpol_status s = pme_convolve(I, st, box);
             if (s) return s;
+            count_launch();
             pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 4, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
             prof_end(st, K_ELEC_PME);
         }
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2.p, 0, sizeof(double), st));
         prof_begin(st, K_ELEC_INDUCED);
+        count_launch();
         if (I.pme)
             induced_update_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
@@ -1403,16 +1464,20 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     I.have_prev = conv;
     if (I.pme) {
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
+        count_launch();
         pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 1, nullptr, mu_final, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
         mbpol_status s = pme_convolve(I, st, box);
         if (s) return s;
+        count_launch();
         pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 10, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
         prof_begin(st, K_ELEC_FORCES);
+        count_launch();
         energy_force_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p, I.d_type.p,
                                                             I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, mu_final,
                                                             I.d_phi_fix.p, I.d_phi_mu.p, redist, force, energy);
         prof_end(st, K_ELEC_FORCES);
     } else {
+        count_launch();
         energy_force_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p,
                                                              I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
                                                              mu_final, nullptr, nullptr, redist, force, energy);

@@ -65,11 +65,13 @@ __global__ void verlet_kick_kernel(int n, const double* __restrict__ invm, doubl
 
 void launch_kick_drift(cudaStream_t st, int n, const double* invm, double* vel, double* pos, const double* force,
                        double dt) {
+    count_launch();
     verlet_kick_drift_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, invm, vel, pos, force, dt);
 }
 
 void launch_kick(cudaStream_t st, int n, const double* invm, double* vel, const double* force, double dt, double kT,
                  double nu, unsigned long long seed, unsigned long long step, double* ekin) {
+    count_launch();
     verlet_kick_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, invm, vel, force, dt, kT, nu, seed, step, ekin);
 }
 

@@ -174,6 +174,7 @@ void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const dou
     if (nw <= 0) return;
     const int threads = 256;
     const int blocks = (nw * 32 + threads - 1) / threads;
+    count_launch();
     mol_neighbors_kernel<<<blocks, threads, 0, st>>>(nw, waters, pos, box, r_full * r_full, r_3b * r_3b,
                                                      r_2b * r_2b, cap_full, cap_lower, full, nfull, lower, nlower,
                                                      pairs, cap_pairs, npairs, overflow, cluster);
@@ -182,13 +183,16 @@ void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const dou
 void launch_trimer_count(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower, int* count,
                          int* offs) {
     if (nw <= 0) return;
+    count_launch();
     trimer_count_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, lower, nlower, cap_lower, count);
+    count_launch();
     scan_kernel<<<1, 1024, 0, st>>>(nw, count, offs);
 }
 
 void launch_trimer_fill(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower,
                         const int* offs, int cap_trip, int4* trips) {
     if (nw <= 0) return;
+    count_launch();
     trimer_fill_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, lower, nlower, cap_lower, offs, cap_trip, trips);
 }
 
@@ -197,10 +201,13 @@ void launch_trimer_complete(cudaStream_t st, int nw, const int4* waters, const d
                             int4* trips, bool fill) {
     if (nw <= 0) return;
     if (!fill) {
+        count_launch();
         trimer_complete_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, rc * rc, full, nfull,
                                                                  cap_full, count, nullptr, 0, nullptr);
+        count_launch();
         scan_kernel<<<1, 1024, 0, st>>>(nw, count, offs);
     } else {
+        count_launch();
         trimer_complete_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, rc * rc, full, nfull,
                                                                  cap_full, nullptr, offs, cap_trip, trips);
     }

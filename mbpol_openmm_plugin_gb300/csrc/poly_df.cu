@@ -210,6 +210,7 @@ void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, i
     if (n <= 0) return;
     int blocks = (n + kBlock - 1) / kBlock;
     if (blocks > num_sms * 4) blocks = num_sms * 4;
+    count_launch();
     poly_df_kernel<31><<<blocks, kBlock, 4 * 31 * kBlock * sizeof(float), st>>>(g_t2.l1, g_t2.n1, g_t2.l2, g_t2.l3,
                                                                                 g_t2.lv, X, G, E, n, stride);
 }
@@ -218,6 +219,7 @@ void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, i
     if (n <= 0) return;
     int blocks = (n + kBlock - 1) / kBlock;
     if (blocks > num_sms * 4) blocks = num_sms * 4;
+    count_launch();
     poly_df_kernel<36><<<blocks, kBlock, 4 * 36 * kBlock * sizeof(float), st>>>(g_t3.l1, g_t3.n1, g_t3.l2, g_t3.l3,
                                                                                 g_t3.lv, X, G, E, n, stride);
 }

@@ -469,18 +469,21 @@ void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245)
 void launch_onebody(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double* force,
                     double* energy) {
     if (nw <= 0) return;
+    count_launch();
     onebody_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, force, energy);
 }
 
 void launch_twobody_vars(cudaStream_t st, int npairs, const int2* pairs, const int4* waters, const double* pos,
                          Box box, float* X, int stride) {
     if (npairs <= 0) return;
+    count_launch();
     twobody_vars_kernel<<<(npairs + 127) / 128, 128, 0, st>>>(npairs, pairs, waters, pos, box, X, stride);
 }
 
 void launch_twobody_forces(cudaStream_t st, int npairs, const int2* pairs, const int4* waters, const double* pos,
                            Box box, const float* G, const float* E, int stride, double* force, double* energy) {
     if (npairs <= 0) return;
+    count_launch();
     twobody_forces_kernel<<<(npairs + 127) / 128, 128, 0, st>>>(npairs, pairs, waters, pos, box, G, E, stride,
                                                                  force, energy);
 }
@@ -488,6 +491,7 @@ void launch_twobody_forces(cudaStream_t st, int npairs, const int2* pairs, const
 void launch_threebody_vars(cudaStream_t st, int ntrip, const int4* trips, const int4* waters, const double* pos,
                            Box box, float* X, int stride) {
     if (ntrip <= 0) return;
+    count_launch();
     threebody_vars_kernel<<<(ntrip + 127) / 128, 128, 0, st>>>(ntrip, trips, waters, pos, box, X, stride);
 }
 
@@ -495,6 +499,7 @@ void launch_threebody_forces(cudaStream_t st, int ntrip, const int4* trips, cons
                              const double* pos, Box box, const float* G, const float* E, int stride,
                              double* force, double* energy) {
     if (ntrip <= 0) return;
+    count_launch();
     threebody_forces_kernel<<<(ntrip + 127) / 128, 128, 0, st>>>(ntrip, trips, waters, pos, box, G, E, stride,
                                                                   force, energy);
 }

@@ -33,11 +33,15 @@ __global__ void spread_vsites_kernel(int n, const int4* __restrict__ idx, const 
 }
 
 void launch_place_vsites(cudaStream_t st, int n, const int4* idx, const double* w, double* pos) {
-    if (n > 0) place_vsites_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, idx, w, pos);
+    if (n <= 0) return;
+    count_launch();
+    place_vsites_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, idx, w, pos);
 }
 
 void launch_spread_vsites(cudaStream_t st, int n, const int4* idx, const double* w, double* force) {
-    if (n > 0) spread_vsites_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, idx, w, force);
+    if (n <= 0) return;
+    count_launch();
+    spread_vsites_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, idx, w, force);
 }
 
 }  // namespace mbpol

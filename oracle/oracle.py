@@ -71,6 +71,198 @@ def build_port(force=False):
     os.makedirs(PORT_DIR, exist_ok=True)
     if not force and os.path.exists(PORT_LIB) and os.path.getmtime(PORT_LIB) >= os.path.getmtime(src):
         return PORT_LIB
-    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-I", os.path.join(HERE, "gen"),
-                           src, "-o", PORT_LIB, "-lm"])
+    srcs = [src, os.path.join(HERE, "mbpol_oracle_elec.c")]
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-I", os.path.join(HERE, "gen"),
+                           "-I", HERE] + srcs + ["-o", PORT_LIB, "-lm"])
     return PORT_LIB
+
+
+_port = None
+
+
+def port():
+    """Load the C port (building it if needed) with its tables set."""
+    global _port
+    if _port is not None:
+        return _port
+    build_port()
+    L = ctypes.CDLL(PORT_LIB)
+    D, I, P, LP = ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_long)
+    L.orc_onebody.restype = D
+    L.orc_onebody.argtypes = [I, P, P, P, P]
+    L.orc_twobody.restype = D
+    L.orc_twobody.argtypes = [I, P, P, P, D, P, LP]
+    L.orc_twobody_sample.restype = D
+    L.orc_twobody_sample.argtypes = [I, P, P, P, D, ctypes.c_long, P, LP, LP]
+    L.orc_threebody.restype = D
+    L.orc_threebody.argtypes = [I, P, P, P, D, ctypes.c_long, P, LP, LP]
+    L.orc_dispersion.restype = D
+    L.orc_dispersion.argtypes = [I, P, P, P, D, P]
+    L.orc_electrostatics.restype = I
+    L.orc_electrostatics.argtypes = [I, P, P, I, D, P, D, D, I, P, I, P, P, P, ctypes.POINTER(I), P]
+    L.orc_set_onebody_tables.restype = None
+    L.orc_set_onebody_tables.argtypes = [P, P]
+    import numpy as np
+    rows = [ln.split() for ln in open(os.path.join(os.path.dirname(HERE), "mbpol_openmm_plugin_gb300", "data",
+                                                 "onebody_tables.txt")) if not ln.startswith(("#", "n "))]
+    f5z, fb, fc, fr = 0.999677885, 0.15860145369897, -1.6351695982132, 1.0
+    c5z = np.array([f5z * float(r[0]) + fb * float(r[1]) + fc * float(r[2]) + fr * float(r[3]) for r in rows])
+    idx = np.array([[int(r[4 + k]) for r in rows] for k in range(3)], dtype=np.int32)
+    L.orc_set_onebody_tables(c5z.ctypes.data_as(P), np.ascontiguousarray(idx).ctypes.data_as(P))
+    _port = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def full_model(pos, box, alpha=0.0, grid=(0, 0, 0), eps=1e-8, maxiter=200, cut2=0.65, cut3=0.45, rc=0.9):
+    """All five terms (kJ/mol, forces kJ/mol/nm) for O,H1,H2,M waters; M
+    forces are spread onto O, H1, H2 with the M-site weights."""
+    import numpy as np
+    L = port()
+    pos = np.ascontiguousarray(pos, np.float64)
+    n = pos.shape[0]
+    nw = n // 4
+    w = np.stack([4 * np.arange(nw), 4 * np.arange(nw) + 1, 4 * np.arange(nw) + 2], 1).astype(np.int32)
+    b = None if box is None else np.ascontiguousarray(box, np.float64)
+    out = {}
+    f = np.zeros((n, 3))
+    out["e1"] = L.orc_onebody(nw, _p(w), _p(pos), _p(b), _p(f))
+    out["f1"] = f
+    f = np.zeros((n, 3))
+    npairs = ctypes.c_long()
+    out["e2"] = L.orc_twobody(nw, _p(w), _p(pos), _p(b), cut2, _p(f), ctypes.byref(npairs))
+    out["f2"] = f
+    f = np.zeros((n, 3))
+    nt, ns = ctypes.c_long(), ctypes.c_long()
+    out["e3"] = L.orc_threebody(nw, _p(w), _p(pos), _p(b), cut3, 1, _p(f), ctypes.byref(nt), ctypes.byref(ns))
+    out["f3"] = f
+    out["ntrip"] = nt.value
+    f = np.zeros((n, 3))
+    out["edisp"] = L.orc_dispersion(nw, _p(w), _p(pos), _p(b), rc if b is not None else 1e30, _p(f))
+    out["fdisp"] = f
+    f = np.zeros((n, 3))
+    e = ctypes.c_double()
+    it = ctypes.c_int()
+    g = np.array(grid, np.int32)
+    th = np.array([0.4, 0.4, 0.055, 0.626, 0.055])
+    dip = np.zeros((n, 3))
+    rcode = L.orc_electrostatics(n, _p(pos), _p(b), 1 if b is not None else 0, alpha, _p(g), rc, eps, maxiter,
+                                 _p(th), 1, _p(f), ctypes.byref(e), _p(dip), ctypes.byref(it), None)
+    mw = (0.573293118, 0.213353441, 0.213353441)
+    for wi in range(nw):
+        fm = f[4 * wi + 3].copy()
+        f[4 * wi + 3] = 0
+        for k in range(3):
+            f[4 * wi + k] += mw[k] * fm
+    out["eelec"], out["felec"], out["iterations"], out["converged"], out["dipoles"] = e.value, f, it.value, rcode == 0, dip
+    out["etotal"] = out["e1"] + out["e2"] + out["e3"] + out["edisp"] + out["eelec"]
+    out["ftotal"] = out["f1"] + out["f2"] + out["f3"] + out["fdisp"] + out["felec"]
+    return out
+
+
+def electrostatics_forces(pos, box, alpha, grid, eps=1e-8, maxiter=200, rc=0.9):
+    """Port electrostatics forces (M forces spread onto O, H1, H2)."""
+    import numpy as np
+    L = port()
+    pos = np.ascontiguousarray(pos, np.float64)
+    n = pos.shape[0]
+    b = None if box is None else np.ascontiguousarray(box, np.float64)
+    f = np.zeros((n, 3))
+    e = ctypes.c_double()
+    it = ctypes.c_int()
+    g = np.array(grid, np.int32)
+    th = np.array([0.4, 0.4, 0.055, 0.626, 0.055])
+    L.orc_electrostatics(n, _p(pos), _p(b), 1 if b is not None else 0, alpha, _p(g), rc, eps, maxiter, _p(th), 1,
+                         _p(f), ctypes.byref(e), None, ctypes.byref(it), None)
+    mw = (0.573293118, 0.213353441, 0.213353441)
+    for wi in range(n // 4):
+        fm = f[4 * wi + 3].copy()
+        f[4 * wi + 3] = 0
+        for k in range(3):
+            f[4 * wi + k] += mw[k] * fm
+    return f
+
+
+def time_reference_step(workload="box4096", seed=0, budget_s=20.0, solver_iterations=None):
+    """Time the reference's algorithm (this C port: FP64, one thread, O(N^2)
+    direct-space electrostatics as in the Reference platform) for one MD
+    step of `workload`, from a bounded sample:
+      * one-body and dispersion: full;
+      * two- and three-body: every k-th pair / trimer, scaled by the counts;
+      * electrostatics: one solver iteration with the direct-space loops
+        restricted to every R-th row (scaled by R), reciprocal parts full,
+        the iteration cost multiplied by the reference's iteration count
+        (the reference starts every step from alpha*E_fixed) -- measured on
+        the smaller box256 configuration at the same threshold unless given.
+    Returns the cpu_baseline record (ns/day at 0.2 fs)."""
+    import sys
+    import time
+    import numpy as np
+    sys.path.insert(0, os.path.dirname(HERE))
+    from mbpol_openmm_plugin_gb300 import systems
+    from mbpol_openmm_plugin_gb300.plugin import pme_parameters
+    L = port()
+    ws = systems.workload(workload, seed)
+    pos = np.ascontiguousarray(ws.positions, np.float64)
+    for w in range(pos.shape[0] // 4):
+        pos[4 * w + 3] = 0.573293118 * pos[4 * w] + 0.213353441 * (pos[4 * w + 1] + pos[4 * w + 2])
+    box = np.ascontiguousarray(ws.box, np.float64)
+    alpha, grid = pme_parameters(ws.box, 0.9, 1e-5)
+    n = pos.shape[0]
+    nw = n // 4
+    w = np.stack([4 * np.arange(nw), 4 * np.arange(nw) + 1, 4 * np.arange(nw) + 2], 1).astype(np.int32)
+    f = np.zeros((n, 3))
+    t = {}
+    t0 = time.perf_counter()
+    L.orc_onebody(nw, _p(w), _p(pos), _p(box), _p(f))
+    t["onebody"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    L.orc_dispersion(nw, _p(w), _p(pos), _p(box), 0.9, _p(f))
+    t["dispersion"] = time.perf_counter() - t0
+    k2 = 50
+    np_, ns = ctypes.c_long(), ctypes.c_long()
+    t0 = time.perf_counter()
+    L.orc_twobody_sample(nw, _p(w), _p(pos), _p(box), 0.65, k2, _p(f), ctypes.byref(np_), ctypes.byref(ns))
+    t["twobody"] = (time.perf_counter() - t0) * np_.value / max(ns.value, 1)
+    k3 = 200
+    nt = ctypes.c_long()
+    t0 = time.perf_counter()
+    L.orc_threebody(nw, _p(w), _p(pos), _p(box), 0.45, k3, _p(f), ctypes.byref(nt), ctypes.byref(ns))
+    t["threebody"] = (time.perf_counter() - t0) * nt.value / max(ns.value, 1)
+    if solver_iterations is None:
+        # the reference's own iteration count at this threshold, from the
+        # 256-water box (same density and settings)
+        wsb = systems.workload("box256", seed)
+        pb = np.ascontiguousarray(wsb.positions, np.float64)
+        for q in range(pb.shape[0] // 4):
+            pb[4 * q + 3] = 0.573293118 * pb[4 * q] + 0.213353441 * (pb[4 * q + 1] + pb[4 * q + 2])
+        ab, gb = pme_parameters(wsb.box, 0.9, 1e-5)
+        it = ctypes.c_int()
+        e = ctypes.c_double()
+        fb = np.zeros_like(pb)
+        L.orc_electrostatics(pb.shape[0], _p(pb), _p(np.ascontiguousarray(wsb.box, np.float64)), 1, ab,
+                             _p(np.array(gb, np.int32)), 0.9, 1e-8, 200, _p(np.array([0.4, 0.4, 0.055, 0.626, 0.055])),
+                             1, _p(fb), ctypes.byref(e), None, ctypes.byref(it), None)
+        solver_iterations = it.value
+    R = 16
+    tm = np.zeros(6)
+    it = ctypes.c_int()
+    e = ctypes.c_double()
+    t0 = time.perf_counter()
+    L.orc_electrostatics(n, _p(pos), _p(box), 1, alpha, _p(np.array(grid, np.int32)), 0.9, 1e-8, 0,
+                         _p(np.array([0.4, 0.4, 0.055, 0.626, 0.055])), R, _p(f), ctypes.byref(e), None,
+                         ctypes.byref(it), _p(tm))
+    wall = time.perf_counter() - t0
+    # tm: setup+fixed recip, fixed direct (1/R rows), recip/iteration, induced direct (1/R), energy direct (1/R), final
+    per_iter = tm[2] / max(it.value, 1) + R * tm[3] / max(it.value, 1)
+    t["electrostatics"] = tm[0] + R * tm[1] + solver_iterations * per_iter + R * tm[4] + tm[5]
+    step = sum(t.values())
+    sample = ("%s seed %d: 1B and dispersion full; 2B every %dth of %d pairs; 3B every %dth of %d trimers; "
+              "electrostatics one SOR iteration with direct-space rows 1/%d (scaled x%d), reciprocal full "
+              "(grid %s), times %d iterations (the reference's count on box256 at 1e-8 D); sample wall %.1f s"
+              % (workload, seed, k2, np_.value, k3, nt.value, R, R, grid, solver_iterations, wall + t["onebody"]))
+    return {"value": 0.0002e-3 * 86400.0 / step, "unit": "ns/day", "cores": 1, "kind": "port",
+            "sample": sample, "seconds_per_step": step, "per_term_s": t}
