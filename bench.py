@@ -117,16 +117,18 @@ def maxwell_boltzmann(masses, T, seed):
 
 
 def fp32_ops_per_unit(name):
-    """FP32 operations (add/sub/mul = 1, fma = 2) of the double-float walk per
-    dimer/trimer, counted from the trie sizes (csrc/poly_df.cu):
-    leaf 32, level-3 node 38, level-2 node 36, level-1 node 28."""
+    """FP32 operations (add/sub/mul = 1, fma = 2) of the polynomial walk per
+    dimer/trimer, counted from the trie sizes (csrc/poly_df.cu): a leaf is a
+    double-float multiply-add into V (9) plus a TwoSum (8) and an FMA into
+    the gradient (2) = 17 (19 with the product); nodes of levels 3/2/1 cost
+    18/18/16."""
     path = os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "csrc", "gen", "%s_tables.inc" % name)
     sizes = {}
     for ln in open(path):
         if ln.startswith("#define"):
             _, k, v = ln.split()
             sizes[k.split("_")[-1]] = int(v)
-    return 32 * sizes["NL"] + 38 * sizes["N3"] + 36 * sizes["N2"] + 28 * sizes["N1"]
+    return 19 * sizes["NL"] + 18 * sizes["N3"] + 18 * sizes["N2"] + 16 * sizes["N1"]
 
 
 def run_ours(args):

@@ -278,12 +278,13 @@ __device__ void water_charges(const double3 O, const double3 H1, const double3 H
 __global__ void elec_prepare_kernel(int nmol, const double* __restrict__ pos, int periodic, int redist,
                                     const float* __restrict__ q_static, float* __restrict__ off,
                                     float* __restrict__ q, float* __restrict__ dq, int pme,
-                                    int* __restrict__ gidx, float* __restrict__ gfrac) {
+                                    int* __restrict__ gidx, float* __restrict__ gfrac, float* __restrict__ reach) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmol) return;
     const int K = c_el.K, s0 = K * m;
     const double3 O = load_pos(pos, s0);
     double3 S[kMaxK];
+    double r2max = 0.0;
     for (int s = 0; s < K; ++s) {
         double3 p = load_pos(pos, s0 + s);
         if (periodic) {
@@ -295,10 +296,18 @@ __global__ void elec_prepare_kernel(int nmol, const double* __restrict__ pos, in
         off[3 * (s0 + s)] = (float)(p.x - O.x);
         off[3 * (s0 + s) + 1] = (float)(p.y - O.y);
         off[3 * (s0 + s) + 2] = (float)(p.z - O.z);
+        const double r2 = (p.x - O.x) * (p.x - O.x) + (p.y - O.y) * (p.y - O.y) + (p.z - O.z) * (p.z - O.z);
+        r2max = r2 > r2max ? r2 : r2max;
     }
+    // largest site distance from the first site: the neighbour list takes
+    // molecule pairs with O-O <= cutoff + reach_A + reach_B
+    reach[m] = (float)sqrt(r2max) + 1e-4f;
     if (redist) {
+        // The reference computes the charges from the raw, unimaged positions
+        // (MBPolReferenceElectrostaticsForce.cpp:2873-2884), also for waters
+        // split across the periodic boundary; reproduced for parity.
         double qq[4], dd[4][3][3];
-        water_charges(S[0], S[1], S[2], qq, dd);
+        water_charges(load_pos(pos, s0), load_pos(pos, s0 + 1), load_pos(pos, s0 + 2), qq, dd);
         for (int s = 0; s < 4; ++s) {
             q[s0 + s] = (float)qq[s];
             for (int o = 0; o < 3; ++o)
@@ -330,11 +339,11 @@ __global__ void elec_prepare_kernel(int nmol, const double* __restrict__ pos, in
     }
 }
 
-// Molecule neighbour list: j != i, O-O <= rlist (cluster-restricted when
+// Molecule neighbour list: j != i, O-O <= cutoff + reach_i + reach_j (cluster-restricted when
 // cluster ids are given), with the FP64 minimum-image O-O vector in FP32.
-__global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, int periodic, double rlist2,
-                                      int cap, int* __restrict__ nb, float* __restrict__ nbd,
-                                      int* __restrict__ nnb, int* __restrict__ overflow,
+__global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, int periodic, double rc,
+                                      const float* __restrict__ reach, int cap, int* __restrict__ nb,
+                                      float* __restrict__ nbd, int* __restrict__ nnb, int* __restrict__ overflow,
                                       const int* __restrict__ cluster) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -357,7 +366,8 @@ __global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, 
                 dy = min_image(dy, c_el.box[1], c_el.inv[1]);
                 dz = min_image(dz, c_el.box[2], c_el.inv[2]);
             }
-            in = dx * dx + dy * dy + dz * dz <= rlist2;
+            const double rl = rc + (double)reach[i] + (double)reach[j];
+            in = dx * dx + dy * dy + dz * dz <= rl * rl;
         }
         const unsigned msk = __ballot_sync(0xffffffffu, in);
         if (in) {
@@ -422,10 +432,14 @@ __device__ __forceinline__ void bspline5(float w, float th[5], float d1[5], floa
     d2[0] = -E[0];
 }
 
-// Spread charges (mode 0) or dipoles (mode 1) of every site onto the grid.
+// Spread charges (mode 0) or dipoles (mode 1) of every site onto the grid
+// as 64-bit fixed point (scale 2^40): integer atomics are order independent,
+// so the grid, and the solver, are deterministic.  FP32 atomics left a
+// run-to-run noise floor of ~1e-8 D in the dipole convergence measure.
+constexpr double kGridFix = 1099511627776.0;  // 2^40
 __global__ void pme_spread_kernel(int nsite, int mode, const float* __restrict__ q, const float* __restrict__ mu,
                                   const int* __restrict__ gidx, const float* __restrict__ gfrac,
-                                  float* __restrict__ grid) {
+                                  unsigned long long* __restrict__ grid) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsite) return;
     float tx[5], ty[5], tz[5], dx[5], dy[5], dz[5], sx[5];
@@ -454,15 +468,21 @@ __global__ void pme_spread_kernel(int nsite, int mode, const float* __restrict__
             const float wA = mode == 0 ? c0 * txy : mx * dx[a] * ty[b];
             const float wB = mode == 0 ? 0.f : my * tx[a] * dy[b];
             const float wC = mode == 0 ? 0.f : mz * txy;
-            float* row = grid + ((size_t)x * Ny + y) * Nz;
+            unsigned long long* row = grid + ((size_t)x * Ny + y) * Nz;
             for (int c = 0; c < 5; ++c) {
                 int z = gz + c;
                 if (z >= Nz) z -= Nz;
                 const float v = mode == 0 ? wA * tz[c] : (wA + wB) * tz[c] + wC * dz[c];
-                atomicAdd(row + z, v);
+                atomicAdd(row + z, (unsigned long long)__double2ll_rn((double)v * kGridFix));
             }
         }
     }
+}
+
+// Fixed-point grid -> FP32 grid for the FFT.
+__global__ void pme_fix_to_float_kernel(long n, const unsigned long long* __restrict__ a, float* __restrict__ b) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        b[i] = (float)((double)(long long)a[i] * (1.0 / kGridFix));
 }
 
 // Reciprocal convolution on the R2C half grid (reference :1676-1713).
@@ -1151,7 +1171,8 @@ struct ElecImpl {
     bool pme = false;
     std::vector<float> q_static, damp, pol;
     std::vector<int> type;
-    DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd, d_gfrac;
+    DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd, d_gfrac,
+        d_reach;
     DBuf<int> d_type, d_nb, d_nnb, d_gidx, d_flags;
     DBuf<double> d_eps2, d_mud, d_mud_prev;
     int cap = 0;
@@ -1159,6 +1180,7 @@ struct ElecImpl {
     int grid[3] = {0, 0, 0};
     double alpha = 0.0;
     DBuf<float> d_grid, d_gridfix, d_bx, d_by, d_bz;
+    DBuf<unsigned long long> d_gridq;
     DBuf<cufftComplex> d_cgrid;
     cufftHandle plan_f = 0, plan_b = 0;
     bool plans = false;
@@ -1239,6 +1261,7 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     MBPOL_CUDA_OK(I.d_phi_mu.ensure(10 * (size_t)n));
     MBPOL_CUDA_OK(I.d_gidx.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_nnb.ensure(I.nmol));
+    MBPOL_CUDA_OK(I.d_reach.ensure(I.nmol));
     MBPOL_CUDA_OK(I.d_flags.ensure(4));
     MBPOL_CUDA_OK(I.d_eps2.ensure(1));
     MBPOL_CUDA_OK(I.d_mud.ensure(3 * (size_t)n));
@@ -1285,6 +1308,7 @@ static mbpol_status pme_setup(ElecImpl& I, const Box& box) {
         const size_t nreal = (size_t)g[0] * g[1] * g[2];
         const size_t ncplx = (size_t)g[0] * g[1] * (g[2] / 2 + 1);
         MBPOL_CUDA_OK(I.d_grid.ensure(2 * ncplx));  // in-place friendly size
+        MBPOL_CUDA_OK(I.d_gridq.ensure(nreal));
         MBPOL_CUDA_OK(I.d_gridfix.ensure(nreal));
         MBPOL_CUDA_OK(I.d_cgrid.ensure(ncplx));
         std::vector<double> mod;
@@ -1297,6 +1321,18 @@ static mbpol_status pme_setup(ElecImpl& I, const Box& box) {
         }
     }
     return MBPOL_OK;
+}
+
+// spread (fixed point) and convert to the FP32 grid d_grid
+static cudaError_t pme_spread(ElecImpl& I, cudaStream_t st, int mode, const float* mu, int n, size_t nreal) {
+    cudaError_t e = cudaMemsetAsync(I.d_gridq.p, 0, sizeof(unsigned long long) * nreal, st);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, mode, I.d_q.p, mu, I.d_gidx.p, I.d_gfrac.p, I.d_gridq.p);
+    count_launch();
+    pme_fix_to_float_kernel<<<(int)std::min<size_t>((nreal + 255) / 256, 152 * 16), 256, 0, st>>>(
+        (long)nreal, I.d_gridq.p, I.d_grid.p);
+    return cudaGetLastError();
 }
 
 // grid (real) -> FFT -> convolution -> inverse FFT, in place in d_grid
@@ -1348,9 +1384,9 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     const int redist = I.prm.include_charge_redistribution ? 1 : 0;
     count_launch();
     elec_prepare_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, pos, box.periodic, redist, I.d_qs.p, I.d_off.p,
-                                                            I.d_q.p, I.d_dq.p, I.pme ? 1 : 0, I.d_gidx.p, I.d_gfrac.p);
+                                                            I.d_q.p, I.d_dq.p, I.pme ? 1 : 0, I.d_gidx.p, I.d_gfrac.p, I.d_reach.p);
     // neighbour list
-    const double rlist = I.pme ? I.prm.cutoff + 0.24 : 1e30;
+    const double rcut = I.pme ? I.prm.cutoff : 1e30;
     if (I.cap == 0) I.cap = I.pme ? 256 : ((nmol + 31) / 32) * 32;
     for (int attempt = 0;; ++attempt) {
         MBPOL_CUDA_OK(I.d_nb.ensure((size_t)nmol * I.cap));
@@ -1358,8 +1394,8 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_flags.p, 0, sizeof(int), st));
         count_launch();
         elec_neighbors_kernel<<<(nmol * 32 + 127) / 128, 128, 0, st>>>(
-            nmol, pos, box.periodic && I.pme, rlist * rlist, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.d_flags.p,
-            nullptr);
+            nmol, pos, box.periodic && I.pme, rcut, I.d_reach.p, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p,
+            I.d_flags.p, nullptr);
         int ovf = 0;
         MBPOL_CUDA_OK(cudaMemcpyAsync(&ovf, I.d_flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(st));
@@ -1371,9 +1407,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     const size_t nreal = I.pme ? (size_t)I.grid[0] * I.grid[1] * I.grid[2] : 0;
     // fixed field
     if (I.pme) {
-        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
-        count_launch();
-        pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 0, I.d_q.p, nullptr, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
+        MBPOL_CUDA_OK(pme_spread(I, st, 0, nullptr, n, nreal));
         mbpol_status s = pme_convolve(I, st, box);
         if (s) return s;
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_gridfix.p, I.d_grid.p, sizeof(float) * nreal, cudaMemcpyDeviceToDevice, st));
@@ -1413,9 +1447,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         float* mu_out = mu[cur ^ 1];
         if (I.pme) {
             prof_begin(st, K_ELEC_PME);
-            MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
-            count_launch();
-            pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 1, nullptr, mu_in, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
+            MBPOL_CUDA_OK(pme_spread(I, st, 1, mu_in, n, nreal));
             mbpol_status s = pme_convolve(I, st, box);
             if (s) return s;
             count_launch();
@@ -1463,9 +1495,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     }
     I.have_prev = conv;
     if (I.pme) {
-        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_grid.p, 0, sizeof(float) * nreal, st));
-        count_launch();
-        pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 1, nullptr, mu_final, I.d_gidx.p, I.d_gfrac.p, I.d_grid.p);
+        MBPOL_CUDA_OK(pme_spread(I, st, 1, mu_final, n, nreal));
         mbpol_status s = pme_convolve(I, st, box);
         if (s) return s;
         count_launch();
