@@ -117,18 +117,18 @@ def maxwell_boltzmann(masses, T, seed):
 
 
 def fp32_ops_per_unit(name):
-    """FP32 operations (add/sub/mul = 1, fma = 2) of the polynomial walk per
+    """FP32 operations (add/sub/mul = 1, fma = 2) of the double-float walk per
     dimer/trimer, counted from the trie sizes (csrc/poly_df.cu): a leaf is a
-    double-float multiply-add into V (9) plus a TwoSum (8) and an FMA into
-    the gradient (2) = 17 (19 with the product); nodes of levels 3/2/1 cost
-    18/18/16."""
+    double-float multiply-add into V (1 mul + 3 fma + TwoSum 6 + 2 adds = 15)
+    and into the gradient (1 mul + 3 fma + 6 + 2 = 15) = 30; nodes of levels
+    3/2/1 cost 40/33/26 (prefix product, two double-float updates)."""
     path = os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "csrc", "gen", "%s_tables.inc" % name)
     sizes = {}
     for ln in open(path):
         if ln.startswith("#define"):
             _, k, v = ln.split()
             sizes[k.split("_")[-1]] = int(v)
-    return 19 * sizes["NL"] + 18 * sizes["N3"] + 18 * sizes["N2"] + 16 * sizes["N1"]
+    return 30 * sizes["NL"] + 40 * sizes["N3"] + 33 * sizes["N2"] + 26 * sizes["N1"]
 
 
 def run_ours(args):

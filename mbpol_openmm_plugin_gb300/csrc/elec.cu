@@ -687,7 +687,12 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
 }
 
 // Induced field from mu_in at the sites of molecule A, then the SOR update
-// mu_out = mu_in + 0.55 (alpha (E0 + E_ind) - mu_in) and sum |delta|^2.
+// mu <- mu + 0.55 (alpha (E0 + E_ind) - mu) on the FP64 dipoles and the sum
+// of |delta|^2.  Any FP32 evaluation of the field carries rounding noise of
+// ~1e-7 |mu|, which can keep the convergence measure from reaching 1e-8 D;
+// so once the iteration is close, the current dipoles become an anchor whose
+// field is stored once (mode 1) and later iterations evaluate only the field
+// of mu - anchor (mode 2), whose rounding noise is smaller by |mu - anchor|/|mu|.
 template <bool PME>
 __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ damp,
                                       const float* __restrict__ pol, const int* __restrict__ type,
@@ -695,7 +700,8 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                                       const int* __restrict__ nnb, int cap, const float* __restrict__ E0,
                                       const float* __restrict__ phi_mu, const float* __restrict__ mu_in,
                                       float* __restrict__ mu_out, double* __restrict__ mu_d,
-                                      double* __restrict__ eps2) {
+                                      double* __restrict__ eps2, int mode, float* __restrict__ Ebase,
+                                      const float* __restrict__ anchor) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     double d2sum = 0.0;
@@ -795,6 +801,17 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                     ey += c_el.self_term * mu.y - c_el.scale[1] * phi_mu[4 * i + 2];
                     ez += c_el.self_term * mu.z - c_el.scale[2] * phi_mu[4 * i + 3];
                 }
+                // mode 1 (anchoring): mu_in is the anchor; store its field.
+                // mode 2 (anchored): mu_in is mu - anchor; add the anchor's field.
+                if (mode == 1) {
+                    Ebase[3 * i] = ex;
+                    Ebase[3 * i + 1] = ey;
+                    Ebase[3 * i + 2] = ez;
+                } else if (mode == 2) {
+                    ex += Ebase[3 * i];
+                    ey += Ebase[3 * i + 1];
+                    ez += Ebase[3 * i + 2];
+                }
                 const float al = pol[i];
                 // reference updateInducedDipole (:516-531); E0 is unscaled here
                 const double nx = (double)al * ((double)E0[3 * i] + ex);
@@ -807,9 +824,16 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                 mu_d[3 * i] = u0;
                 mu_d[3 * i + 1] = u1;
                 mu_d[3 * i + 2] = u2;
-                mu_out[3 * i] = (float)u0;
-                mu_out[3 * i + 1] = (float)u1;
-                mu_out[3 * i + 2] = (float)u2;
+                if (mode == 0) {
+                    mu_out[3 * i] = (float)u0;
+                    mu_out[3 * i + 1] = (float)u1;
+                    mu_out[3 * i + 2] = (float)u2;
+                } else {
+                    const float* an = mode == 1 ? mu_in : anchor;
+                    mu_out[3 * i] = (float)(u0 - (double)an[3 * i]);
+                    mu_out[3 * i + 1] = (float)(u1 - (double)an[3 * i + 1]);
+                    mu_out[3 * i + 2] = (float)(u2 - (double)an[3 * i + 2]);
+                }
                 d2sum += dx * dx + dy * dy + dz * dz;
             }
         }
@@ -1051,6 +1075,11 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
     block_sum_atomic<128>(e_out, energy);
 }
 
+__global__ void narrow_kernel(int n, const double* __restrict__ a, float* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
 __global__ void widen_kernel(int n, const float* __restrict__ a, double* __restrict__ b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = a[i];
@@ -1171,8 +1200,8 @@ struct ElecImpl {
     bool pme = false;
     std::vector<float> q_static, damp, pol;
     std::vector<int> type;
-    DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd, d_gfrac,
-        d_reach;
+    DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu2, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd,
+        d_gfrac, d_reach, d_ebase;
     DBuf<int> d_type, d_nb, d_nnb, d_gidx, d_flags;
     DBuf<double> d_eps2, d_mud, d_mud_prev;
     int cap = 0;
@@ -1254,7 +1283,8 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     MBPOL_CUDA_OK(cudaMemcpy(I.d_damp.p, I.damp.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     MBPOL_CUDA_OK(cudaMemcpy(I.d_pol.p, I.pol.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     MBPOL_CUDA_OK(cudaMemcpy(I.d_type.p, I.type.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    for (auto* b : {&I.d_off, &I.d_E0, &I.d_mu0, &I.d_mu1, &I.d_mu_prev, &I.d_gfrac}) MBPOL_CUDA_OK(b->ensure(3 * (size_t)n));
+    for (auto* b : {&I.d_off, &I.d_E0, &I.d_mu0, &I.d_mu1, &I.d_mu2, &I.d_mu_prev, &I.d_gfrac, &I.d_ebase})
+        MBPOL_CUDA_OK(b->ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_q.ensure(n));
     MBPOL_CUDA_OK(I.d_dq.ensure(9 * (size_t)n));
     MBPOL_CUDA_OK(I.d_phi_fix.ensure(10 * (size_t)n));
@@ -1425,10 +1455,10 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                                                             I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
                                                             nullptr, I.d_E0.p, I.d_mu0.p);
     }
-    float* mu[2] = {I.d_mu0.p, I.d_mu1.p};
-    int cur = 0;
+    // d_mu0 holds float(mu) of the starting dipoles (alpha*E0 from the
+    // fixed-field kernel, or the previous call's dipoles)
+    float* bufs[3] = {I.d_mu0.p, I.d_mu1.p, I.d_mu2.p};
     if (I.prm.guess == 1 && I.have_prev) {
-        // start from the previous call's converged dipoles instead of alpha*E0
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mu0.p, I.d_mu_prev.p, sizeof(float) * 3 * (size_t)n,
                                       cudaMemcpyDeviceToDevice, st));
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mud.p, I.d_mud_prev.p, sizeof(double) * 3 * (size_t)n,
@@ -1437,14 +1467,25 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         count_launch();
         widen_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, I.d_mu0.p, I.d_mud.p);
     }
-    // solver (reference convergeInduceDipoles :557-616)
+    // solver (reference convergeInduceDipoles :557-616); the anchoring switch
+    // is taken once the measure is 100x above the target (at most 1e-6 D)
+    const double switch_eps = std::min(1e-6, 100.0 * I.prm.target_epsilon);
     double current = 1.0e+50;
     int it = 0;
     bool done = false, conv = false;
     double eps = 0.0;
+    float* mu_in = bufs[0];
+    float* anchor = nullptr;
+    int mode = 0;
     while (!done) {
-        float* mu_in = mu[cur];
-        float* mu_out = mu[cur ^ 1];
+        int kmode = mode;
+        if (mode == 0 && current < switch_eps) kmode = 1;
+        float* mu_out = nullptr;
+        for (float* b : bufs)
+            if (b != mu_in && b != anchor) {
+                mu_out = b;
+                break;
+            }
         if (I.pme) {
             prof_begin(st, K_ELEC_PME);
             MBPOL_CUDA_OK(pme_spread(I, st, 1, mu_in, n, nreal));
@@ -1460,16 +1501,20 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         if (I.pme)
             induced_update_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
-                                                                  I.d_phi_mu.p, mu_in, mu_out, I.d_mud.p, I.d_eps2.p);
+                                                                  I.d_phi_mu.p, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
+                                                                  kmode, I.d_ebase.p, anchor);
         else
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                    I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
-                                                                   nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p);
+                                                                   nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
+                                                                   kmode, I.d_ebase.p, anchor);
         prof_end(st, K_ELEC_INDUCED);
+        if (kmode == 1) anchor = mu_in;
+        mode = kmode == 0 ? 0 : 2;
+        mu_in = mu_out;
         double e2 = 0.0;
         MBPOL_CUDA_OK(cudaMemcpyAsync(&e2, I.d_eps2.p, sizeof(double), cudaMemcpyDeviceToHost, st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(st));
-        cur ^= 1;
         eps = kSOR * kDebye * sqrt(e2 / (double)n);
         if (!std::isfinite(eps)) {
             done = true;
@@ -1485,8 +1530,10 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     I.iterations = it;
     I.epsilon = current;
     I.converged = conv;
-    I.mu_cur = mu[cur] == I.d_mu0.p ? 0 : 1;
-    float* mu_final = mu[cur];
+    // final dipoles (FP32 copy of the FP64 state) for the energy and forces
+    float* mu_final = bufs[0];
+    count_launch();
+    narrow_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, I.d_mud.p, mu_final);
     if (conv) {
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mu_prev.p, mu_final, sizeof(float) * 3 * (size_t)n,
                                       cudaMemcpyDeviceToDevice, st));

@@ -9,16 +9,13 @@
 //     P_d = P_{d-1} x_{v_d};  V_d = c_d + sum_children x_child V_child;
 //     g_{v_d} += V_d P_{d-1};  E = V_root.
 // Plain FP32 is not accurate enough: the monomial terms cancel by a factor of
-// 1e4-1e5, leaving ~1e-3 relative error in E.  The value chain (V per level
-// and E) is therefore a pair (s, c) of FP32 values updated Dot2-style
-// (error-free TwoProd by FMA and TwoSum, errors collected in c; Ogita, Rump
-// & Oishi, SIAM J. Sci. Comput. 26 (2005)), which gives FP64-level results on
-// the FP32 pipe.  The gradient does not need it: its terms c*P and V*P are
-// accurate once V is, and plain FP32 sums of them stay at ~1e-5 relative
-// (measured against FP64), so g is accumulated with single FP32 FMAs.
+// 1e4-1e5, leaving ~1e-3 relative error.  Every accumulation is therefore a
+// pair (s, c) of FP32 values updated Dot2-style (error-free TwoProd by FMA
+// and TwoSum, errors collected in c; Ogita, Rump & Oishi, SIAM J. Sci.
+// Comput. 26 (2005)), which gives FP64-level results on the FP32 pipe.
 //
 // One thread per unit (dimer or trimer).  The variables x and the gradient
-// live in shared memory, [variable][thread], so every access
+// pairs (gh, gl) live in shared memory, [variable][thread], so every access
 // of a warp is one conflict-free wavefront; the trie tables are read with
 // warp-uniform addresses.  X: [2][nvars][stride] floats (FP64 variables as
 // hi and lo planes); G: [nvars][stride]; E: [stride].
@@ -58,6 +55,14 @@ __device__ __forceinline__ void mul_df_f(const DF a, float x, float& p, float& q
     q = __fmaf_rn(a.l, x, q);
 }
 
+// (p, q) = (a.h + a.l) * (b.h + b.l), dropping a.l * b.l
+__device__ __forceinline__ void mul_df_df(const DF a, const DF b, float& p, float& q) {
+    p = __fmul_rn(a.h, b.h);
+    q = __fmaf_rn(a.h, b.h, -p);
+    q = __fmaf_rn(a.h, b.l, q);
+    q = __fmaf_rn(a.l, b.h, q);
+}
+
 template <int NV>
 __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restrict__ l1, int n1,
                                                           const PolyNode* __restrict__ l2,
@@ -68,7 +73,8 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
     extern __shared__ float smem[];
     float* xs = smem;                  // [NV][kBlock]   variables, high part
     float* xq = smem + NV * kBlock;    // [NV][kBlock]   variables, low part
-    float* gs = xq + NV * kBlock;      // [NV][kBlock]   gradient (FP32)
+    float* gh = xq + NV * kBlock;      // [NV][kBlock]
+    float* gl = gh + NV * kBlock;      // [NV][kBlock]
     const int t = threadIdx.x;
     for (int base = blockIdx.x * kBlock; base < n; base += gridDim.x * kBlock) {
         const int u = base + t;
@@ -77,61 +83,88 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
         for (int v = 0; v < NV; ++v) {
             xs[v * kBlock + t] = live ? X[(size_t)v * stride + u] : 0.f;
             xq[v * kBlock + t] = live ? X[(size_t)(NV + v) * stride + u] : 0.f;
-            gs[v * kBlock + t] = 0.f;
+            gh[v * kBlock + t] = 0.f;
+            gl[v * kBlock + t] = 0.f;
         }
         DF Ev = {0.f, 0.f};
         int c2 = 0, c3 = 0, cl = 0;
         for (int a = 0; a < n1; ++a) {
             const PolyNode A = l1[a];
-            const int oi = A.var * kBlock + t;
-            const float xi = xs[oi], xil = xq[oi];
+            const float xi = xs[A.var * kBlock + t], xil = xq[A.var * kBlock + t];
             DF V1 = {A.hi, A.lo};
             for (; c2 < A.end; ++c2) {
                 const PolyNode B = l2[c2];
-                const int oj = B.var * kBlock + t;
-                const float xj = xs[oj], xjl = xq[oj];
+                const float xj = xs[B.var * kBlock + t], xjl = xq[B.var * kBlock + t];
                 DF V2 = {B.hi, B.lo};
-                const float P2 = __fmul_rn(xi, xj);
+                DF P2;
+                P2.h = __fmul_rn(xi, xj);
+                P2.l = __fmaf_rn(xi, xj, -P2.h);
+                P2.l = __fmaf_rn(xi, xjl, P2.l);
+                P2.l = __fmaf_rn(xil, xj, P2.l);
                 for (; c3 < B.end; ++c3) {
                     const PolyNode C = l3[c3];
-                    const int ok = C.var * kBlock + t;
-                    const float xk = xs[ok], xkl = xq[ok];
+                    const float xk = xs[C.var * kBlock + t], xkl = xq[C.var * kBlock + t];
                     DF V3 = {C.hi, C.lo};
-                    const float P3 = __fmul_rn(P2, xk);
+                    DF P3;
+                    mul_df_f(P2, xk, P3.h, P3.l);
+                    P3.l = __fmaf_rn(P2.h, xkl, P3.l);
                     for (; cl < C.end; ++cl) {
                         const PolyNode L = lv[cl];
                         const int o = L.var * kBlock + t;
                         const float xl = xs[o], xll = xq[o];
-                        // V3 += c x_l in double-float
-                        const float p = __fmul_rn(xl, L.hi);
-                        float q = __fmaf_rn(xl, L.hi, -p);
+                        float p, q;
+                        // V3 += c x_l
+                        p = __fmul_rn(xl, L.hi);
+                        q = __fmaf_rn(xl, L.hi, -p);
                         q = __fmaf_rn(xl, L.lo, q);
                         q = __fmaf_rn(xll, L.hi, q);
                         acc(V3, p, q);
-                        // g_l += c P3 in FP32
-                        gs[o] = __fmaf_rn(L.hi, P3, gs[o]);
+                        // g_l += c P3
+                        p = __fmul_rn(P3.h, L.hi);
+                        q = __fmaf_rn(P3.h, L.hi, -p);
+                        q = __fmaf_rn(P3.l, L.hi, q);
+                        q = __fmaf_rn(P3.h, L.lo, q);
+                        DF g = {gh[o], gl[o]};
+                        acc(g, p, q);
+                        gh[o] = g.h;
+                        gl[o] = g.l;
                     }
                     float p, q;
                     mul_df_f(V3, xk, p, q);
                     q = __fmaf_rn(V3.h, xkl, q);
                     acc(V2, p, q);
-                    gs[ok] = __fmaf_rn(V3.h, P2, gs[ok]);
+                    mul_df_df(V3, P2, p, q);
+                    const int o = C.var * kBlock + t;
+                    DF g = {gh[o], gl[o]};
+                    acc(g, p, q);
+                    gh[o] = g.h;
+                    gl[o] = g.l;
                 }
                 float p, q;
                 mul_df_f(V2, xj, p, q);
                 q = __fmaf_rn(V2.h, xjl, q);
                 acc(V1, p, q);
-                gs[oj] = __fmaf_rn(V2.h, xi, gs[oj]);
+                mul_df_f(V2, xi, p, q);
+                q = __fmaf_rn(V2.h, xil, q);
+                const int o = B.var * kBlock + t;
+                DF g = {gh[o], gl[o]};
+                acc(g, p, q);
+                gh[o] = g.h;
+                gl[o] = g.l;
             }
             float p, q;
             mul_df_f(V1, xi, p, q);
             q = __fmaf_rn(V1.h, xil, q);
             acc(Ev, p, q);
-            gs[oi] = __fadd_rn(gs[oi], V1.h);
+            const int o = A.var * kBlock + t;
+            DF g = {gh[o], gl[o]};
+            acc(g, V1.h, V1.l);
+            gh[o] = g.h;
+            gl[o] = g.l;
         }
         if (live) {
             #pragma unroll
-            for (int v = 0; v < NV; ++v) G[(size_t)v * stride + u] = gs[v * kBlock + t];
+            for (int v = 0; v < NV; ++v) G[(size_t)v * stride + u] = __fadd_rn(gh[v * kBlock + t], gl[v * kBlock + t]);
             E[u] = __fadd_rn(Ev.h, Ev.l);
         }
     }
@@ -166,7 +199,7 @@ cudaError_t poly_tables_upload(int device) {
         return e;
     g_t2.n1 = POLY2B_N1;
     g_t3.n1 = POLY3B_N1;
-    const int sm2 = 3 * 31 * kBlock * (int)sizeof(float), sm3 = 3 * 36 * kBlock * (int)sizeof(float);
+    const int sm2 = 4 * 31 * kBlock * (int)sizeof(float), sm3 = 4 * 36 * kBlock * (int)sizeof(float);
     if ((e = cudaFuncSetAttribute(poly_df_kernel<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm2))) return e;
     if ((e = cudaFuncSetAttribute(poly_df_kernel<36>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm3))) return e;
     g_dev_uploaded = device;
@@ -178,7 +211,7 @@ void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, i
     int blocks = (n + kBlock - 1) / kBlock;
     if (blocks > num_sms * 4) blocks = num_sms * 4;
     count_launch();
-    poly_df_kernel<31><<<blocks, kBlock, 3 * 31 * kBlock * sizeof(float), st>>>(g_t2.l1, g_t2.n1, g_t2.l2, g_t2.l3,
+    poly_df_kernel<31><<<blocks, kBlock, 4 * 31 * kBlock * sizeof(float), st>>>(g_t2.l1, g_t2.n1, g_t2.l2, g_t2.l3,
                                                                                 g_t2.lv, X, G, E, n, stride);
 }
 
@@ -187,7 +220,7 @@ void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, i
     int blocks = (n + kBlock - 1) / kBlock;
     if (blocks > num_sms * 4) blocks = num_sms * 4;
     count_launch();
-    poly_df_kernel<36><<<blocks, kBlock, 3 * 36 * kBlock * sizeof(float), st>>>(g_t3.l1, g_t3.n1, g_t3.l2, g_t3.l3,
+    poly_df_kernel<36><<<blocks, kBlock, 4 * 36 * kBlock * sizeof(float), st>>>(g_t3.l1, g_t3.n1, g_t3.l2, g_t3.l3,
                                                                                 g_t3.lv, X, G, E, n, stride);
 }
 

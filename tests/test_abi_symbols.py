@@ -33,3 +33,17 @@ def test_status_strings_without_gpu():
         pytest.skip("library not built")
     lib = _capi.load()
     assert lib.mbpol_status_string(3) == b"induced dipoles did not converge"
+
+
+def test_cxx_layer_compiles_and_links(tmp_path):
+    """The C++ Force-class header compiles against the C ABI and links."""
+    import shutil
+    import subprocess
+    if not os.path.exists(_capi.LIB_PATH) or shutil.which("g++") is None:
+        pytest.skip("library not built or no g++")
+    exe = tmp_path / "example_water2"
+    subprocess.check_call(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "cxx", "example_water2.cpp"), "-o", str(exe),
+                           "-L", os.path.dirname(_capi.LIB_PATH), "-lmbpol_gb300",
+                           "-Wl,-rpath," + os.path.dirname(_capi.LIB_PATH)])
+    assert exe.exists()
