@@ -116,12 +116,18 @@ def maxwell_boltzmann(masses, T, seed):
     return v
 
 
+# Algorithmic work per unit (reference operation counts, one flop per add or
+# multiply, counted in poly-2b-v6x.cpp / poly-3b-v2x.cpp plus the variables,
+# switch and chain rule around them): these stay fixed whatever the kernels do.
+ALGO_FLOP_PER_UNIT = {"poly2b": 31200, "poly3b": 112600}
+
+
 def fp32_ops_per_unit(name):
-    """FP32 operations (add/sub/mul = 1, fma = 2) of the double-float walk per
-    dimer/trimer, counted from the trie sizes (csrc/poly_df.cu): a leaf is a
-    double-float multiply-add into V (1 mul + 3 fma + TwoSum 6 + 2 adds = 15)
-    and into the gradient (1 mul + 3 fma + 6 + 2 = 15) = 30; nodes of levels
-    3/2/1 cost 40/33/26 (prefix product, two double-float updates)."""
+    """FP32 operations (add/sub/mul = 1, fma = 2) that the double-float walk
+    executes per dimer/trimer, counted from the trie sizes (csrc/poly_df.cu):
+    a leaf is a double-float multiply-add into V (1 mul + 3 fma + TwoSum 6 +
+    2 adds = 15) and into the gradient (15) = 30; nodes of levels 3/2/1 cost
+    40/33/26 (prefix product, two double-float updates)."""
     path = os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "csrc", "gen", "%s_tables.inc" % name)
     sizes = {}
     for ln in open(path):
@@ -200,15 +206,19 @@ def run_ours(args):
     roof = None
     if dom in ("poly3b", "poly2b") and kern[dom]["launches"]:
         units = int(counts[1] if dom == "poly3b" else counts[0])
-        ops = fp32_ops_per_unit(dom)
         per_launch_ms = kern[dom]["total_ms"] / kern[dom]["launches"]
-        achieved = units * ops / (per_launch_ms * 1e-3) / 1e12
+        algo = ALGO_FLOP_PER_UNIT[dom]
+        achieved = units * algo / (per_launch_ms * 1e-3) / 1e12
+        executed = units * fp32_ops_per_unit(dom) / (per_launch_ms * 1e-3) / 1e12
         sm_mhz = clocks.get("sm_mhz") or 2070.0
         peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
         roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": None,
-                "work": "%d units x %d FP32 flop (double-float walk)" % (units, ops),
-                "peak_kind": "nominal FP32 FMA rate at the median sampled SM clock (152 SM x 128 lanes x 2)",
+                "work": "%d units x %d algorithmic flop (reference operation count)" % (units, algo),
+                "executed_fp32_tflops": executed, "executed_frac": executed / peak,
+                "executed_work": "%d FP32 flop per unit in the double-float walk" % fp32_ops_per_unit(dom),
+                "peak_kind": "nominal FP32 FMA rate at the median sampled SM clock (152 SM x 128 lanes x 2); "
+                             "the measured-peaks file has no FP32 figure",
                 "launch_ms": per_launch_ms}
     out = {
         "metric": "ns/day @4096 H2O PME, learned-guess vs plain GPU at <=1e-4 rel RMS force err",
@@ -218,7 +228,10 @@ def run_ours(args):
         "config": {"workload": args.workload, "waters": n // 4, "box_nm": float(ws.box[0]), "pme_alpha": alpha,
                    "pme_grid": grid, "cutoff_nm": 0.9, "ewald_tol": 1e-5, "target_epsilon_D": 1e-8,
                    "dt_fs": 0.2, "guess": args.guess, "seed": args.seed,
-                   "l2": "no flush; per-step buffers (pair/trimer variables, PME grids) exceed L2 in part"},
+                   "l2": "no flush: inputs larger than L2 (per-step trimer and pair variable/gradient planes "
+                         "%.0f MB, PME grids %.0f MB, against 129 MB of L2)" % (
+                             (int(counts[1]) * 36 * 3 + int(counts[0]) * 31 * 3) * 4 / 1e6,
+                             (grid[0] * grid[1] * grid[2] * 16) / 1e6 if grid else 0.0)},
         "e2e": {"value": ns_per_day(e2e_s), "unit": "ns/day", "h2d_bytes_per_step": int(pos.nbytes),
                 "d2h_bytes_per_step": int(pos.nbytes + 5 * 8)},
         "gpu_launches": launches,

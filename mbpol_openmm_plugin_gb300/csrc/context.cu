@@ -122,6 +122,10 @@ struct mbpol_context {
     // dispersion buffers
     DevBuf full_d, nfull_d, lower_d, nlower_d;
     int cap_full_d = 0;
+    // FP32 O positions for the neighbour prefilter; lists built by one
+    // shared pass for the two-body, three-body and dispersion terms
+    DevBuf opos;
+    bool shared_lists = false;
     double disp_c6[16], disp_d6[16];
     // electrostatics
     std::unique_ptr<ElecEngine> elec;
@@ -173,6 +177,32 @@ mbpol_status check_box(const mbpol_context* ctx, double cutoff) {
     return MBPOL_OK;
 }
 
+// Two-body pair list on its own (one neighbour pass, one host sync).
+mbpol_status twobody_list(mbpol_context* ctx, const Box& box, double rc, int* np_out) {
+    WaterTerm& t = ctx->t2;
+    const int nw = (int)t.waters.size();
+    int* cnt = ctx->d_counters.as<int>();
+    MBPOL_CUDA_OK(ctx->opos.ensure(sizeof(float4) * (size_t)nw));
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (ctx->cap2 == 0) ctx->cap2 = nw * 24 + 64;
+        MBPOL_CUDA_OK(ctx->p2.ensure(sizeof(int2) * (size_t)ctx->cap2));
+        MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
+        launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(),
+                             box, -1.0, -1.0, rc, 0, 0, nullptr, nullptr, nullptr, nullptr, ctx->p2.as<int2>(),
+                             ctx->cap2, cnt, cnt + 1, nullptr);
+        int h[2];
+        MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+        if (h[0] > ctx->cap2) {
+            ctx->cap2 = h[0] + h[0] / 4 + 64;
+            continue;
+        }
+        *np_out = h[0];
+        return MBPOL_OK;
+    }
+    return mbpol_fail(MBPOL_ERR_CAPACITY, "two-body pair list capacity");
+}
+
 mbpol_status run_twobody(mbpol_context* ctx, double* energy) {
     WaterTerm& t = ctx->t2;
     const int nw = (int)t.waters.size();
@@ -184,53 +214,35 @@ mbpol_status run_twobody(mbpol_context* ctx, double* energy) {
     }
     const Box box = term_box(ctx, periodic);
     const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
-    int* cnt = ctx->d_counters.as<int>();
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        if (ctx->cap2 == 0) ctx->cap2 = nw * 24 + 64;
-        MBPOL_CUDA_OK(ctx->p2.ensure(sizeof(int2) * (size_t)ctx->cap2));
-        MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
-        launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, -1.0, -1.0, rc, 0, 0,
-                             nullptr, nullptr, nullptr, nullptr, ctx->p2.as<int2>(),
-                             ctx->cap2, cnt, cnt + 1, nullptr);
-        int h[2];
-        MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
-        MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
-        if (h[0] > ctx->cap2) {
-            ctx->cap2 = h[0] + h[0] / 4 + 64;
-            continue;
-        }
-        const int np = h[0];
-        ctx->counts[0] = np;
-        const int stride = ctx->cap2;
-        MBPOL_CUDA_OK(ctx->x2.ensure(sizeof(float) * 2 * 31 * (size_t)stride));
-        MBPOL_CUDA_OK(ctx->g2.ensure(sizeof(float) * 31 * (size_t)stride));
-        MBPOL_CUDA_OK(ctx->e2.ensure(sizeof(float) * (size_t)stride));
-        launch_twobody_vars(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
-                            ctx->x2.as<float>(), stride);
-        prof_begin(ctx->st, K_POLY2B);
-        launch_poly2b(ctx->st, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride,
-                      ctx->num_sms);
-        prof_end(ctx->st, K_POLY2B);
-        launch_twobody_forces(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
-                              ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy);
-        return MBPOL_OK;
-    }
-    return mbpol_fail(MBPOL_ERR_CAPACITY, "two-body pair list capacity");
-}
-
-mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
-    WaterTerm& t = ctx->t3;
-    const int nw = (int)t.waters.size();
-    if (nw < 3) return MBPOL_OK;
-    const bool periodic = t.method == MBPOL_CUTOFF_PERIODIC;
-    if (periodic) {
-        mbpol_status s = check_box(ctx, t.cutoff);
+    int np = 0;
+    if (ctx->shared_lists) {
+        np = (int)ctx->counts[0];
+    } else {
+        mbpol_status s = twobody_list(ctx, box, rc, &np);
         if (s) return s;
     }
-    const Box box = term_box(ctx, periodic);
-    const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
+    ctx->counts[0] = np;
+    const int stride = ctx->cap2;
+    MBPOL_CUDA_OK(ctx->x2.ensure(sizeof(float) * 2 * 31 * (size_t)stride));
+    MBPOL_CUDA_OK(ctx->g2.ensure(sizeof(float) * 31 * (size_t)stride));
+    MBPOL_CUDA_OK(ctx->e2.ensure(sizeof(float) * (size_t)stride));
+    launch_twobody_vars(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
+                        ctx->x2.as<float>(), stride);
+    prof_begin(ctx->st, K_POLY2B);
+    launch_poly2b(ctx->st, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride, ctx->num_sms);
+    prof_end(ctx->st, K_POLY2B);
+    launch_twobody_forces(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
+                          ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy);
+    return MBPOL_OK;
+}
+
+// Three-body neighbour lists and trimer count on their own (one host sync).
+mbpol_status threebody_list(mbpol_context* ctx, const Box& box, double rc, int* ntrip_out) {
+    WaterTerm& t = ctx->t3;
+    const int nw = (int)t.waters.size();
     int* cnt = ctx->d_counters.as<int>();
     const bool complete = t.rule == MBPOL_TRIMER_COMPLETE;
+    MBPOL_CUDA_OK(ctx->opos.ensure(sizeof(float4) * (size_t)nw));
     for (int attempt = 0; attempt < 4; ++attempt) {
         MBPOL_CUDA_OK(ctx->nlower3.ensure(sizeof(int) * (size_t)nw));
         MBPOL_CUDA_OK(ctx->count3.ensure(sizeof(int) * (size_t)nw));
@@ -238,17 +250,17 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
         MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
         if (!complete) {
             MBPOL_CUDA_OK(ctx->lower3.ensure(sizeof(int) * (size_t)nw * ctx->cap_lower3));
-            launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, -1.0, rc, -1.0, 0,
-                                 ctx->cap_lower3, nullptr, nullptr, ctx->lower3.as<int>(),
-                                 ctx->nlower3.as<int>(), nullptr, 0, cnt, cnt + 1, nullptr);
+            launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+                                 ctx->opos.as<float4>(), box, -1.0, rc, -1.0, 0, ctx->cap_lower3, nullptr, nullptr,
+                                 ctx->lower3.as<int>(), ctx->nlower3.as<int>(), nullptr, 0, cnt, cnt + 1, nullptr);
             launch_trimer_count(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
                                 ctx->count3.as<int>(), ctx->offs3.as<int>());
         } else {
             MBPOL_CUDA_OK(ctx->full3.ensure(sizeof(int) * (size_t)nw * ctx->cap_full3));
             MBPOL_CUDA_OK(ctx->nfull3.ensure(sizeof(int) * (size_t)nw));
-            launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc, -1.0, -1.0,
-                                 ctx->cap_full3, 0, ctx->full3.as<int>(), ctx->nfull3.as<int>(), nullptr,
-                                 nullptr, nullptr, 0, cnt, cnt + 1, nullptr);
+            launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+                                 ctx->opos.as<float4>(), box, rc, -1.0, -1.0, ctx->cap_full3, 0, ctx->full3.as<int>(),
+                                 ctx->nfull3.as<int>(), nullptr, nullptr, nullptr, 0, cnt, cnt + 1, nullptr);
             launch_trimer_complete(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
                                    ctx->full3.as<int>(), ctx->nfull3.as<int>(), ctx->cap_full3,
                                    ctx->count3.as<int>(), ctx->offs3.as<int>(), 0, nullptr, false);
@@ -262,33 +274,86 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
             else ctx->cap_lower3 *= 2;
             continue;
         }
-        const int ntrip = h[2];
-        ctx->counts[1] = ntrip;
-        if (ntrip > ctx->cap3) ctx->cap3 = ntrip + ntrip / 4 + 64;
-        const int stride = ctx->cap3;
-        MBPOL_CUDA_OK(ctx->trips3.ensure(sizeof(int4) * (size_t)stride));
-        MBPOL_CUDA_OK(ctx->x3.ensure(sizeof(float) * 2 * 36 * (size_t)stride));
-        MBPOL_CUDA_OK(ctx->g3.ensure(sizeof(float) * 36 * (size_t)stride));
-        MBPOL_CUDA_OK(ctx->e3.ensure(sizeof(float) * (size_t)stride));
-        if (!complete)
-            launch_trimer_fill(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
-                               ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>());
-        else
-            launch_trimer_complete(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
-                                   ctx->full3.as<int>(), ctx->nfull3.as<int>(), ctx->cap_full3, nullptr,
-                                   ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>(), true);
-        launch_threebody_vars(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
-                              box, ctx->x3.as<float>(), stride);
-        prof_begin(ctx->st, K_POLY3B);
-        launch_poly3b(ctx->st, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
-                      ctx->num_sms);
-        prof_end(ctx->st, K_POLY3B);
-        launch_threebody_forces(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(),
-                                ctx->d_pos.as<double>(), box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride,
-                                ctx->d_force.as<double>(), energy);
+        *ntrip_out = h[2];
         return MBPOL_OK;
     }
     return mbpol_fail(MBPOL_ERR_CAPACITY, "three-body neighbour capacity");
+}
+
+mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
+    WaterTerm& t = ctx->t3;
+    const int nw = (int)t.waters.size();
+    if (nw < 3) return MBPOL_OK;
+    const bool periodic = t.method == MBPOL_CUTOFF_PERIODIC;
+    if (periodic) {
+        mbpol_status s = check_box(ctx, t.cutoff);
+        if (s) return s;
+    }
+    const Box box = term_box(ctx, periodic);
+    const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
+    const bool complete = t.rule == MBPOL_TRIMER_COMPLETE;
+    int ntrip = 0;
+    if (ctx->shared_lists) {
+        ntrip = (int)ctx->counts[1];
+    } else {
+        mbpol_status s = threebody_list(ctx, box, rc, &ntrip);
+        if (s) return s;
+    }
+    ctx->counts[1] = ntrip;
+    if (ntrip > ctx->cap3) ctx->cap3 = ntrip + ntrip / 4 + 64;
+    const int stride = ctx->cap3;
+    MBPOL_CUDA_OK(ctx->trips3.ensure(sizeof(int4) * (size_t)stride));
+    MBPOL_CUDA_OK(ctx->x3.ensure(sizeof(float) * 2 * 36 * (size_t)stride));
+    MBPOL_CUDA_OK(ctx->g3.ensure(sizeof(float) * 36 * (size_t)stride));
+    MBPOL_CUDA_OK(ctx->e3.ensure(sizeof(float) * (size_t)stride));
+    if (!complete)
+        launch_trimer_fill(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
+                           ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>());
+    else
+        launch_trimer_complete(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
+                               ctx->full3.as<int>(), ctx->nfull3.as<int>(), ctx->cap_full3, nullptr,
+                               ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>(), true);
+    launch_threebody_vars(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+                          box, ctx->x3.as<float>(), stride);
+    prof_begin(ctx->st, K_POLY3B);
+    launch_poly3b(ctx->st, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
+                  ctx->num_sms);
+    prof_end(ctx->st, K_POLY3B);
+    launch_threebody_forces(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+                            box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride, ctx->d_force.as<double>(), energy);
+    return MBPOL_OK;
+}
+
+// Dispersion molecule list radius: site cutoff plus twice the largest O-H
+// extent (every H-H, O-H pair within the cutoff has its waters listed).
+double dispersion_list_radius(const WaterTerm& t) {
+    return t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff + 0.25;
+}
+
+// Dispersion molecule list on its own (one host sync).
+mbpol_status dispersion_list(mbpol_context* ctx, const Box& box) {
+    WaterTerm& t = ctx->tdisp;
+    const int nw = (int)t.waters.size();
+    const double rlist = dispersion_list_radius(t);
+    int* cnt = ctx->d_counters.as<int>();
+    MBPOL_CUDA_OK(ctx->opos.ensure(sizeof(float4) * (size_t)nw));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        MBPOL_CUDA_OK(ctx->full_d.ensure(sizeof(int) * (size_t)nw * ctx->cap_full_d));
+        MBPOL_CUDA_OK(ctx->nfull_d.ensure(sizeof(int) * (size_t)nw));
+        MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
+        launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(),
+                             box, rlist, -1.0, -1.0, ctx->cap_full_d, 0, ctx->full_d.as<int>(),
+                             ctx->nfull_d.as<int>(), nullptr, nullptr, nullptr, 0, cnt, cnt + 1, nullptr);
+        int h[2];
+        MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+        if (h[1]) {
+            ctx->cap_full_d *= 2;
+            continue;
+        }
+        return MBPOL_OK;
+    }
+    return mbpol_fail(MBPOL_ERR_CAPACITY, "dispersion neighbour capacity");
 }
 
 mbpol_status run_dispersion(mbpol_context* ctx, double* energy) {
@@ -302,30 +367,86 @@ mbpol_status run_dispersion(mbpol_context* ctx, double* energy) {
     }
     const Box box = term_box(ctx, periodic);
     const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
-    // molecule list radius: site cutoff plus twice the largest O-H extent
-    const double rlist = t.method == MBPOL_NOCUTOFF ? 1e30 : rc + 0.25;
-    int* cnt = ctx->d_counters.as<int>();
     if (ctx->cap_full_d == 0) ctx->cap_full_d = t.method == MBPOL_NOCUTOFF ? ((nw + 31) / 32) * 32 : 256;
-    for (int attempt = 0; attempt < 4; ++attempt) {
+    if (!ctx->shared_lists) {
+        mbpol_status s = dispersion_list(ctx, box);
+        if (s) return s;
+    }
+    launch_dispersion(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, ctx->full_d.as<int>(),
+                      ctx->nfull_d.as<int>(), ctx->cap_full_d, rc, ctx->d_force.as<double>(), energy);
+    return MBPOL_OK;
+}
+
+bool same_waters(const WaterTerm& a, const WaterTerm& b) {
+    if (a.waters.size() != b.waters.size()) return false;
+    for (size_t i = 0; i < a.waters.size(); ++i)
+        if (a.waters[i].x != b.waters[i].x || a.waters[i].y != b.waters[i].y || a.waters[i].z != b.waters[i].z)
+            return false;
+    return true;
+}
+
+// One neighbour pass for the two-body pairs, the three-body chain-rule
+// lists (and trimer count) and the dispersion list, when the three terms
+// share the water list and are all periodic with cutoffs: one launch and one
+// host synchronisation per evaluation instead of three of each.  Returns
+// false (and builds nothing) when the terms cannot share.
+mbpol_status build_shared_lists(mbpol_context* ctx, unsigned mask, bool* built) {
+    *built = false;
+    const unsigned need = MBPOL_TERM_BIT(MBPOL_TERM_TWOBODY) | MBPOL_TERM_BIT(MBPOL_TERM_THREEBODY) |
+                          MBPOL_TERM_BIT(MBPOL_TERM_DISPERSION);
+    const WaterTerm &t2 = ctx->t2, &t3 = ctx->t3, &td = ctx->tdisp;
+    if ((mask & need) != need || !t2.on || !t3.on || !td.on) return MBPOL_OK;
+    if (t2.method != MBPOL_CUTOFF_PERIODIC || t3.method != MBPOL_CUTOFF_PERIODIC ||
+        td.method != MBPOL_CUTOFF_PERIODIC || t3.rule == MBPOL_TRIMER_COMPLETE)
+        return MBPOL_OK;
+    if (!same_waters(t2, t3) || !same_waters(t2, td)) return MBPOL_OK;
+    const int nw = (int)t2.waters.size();
+    if (nw < 3) return MBPOL_OK;
+    for (const WaterTerm* t : {&t2, &t3, &td}) {
+        mbpol_status s = check_box(ctx, t->cutoff);
+        if (s) return s;
+    }
+    const Box box = term_box(ctx, true);
+    int* cnt = ctx->d_counters.as<int>();
+    if (ctx->cap2 == 0) ctx->cap2 = nw * 24 + 64;
+    if (ctx->cap_full_d == 0) ctx->cap_full_d = 256;
+    MBPOL_CUDA_OK(ctx->opos.ensure(sizeof(float4) * (size_t)nw));
+    MBPOL_CUDA_OK(ctx->nlower3.ensure(sizeof(int) * (size_t)nw));
+    MBPOL_CUDA_OK(ctx->count3.ensure(sizeof(int) * (size_t)nw));
+    MBPOL_CUDA_OK(ctx->offs3.ensure(sizeof(int) * (size_t)(nw + 1)));
+    MBPOL_CUDA_OK(ctx->nfull_d.ensure(sizeof(int) * (size_t)nw));
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        MBPOL_CUDA_OK(ctx->p2.ensure(sizeof(int2) * (size_t)ctx->cap2));
+        MBPOL_CUDA_OK(ctx->lower3.ensure(sizeof(int) * (size_t)nw * ctx->cap_lower3));
         MBPOL_CUDA_OK(ctx->full_d.ensure(sizeof(int) * (size_t)nw * ctx->cap_full_d));
-        MBPOL_CUDA_OK(ctx->nfull_d.ensure(sizeof(int) * (size_t)nw));
-        MBPOL_CUDA_OK(ctx->nlower_d.ensure(sizeof(int) * (size_t)nw));
         MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
-        launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rlist, -1.0, -1.0,
-                             ctx->cap_full_d, 0, ctx->full_d.as<int>(), ctx->nfull_d.as<int>(), nullptr,
-                             nullptr, nullptr, 0, cnt, cnt + 1, nullptr);
-        int h[2];
+        launch_mol_neighbors(ctx->st, nw, t2.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(),
+                             box, dispersion_list_radius(td), t3.cutoff, t2.cutoff, ctx->cap_full_d,
+                             ctx->cap_lower3, ctx->full_d.as<int>(), ctx->nfull_d.as<int>(), ctx->lower3.as<int>(),
+                             ctx->nlower3.as<int>(), ctx->p2.as<int2>(), ctx->cap2, cnt, cnt + 1, nullptr);
+        launch_trimer_count(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
+                            ctx->count3.as<int>(), ctx->offs3.as<int>());
+        int h[3];
         MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(h + 2, ctx->offs3.as<int>() + nw, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
-        if (h[1]) {
+        bool again = false;
+        if (h[1]) {  // a per-water list overflowed (which one is not recorded): grow both
+            ctx->cap_lower3 *= 2;
             ctx->cap_full_d *= 2;
-            continue;
+            again = true;
         }
-        launch_dispersion(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, ctx->full_d.as<int>(),
-                          ctx->nfull_d.as<int>(), ctx->cap_full_d, rc, ctx->d_force.as<double>(), energy);
+        if (h[0] > ctx->cap2) {
+            ctx->cap2 = h[0] + h[0] / 4 + 64;
+            again = true;
+        }
+        if (again) continue;
+        ctx->counts[0] = h[0];
+        ctx->counts[1] = h[2];
+        *built = true;
         return MBPOL_OK;
     }
-    return mbpol_fail(MBPOL_ERR_CAPACITY, "dispersion neighbour capacity");
+    return mbpol_fail(MBPOL_ERR_CAPACITY, "neighbour list capacity");
 }
 
 }  // namespace
@@ -483,11 +604,14 @@ mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
         launch_onebody(ctx->st, (int)ctx->t1.waters.size(), ctx->t1.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                        term_box(ctx, periodic), ctx->d_force.as<double>(), e + MBPOL_TERM_ONEBODY);
     }
+    ctx->shared_lists = false;
+    if (!s) s = build_shared_lists(ctx, mask, &ctx->shared_lists);
     if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_TWOBODY)) && ctx->t2.on) s = run_twobody(ctx, e + MBPOL_TERM_TWOBODY);
     if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_THREEBODY)) && ctx->t3.on)
         s = run_threebody(ctx, e + MBPOL_TERM_THREEBODY);
     if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_DISPERSION)) && ctx->tdisp.on)
         s = run_dispersion(ctx, e + MBPOL_TERM_DISPERSION);
+    ctx->shared_lists = false;
     if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS)) && ctx->elec) {
         s = ctx->elec->compute(ctx->st, ctx->d_pos.as<double>(), ctx->box, ctx->d_force.as<double>(),
                                e + MBPOL_TERM_ELECTROSTATICS);

@@ -170,6 +170,56 @@ __device__ __forceinline__ Bn ewald_bn(float r, float r2) {
     return b;
 }
 
+// Erf parts E_k = (2k-1)!!/r^(2k+1) - bn_k of the real-space functions, for
+// the intramolecular pairs whose reciprocal-space interaction has to be taken
+// out again.  Formed as rr_k - bn_k they cancel catastrophically when
+// alpha r << 1: the M site is 0.025 nm from O, where 1/r^3 ~ 6e4 and
+// rr_1 - bn_1 ~ 4 alpha^3 / (3 sqrt(pi)) ~ 37 nm^-3, so FP32 keeps three
+// digits.  With D = -(1/r) d/dr, E_k = D^k [erf(alpha r) / r]; the Maclaurin
+// series of erf gives, with x = alpha r,
+//   E_k = (2 alpha / sqrt(pi)) (2 alpha^2)^k sum_m (-1)^m x^(2m) / (m! (2m+2k+1))
+// (= (2 alpha/sqrt(pi)) (2 alpha^2)^k int_0^1 t^(2k) exp(-x^2 t^2) dt), whose
+// terms stay below the sum for x < 1.  Larger x (never an intramolecular
+// water pair at the usual alpha) falls back to the difference in FP64.
+__device__ Bn ewald_erf_part(float r) {
+    const float al = c_el.alpha;
+    const float x = al * r;
+    Bn e;
+    if (x < 1.f) {
+        const float x2 = x * x;
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, t = 1.f;  // t = (-x^2)^m / m!
+        for (int m = 0; m < 16; ++m) {
+            const float tm = 2.f * m;
+            s0 += t / (tm + 1.f);
+            s1 += t / (tm + 3.f);
+            s2 += t / (tm + 5.f);
+            s3 += t / (tm + 7.f);
+            t *= -x2 / (float)(m + 1);
+            if (fabsf(t) < 1e-9f) break;
+        }
+        const float c0 = 2.f * al / kSqrtPiF, a2 = 2.f * al * al;
+        e.b0 = c0 * s0;
+        e.b1 = c0 * a2 * s1;
+        e.b2 = c0 * a2 * a2 * s2;
+        e.b3 = c0 * a2 * a2 * a2 * s3;
+        return e;
+    }
+    const double rd = r, r2 = rd * rd, ad = al, ra = ad * rd;
+    const double b0 = erfc(ra) / rd, ex = exp(-ra * ra), a2 = 2.0 * ad * ad;
+    double a2n = a2 / (kSqrtPi * ad);
+    const double b1 = (b0 + a2n * ex) / r2;
+    a2n *= a2;
+    const double b2 = (3.0 * b1 + a2n * ex) / r2;
+    a2n *= a2;
+    const double b3 = (5.0 * b2 + a2n * ex) / r2;
+    const double q1 = 1.0 / rd, q3 = q1 / r2, q5 = 3.0 * q3 / r2, q7 = 5.0 * q5 / r2;
+    e.b0 = (float)(q1 - b0);
+    e.b1 = (float)(q3 - b1);
+    e.b2 = (float)(q5 - b2);
+    e.b3 = (float)(q7 - b3);
+    return e;
+}
+
 __device__ __forceinline__ f3 ld3(const float* p, int i) { return mk(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
 
 // ------------------------------------------------------ per-molecule prep
@@ -278,11 +328,23 @@ __device__ void water_charges(const double3 O, const double3 H1, const double3 H
 __global__ void elec_prepare_kernel(int nmol, const double* __restrict__ pos, int periodic, int redist,
                                     const float* __restrict__ q_static, float* __restrict__ off,
                                     float* __restrict__ q, float* __restrict__ dq, int pme,
-                                    int* __restrict__ gidx, float* __restrict__ gfrac, float* __restrict__ reach) {
+                                    int* __restrict__ gidx, float* __restrict__ gfrac, float* __restrict__ reach,
+                                    float4* __restrict__ opos) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmol) return;
     const int K = c_el.K, s0 = K * m;
     const double3 O = load_pos(pos, s0);
+    {
+        // FP32 first-site position for the neighbour prefilter, wrapped into
+        // the box when periodic so that FP32 keeps its absolute precision
+        double3 w = O;
+        if (periodic) {
+            w.x -= c_el.box[0] * floor(w.x * c_el.inv[0]);
+            w.y -= c_el.box[1] * floor(w.y * c_el.inv[1]);
+            w.z -= c_el.box[2] * floor(w.z * c_el.inv[2]);
+        }
+        opos[m] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
+    }
     double3 S[kMaxK];
     double r2max = 0.0;
     for (int s = 0; s < K; ++s) {
@@ -341,15 +403,18 @@ __global__ void elec_prepare_kernel(int nmol, const double* __restrict__ pos, in
 
 // Molecule neighbour list: j != i, O-O <= cutoff + reach_i + reach_j (cluster-restricted when
 // cluster ids are given), with the FP64 minimum-image O-O vector in FP32.
-__global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, int periodic, double rc,
-                                      const float* __restrict__ reach, int cap, int* __restrict__ nb,
-                                      float* __restrict__ nbd, int* __restrict__ nnb, int* __restrict__ overflow,
-                                      const int* __restrict__ cluster) {
+__global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, const float4* __restrict__ opos,
+                                      int periodic, double rc, const float* __restrict__ reach, int cap,
+                                      int* __restrict__ nb, float* __restrict__ nbd, int* __restrict__ nnb,
+                                      int* __restrict__ overflow, const int* __restrict__ cluster) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= nmol) return;
     const int K = c_el.K;
     const double3 oi = load_pos(pos, K * i);
+    const float4 fi = opos[i];
+    const float ai = fmaxf(fabsf(fi.x), fmaxf(fabsf(fi.y), fabsf(fi.z)));
+    const float rci = (float)rc + reach[i];
     const int ci = cluster ? cluster[i] : 0;
     int n = 0;
     for (int base = 0; base < nmol; base += 32) {
@@ -357,17 +422,30 @@ __global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, 
         bool in = false;
         double dx = 0, dy = 0, dz = 0;
         if (j < nmol && j != i && (!cluster || cluster[j] == ci)) {
-            const double3 oj = load_pos(pos, K * j);
-            dx = oj.x - oi.x;
-            dy = oj.y - oi.y;
-            dz = oj.z - oi.z;
+            // FP32 prefilter, padded well above its error (2^-24 of each
+            // coordinate): the list only has to contain every molecule pair
+            // with a site pair within the cutoff, which the pair kernels test
+            const float4 fj = opos[j];
+            float fx = fj.x - fi.x, fy = fj.y - fi.y, fz = fj.z - fi.z;
             if (periodic) {
-                dx = min_image(dx, c_el.box[0], c_el.inv[0]);
-                dy = min_image(dy, c_el.box[1], c_el.inv[1]);
-                dz = min_image(dz, c_el.box[2], c_el.inv[2]);
+                fx -= c_el.boxf[0] * rintf(fx * c_el.invf[0]);
+                fy -= c_el.boxf[1] * rintf(fy * c_el.invf[1]);
+                fz -= c_el.boxf[2] * rintf(fz * c_el.invf[2]);
             }
-            const double rl = rc + (double)reach[i] + (double)reach[j];
-            in = dx * dx + dy * dy + dz * dz <= rl * rl;
+            const float aj = fmaxf(fabsf(fj.x), fmaxf(fabsf(fj.y), fabsf(fj.z)));
+            const float rl = rci + reach[j] + 1e-4f + 1e-6f * (ai + aj);
+            if (fx * fx + fy * fy + fz * fz <= rl * rl) {
+                const double3 oj = load_pos(pos, K * j);
+                dx = oj.x - oi.x;
+                dy = oj.y - oi.y;
+                dz = oj.z - oi.z;
+                if (periodic) {
+                    dx = min_image(dx, c_el.box[0], c_el.inv[0]);
+                    dy = min_image(dy, c_el.box[1], c_el.inv[1]);
+                    dz = min_image(dz, c_el.box[2], c_el.inv[2]);
+                }
+                in = true;
+            }
         }
         const unsigned msk = __ballot_sync(0xffffffffu, in);
         if (in) {
@@ -593,21 +671,70 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// Dipole-dipole field coefficients (pf1, pf2) of the inter-molecular site
+// pair (a of molecule A, b of its neighbour in list slot t): planes
+// [A][a][b][c] of cap floats each, so that the lanes of a warp (consecutive
+// slots) read consecutive words.  The field at a from mu_b is
+// d (mu_b . d) pf2 + mu_b pf1, d = r_b - r_a.
+__device__ __forceinline__ size_t pair_coef_index(int A, int a, int b, int c, int t, int cap) {
+    return ((((size_t)A * kMaxK + a) * kMaxK + b) * 2 + c) * (size_t)cap + t;
+}
+
+// Intramolecular site pairs a < b of a K-site molecule, numbered
+// a (2K - a - 1) / 2 + (b - a - 1): (0,1) (0,2) (0,3) (1,2) (1,3) (2,3).
+constexpr int kMaxIntra = kMaxK * (kMaxK - 1) / 2;
+__device__ __forceinline__ int intra_pair(int a, int b, int K) {
+    if (a > b) { const int t = a; a = b; b = t; }
+    return a * (2 * K - a - 1) / 2 + (b - a - 1);
+}
+
 // Fixed field at the sites of molecule A (one warp).  PME adds E_rec (from
-// the gathered potential, -scale * dphi).  Writes E0 and mu0 = alpha E0.
+// the gathered potential, -scale * dphi).  Writes E0 and mu0 = alpha E0, and
+// the intramolecular dipole-field coefficients of the geometry: for pair
+// p = (a, b), intra[2p] = pf1 and intra[2p + 1] = pf2 such that the field at
+// a from mu_b is d (mu_b . d) pf2 + mu_b pf1 with d = r_b - r_a (same-water
+// Thole parameters; with PME the reciprocal-space part is taken out and
+// pairs beyond the cutoff get zeros).  They are used by every solver
+// iteration, so the Thole and Ewald functions of these pairs run once.
 template <bool PME>
 __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ q,
                                    const float* __restrict__ damp, const float* __restrict__ pol,
                                    const int* __restrict__ type, const int* __restrict__ nb,
                                    const float* __restrict__ nbd, const int* __restrict__ nnb, int cap,
                                    const float* __restrict__ phi_fix, float* __restrict__ E0,
-                                   float* __restrict__ mu_out) {
+                                   float* __restrict__ mu_out, float* __restrict__ intra,
+                                   float* __restrict__ pcoef) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (A >= nmol) return;
     const int K = c_el.K;
     MolSites MA;
     load_mol(A, off, q, damp, pol, type, MA);
+    #pragma unroll
+    for (int a = 0; a < kMaxK; ++a)
+    #pragma unroll
+    for (int b = a + 1; b < kMaxK; ++b) {
+        if (b >= K || lane != intra_pair(a, b, K)) continue;
+        const f3 d = MA.off[b] - MA.off[a];
+        const float r2 = dot(d, d);
+        float pf1 = 0.f, pf2 = 0.f;
+        if (!PME || r2 <= c_el.rc2) {
+            const float r = sqrtf(r2);
+            const Thole th = thole(r, MA.damp[a] * MA.damp[b], tdd_gamma(true, MA.type[a], MA.type[b]));
+            const float rr3 = 1.f / (r2 * r), rr5 = 3.f * rr3 / r2;
+            if (PME) {
+                // (1 - s3) rr3 - bn1 and bn2 - (1 - s5) rr5, as E_k - s rr
+                const Bn ek = ewald_erf_part(r);
+                pf1 = ek.b1 - s3_of(th) * rr3;
+                pf2 = s5_of(th) * rr5 - ek.b2;
+            } else {
+                pf1 = -s3_of(th) * rr3;
+                pf2 = s5_of(th) * rr5;
+            }
+        }
+        intra[(size_t)2 * kMaxIntra * A + 2 * lane] = pf1;
+        intra[(size_t)2 * kMaxIntra * A + 2 * lane + 1] = pf2;
+    }
     float E[kMaxK][3];
     #pragma unroll
     for (int a = 0; a < kMaxK; ++a) E[a][0] = E[a][1] = E[a][2] = 0.f;
@@ -618,6 +745,36 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
         const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
         MolSites MB;
         load_mol(B, off, q, damp, pol, type, MB);
+        // dipole-dipole field coefficients of this geometry for the solver
+        // iterations (layout of pair_coef_index); pairs with an unpolarizable
+        // site are never read and not written
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) {
+            if (a >= K || MA.pol[a] == 0.f) continue;
+            #pragma unroll
+            for (int b = 0; b < kMaxK; ++b) {
+                if (b >= K || MB.pol[b] == 0.f) continue;
+                const f3 d = site_delta(dAB, MB.off[b], MA.off[a]);
+                const float r2 = dot(d, d);
+                float pf1 = 0.f, pf2 = 0.f;
+                if (!PME || r2 <= c_el.rc2) {
+                    const float r = sqrtf(r2);
+                    const Thole th = thole(r, MA.damp[a] * MB.damp[b], c_el.thole[2]);
+                    if (PME) {
+                        const Bn bn = ewald_bn(r, r2);
+                        const float rr3 = (1.f - s3_of(th)) / (r2 * r);
+                        const float rr5 = 3.f * (1.f - s5_of(th)) / (r2 * r2 * r);
+                        pf1 = rr3 - bn.b1;
+                        pf2 = bn.b2 - rr5;
+                    } else {
+                        pf1 = -s3_of(th) / (r2 * r);
+                        pf2 = 3.f * s5_of(th) / (r2 * r2 * r);
+                    }
+                }
+                pcoef[pair_coef_index(A, a, b, 0, t, cap)] = pf1;
+                pcoef[pair_coef_index(A, a, b, 1, t, cap)] = pf2;
+            }
+        }
         #pragma unroll
         for (int a = 0; a < kMaxK; ++a) {
             if (a >= K) continue;
@@ -653,22 +810,24 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
     if (lane == 0) {
         if (PME) {
             // intramolecular pairs: s3 = 2 (reference :1375-1377), within the cutoff
-            for (int a = 0; a < K; ++a)
-                for (int b = 0; b < K; ++b) {
-                    if (a == b || MA.q[b] == 0.f) continue;
+            #pragma unroll
+            for (int a = 0; a < kMaxK; ++a)
+                #pragma unroll
+                for (int b = 0; b < kMaxK; ++b) {
+                    if (a >= K || b >= K || a == b || MA.q[b] == 0.f) continue;
                     const f3 d = MA.off[b] - MA.off[a];
                     const float r2 = dot(d, d);
                     if (r2 > c_el.rc2) continue;
-                    const float r = sqrtf(r2);
-                    const Bn bn = ewald_bn(r, r2);
-                    const float fac = bn.b1 - 1.f / (r2 * r);
+                    const float fac = -ewald_erf_part(sqrtf(r2)).b1;  // bn1 - 1/r^3
                     const float c = -MA.q[b] * fac;
                     E[a][0] += d.x * c;
                     E[a][1] += d.y * c;
                     E[a][2] += d.z * c;
                 }
         }
-        for (int a = 0; a < K; ++a) {
+        #pragma unroll
+        for (int a = 0; a < kMaxK; ++a) {
+            if (a >= K) continue;
             const int i = K * A + a;
             float ex = E[a][0], ey = E[a][1], ez = E[a][2];
             if (PME) {
@@ -701,21 +860,22 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                                       const float* __restrict__ phi_mu, const float* __restrict__ mu_in,
                                       float* __restrict__ mu_out, double* __restrict__ mu_d,
                                       double* __restrict__ eps2, int mode, float* __restrict__ Ebase,
-                                      const float* __restrict__ anchor) {
+                                      const float* __restrict__ anchor, const float* __restrict__ intra,
+                                      const float* __restrict__ pcoef) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     double d2sum = 0.0;
     if (A < nmol) {
         const int K = c_el.K;
         f3 offA[kMaxK];
-        float dA[kMaxK];
-        int tA[kMaxK];
+        float polA[kMaxK];
         #pragma unroll
         for (int a = 0; a < kMaxK; ++a) {
+            offA[a] = mk(0.f, 0.f, 0.f);
+            polA[a] = 0.f;
             if (a < K) {
                 offA[a] = ld3(off, K * A + a);
-                dA[a] = damp[K * A + a];
-                tA[a] = type[K * A + a];
+                polA[a] = pol[K * A + a];
             }
         }
         float E[kMaxK][3];
@@ -729,29 +889,17 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
             for (int b = 0; b < kMaxK; ++b) {
                 if (b >= K) continue;
                 const int jb = K * B + b;
+                if (pol[jb] == 0.f) continue;
                 const f3 mub = ld3(mu_in, jb);
-                if (mub.x == 0.f && mub.y == 0.f && mub.z == 0.f) continue;
                 const f3 offb = ld3(off, jb);
-                const float db = damp[jb];
                 #pragma unroll
                 for (int a = 0; a < kMaxK; ++a) {
-                    if (a >= K) continue;
+                    if (a >= K || polA[a] == 0.f) continue;
                     const f3 d = site_delta(dAB, offb, offA[a]);
-                    const float r2 = dot(d, d);
-                    if (PME && r2 > c_el.rc2) continue;
-                    const float r = sqrtf(r2);
-                    const Thole th = thole(r, dA[a] * db, c_el.thole[2]);
-                    float pf1, pf2;
-                    if (PME) {
-                        const Bn bn = ewald_bn(r, r2);
-                        const float rr3 = (1.f - s3_of(th)) / (r2 * r);
-                        const float rr5 = 3.f * (1.f - s5_of(th)) / (r2 * r2 * r);
-                        pf1 = rr3 - bn.b1;
-                        pf2 = bn.b2 - rr5;
-                    } else {
-                        pf1 = -s3_of(th) / (r2 * r);
-                        pf2 = 3.f * s5_of(th) / (r2 * r2 * r);
-                    }
+                    // coefficients of this geometry from the fixed-field pass
+                    // (zero beyond the cutoff)
+                    const float pf1 = pcoef[pair_coef_index(A, a, b, 0, t, cap)];
+                    const float pf2 = pcoef[pair_coef_index(A, a, b, 1, t, cap)];
                     const float dur = dot(mub, d) * pf2;
                     E[a][0] += d.x * dur + mub.x * pf1;
                     E[a][1] += d.y * dur + mub.y * pf1;
@@ -766,32 +914,26 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
             E[a][2] = warp_sum(E[a][2]);
         }
         if (lane == 0) {
-            // intramolecular pairs (same-water Thole parameters)
-            for (int a = 0; a < K; ++a)
-                for (int b = 0; b < K; ++b) {
-                    if (a == b) continue;
-                    const int jb = K * A + b;
-                    const f3 mub = ld3(mu_in, jb);
+            // intramolecular pairs: coefficients of this geometry from the
+            // fixed-field pass
+            const float* pin = intra + (size_t)2 * kMaxIntra * A;
+            #pragma unroll
+            for (int a = 0; a < kMaxK; ++a)
+                #pragma unroll
+                for (int b = 0; b < kMaxK; ++b) {
+                    if (a >= K || b >= K || a == b) continue;
+                    const int p = intra_pair(a, b, K);
+                    const float pf1 = pin[2 * p], pf2 = pin[2 * p + 1];
+                    const f3 mub = ld3(mu_in, K * A + b);
                     const f3 d = offA[b] - offA[a];
-                    const float r2 = dot(d, d);
-                    if (PME && r2 > c_el.rc2) continue;
-                    const float r = sqrtf(r2);
-                    const Thole th = thole(r, dA[a] * dA[b], tdd_gamma(true, tA[a], tA[b]));
-                    float pf1, pf2;
-                    if (PME) {
-                        const Bn bn = ewald_bn(r, r2);
-                        pf1 = (1.f - s3_of(th)) / (r2 * r) - bn.b1;
-                        pf2 = bn.b2 - 3.f * (1.f - s5_of(th)) / (r2 * r2 * r);
-                    } else {
-                        pf1 = -s3_of(th) / (r2 * r);
-                        pf2 = 3.f * s5_of(th) / (r2 * r2 * r);
-                    }
                     const float dur = dot(mub, d) * pf2;
                     E[a][0] += d.x * dur + mub.x * pf1;
                     E[a][1] += d.y * dur + mub.y * pf1;
                     E[a][2] += d.z * dur + mub.z * pf1;
                 }
-            for (int a = 0; a < K; ++a) {
+            #pragma unroll
+            for (int a = 0; a < kMaxK; ++a) {
+                if (a >= K) continue;
                 const int i = K * A + a;
                 const f3 mu = ld3(mu_in, i);
                 const double m0 = mu_d[3 * i], m1 = mu_d[3 * i + 1], m2 = mu_d[3 * i + 2];
@@ -975,8 +1117,11 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
         }
         if (lane == 0) {
             // intramolecular pairs, a < b (both sites are A's)
-            for (int a = 0; a < K; ++a)
-                for (int b = a + 1; b < K; ++b) {
+            #pragma unroll
+            for (int a = 0; a < kMaxK; ++a)
+                #pragma unroll
+                for (int b = a + 1; b < kMaxK; ++b) {
+                    if (b >= K) continue;
                     const f3 d = offA[b] - offA[a];
                     const float r2 = dot(d, d);
                     if (PME && r2 > c_el.rc2) continue;
@@ -988,29 +1133,19 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                     const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd2);
                     f3 fo;
                     if (PME) {
-                        const Bn bn = ewald_bn(r, r2);
+                        // same water: s1CC = s3CD = s3CC = s5CD = 0, so every
+                        // term is bn_k - rr_k = -E_k, or bn_k - (1 - s) rr_k
+                        // = s rr_k - E_k for the dipole-dipole ones
+                        const Bn ek = ewald_erf_part(r);
                         const float gl0 = qA[a] * qA[b];
                         const float gli = qA[b] * sci3 - qA[a] * sci4;
-                        // same water: s1CC = s3CD = s3CC = s5CD = 0
-                        {
-                            const double rd = sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z);
-                            const double r1d = 1.0 / rd, r3d = r1d / (rd * rd);
-                            const double gl0d = (double)qA[a] * qA[b];
-                            const double glid = (double)qA[b] * ((double)muA[a].x * d.x + (double)muA[a].y * d.y +
-                                                                 (double)muA[a].z * d.z) -
-                                                (double)qA[a] * ((double)muA[b].x * d.x + (double)muA[b].y * d.y +
-                                                                 (double)muA[b].z * d.z);
-                            e += (double)bn.b0 * gl0d + 0.5 * (double)bn.b1 * glid - r1d * gl0d - 0.5 * r3d * glid;
-                        }
-                        P[a] += qA[b] * (bn.b0 - rr1) - sci4 * (bn.b1 - rr3);
-                        P[b] += qA[a] * (bn.b0 - rr1) + sci3 * (bn.b1 - rr3);
-                        const float gf1 = bn.b1 * gl0, gfr1 = rr3 * gl0;
-                        const float gfi1 = bn.b2 * (gli + mumu) - bn.b3 * sci3 * sci4;
-                        const float gfri1 = rr5 * (gli + mumu * (1.f - s5DD)) - rr7 * sci3 * sci4 * (1.f - s7DD);
-                        const float c_d = gf1 - gfr1 + gfi1 - gfri1;
-                        const float c_i = -qA[b] * bn.b1 + qA[b] * rr3;
-                        const float c_j = qA[a] * bn.b1 - qA[a] * rr3;
-                        const float c_dd = bn.b2 - rr5 * (1.f - s5DD);
+                        e -= (double)ek.b0 * gl0 + 0.5 * (double)ek.b1 * gli;
+                        P[a] += sci4 * ek.b1 - qA[b] * ek.b0;
+                        P[b] -= qA[a] * ek.b0 + sci3 * ek.b1;
+                        const float c_dd = s5DD * rr5 - ek.b2;
+                        const float c_d = -ek.b1 * gl0 - ek.b2 * gli + c_dd * mumu - (s7DD * rr7 - ek.b3) * sci3 * sci4;
+                        const float c_i = qA[b] * ek.b1;
+                        const float c_j = -qA[a] * ek.b1;
                         fo = d * c_d + muA[a] * (c_i + sci4 * c_dd) + muA[b] * (c_j + sci3 * c_dd);
                     } else {
                         // same water: no charge-charge or charge-dipole terms
@@ -1029,7 +1164,9 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                 const float sx = c_el.scale[0], sy = c_el.scale[1], sz = c_el.scale[2];
                 const float sc[3] = {sx, sy, sz};
                 const float ak = c_el.alpha;
-                for (int a = 0; a < K; ++a) {
+                #pragma unroll
+                for (int a = 0; a < kMaxK; ++a) {
+                    if (a >= K) continue;
                     const int i = K * A + a;
                     const float* pf = phi_fix + 10 * i;
                     const float* pm = phi_mu + 10 * i;
@@ -1042,8 +1179,10 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                     // hessian index of (a, k): xx 4, yy 5, zz 6, xy 7, xz 8, yz 9
                     const int H[3][3] = {{4, 7, 8}, {7, 5, 9}, {8, 9, 6}};
                     const float m3[3] = {muA[a].x, muA[a].y, muA[a].z};
+                    #pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         float fdip = 0.f;
+                        #pragma unroll
                         for (int k = 0; k < 3; ++k) fdip += sc[k] * m3[k] * (pf[H[c][k]] + pm[H[c][k]]);
                         const float fc = sc[c] * (fdip + qA[a] * (pf[1 + c] + pm[1 + c]));
                         F[a][c] -= fc;
@@ -1053,8 +1192,10 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
             // charge-derivative forces: F_i -= sum_s dq_i[s] * phi(other site s)
             // (reference :2767-2773 for PME, :791-827 for NoCutoff)
             if (redist && K == 4) {
-                for (int a = 0; a < K; ++a) {
+                #pragma unroll
+                for (int a = 0; a < kMaxK; ++a) {
                     const int i = K * A + a;
+                    #pragma unroll
                     for (int s = 0; s < 3; ++s) {
                         const float phis = P[s + 1];
                         F[a][0] -= dq[9 * i + 3 * s] * phis;
@@ -1063,7 +1204,9 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                     }
                 }
             }
-            for (int a = 0; a < K; ++a) {
+            #pragma unroll
+            for (int a = 0; a < kMaxK; ++a) {
+                if (a >= K) continue;
                 const int i = K * A + a;
                 force[3 * i] += (double)F[a][0] * f;
                 force[3 * i + 1] += (double)F[a][1] * f;
@@ -1201,8 +1344,9 @@ struct ElecImpl {
     std::vector<float> q_static, damp, pol;
     std::vector<int> type;
     DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu2, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd,
-        d_gfrac, d_reach, d_ebase;
+        d_gfrac, d_reach, d_ebase, d_intra, d_pcoef;
     DBuf<int> d_type, d_nb, d_nnb, d_gidx, d_flags;
+    DBuf<float4> d_opos;
     DBuf<double> d_eps2, d_mud, d_mud_prev;
     int cap = 0;
     // PME
@@ -1292,6 +1436,8 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     MBPOL_CUDA_OK(I.d_gidx.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_nnb.ensure(I.nmol));
     MBPOL_CUDA_OK(I.d_reach.ensure(I.nmol));
+    MBPOL_CUDA_OK(I.d_opos.ensure(I.nmol));
+    MBPOL_CUDA_OK(I.d_intra.ensure((size_t)2 * kMaxIntra * I.nmol));
     MBPOL_CUDA_OK(I.d_flags.ensure(4));
     MBPOL_CUDA_OK(I.d_eps2.ensure(1));
     MBPOL_CUDA_OK(I.d_mud.ensure(3 * (size_t)n));
@@ -1414,7 +1560,8 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     const int redist = I.prm.include_charge_redistribution ? 1 : 0;
     count_launch();
     elec_prepare_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, pos, box.periodic, redist, I.d_qs.p, I.d_off.p,
-                                                            I.d_q.p, I.d_dq.p, I.pme ? 1 : 0, I.d_gidx.p, I.d_gfrac.p, I.d_reach.p);
+                                                            I.d_q.p, I.d_dq.p, I.pme ? 1 : 0, I.d_gidx.p, I.d_gfrac.p, I.d_reach.p,
+                                                            I.d_opos.p);
     // neighbour list
     const double rcut = I.pme ? I.prm.cutoff : 1e30;
     if (I.cap == 0) I.cap = I.pme ? 256 : ((nmol + 31) / 32) * 32;
@@ -1424,7 +1571,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_flags.p, 0, sizeof(int), st));
         count_launch();
         elec_neighbors_kernel<<<(nmol * 32 + 127) / 128, 128, 0, st>>>(
-            nmol, pos, box.periodic && I.pme, rcut, I.d_reach.p, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p,
+            nmol, pos, I.d_opos.p, box.periodic && I.pme, rcut, I.d_reach.p, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p,
             I.d_flags.p, nullptr);
         int ovf = 0;
         MBPOL_CUDA_OK(cudaMemcpyAsync(&ovf, I.d_flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1433,6 +1580,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         if (attempt > 6) return mbpol_fail(MBPOL_ERR_CAPACITY, "electrostatics neighbour capacity");
         I.cap *= 2;
     }
+    MBPOL_CUDA_OK(I.d_pcoef.ensure((size_t)nmol * kMaxK * kMaxK * 2 * I.cap));
     const int wblocks = (nmol * 32 + 127) / 128;
     const size_t nreal = I.pme ? (size_t)I.grid[0] * I.grid[1] * I.grid[2] : 0;
     // fixed field
@@ -1447,13 +1595,14 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         count_launch();
         fixed_field_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                            I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_phi_fix.p,
-                                                           I.d_E0.p, I.d_mu0.p);
+                                                           I.d_E0.p, I.d_mu0.p, I.d_intra.p, I.d_pcoef.p);
         prof_end(st, K_ELEC_FIXED);
     } else {
         count_launch();
         fixed_field_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p,
                                                             I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
-                                                            nullptr, I.d_E0.p, I.d_mu0.p);
+                                                            nullptr, I.d_E0.p, I.d_mu0.p, I.d_intra.p,
+                                                            I.d_pcoef.p);
     }
     // d_mu0 holds float(mu) of the starting dipoles (alpha*E0 from the
     // fixed-field kernel, or the previous call's dipoles)
@@ -1502,12 +1651,14 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
             induced_update_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                                                                   I.d_phi_mu.p, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
-                                                                  kmode, I.d_ebase.p, anchor);
+                                                                  kmode, I.d_ebase.p, anchor, I.d_intra.p,
+                                                                  I.d_pcoef.p);
         else
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                    I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                                                                    nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
-                                                                   kmode, I.d_ebase.p, anchor);
+                                                                   kmode, I.d_ebase.p, anchor, I.d_intra.p,
+                                                                  I.d_pcoef.p);
         prof_end(st, K_ELEC_INDUCED);
         if (kmode == 1) anchor = mu_in;
         mode = kmode == 0 ? 0 : 2;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "mbpol_internal.cuh"
+#include "poly_tables.h"
 
 namespace mbpol {
 
@@ -23,11 +24,18 @@ void launch_threebody_forces(cudaStream_t st, int ntrip, const int4* trips, cons
 cudaError_t poly_tables_upload(int device);
 void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms);
 void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms);
+// the two-body kernel on caller-supplied device tables (raise its dynamic
+// shared-memory limit once per device with poly2b_kernel_setup first)
+cudaError_t poly2b_kernel_setup();
+void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, int n1, const PolyNode* l2, const PolyNode* l3,
+                        const PolyNode* lv, const float* X, float* G, float* E, int n, int stride, int num_sms);
 
 // neighbor.cu
-void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double r_full,
-                          double r_3b, double r_2b, int cap_full, int cap_lower, int* full, int* nfull, int* lower,
-                          int* nlower, int2* pairs, int cap_pairs, int* npairs, int* overflow, const int* cluster);
+// opos: scratch of nw float4 (FP32 O positions for the distance prefilter)
+void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, float4* opos, Box box,
+                          double r_full, double r_3b, double r_2b, int cap_full, int cap_lower, int* full,
+                          int* nfull, int* lower, int* nlower, int2* pairs, int cap_pairs, int* npairs,
+                          int* overflow, const int* cluster);
 void launch_trimer_count(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower, int* count,
                          int* offs);
 void launch_trimer_fill(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower,

@@ -1,7 +1,8 @@
 // O-O neighbour structures for the many-body terms.
 //
 //  * mol_neighbors_kernel: one warp per water i scans all waters j (tiles of
-//    32, ballot-compacted appends) and records
+//    32, ballot-compacted appends; distances prefiltered in FP32 and settled
+//    in FP64 near each threshold) and records
 //      - full[i][*]   j != i with d(i,j) <= r_full   (electrostatics, dispersion)
 //      - lower[i][*]  j <  i with d(i,j) <= r_3b     (three-body chain rule)
 //      - pairs        (i,j), j > i, d <= r_2b        (two-body half list)
@@ -31,26 +32,86 @@ __device__ __forceinline__ double oo_dist2(double3 a, double3 b, const Box& box)
     return dx * dx + dy * dy + dz * dz;
 }
 
-__global__ void mol_neighbors_kernel(int nw, const int4* __restrict__ waters, const double* __restrict__ pos, Box box,
-                                     double r_full2, double r_3b2, double r_2b2, int cap_full, int cap_lower,
-                                     int* __restrict__ full, int* __restrict__ nfull, int* __restrict__ lower,
-                                     int* __restrict__ nlower, int2* __restrict__ pairs, int cap_pairs,
-                                     int* __restrict__ npairs, int* __restrict__ overflow, const int* __restrict__ cluster) {
+// FP32 copy of each water's O position (wrapped into the box when periodic,
+// so FP32 keeps its absolute precision) for the distance prefilter.
+__global__ void o_positions_kernel(int nw, const int4* __restrict__ waters, const double* __restrict__ pos, Box box,
+                                   float4* __restrict__ opos) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nw) return;
+    double3 o = load_pos(pos, waters[i].x);
+    if (box.periodic) {
+        o.x -= box.L[0] * floor(o.x * box.inv[0]);
+        o.y -= box.L[1] * floor(o.y * box.inv[1]);
+        o.z -= box.L[2] * floor(o.z * box.inv[2]);
+    }
+    opos[i] = make_float4((float)o.x, (float)o.y, (float)o.z, 0.f);
+}
+
+// d^2 <= r^2 decided in FP32 when d^2 is farther than the FP32 error bound
+// from r^2, else in FP64 (d2 is computed at most once per pair, lazily), so
+// list membership is exactly the FP64 test.  Bound: each FP32 coordinate is
+// off by <= 2^-24 |x|, so d^2 is off by <= ~2 |d| 2^-23 (|x_i| + |x_j|);
+// the margin is 8x that, plus 1e-6 nm^2.
+struct PairTest {
+    const double3& oi;
+    double d2 = -1.0;
+    __device__ bool le(float d2f, float r, float slack, double r2, const int4* __restrict__ waters,
+                       const double* __restrict__ pos, int j, const Box& box) {
+        const float r2f = r * r;
+        const float m = 1e-6f + slack * r;
+        if (d2f < r2f - m) return true;
+        if (d2f > r2f + m) return false;
+        if (d2 < 0.0) {
+            const double3 o = load_pos(pos, waters[j].x);
+            double dx = o.x - oi.x, dy = o.y - oi.y, dz = o.z - oi.z;
+            if (box.periodic) {
+                dx = min_image(dx, box.L[0], box.inv[0]);
+                dy = min_image(dy, box.L[1], box.inv[1]);
+                dz = min_image(dz, box.L[2], box.inv[2]);
+            }
+            d2 = dx * dx + dy * dy + dz * dz;
+        }
+        return d2 <= r2;
+    }
+};
+
+__global__ void mol_neighbors_kernel(int nw, const int4* __restrict__ waters, const double* __restrict__ pos,
+                                     const float4* __restrict__ opos, Box box, double r_full2, double r_3b2,
+                                     double r_2b2, int cap_full, int cap_lower, int* __restrict__ full,
+                                     int* __restrict__ nfull, int* __restrict__ lower, int* __restrict__ nlower,
+                                     int2* __restrict__ pairs, int cap_pairs, int* __restrict__ npairs,
+                                     int* __restrict__ overflow, const int* __restrict__ cluster) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nw) return;
     const int i = warp;
     const double3 oi = load_pos(pos, waters[i].x);
+    const float4 fi = opos[i];
+    const float ai = fmaxf(fabsf(fi.x), fmaxf(fabsf(fi.y), fabsf(fi.z)));
+    const float Lx = (float)box.L[0], Ly = (float)box.L[1], Lz = (float)box.L[2];
+    const float ix = (float)box.inv[0], iy = (float)box.inv[1], iz = (float)box.inv[2];
+    const float rf = full ? (float)sqrt(r_full2) : 0.f, r3 = lower ? (float)sqrt(r_3b2) : 0.f,
+                r2 = pairs ? (float)sqrt(r_2b2) : 0.f;
     const int ci = cluster ? cluster[i] : 0;
     int nf = 0, nl = 0;
     for (int base = 0; base < nw; base += 32) {
         const int j = base + lane;
         bool in_full = false, in_lower = false, in_pair = false;
         if (j < nw && j != i && (!cluster || cluster[j] == ci)) {
-            const double d2 = oo_dist2(oi, load_pos(pos, waters[j].x), box);
-            in_full = full && d2 <= r_full2;
-            in_lower = lower && j < i && d2 <= r_3b2;
-            in_pair = pairs && j > i && d2 <= r_2b2;
+            const float4 fj = opos[j];
+            float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
+            if (box.periodic) {
+                dx -= Lx * rintf(dx * ix);
+                dy -= Ly * rintf(dy * iy);
+                dz -= Lz * rintf(dz * iz);
+            }
+            const float d2f = dx * dx + dy * dy + dz * dz;
+            const float aj = fmaxf(fabsf(fj.x), fmaxf(fabsf(fj.y), fabsf(fj.z)));
+            const float slack = 16.f * 1.2e-7f * 3.f * (ai + aj);
+            PairTest pt{oi};
+            in_full = full && pt.le(d2f, rf, slack, r_full2, waters, pos, j, box);
+            in_lower = lower && j < i && pt.le(d2f, r3, slack, r_3b2, waters, pos, j, box);
+            in_pair = pairs && j > i && pt.le(d2f, r2, slack, r_2b2, waters, pos, j, box);
         }
         unsigned m = __ballot_sync(0xffffffffu, in_full);
         if (in_full) {
@@ -168,14 +229,17 @@ __global__ void trimer_complete_kernel(int nw, const int4* __restrict__ waters, 
     if (count) count[v] = cnt;
 }
 
-void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double r_full,
-                          double r_3b, double r_2b, int cap_full, int cap_lower, int* full, int* nfull, int* lower,
-                          int* nlower, int2* pairs, int cap_pairs, int* npairs, int* overflow, const int* cluster) {
+void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, float4* opos, Box box,
+                          double r_full, double r_3b, double r_2b, int cap_full, int cap_lower, int* full,
+                          int* nfull, int* lower, int* nlower, int2* pairs, int cap_pairs, int* npairs,
+                          int* overflow, const int* cluster) {
     if (nw <= 0) return;
+    count_launch();
+    o_positions_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, opos);
     const int threads = 256;
     const int blocks = (nw * 32 + threads - 1) / threads;
     count_launch();
-    mol_neighbors_kernel<<<blocks, threads, 0, st>>>(nw, waters, pos, box, r_full * r_full, r_3b * r_3b,
+    mol_neighbors_kernel<<<blocks, threads, 0, st>>>(nw, waters, pos, opos, box, r_full * r_full, r_3b * r_3b,
                                                      r_2b * r_2b, cap_full, cap_lower, full, nfull, lower, nlower,
                                                      pairs, cap_pairs, npairs, overflow, cluster);
 }

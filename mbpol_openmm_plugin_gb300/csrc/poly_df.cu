@@ -20,13 +20,9 @@
 // warp-uniform addresses.  X: [2][nvars][stride] floats (FP64 variables as
 // hi and lo planes); G: [nvars][stride]; E: [stride].
 #include "mbpol_internal.cuh"
+#include "poly_tables.h"
 
 namespace mbpol {
-
-struct PolyNode {
-    float hi, lo;
-    int var, end;
-};
 
 #include "gen/poly2b_tables.inc"
 #include "gen/poly3b_tables.inc"
@@ -63,10 +59,26 @@ __device__ __forceinline__ void mul_df_df(const DF a, const DF b, float& p, floa
     q = __fmaf_rn(a.l, b.h, q);
 }
 
+// One leaf L (coefficient c, variable l) under a level-3 node with prefix
+// product P3: V3 += c x_l and g_l += c P3.
+__device__ __forceinline__ void leaf_update(const PolyNode& L, float xl, float xll, const DF& P3, DF& V3, DF& g) {
+    float p, q;
+    p = __fmul_rn(xl, L.hi);
+    q = __fmaf_rn(xl, L.hi, -p);
+    q = __fmaf_rn(xl, L.lo, q);
+    q = __fmaf_rn(xll, L.hi, q);
+    acc(V3, p, q);
+    p = __fmul_rn(P3.h, L.hi);
+    q = __fmaf_rn(P3.h, L.hi, -p);
+    q = __fmaf_rn(P3.l, L.hi, q);
+    q = __fmaf_rn(P3.h, L.lo, q);
+    acc(g, p, q);
+}
+
 template <int NV>
 __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restrict__ l1, int n1,
                                                           const PolyNode* __restrict__ l2,
-                                                          const PolyNode* __restrict__ l3,
+                                                          const PolyNode* __restrict__ l3, int n3,
                                                           const PolyNode* __restrict__ lv,
                                                           const float* __restrict__ X, float* __restrict__ G,
                                                           float* __restrict__ E, int n, int stride) {
@@ -88,6 +100,12 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
         }
         DF Ev = {0.f, 0.f};
         int c2 = 0, c3 = 0, cl = 0;
+        // The next level-3 node is read one step ahead.  Children of a node
+        // have distinct variables, so several leaves' gradient pairs can be
+        // read before any of them is written back; a parent's own pair is
+        // read only after its children's writes (a child may share its
+        // variable).
+        PolyNode Cn = n3 > 0 ? l3[0] : PolyNode{0.f, 0.f, 0, 0};
         for (int a = 0; a < n1; ++a) {
             const PolyNode A = l1[a];
             const float xi = xs[A.var * kBlock + t], xil = xq[A.var * kBlock + t];
@@ -102,32 +120,49 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                 P2.l = __fmaf_rn(xi, xjl, P2.l);
                 P2.l = __fmaf_rn(xil, xj, P2.l);
                 for (; c3 < B.end; ++c3) {
-                    const PolyNode C = l3[c3];
+                    const PolyNode C = Cn;
+                    if (c3 + 1 < n3) Cn = l3[c3 + 1];
                     const float xk = xs[C.var * kBlock + t], xkl = xq[C.var * kBlock + t];
                     DF V3 = {C.hi, C.lo};
-                    DF P3;
-                    mul_df_f(P2, xk, P3.h, P3.l);
-                    P3.l = __fmaf_rn(P2.h, xkl, P3.l);
-                    for (; cl < C.end; ++cl) {
-                        const PolyNode L = lv[cl];
-                        const int o = L.var * kBlock + t;
-                        const float xl = xs[o], xll = xq[o];
-                        float p, q;
-                        // V3 += c x_l
-                        p = __fmul_rn(xl, L.hi);
-                        q = __fmaf_rn(xl, L.hi, -p);
-                        q = __fmaf_rn(xl, L.lo, q);
-                        q = __fmaf_rn(xll, L.hi, q);
-                        acc(V3, p, q);
-                        // g_l += c P3
-                        p = __fmul_rn(P3.h, L.hi);
-                        q = __fmaf_rn(P3.h, L.hi, -p);
-                        q = __fmaf_rn(P3.l, L.hi, q);
-                        q = __fmaf_rn(P3.h, L.lo, q);
-                        DF g = {gh[o], gl[o]};
-                        acc(g, p, q);
-                        gh[o] = g.h;
-                        gl[o] = g.l;
+                    const int cend = C.end;
+                    if (cl < cend) {
+                        DF P3;
+                        mul_df_f(P2, xk, P3.h, P3.l);
+                        P3.l = __fmaf_rn(P2.h, xkl, P3.l);
+                        // four leaves at a time: their nodes and operands are
+                        // loaded together, so the L2 latency of the node reads
+                        // overlaps (leaf variables of one node are distinct)
+                        for (; cl + 4 <= cend; cl += 4) {
+                            PolyNode L[4];
+                            int o[4];
+                            float x[4], xl[4];
+                            DF g[4];
+                            #pragma unroll
+                            for (int u = 0; u < 4; ++u) L[u] = lv[cl + u];
+                            #pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                o[u] = L[u].var * kBlock + t;
+                                x[u] = xs[o[u]];
+                                xl[u] = xq[o[u]];
+                                g[u].h = gh[o[u]];
+                                g[u].l = gl[o[u]];
+                            }
+                            #pragma unroll
+                            for (int u = 0; u < 4; ++u) leaf_update(L[u], x[u], xl[u], P3, V3, g[u]);
+                            #pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                gh[o[u]] = g[u].h;
+                                gl[o[u]] = g[u].l;
+                            }
+                        }
+                        for (; cl < cend; ++cl) {
+                            const PolyNode L = lv[cl];
+                            const int o = L.var * kBlock + t;
+                            DF g = {gh[o], gl[o]};
+                            leaf_update(L, xs[o], xq[o], P3, V3, g);
+                            gh[o] = g.h;
+                            gl[o] = g.l;
+                        }
                     }
                     float p, q;
                     mul_df_f(V3, xk, p, q);
@@ -212,7 +247,22 @@ void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, i
     if (blocks > num_sms * 4) blocks = num_sms * 4;
     count_launch();
     poly_df_kernel<31><<<blocks, kBlock, 4 * 31 * kBlock * sizeof(float), st>>>(g_t2.l1, g_t2.n1, g_t2.l2, g_t2.l3,
-                                                                                g_t2.lv, X, G, E, n, stride);
+                                                                                POLY2B_N3, g_t2.lv, X, G, E, n, stride);
+}
+
+cudaError_t poly2b_kernel_setup() {
+    return cudaFuncSetAttribute(poly_df_kernel<31>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                4 * 31 * kBlock * (int)sizeof(float));
+}
+
+void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, int n1, const PolyNode* l2, const PolyNode* l3,
+                        const PolyNode* lv, const float* X, float* G, float* E, int n, int stride, int num_sms) {
+    if (n <= 0) return;
+    int blocks = (n + kBlock - 1) / kBlock;
+    if (blocks > num_sms * 4) blocks = num_sms * 4;
+    count_launch();
+    poly_df_kernel<31><<<blocks, kBlock, 4 * 31 * kBlock * sizeof(float), st>>>(l1, n1, l2, l3, POLY2B_N3, lv, X, G, E, n,
+                                                                                stride);
 }
 
 void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms) {
@@ -221,7 +271,7 @@ void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, i
     if (blocks > num_sms * 4) blocks = num_sms * 4;
     count_launch();
     poly_df_kernel<36><<<blocks, kBlock, 4 * 36 * kBlock * sizeof(float), st>>>(g_t3.l1, g_t3.n1, g_t3.l2, g_t3.l3,
-                                                                                g_t3.lv, X, G, E, n, stride);
+                                                                                POLY3B_N3, g_t3.lv, X, G, E, n, stride);
 }
 
 }  // namespace mbpol
