@@ -171,6 +171,34 @@ mbpol_status mbpol_profile_read(int kernel, double* total_ms, long* launches);
 const char* mbpol_status_string(mbpol_status s);
 const char* mbpol_last_error(void);
 
+/* ---- Two-body term without device allocation ---------------------------
+ * No reference counterpart: the reference evaluates the two-body term only
+ * inside MBPolReferenceTwoBodyForce::calculateForceAndEnergy
+ * (platforms/reference/src/MBPolReferenceTwoBodyForce.cpp) over the
+ * neighbour list it builds itself.  This entry point is for callers that own
+ * all device memory and cannot let the library allocate (their own pool, no
+ * cudaMalloc/cudaFree inside a step loop): it evaluates the two-body energy
+ * and forces for a caller-built dimer list on caller-owned DEVICE buffers,
+ * using per-device scratch held in static device arrays, and never calls
+ * cudaMalloc, cudaFree or an allocating library.
+ *   positions  device, 3*num_particles doubles (nm)
+ *   waters     device, 4 ints per water {O, H1, H2, unused}, 16-byte aligned
+ *   dimers     device, 2 ints per dimer (water indices), 8-byte aligned;
+ *              indices are NOT checked and must be in range
+ *   box_nm     HOST, 3 doubles (rectangular, each >= 1.3 nm), or NULL
+ *   forces     device, 3*num_particles doubles, accumulated (+=), kJ/mol/nm
+ *   energy     device, one double, accumulated (+=), kJ/mol
+ *   stream     cudaStream_t (NULL: the default stream)
+ * More than MBPOL_NOALLOC_MAX_DIMERS dimers is MBPOL_ERR_CAPACITY (split the
+ * list into ordered calls).  The first call on a device does a synchronous
+ * set-up (symbol addresses, tables, constants) and should precede any stream
+ * capture.  The scratch is shared by all calls on a device: calls whose
+ * kernels could overlap (other streams or threads) must be ordered. */
+#define MBPOL_NOALLOC_MAX_DIMERS 65536
+mbpol_status mbpol_twobody_dimers_noalloc(const double* positions, const int* waters, const int* dimers,
+                                         int num_dimers, const double* box_nm, double* forces, double* energy,
+                                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

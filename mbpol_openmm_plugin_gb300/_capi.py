@@ -27,7 +27,9 @@ EXPORTED = [
     "mbpol_set_positions", "mbpol_compute", "mbpol_set_masses", "mbpol_set_velocities", "mbpol_md_run",
     "mbpol_get_state", "mbpol_get_induced_dipoles", "mbpol_get_counts",
     "mbpol_profile_enable", "mbpol_profile_read", "mbpol_launch_count", "mbpol_status_string", "mbpol_last_error",
+    "mbpol_twobody_dimers_noalloc",
 ]
+NOALLOC_MAX_DIMERS = 65536  # MBPOL_NOALLOC_MAX_DIMERS
 KERNELS = ["poly2b", "poly3b", "elec_fixed_field", "elec_induced_update", "elec_pme_dipoles", "elec_energy_forces"]
 
 
@@ -89,6 +91,7 @@ def load(path=None):
         "mbpol_profile_read": (I, [I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_long)]),
         "mbpol_status_string": (ctypes.c_char_p, [I]),
         "mbpol_last_error": (ctypes.c_char_p, []),
+        "mbpol_twobody_dimers_noalloc": (I, [P, P, P, I, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

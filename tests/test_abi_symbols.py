@@ -47,3 +47,19 @@ def test_cxx_layer_compiles_and_links(tmp_path):
                            "-L", os.path.dirname(_capi.LIB_PATH), "-lmbpol_gb300",
                            "-Wl,-rpath," + os.path.dirname(_capi.LIB_PATH)])
     assert exe.exists()
+
+
+def test_noalloc_capacity_and_argument_checks_without_gpu():
+    """The no-allocation two-body entry point: the capacity in the header
+    matches the binding, and oversize or negative dimer counts are rejected
+    on the host before any CUDA call."""
+    src = open(os.path.join(ROOT, "include", "mbpol_gb300.h")).read()
+    m = re.search(r"#define\s+MBPOL_NOALLOC_MAX_DIMERS\s+(\d+)", src)
+    assert m and int(m.group(1)) == _capi.NOALLOC_MAX_DIMERS
+    if not os.path.exists(_capi.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _capi.load()
+    fn = lib.mbpol_twobody_dimers_noalloc
+    assert fn(None, None, None, _capi.NOALLOC_MAX_DIMERS + 1, None, None, None, None) == 5  # MBPOL_ERR_CAPACITY
+    assert fn(None, None, None, -1, None, None, None, None) == 1  # MBPOL_ERR_INVALID_ARGUMENT
+    assert fn(None, None, None, 0, None, None, None, None) == 0
