@@ -120,6 +120,10 @@ def maxwell_boltzmann(masses, T, seed):
 # multiply, counted in poly-2b-v6x.cpp / poly-3b-v2x.cpp plus the variables,
 # switch and chain rule around them): these stay fixed whatever the kernels do.
 ALGO_FLOP_PER_UNIT = {"poly2b": 31200, "poly3b": 112600}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# each walk on box4096, measured with ncu --set full, and the units that launch
+# processed; the traffic of a launch is scaled by its unit count.
+NCU_TRAFFIC = {"poly3b": (53.078e6 + 2.419e6, 181889), "poly2b": (16.481e6, 65434)}
 
 
 def fp32_ops_per_unit(name):
@@ -137,15 +141,34 @@ def fp32_ops_per_unit(name):
     return 30 * sizes["NL"] + 40 * sizes["N3"] + 33 * sizes["N2"] + 26 * sizes["N1"]
 
 
-def run_ours(args):
+GUESS_MODE = {"plain": 1, "learned": 2, "extrapolation": 3}
+GUESS_WEIGHTS = os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "data", "dipole_guess_%s.npy")
+
+
+def guess_params(args):
+    """The learned guess's parameter block: the committed one for the
+    workload (trained by mbpol_openmm_plugin_gb300.train_guess on 2000 NVT
+    frames of the same box), else one trained here on a short trajectory."""
+    path = GUESS_WEIGHTS % args.workload
+    if os.path.exists(path):
+        return np.load(path), "committed (%s)" % os.path.relpath(path, ROOT)
+    out = os.path.join("/tmp", "dipole_guess_%s_%d.npy" % (args.workload, os.getpid()))
+    from mbpol_openmm_plugin_gb300 import train_guess
+    train_guess.main(["--workload", args.workload, "--frames", "200", "--steps", "5000", "--out", out])
+    return np.load(out), "trained in this run on 200 NVT frames"
+
+
+def timed_md(args, guess, params=None, profile=False):
+    """Warm-up, then K timed MD steps (CUDA events inside mbpol_md_run)."""
     import mbpol_openmm_plugin_gb300 as mb
     from mbpol_openmm_plugin_gb300 import _capi
     lib = _capi.load()
-    guess = 2 if args.guess == "learned" else 1
-    ws, sysm, alpha, grid = build_workload(args.workload, args.seed, guess)
+    ws, sysm, alpha, grid = build_workload(args.workload, args.seed, GUESS_MODE[guess])
     ctx = mb.Context(sysm)
     ctx.setPositions(ws.positions)
     ctx._build()
+    if params is not None:
+        ctx.setDipoleGuessParameters(params)
     h = ctx._h
     box = np.ascontiguousarray(ws.box, np.float64)
     pos = np.ascontiguousarray(ws.positions, np.float64)
@@ -160,27 +183,54 @@ def run_ours(args):
     # warm-up (includes the first force evaluation and buffer growth)
     _capi.check(lib.mbpol_md_run(h, args.warmup, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(ms), _capi.ptr(en),
                                  ctypes.byref(iters)))
-    counts = ctx.getCounts()
-    # timed region: device resident
-    sampler = ClockSampler()
-    sampler.start()
-    lib.mbpol_profile_enable(1)
+    r = {"ctx": ctx, "ws": ws, "sysm": sysm, "alpha": alpha, "grid": grid, "counts": ctx.getCounts(),
+         "box": box, "pos": pos, "masses": masses}
+    sampler = ClockSampler() if profile else None
+    if profile:
+        sampler.start()
+        lib.mbpol_profile_enable(1)
     l0 = lib.mbpol_launch_count()
     _capi.check(lib.mbpol_md_run(h, args.steps, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(ms), _capi.ptr(en),
                                  ctypes.byref(iters)))
-    launches = int(lib.mbpol_launch_count() - l0)
-    clocks = sampler.stop()
-    gpu_ms = ms.value
-    kern = {}
-    for kid, kname in enumerate(_capi.KERNELS):
-        t = ctypes.c_double()
-        n = ctypes.c_long()
-        lib.mbpol_profile_read(kid, ctypes.byref(t), ctypes.byref(n))
-        kern[kname] = {"total_ms": t.value, "launches": n.value}
-    lib.mbpol_profile_enable(0)
-    step_s = gpu_ms / 1e3 / args.steps
+    r["launches"] = int(lib.mbpol_launch_count() - l0)
+    if profile:
+        r["clocks"] = sampler.stop()
+        kern = {}
+        for kid, kname in enumerate(_capi.KERNELS):
+            t = ctypes.c_double()
+            n = ctypes.c_long()
+            lib.mbpol_profile_read(kid, ctypes.byref(t), ctypes.byref(n))
+            kern[kname] = {"total_ms": t.value, "launches": n.value}
+        lib.mbpol_profile_enable(0)
+        r["kern"] = kern
+    r["step_s"] = ms.value / 1e3 / args.steps
+    r["iterations"] = iters.value / max(args.steps, 1)
+    r["energies"] = en.copy()
+    return r
+
+
+def run_ours(args):
+    from mbpol_openmm_plugin_gb300 import _capi
+    lib = _capi.load()
+    params, params_src = guess_params(args)
+    # comparison arms first (same initial state), the headline arm last
+    others = {}
+    for g in ("plain", "extrapolation", "learned"):
+        if g == args.guess:
+            continue
+        rr = timed_md(args, g, params if g == "learned" else None)
+        others[g] = {"ns_per_day": ns_per_day(rr["step_s"]), "ms_per_step": rr["step_s"] * 1e3,
+                     "solver_iterations_per_step": rr["iterations"]}
+        del rr
+    r = timed_md(args, args.guess, params, profile=True)
+    ctx, ws, sysm, alpha, grid = r["ctx"], r["ws"], r["sysm"], r["alpha"], r["grid"]
+    h = ctx._h
+    box, pos, masses, counts, kern, clocks = r["box"], r["pos"], r["masses"], r["counts"], r["kern"], r["clocks"]
+    launches = r["launches"]
+    step_s = r["step_s"]
     value = ns_per_day(step_s)
-    solver_it = iters.value / max(args.steps, 1)
+    solver_it = r["iterations"]
+    en = r["energies"]
 
     # e2e: public API with host buffers, host-side velocity Verlet
     hpos = np.zeros_like(pos)
@@ -213,7 +263,9 @@ def run_ours(args):
         sm_mhz = clocks.get("sm_mhz") or 2070.0
         peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
         roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None,
+                "frac": achieved / peak,
+                "traffic": NCU_TRAFFIC[dom][0] * units / NCU_TRAFFIC[dom][1],
+                "traffic_note": "DRAM bytes per launch from one ncu capture on this workload, scaled by units",
                 "work": "%d units x %d algorithmic flop (reference operation count)" % (units, algo),
                 "executed_fp32_tflops": executed, "executed_frac": executed / peak,
                 "executed_work": "%d FP32 flop per unit in the double-float walk" % fp32_ops_per_unit(dom),
@@ -227,7 +279,7 @@ def run_ours(args):
         "dtype": "fp32+double-float polynomials, fp64 accumulation", "data": "synthetic (seeded lattice box)",
         "config": {"workload": args.workload, "waters": n // 4, "box_nm": float(ws.box[0]), "pme_alpha": alpha,
                    "pme_grid": grid, "cutoff_nm": 0.9, "ewald_tol": 1e-5, "target_epsilon_D": 1e-8,
-                   "dt_fs": 0.2, "guess": args.guess, "seed": args.seed,
+                   "dt_fs": 0.2, "guess": args.guess, "guess_parameters": params_src, "seed": args.seed,
                    "l2": "no flush: inputs larger than L2 (per-step trimer and pair variable/gradient planes "
                          "%.0f MB, PME grids %.0f MB, against 129 MB of L2)" % (
                              (int(counts[1]) * 36 * 3 + int(counts[0]) * 31 * 3) * 4 / 1e6,
@@ -236,6 +288,8 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(pos.nbytes + 5 * 8)},
         "gpu_launches": launches,
         "solver_iterations_per_step": solver_it,
+        "guess_comparison": dict(others, **{args.guess: {"ns_per_day": value, "ms_per_step": step_s * 1e3,
+                                                         "solver_iterations_per_step": solver_it}}),
         "counts": {"pairs_2b": int(counts[0]), "trimers": int(counts[1])},
         "kernels_ms_per_step": {k: v["total_ms"] / args.steps for k, v in kern.items()},
         "clocks": clocks,
@@ -265,7 +319,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="box4096")
-    ap.add_argument("--guess", default="plain", choices=["plain", "learned"])
+    ap.add_argument("--guess", default="learned", choices=["plain", "extrapolation", "learned"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

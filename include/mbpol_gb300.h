@@ -75,7 +75,9 @@ typedef struct {
     double thole[5];             /* TCC, TCD, TDD, TDDOH, TDDHH; default {0.4,0.4,0.055,0.626,0.055} */
     int include_charge_redistribution; /* default 1                                              */
     int guess;                   /* initial dipole guess: 0 direct (alpha*E_fixed, as the reference),
-                                    1 previous call's dipoles, 2 learned (MLP) with direct fallback */
+                                    1 previous call's dipoles, 2 learned (network prediction plus the
+                                    extrapolated residual of the last solves; 3 without a network),
+                                    3 polynomial extrapolation of the last (up to) three solves */
 } mbpol_electrostatics_params;
 
 /* Fill p with the reference's defaults. */
@@ -170,6 +172,58 @@ mbpol_status mbpol_profile_read(int kernel, double* total_ms, long* launches);
 
 const char* mbpol_status_string(mbpol_status s);
 const char* mbpol_last_error(void);
+
+/* ---- Batched independent clusters ---------------------------------------
+ * No reference counterpart as one call: the reference evaluates each water
+ * cluster in its own OpenMM Context.  Here one context holds many clusters
+ * and every kernel runs over all of them at once: particle i belongs to
+ * cluster cluster_of_particle[i] (0 .. num_clusters-1) and no term couples
+ * two clusters (neighbour lists, dispersion and electrostatics are
+ * restricted to the cluster; each cluster's induced dipoles converge on their
+ * own epsilon with the reference's stopping rules).  All forces must use
+ * non-periodic methods (NoCutoff electrostatics).  num_clusters = 0 ends
+ * batching.  mbpol_compute's energies are then the sums over clusters. */
+mbpol_status mbpol_set_clusters(mbpol_context* ctx, const int* cluster_of_particle, int num_clusters);
+/* Per-cluster energies [num_clusters][MBPOL_NUM_TERMS] (kJ/mol, term order
+ * of MBPOL_TERM_*) and solver iterations [num_clusters] of the last
+ * evaluation (either pointer may be NULL). */
+mbpol_status mbpol_get_cluster_results(mbpol_context* ctx, double* energies, int* iterations);
+
+/* ---- Learned initial guess for the induced dipoles ----------------------
+ * No reference counterpart: the reference starts every solve from
+ * alpha * E_fixed (MBPolReferenceElectrostaticsForce.cpp:557-616).  The
+ * network (64-64-64-9, SiLU, BF16 weights on the tensor cores) predicts the
+ * O, H1, H2 dipoles in the water's own frame from 48 descriptors of the
+ * water's neighbourhood within 0.6 nm and the permanent field at its three
+ * sites.  With mbpol_electrostatics_params.guess = 2 and a trained network
+ * the solver starts from the prediction (cold start, or mu_prev + m - m_prev
+ * after one solve) and, once two solves exist, from the polynomial
+ * extrapolation of the last solves (guess 3), which in a smooth trajectory
+ * is more precise than a BF16 network.  The solver, its threshold and its
+ * stopping rules are unchanged, so the results agree with the plain path
+ * within the solver tolerance.
+ * A parameter block is MBPOL_GUESS_BLOCK_FLOATS floats: W1[64][64], b1[64],
+ * W2[64][64], b2[64], W3[9][64], b3[9], then the input means[64] and
+ * inverse standard deviations[64]. */
+#define MBPOL_GUESS_BLOCK_FLOATS 9033
+/* Append the last evaluation's descriptors and converged dipoles (one sample
+ * per water) to the context's training set on the device. */
+mbpol_status mbpol_guess_collect(mbpol_context* ctx);
+mbpol_status mbpol_guess_num_samples(mbpol_context* ctx, long* n);
+/* Train on the collected samples on the GPU (Adam, cosine step decay,
+ * batches drawn uniformly); final_loss = mean batch loss of the last 10% of
+ * the steps (units: (1e-3 e nm)^2 / 2 per output). */
+mbpol_status mbpol_guess_train(mbpol_context* ctx, int steps, int batch, double learning_rate,
+                               unsigned long long seed, double* final_loss);
+mbpol_status mbpol_guess_get_params(mbpol_context* ctx, float* block);
+mbpol_status mbpol_guess_set_params(mbpol_context* ctx, const float* block);
+/* Network inputs [n_waters][64] of the last evaluation (48 descriptors,
+ * 9 field components, 7 zeros). */
+mbpol_status mbpol_guess_descriptors(mbpol_context* ctx, float* out);
+/* Loss, gradient [8905] and outputs [n][9] of the current network on host
+ * data X [n][64] (raw inputs), T [n][9] (targets), without an update. */
+mbpol_status mbpol_guess_loss_grad(mbpol_context* ctx, const float* X, const float* T, int n, double* loss,
+                                   float* grad, float* Y);
 
 /* ---- Two-body term without device allocation ---------------------------
  * No reference counterpart: the reference evaluates the two-body term only

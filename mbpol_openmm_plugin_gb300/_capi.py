@@ -28,7 +28,13 @@ EXPORTED = [
     "mbpol_get_state", "mbpol_get_induced_dipoles", "mbpol_get_counts",
     "mbpol_profile_enable", "mbpol_profile_read", "mbpol_launch_count", "mbpol_status_string", "mbpol_last_error",
     "mbpol_twobody_dimers_noalloc",
+    "mbpol_guess_collect", "mbpol_guess_num_samples", "mbpol_guess_train", "mbpol_guess_get_params",
+    "mbpol_guess_set_params", "mbpol_guess_descriptors", "mbpol_guess_loss_grad",
+    "mbpol_set_clusters", "mbpol_get_cluster_results",
 ]
+GUESS_BLOCK_FLOATS = 9033  # MBPOL_GUESS_BLOCK_FLOATS
+GUESS_PARAMS = 8905
+GUESS_INPUTS = 64
 NOALLOC_MAX_DIMERS = 65536  # MBPOL_NOALLOC_MAX_DIMERS
 KERNELS = ["poly2b", "poly3b", "elec_fixed_field", "elec_induced_update", "elec_pme_dipoles", "elec_energy_forces"]
 
@@ -92,6 +98,15 @@ def load(path=None):
         "mbpol_status_string": (ctypes.c_char_p, [I]),
         "mbpol_last_error": (ctypes.c_char_p, []),
         "mbpol_twobody_dimers_noalloc": (I, [P, P, P, I, P, P, P, P]),
+        "mbpol_guess_collect": (I, [P]),
+        "mbpol_guess_num_samples": (I, [P, ctypes.POINTER(ctypes.c_long)]),
+        "mbpol_guess_train": (I, [P, I, I, D, ctypes.c_ulonglong, ctypes.POINTER(D)]),
+        "mbpol_guess_get_params": (I, [P, P]),
+        "mbpol_guess_set_params": (I, [P, P]),
+        "mbpol_guess_descriptors": (I, [P, P]),
+        "mbpol_guess_loss_grad": (I, [P, P, P, I, ctypes.POINTER(D), P, P]),
+        "mbpol_set_clusters": (I, [P, P, I]),
+        "mbpol_get_cluster_results": (I, [P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -93,6 +93,9 @@ struct WaterTerm {
     int rule = 0;
     std::vector<int4> waters;
     DevBuf d_waters;
+    // batched clusters: cluster of each water of this term's list
+    DevBuf d_cluster;
+    int max_cluster = 0;
 };
 
 }  // namespace mbpol
@@ -126,6 +129,11 @@ struct mbpol_context {
     // shared pass for the two-body, three-body and dispersion terms
     DevBuf opos;
     bool shared_lists = false;
+    // batched independent clusters (cluster of every particle)
+    int ncl = 0;
+    std::vector<int> cl_of_particle;
+    bool cl_dirty = false;
+    DevBuf d_cl_energy;  // [ncl][MBPOL_NUM_TERMS]
     double disp_c6[16], disp_d6[16];
     // electrostatics
     std::unique_ptr<ElecEngine> elec;
@@ -177,6 +185,55 @@ mbpol_status check_box(const mbpol_context* ctx, double cutoff) {
     return MBPOL_OK;
 }
 
+const int* term_clusters(const mbpol_context* ctx, const WaterTerm& t) {
+    return ctx->ncl > 0 ? t.d_cluster.as<int>() : nullptr;
+}
+
+ClusterSink term_sink(mbpol_context* ctx, const WaterTerm& t, int term) {
+    ClusterSink cs;
+    if (ctx->ncl > 0) {
+        cs.wcl = t.d_cluster.as<int>();
+        cs.e = ctx->d_cl_energy.as<double>() + term;
+        cs.stride = MBPOL_NUM_TERMS;
+    }
+    return cs;
+}
+
+// Per-term cluster arrays and the electrostatics engine's clusters, built at
+// the first evaluation after mbpol_set_clusters.
+mbpol_status apply_clusters(mbpol_context* ctx) {
+    ctx->cl_dirty = false;
+    const int ncl = ctx->ncl;
+    if (ncl > 0) {
+        MBPOL_CUDA_OK(ctx->d_cl_energy.ensure(sizeof(double) * MBPOL_NUM_TERMS * (size_t)ncl));
+        for (WaterTerm* t : {&ctx->t1, &ctx->t2, &ctx->t3, &ctx->tdisp}) {
+            const int nw = (int)t->waters.size();
+            if (nw == 0) continue;
+            std::vector<int> wc(nw), count(ncl, 0);
+            for (int w = 0; w < nw; ++w) {
+                const int4 wi = t->waters[w];
+                const int c = ctx->cl_of_particle[wi.x];
+                if (ctx->cl_of_particle[wi.y] != c || ctx->cl_of_particle[wi.z] != c)
+                    return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "the atoms of one water are in different clusters");
+                wc[w] = c;
+                ++count[c];
+            }
+            t->max_cluster = 0;
+            for (int c = 0; c < ncl; ++c) t->max_cluster = std::max(t->max_cluster, count[c]);
+            MBPOL_CUDA_OK(t->d_cluster.ensure(sizeof(int) * (size_t)nw));
+            MBPOL_CUDA_OK(cudaMemcpy(t->d_cluster.p, wc.data(), sizeof(int) * nw, cudaMemcpyHostToDevice));
+        }
+    }
+    ctx->cap_full_d = 0;
+    if (ctx->elec) {
+        mbpol_status s = ctx->elec->set_clusters(
+            ncl > 0 ? ctx->cl_of_particle.data() : nullptr, ncl,
+            ncl > 0 ? ctx->d_cl_energy.as<double>() + MBPOL_TERM_ELECTROSTATICS : nullptr, MBPOL_NUM_TERMS);
+        if (s) return s;
+    }
+    return MBPOL_OK;
+}
+
 // Two-body pair list on its own (one neighbour pass, one host sync).
 mbpol_status twobody_list(mbpol_context* ctx, const Box& box, double rc, int* np_out) {
     WaterTerm& t = ctx->t2;
@@ -189,7 +246,7 @@ mbpol_status twobody_list(mbpol_context* ctx, const Box& box, double rc, int* np
         MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
         launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(),
                              box, -1.0, -1.0, rc, 0, 0, nullptr, nullptr, nullptr, nullptr, ctx->p2.as<int2>(),
-                             ctx->cap2, cnt, cnt + 1, nullptr);
+                             ctx->cap2, cnt, cnt + 1, term_clusters(ctx, t));
         int h[2];
         MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
@@ -232,7 +289,8 @@ mbpol_status run_twobody(mbpol_context* ctx, double* energy) {
     launch_poly2b(ctx->st, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride, ctx->num_sms);
     prof_end(ctx->st, K_POLY2B);
     launch_twobody_forces(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
-                          ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy);
+                          ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy,
+                          term_sink(ctx, t, MBPOL_TERM_TWOBODY));
     return MBPOL_OK;
 }
 
@@ -252,7 +310,8 @@ mbpol_status threebody_list(mbpol_context* ctx, const Box& box, double rc, int* 
             MBPOL_CUDA_OK(ctx->lower3.ensure(sizeof(int) * (size_t)nw * ctx->cap_lower3));
             launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                                  ctx->opos.as<float4>(), box, -1.0, rc, -1.0, 0, ctx->cap_lower3, nullptr, nullptr,
-                                 ctx->lower3.as<int>(), ctx->nlower3.as<int>(), nullptr, 0, cnt, cnt + 1, nullptr);
+                                 ctx->lower3.as<int>(), ctx->nlower3.as<int>(), nullptr, 0, cnt, cnt + 1,
+                                 term_clusters(ctx, t));
             launch_trimer_count(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
                                 ctx->count3.as<int>(), ctx->offs3.as<int>());
         } else {
@@ -260,7 +319,8 @@ mbpol_status threebody_list(mbpol_context* ctx, const Box& box, double rc, int* 
             MBPOL_CUDA_OK(ctx->nfull3.ensure(sizeof(int) * (size_t)nw));
             launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                                  ctx->opos.as<float4>(), box, rc, -1.0, -1.0, ctx->cap_full3, 0, ctx->full3.as<int>(),
-                                 ctx->nfull3.as<int>(), nullptr, nullptr, nullptr, 0, cnt, cnt + 1, nullptr);
+                                 ctx->nfull3.as<int>(), nullptr, nullptr, nullptr, 0, cnt, cnt + 1,
+                                 term_clusters(ctx, t));
             launch_trimer_complete(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
                                    ctx->full3.as<int>(), ctx->nfull3.as<int>(), ctx->cap_full3,
                                    ctx->count3.as<int>(), ctx->offs3.as<int>(), 0, nullptr, false);
@@ -320,7 +380,8 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
                   ctx->num_sms);
     prof_end(ctx->st, K_POLY3B);
     launch_threebody_forces(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
-                            box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride, ctx->d_force.as<double>(), energy);
+                            box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride, ctx->d_force.as<double>(), energy,
+                            term_sink(ctx, t, MBPOL_TERM_THREEBODY));
     return MBPOL_OK;
 }
 
@@ -343,7 +404,8 @@ mbpol_status dispersion_list(mbpol_context* ctx, const Box& box) {
         MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
         launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(),
                              box, rlist, -1.0, -1.0, ctx->cap_full_d, 0, ctx->full_d.as<int>(),
-                             ctx->nfull_d.as<int>(), nullptr, nullptr, nullptr, 0, cnt, cnt + 1, nullptr);
+                             ctx->nfull_d.as<int>(), nullptr, nullptr, nullptr, 0, cnt, cnt + 1,
+                             term_clusters(ctx, t));
         int h[2];
         MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
@@ -367,13 +429,15 @@ mbpol_status run_dispersion(mbpol_context* ctx, double* energy) {
     }
     const Box box = term_box(ctx, periodic);
     const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
-    if (ctx->cap_full_d == 0) ctx->cap_full_d = t.method == MBPOL_NOCUTOFF ? ((nw + 31) / 32) * 32 : 256;
+    if (ctx->cap_full_d == 0)
+        ctx->cap_full_d = t.method == MBPOL_NOCUTOFF ? (((ctx->ncl > 0 ? t.max_cluster : nw) + 31) / 32) * 32 : 256;
     if (!ctx->shared_lists) {
         mbpol_status s = dispersion_list(ctx, box);
         if (s) return s;
     }
     launch_dispersion(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, ctx->full_d.as<int>(),
-                      ctx->nfull_d.as<int>(), ctx->cap_full_d, rc, ctx->d_force.as<double>(), energy);
+                      ctx->nfull_d.as<int>(), ctx->cap_full_d, rc, ctx->d_force.as<double>(), energy,
+                      term_sink(ctx, t, MBPOL_TERM_DISPERSION));
     return MBPOL_OK;
 }
 
@@ -395,7 +459,7 @@ mbpol_status build_shared_lists(mbpol_context* ctx, unsigned mask, bool* built) 
     const unsigned need = MBPOL_TERM_BIT(MBPOL_TERM_TWOBODY) | MBPOL_TERM_BIT(MBPOL_TERM_THREEBODY) |
                           MBPOL_TERM_BIT(MBPOL_TERM_DISPERSION);
     const WaterTerm &t2 = ctx->t2, &t3 = ctx->t3, &td = ctx->tdisp;
-    if ((mask & need) != need || !t2.on || !t3.on || !td.on) return MBPOL_OK;
+    if ((mask & need) != need || !t2.on || !t3.on || !td.on || ctx->ncl > 0) return MBPOL_OK;
     if (t2.method != MBPOL_CUTOFF_PERIODIC || t3.method != MBPOL_CUTOFF_PERIODIC ||
         td.method != MBPOL_CUTOFF_PERIODIC || t3.rule == MBPOL_TRIMER_COMPLETE)
         return MBPOL_OK;
@@ -599,10 +663,22 @@ mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
     MBPOL_CUDA_OK(cudaMemsetAsync(ctx->d_energy.p, 0, sizeof(double) * MBPOL_NUM_TERMS, ctx->st));
     double* e = ctx->d_energy.as<double>();
     mbpol_status s = MBPOL_OK;
+    if (ctx->cl_dirty) {
+        s = apply_clusters(ctx);
+        if (s) return s;
+    }
+    if (ctx->ncl > 0) {
+        for (const WaterTerm* t : {&ctx->t1, &ctx->t2, &ctx->t3, &ctx->tdisp})
+            if (t->on && (t->method == MBPOL_CUTOFF_PERIODIC || (t == &ctx->t1 && t->method == MBPOL_ONEBODY_PERIODIC)))
+                return mbpol_fail(MBPOL_ERR_STATE, "batched clusters need non-periodic methods");
+        MBPOL_CUDA_OK(cudaMemsetAsync(ctx->d_cl_energy.p, 0, sizeof(double) * MBPOL_NUM_TERMS * (size_t)ctx->ncl,
+                                      ctx->st));
+    }
     if ((mask & MBPOL_TERM_BIT(MBPOL_TERM_ONEBODY)) && ctx->t1.on) {
         const bool periodic = ctx->t1.method == MBPOL_ONEBODY_PERIODIC && ctx->box.periodic;
         launch_onebody(ctx->st, (int)ctx->t1.waters.size(), ctx->t1.d_waters.as<int4>(), ctx->d_pos.as<double>(),
-                       term_box(ctx, periodic), ctx->d_force.as<double>(), e + MBPOL_TERM_ONEBODY);
+                       term_box(ctx, periodic), ctx->d_force.as<double>(), e + MBPOL_TERM_ONEBODY,
+                       term_sink(ctx, ctx->t1, MBPOL_TERM_ONEBODY));
     }
     ctx->shared_lists = false;
     if (!s) s = build_shared_lists(ctx, mask, &ctx->shared_lists);
@@ -781,6 +857,87 @@ mbpol_status mbpol_profile_read(int kernel, double* total_ms, long* launches) {
     }
     if (total_ms) *total_ms = t;
     if (launches) *launches = (long)g_prof.rec[kernel].size();
+    return MBPOL_OK;
+}
+
+
+// ---- learned initial guess for the induced dipoles (no reference counterpart)
+static mbpol_status need_elec(mbpol_context* ctx) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (!ctx->elec) return mbpol_fail(MBPOL_ERR_STATE, "the context has no electrostatics force");
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_guess_collect(mbpol_context* ctx) {
+    mbpol_status s = need_elec(ctx);
+    return s ? s : ctx->elec->guess_collect(ctx->st);
+}
+
+mbpol_status mbpol_guess_num_samples(mbpol_context* ctx, long* n) {
+    mbpol_status s = need_elec(ctx);
+    if (s) return s;
+    if (!n) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    *n = ctx->elec->guess_num_samples();
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_guess_train(mbpol_context* ctx, int steps, int batch, double learning_rate,
+                               unsigned long long seed, double* final_loss) {
+    mbpol_status s = need_elec(ctx);
+    return s ? s : ctx->elec->guess_train(ctx->st, steps, batch, learning_rate, seed, final_loss);
+}
+
+mbpol_status mbpol_guess_get_params(mbpol_context* ctx, float* block) {
+    mbpol_status s = need_elec(ctx);
+    return s ? s : ctx->elec->guess_get_params(block);
+}
+
+mbpol_status mbpol_guess_set_params(mbpol_context* ctx, const float* block) {
+    mbpol_status s = need_elec(ctx);
+    return s ? s : ctx->elec->guess_set_params(block);
+}
+
+mbpol_status mbpol_guess_descriptors(mbpol_context* ctx, float* out) {
+    mbpol_status s = need_elec(ctx);
+    if (s) return s;
+    if (!out) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    return ctx->elec->guess_descriptors(ctx->st, out);
+}
+
+mbpol_status mbpol_guess_loss_grad(mbpol_context* ctx, const float* X, const float* T, int n, double* loss,
+                                   float* grad, float* Y) {
+    mbpol_status s = need_elec(ctx);
+    return s ? s : ctx->elec->guess_loss_grad(ctx->st, X, T, n, loss, grad, Y);
+}
+
+
+// ---- batched independent clusters (no reference counterpart as one call)
+mbpol_status mbpol_set_clusters(mbpol_context* ctx, const int* cluster_of_particle, int num_clusters) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (num_clusters < 0 || (num_clusters > 0 && !cluster_of_particle))
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad cluster arguments");
+    if (num_clusters > 0)
+        for (int i = 0; i < ctx->N; ++i)
+            if (cluster_of_particle[i] < 0 || cluster_of_particle[i] >= num_clusters)
+                return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "cluster index out of range");
+    ctx->ncl = num_clusters;
+    ctx->cl_of_particle.assign(cluster_of_particle, cluster_of_particle + (num_clusters > 0 ? ctx->N : 0));
+    ctx->cl_dirty = true;
+    ctx->forces_valid = false;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_get_cluster_results(mbpol_context* ctx, double* energies, int* iterations) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (ctx->ncl <= 0 || ctx->cl_dirty) return mbpol_fail(MBPOL_ERR_STATE, "no batched-cluster evaluation yet");
+    if (energies) {
+        MBPOL_CUDA_OK(cudaMemcpy(energies, ctx->d_cl_energy.p, sizeof(double) * MBPOL_NUM_TERMS * (size_t)ctx->ncl,
+                                 cudaMemcpyDeviceToHost));
+    }
+    if (iterations) {
+        const std::vector<int>* it = ctx->elec ? &ctx->elec->cluster_iterations() : nullptr;
+        for (int c = 0; c < ctx->ncl; ++c) iterations[c] = it && (int)it->size() == ctx->ncl ? (*it)[c] : 0;
+    }
     return MBPOL_OK;
 }
 

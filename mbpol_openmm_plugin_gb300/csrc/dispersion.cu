@@ -19,7 +19,8 @@ __constant__ float c_disp_d6[16];  // nm^-1
 
 __global__ void dispersion_kernel(int nw, const int4* __restrict__ waters, const double* __restrict__ pos, Box box,
                                   const int* __restrict__ full, const int* __restrict__ nfull, int cap_full,
-                                  float rc2, double* __restrict__ force, double* __restrict__ energy) {
+                                  float rc2, double* __restrict__ force, double* __restrict__ energy,
+                                  ClusterSink cs) {
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = gid / cap_full, slot = gid - i * cap_full;
     double e_out = 0.0;
@@ -77,6 +78,7 @@ __global__ void dispersion_kernel(int nw, const int4* __restrict__ waters, const
                 add_force(force, aj[a], fj[a].x, fj[a].y, fj[a].z);
             }
             e_out = e;
+            cluster_energy(cs, i, e_out);
         }
     }
     block_sum_atomic<128>(e_out, energy);
@@ -93,13 +95,14 @@ void upload_dispersion_tables(const double* c6_4x4, const double* d6_4x4) {
 }
 
 void launch_dispersion(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, const int* full,
-                       const int* nfull, int cap_full, double rc, double* force, double* energy) {
+                       const int* nfull, int cap_full, double rc, double* force, double* energy,
+                       ClusterSink cs) {
     if (nw <= 0 || cap_full <= 0) return;
     const long total = (long)nw * cap_full;
     const float rc2 = rc > 1e15 ? 3.0e38f : (float)(rc * rc);
     count_launch();
     dispersion_kernel<<<(int)((total + 127) / 128), 128, 0, st>>>(nw, waters, pos, box, full, nfull, cap_full, rc2,
-                                                                   force, energy);
+                                                                   force, energy, cs);
 }
 
 }  // namespace mbpol

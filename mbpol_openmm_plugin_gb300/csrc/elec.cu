@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "elec.h"
+#include "guess.h"
 
 namespace mbpol {
 
@@ -557,16 +558,21 @@ __global__ void pme_spread_kernel(int nsite, int mode, const float* __restrict__
     }
 }
 
-// Fixed-point grid -> FP32 grid for the FFT.
-__global__ void pme_fix_to_float_kernel(long n, const unsigned long long* __restrict__ a, float* __restrict__ b) {
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        b[i] = (float)((double)(long long)a[i] * (1.0 / kGridFix));
+// Fixed-point grid -> FP32 grid for the FFT, and the fixed-point grid back
+// to zero for the next spread.  The int64 -> FP32 conversion rounds once and
+// the 2^-40 scaling is exact, which equals rounding the exact value; no FP64
+// arithmetic (a fraction of the FP32 rate on this part).
+__global__ void pme_fix_to_float_kernel(long n, unsigned long long* __restrict__ a, float* __restrict__ b) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        b[i] = __ll2float_rn((long long)a[i]) * (float)(1.0 / kGridFix);
+        a[i] = 0ull;
+    }
 }
 
-// Reciprocal convolution on the R2C half grid (reference :1676-1713).
-__global__ void pme_convolve_kernel(cufftComplex* __restrict__ g, const float* __restrict__ bx,
-                                    const float* __restrict__ by, const float* __restrict__ bz, float expf_,
-                                    float scalef, int nzh) {
+// Per-wavevector convolution factor of the reciprocal sum (reference
+// :1676-1713), tabulated on the R2C half grid for a box and alpha.
+__global__ void pme_eterm_kernel(float* __restrict__ et, const float* __restrict__ bx, const float* __restrict__ by,
+                                 const float* __restrict__ bz, float expf_, float scalef, int nzh) {
     const int Nx = c_el.grid[0], Ny = c_el.grid[1], Nz = c_el.grid[2];
     const long total = (long)Nx * Ny * nzh;
     for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
@@ -575,7 +581,7 @@ __global__ void pme_convolve_kernel(cufftComplex* __restrict__ g, const float* _
         const int ky = (int)(rest % Ny);
         const int kx = (int)(rest / Ny);
         if (kx == 0 && ky == 0 && kz == 0) {
-            g[idx].x = g[idx].y = 0.f;
+            et[idx] = 0.f;
             continue;
         }
         const int mx = kx < (Nx + 1) / 2 ? kx : kx - Nx;
@@ -584,11 +590,21 @@ __global__ void pme_convolve_kernel(cufftComplex* __restrict__ g, const float* _
         const float mhx = mx * (float)c_el.inv[0], mhy = my * (float)c_el.inv[1], mhz = mz * (float)c_el.inv[2];
         const float m2 = mhx * mhx + mhy * mhy + mhz * mhz;
         const float denom = m2 * bx[kx] * by[ky] * bz[kz];
-        const float eterm = scalef * expf(-expf_ * m2) / denom;
-        g[idx].x *= eterm;
-        g[idx].y *= eterm;
+        et[idx] = scalef * expf(-expf_ * m2) / denom;
     }
 }
+
+// g *= eterm on the R2C half grid
+__global__ void pme_scale_kernel(long total, cufftComplex* __restrict__ g, const float* __restrict__ et) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const float e = et[i];
+        cufftComplex v = g[i];
+        v.x *= e;
+        v.y *= e;
+        g[i] = v;
+    }
+}
+
 
 // Gather phi and derivatives (grid units) at every site: ncomp 4 (phi, dx,
 // dy, dz) or 10 (+ xx, yy, zz, xy, xz, yz).
@@ -861,11 +877,20 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                                       float* __restrict__ mu_out, double* __restrict__ mu_d,
                                       double* __restrict__ eps2, int mode, float* __restrict__ Ebase,
                                       const float* __restrict__ anchor, const float* __restrict__ intra,
-                                      const float* __restrict__ pcoef) {
+                                      const float* __restrict__ pcoef, const int* __restrict__ mcl,
+                                      const int* __restrict__ cdone, double* __restrict__ eps2c) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     double d2sum = 0.0;
-    if (A < nmol) {
+    // batched clusters (mcl set): each cluster converges on its own; a
+    // finished cluster keeps its dipoles (copied through, no field work)
+    const int cA = (mcl && A < nmol) ? mcl[A] : -1;
+    const bool frozen = cA >= 0 && cdone[cA] != 0;
+    if (A < nmol && frozen && lane == 0) {
+        for (int i = c_el.K * A; i < c_el.K * (A + 1); ++i)
+            for (int k = 0; k < 3; ++k) mu_out[3 * i + k] = (float)mu_d[3 * i + k];
+    }
+    if (A < nmol && !frozen) {
         const int K = c_el.K;
         f3 offA[kMaxK];
         float polA[kMaxK];
@@ -980,6 +1005,10 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
             }
         }
     }
+    if (mcl) {
+        if (cA >= 0 && !frozen && lane == 0) atomicAdd(eps2c + cA, d2sum);
+        d2sum = 0.0;
+    }
     block_sum_atomic<128>(d2sum, eps2);
 }
 
@@ -994,7 +1023,7 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                                     const float* __restrict__ nbd, const int* __restrict__ nnb, int cap,
                                     const float* __restrict__ mu, const float* __restrict__ phi_fix,
                                     const float* __restrict__ phi_mu, int redist, double* __restrict__ force,
-                                    double* __restrict__ energy) {
+                                    double* __restrict__ energy, ClusterSink cs) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     double e_out = 0.0;
@@ -1213,9 +1242,49 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                 force[3 * i + 2] += (double)F[a][2] * f;
             }
             e_out = e * kElectric;
+            cluster_energy(cs, A, e_out);
         }
     }
     block_sum_atomic<128>(e_out, energy);
+}
+
+// Starting dipoles from the history of solves (guess 2 and 3): with r_k the
+// residual mu - m of the k-th previous converged solve (m the network's
+// prediction, or 0 without a network), mu0 = m + P(r), P the polynomial
+// extrapolation through the available levels: r1; 2 r1 - r2; 3 r1 - 3 r2 + r3.
+// FP64 state and its FP32 copy.
+__global__ void extrapolated_guess_kernel(int n, const float* __restrict__ m, int levels,
+                                          const double* __restrict__ r1, const double* __restrict__ r2,
+                                          const double* __restrict__ r3, double* __restrict__ mu_d,
+                                          float* __restrict__ mu_f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = m ? (double)m[i] : 0.0;
+    if (levels == 1) v += r1[i];
+    else if (levels == 2) v += 2.0 * r1[i] - r2[i];
+    else if (levels >= 3) v += 3.0 * r1[i] - 3.0 * r2[i] + r3[i];
+    mu_d[i] = v;
+    mu_f[i] = (float)v;
+}
+
+// Network start: mu = mu_prev + (m - m_prev) after one solve with a
+// prediction, else mu = m; FP64 state and its FP32 copy.
+__global__ void learned_guess_kernel(int n, const float* __restrict__ m, const float* __restrict__ m_prev,
+                                     const double* __restrict__ mu_prev, double* __restrict__ mu_d,
+                                     float* __restrict__ mu_f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = mu_prev ? mu_prev[i] + ((double)m[i] - (double)m_prev[i]) : (double)m[i];
+    mu_d[i] = v;
+    mu_f[i] = (float)v;
+}
+
+// residual mu - m of a converged solve, for the history
+__global__ void residual_kernel(int n, const double* __restrict__ mu, const float* __restrict__ m,
+                                double* __restrict__ r) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    r[i] = mu[i] - (m ? (double)m[i] : 0.0);
 }
 
 __global__ void narrow_kernel(int n, const double* __restrict__ a, float* __restrict__ b) {
@@ -1352,7 +1421,8 @@ struct ElecImpl {
     // PME
     int grid[3] = {0, 0, 0};
     double alpha = 0.0;
-    DBuf<float> d_grid, d_gridfix, d_bx, d_by, d_bz;
+    DBuf<float> d_grid, d_gridfix, d_bx, d_by, d_bz, d_eterm;
+    double eterm_key[4] = {0, 0, 0, 0};  // box and alpha of d_eterm
     DBuf<unsigned long long> d_gridq;
     DBuf<cufftComplex> d_cgrid;
     cufftHandle plan_f = 0, plan_b = 0;
@@ -1364,6 +1434,25 @@ struct ElecImpl {
     double epsilon = 0.0;
     long npairs = 0;
     bool have_prev = false;
+    // learned guess (guess = 2)
+    GuessNet net;
+    DBuf<float> d_mguess;
+    DBuf<float> d_mprev;  // the network's prediction at the previous solve
+    bool have_mprev = false;
+    // dipoles of the last (up to) three converged solves, a ring of three
+    // 3n planes (FP64)
+    DBuf<double> d_hist;
+    int hist_levels = 0, hist_head = 0;
+    bool evaluated = false;  // neighbour list, offsets and dipoles are current
+    // batched independent clusters (NoCutoff): molecule -> cluster, per-
+    // cluster solver state and energy sink
+    int ncl = 0, max_cl_mol = 0;
+    std::vector<int> cl_nsites, cl_iters;
+    std::vector<char> cl_conv;
+    DBuf<int> d_mcl, d_cdone;
+    DBuf<double> d_eps2c;
+    ClusterSink cl_sink;
+    Box last_box{};
     int mu_cur = 0;  // which buffer holds the current dipoles
 
     ~ElecImpl() {
@@ -1442,9 +1531,15 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     MBPOL_CUDA_OK(I.d_eps2.ensure(1));
     MBPOL_CUDA_OK(I.d_mud.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_mud_prev.ensure(3 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_mguess.ensure(3 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_hist.ensure(9 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_mprev.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms, kDmsCoef, sizeof(kDmsCoef)));
     MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms_idx, kDmsIdx, sizeof(kDmsIdx)));
     I.have_prev = false;
+    I.have_mprev = false;
+    I.hist_levels = 0;
+    I.evaluated = false;
     return MBPOL_OK;
 }
 
@@ -1485,8 +1580,13 @@ static mbpol_status pme_setup(ElecImpl& I, const Box& box) {
         const size_t ncplx = (size_t)g[0] * g[1] * (g[2] / 2 + 1);
         MBPOL_CUDA_OK(I.d_grid.ensure(2 * ncplx));  // in-place friendly size
         MBPOL_CUDA_OK(I.d_gridq.ensure(nreal));
+        // zero once: every spread is followed by the conversion, which
+        // returns the fixed-point grid to zero
+        MBPOL_CUDA_OK(cudaMemset(I.d_gridq.p, 0, sizeof(unsigned long long) * nreal));
         MBPOL_CUDA_OK(I.d_gridfix.ensure(nreal));
         MBPOL_CUDA_OK(I.d_cgrid.ensure(ncplx));
+        MBPOL_CUDA_OK(I.d_eterm.ensure(ncplx));
+        I.eterm_key[3] = 0.0;
         std::vector<double> mod;
         DBuf<float>* bb[3] = {&I.d_bx, &I.d_by, &I.d_bz};
         for (int d = 0; d < 3; ++d) {
@@ -1501,8 +1601,6 @@ static mbpol_status pme_setup(ElecImpl& I, const Box& box) {
 
 // spread (fixed point) and convert to the FP32 grid d_grid
 static cudaError_t pme_spread(ElecImpl& I, cudaStream_t st, int mode, const float* mu, int n, size_t nreal) {
-    cudaError_t e = cudaMemsetAsync(I.d_gridq.p, 0, sizeof(unsigned long long) * nreal, st);
-    if (e != cudaSuccess) return e;
     count_launch();
     pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, mode, I.d_q.p, mu, I.d_gidx.p, I.d_gfrac.p, I.d_gridq.p);
     count_launch();
@@ -1522,8 +1620,17 @@ static mbpol_status pme_convolve(ElecImpl& I, cudaStream_t st, const Box& box) {
     const float scalef = (float)(1.0 / (M_PI * box.L[0] * box.L[1] * box.L[2]));
     const long total = (long)I.grid[0] * I.grid[1] * nzh;
     int blocks = (int)std::min<long>((total + 255) / 256, 152L * 16);
+    if (I.eterm_key[0] != box.L[0] || I.eterm_key[1] != box.L[1] || I.eterm_key[2] != box.L[2] ||
+        I.eterm_key[3] != I.alpha) {
+        count_launch();
+        pme_eterm_kernel<<<blocks, 256, 0, st>>>(I.d_eterm.p, I.d_bx.p, I.d_by.p, I.d_bz.p, expf_, scalef, nzh);
+        I.eterm_key[0] = box.L[0];
+        I.eterm_key[1] = box.L[1];
+        I.eterm_key[2] = box.L[2];
+        I.eterm_key[3] = I.alpha;
+    }
     count_launch();
-    pme_convolve_kernel<<<blocks, 256, 0, st>>>(I.d_cgrid.p, I.d_bx.p, I.d_by.p, I.d_bz.p, expf_, scalef, nzh);
+    pme_scale_kernel<<<blocks, 256, 0, st>>>(total, I.d_cgrid.p, I.d_eterm.p);
     if (cufftExecC2R(I.plan_b, I.d_cgrid.p, I.d_grid.p) != CUFFT_SUCCESS)
         return mbpol_fail(MBPOL_ERR_CUDA, "cufftExecC2R failed");
     return MBPOL_OK;
@@ -1564,7 +1671,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                                                             I.d_opos.p);
     // neighbour list
     const double rcut = I.pme ? I.prm.cutoff : 1e30;
-    if (I.cap == 0) I.cap = I.pme ? 256 : ((nmol + 31) / 32) * 32;
+    if (I.cap == 0) I.cap = I.pme ? 256 : ((((I.ncl > 0 ? I.max_cl_mol : nmol)) + 31) / 32) * 32;
     for (int attempt = 0;; ++attempt) {
         MBPOL_CUDA_OK(I.d_nb.ensure((size_t)nmol * I.cap));
         MBPOL_CUDA_OK(I.d_nbd.ensure((size_t)nmol * I.cap * 3));
@@ -1572,7 +1679,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         count_launch();
         elec_neighbors_kernel<<<(nmol * 32 + 127) / 128, 128, 0, st>>>(
             nmol, pos, I.d_opos.p, box.periodic && I.pme, rcut, I.d_reach.p, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p,
-            I.d_flags.p, nullptr);
+            I.d_flags.p, I.ncl > 0 ? I.d_mcl.p : nullptr);
         int ovf = 0;
         MBPOL_CUDA_OK(cudaMemcpyAsync(&ovf, I.d_flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(st));
@@ -1607,7 +1714,36 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     // d_mu0 holds float(mu) of the starting dipoles (alpha*E0 from the
     // fixed-field kernel, or the previous call's dipoles)
     float* bufs[3] = {I.d_mu0.p, I.d_mu1.p, I.d_mu2.p};
-    if (I.prm.guess == 1 && I.have_prev) {
+    // starting dipoles: 3 polynomial extrapolation of the last solves; 2 the
+    // same once two solves exist, before that the network (cold start, or
+    // mu_prev + m - m_prev after one solve); 1 previous solve; 0 alpha E0
+    // (the reference).  In a smooth trajectory the extrapolation error
+    // (~1e-4 of mu) is below what a BF16 network resolves, so the network
+    // serves the first steps and single-point evaluations.
+    const bool learned = I.prm.guess == 2 && I.net.ready() && (I.K == 3 || I.K == 4);
+    const bool history = I.prm.guess >= 2;
+    const bool extrapolate = history && (I.hist_levels >= 2 || (I.prm.guess == 3 && I.hist_levels >= 1));
+    if (learned && !extrapolate) {
+        MBPOL_CUDA_OK(I.net.descriptors(st, nmol, I.K, I.d_off.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, box.L,
+                                        box.periodic && I.pme, I.d_E0.p));
+        MBPOL_CUDA_OK(I.net.predict(st, nmol, I.K, I.d_mguess.p));
+    }
+    const bool used_net = learned && !extrapolate;
+    if (extrapolate) {
+        const size_t plane = 3 * (size_t)n;
+        const double* r1 = I.d_hist.p + plane * I.hist_head;
+        const double* r2 = I.d_hist.p + plane * ((I.hist_head + 2) % 3);
+        const double* r3 = I.d_hist.p + plane * ((I.hist_head + 1) % 3);
+        count_launch();
+        extrapolated_guess_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, nullptr, I.hist_levels, r1, r2, r3,
+                                                                       I.d_mud.p, I.d_mu0.p);
+    } else if (used_net) {
+        const bool prev = I.have_prev && I.have_mprev;
+        count_launch();
+        learned_guess_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, I.d_mguess.p, prev ? I.d_mprev.p : nullptr,
+                                                                  prev ? I.d_mud_prev.p : nullptr, I.d_mud.p,
+                                                                  I.d_mu0.p);
+    } else if (I.prm.guess >= 1 && I.have_prev) {
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mu0.p, I.d_mu_prev.p, sizeof(float) * 3 * (size_t)n,
                                       cudaMemcpyDeviceToDevice, st));
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mud.p, I.d_mud_prev.p, sizeof(double) * 3 * (size_t)n,
@@ -1626,6 +1762,75 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     float* mu_in = bufs[0];
     float* anchor = nullptr;
     int mode = 0;
+    if (I.ncl > 0) {
+        // batched clusters: each cluster runs the reference's loop on its own
+        // epsilon (its own site count) and stops on its own; the others go on
+        const int ncl = I.ncl;
+        std::vector<double> cur(ncl, 1.0e+50), e2(ncl, 0.0);
+        std::vector<int> its(ncl, 0), cdone(ncl, 0);
+        std::vector<char> cconv(ncl, 0);
+        int active = 0;
+        for (int c = 0; c < ncl; ++c) {
+            if (I.cl_nsites[c] > 0) {
+                ++active;
+            } else {
+                cdone[c] = 1;
+                cconv[c] = 1;
+            }
+        }
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_cdone.p, cdone.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, st));
+        while (active > 0) {
+            float* mu_out = mu_in == bufs[0] ? bufs[1] : bufs[0];
+            MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2c.p, 0, sizeof(double) * ncl, st));
+            prof_begin(st, K_ELEC_INDUCED);
+            count_launch();
+            induced_update_kernel<false><<<wblocks, 128, 0, st>>>(
+                nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
+                nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p, 0, I.d_ebase.p, nullptr, I.d_intra.p, I.d_pcoef.p,
+                I.d_mcl.p, I.d_cdone.p, I.d_eps2c.p);
+            prof_end(st, K_ELEC_INDUCED);
+            mu_in = mu_out;
+            MBPOL_CUDA_OK(cudaMemcpyAsync(e2.data(), I.d_eps2c.p, sizeof(double) * ncl, cudaMemcpyDeviceToHost, st));
+            MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+            bool changed = false;
+            for (int c = 0; c < ncl; ++c) {
+                if (cdone[c]) continue;
+                const double ec = kSOR * kDebye * sqrt(e2[c] / (double)I.cl_nsites[c]);
+                bool stop = false;
+                if (!std::isfinite(ec)) {
+                    stop = true;
+                } else if (ec < I.prm.target_epsilon) {
+                    cconv[c] = 1;
+                    stop = true;
+                } else if (cur[c] < ec || its[c] >= I.prm.max_iterations) {
+                    stop = true;
+                }
+                cur[c] = ec;
+                ++its[c];
+                if (stop) {
+                    cdone[c] = 1;
+                    --active;
+                    changed = true;
+                }
+            }
+            if (changed && active > 0)
+                MBPOL_CUDA_OK(
+                    cudaMemcpyAsync(I.d_cdone.p, cdone.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, st));
+            // the copy reads cdone before the next iteration's host update
+            MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+        }
+        I.cl_iters = its;
+        I.cl_conv = cconv;
+        it = 0;
+        conv = true;
+        current = 0.0;
+        for (int c = 0; c < ncl; ++c) {
+            it = std::max(it, its[c]);
+            conv = conv && cconv[c];
+            if (I.cl_nsites[c] > 0) current = std::max(current, cur[c]);
+        }
+        done = true;
+    }
     while (!done) {
         int kmode = mode;
         if (mode == 0 && current < switch_eps) kmode = 1;
@@ -1652,13 +1857,13 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                                                                   I.d_phi_mu.p, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
                                                                   kmode, I.d_ebase.p, anchor, I.d_intra.p,
-                                                                  I.d_pcoef.p);
+                                                                  I.d_pcoef.p, nullptr, nullptr, nullptr);
         else
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                    I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                                                                    nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
                                                                    kmode, I.d_ebase.p, anchor, I.d_intra.p,
-                                                                  I.d_pcoef.p);
+                                                                  I.d_pcoef.p, nullptr, nullptr, nullptr);
         prof_end(st, K_ELEC_INDUCED);
         if (kmode == 1) anchor = mu_in;
         mode = kmode == 0 ? 0 : 2;
@@ -1690,8 +1895,22 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                                       cudaMemcpyDeviceToDevice, st));
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mud_prev.p, I.d_mud.p, sizeof(double) * 3 * (size_t)n,
                                       cudaMemcpyDeviceToDevice, st));
+        if (history) {
+            I.hist_head = (I.hist_head + 1) % 3;
+            count_launch();
+            residual_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, I.d_mud.p, nullptr,
+                                                                 I.d_hist.p + 3 * (size_t)n * I.hist_head);
+            I.hist_levels = std::min(I.hist_levels + 1, 3);
+        }
+        if (used_net)
+            MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mprev.p, I.d_mguess.p, sizeof(float) * 3 * (size_t)n,
+                                          cudaMemcpyDeviceToDevice, st));
     }
     I.have_prev = conv;
+    I.have_mprev = conv && used_net;
+    if (!conv || !history) I.hist_levels = 0;
+    I.evaluated = true;
+    I.last_box = box;
     if (I.pme) {
         MBPOL_CUDA_OK(pme_spread(I, st, 1, mu_final, n, nreal));
         mbpol_status s = pme_convolve(I, st, box);
@@ -1702,13 +1921,15 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         count_launch();
         energy_force_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p, I.d_type.p,
                                                             I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, mu_final,
-                                                            I.d_phi_fix.p, I.d_phi_mu.p, redist, force, energy);
+                                                            I.d_phi_fix.p, I.d_phi_mu.p, redist, force, energy,
+                                                            I.cl_sink);
         prof_end(st, K_ELEC_FORCES);
     } else {
         count_launch();
         energy_force_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p,
                                                              I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
-                                                             mu_final, nullptr, nullptr, redist, force, energy);
+                                                             mu_final, nullptr, nullptr, redist, force, energy,
+                                                             I.cl_sink);
     }
     MBPOL_CUDA_OK(cudaGetLastError());
     return MBPOL_OK;
@@ -1726,13 +1947,114 @@ mbpol_status ElecEngine::get_dipoles(cudaStream_t st, double* dipoles, int* iter
     return MBPOL_OK;
 }
 
+mbpol_status ElecEngine::guess_descriptors(cudaStream_t st, float* host_out) {
+    ElecImpl& I = *impl_;
+    if (!I.evaluated) return mbpol_fail(MBPOL_ERR_STATE, "no electrostatics evaluation yet");
+    if (I.K != 3 && I.K != 4) return mbpol_fail(MBPOL_ERR_STATE, "the learned guess needs water molecules");
+    MBPOL_CUDA_OK(I.net.descriptors(st, I.nmol, I.K, I.d_off.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.last_box.L,
+                                    I.last_box.periodic && I.pme, I.d_E0.p));
+    if (host_out) {
+        MBPOL_CUDA_OK(cudaMemcpyAsync(host_out, I.net.d_desc(), sizeof(float) * guess::kIn * (size_t)I.nmol,
+                                      cudaMemcpyDeviceToHost, st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+    }
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::guess_collect(cudaStream_t st) {
+    ElecImpl& I = *impl_;
+    if (!I.converged) return mbpol_fail(MBPOL_ERR_STATE, "the last solve did not converge; nothing to collect");
+    mbpol_status s = guess_descriptors(st, nullptr);
+    if (s) return s;
+    MBPOL_CUDA_OK(I.net.collect(st, I.nmol, I.K, I.d_mud.p));
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::guess_train(cudaStream_t st, int steps, int batch, double lr, unsigned long long seed,
+                                     double* loss) {
+    ElecImpl& I = *impl_;
+    if (I.net.num_samples() <= 0) return mbpol_fail(MBPOL_ERR_STATE, "no training samples collected");
+    if (steps <= 0 || batch <= 0 || !(lr > 0)) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad training arguments");
+    MBPOL_CUDA_OK(I.net.train(st, steps, batch, lr, seed, loss));
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::guess_get_params(float* block) {
+    if (!block) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null parameter block");
+    if (!impl_->net.ready()) return mbpol_fail(MBPOL_ERR_STATE, "the network has no parameters yet");
+    MBPOL_CUDA_OK(impl_->net.get_params(block));
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::guess_set_params(const float* block) {
+    if (!block) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null parameter block");
+    MBPOL_CUDA_OK(impl_->net.set_params(block));
+    impl_->hist_levels = 0;
+    impl_->have_mprev = false;
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::guess_loss_grad(cudaStream_t st, const float* X, const float* T, int n, double* loss,
+                                         float* grad, float* Y) {
+    if (!X || !T || !loss || !grad || !Y || n <= 0) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (!impl_->net.ready()) return mbpol_fail(MBPOL_ERR_STATE, "the network has no parameters yet");
+    MBPOL_CUDA_OK(impl_->net.loss_grad(st, X, T, n, loss, grad, Y));
+    return MBPOL_OK;
+}
+
+long ElecEngine::guess_num_samples() const { return impl_->net.num_samples(); }
+
 bool ElecEngine::converged() const { return impl_->converged; }
 int ElecEngine::iterations() const { return impl_->iterations; }
 long ElecEngine::num_site_pairs() const { return impl_->npairs; }
 std::string ElecEngine::convergence_message() const {
     std::ostringstream m;
     m << "Induced dipoles did not converge:  iterations=" << impl_->iterations << " eps=" << impl_->epsilon;
+    for (size_t c = 0; c < impl_->cl_conv.size(); ++c)
+        if (!impl_->cl_conv[c]) {
+            m << " (cluster " << c << " after " << impl_->cl_iters[c] << " iterations)";
+            break;
+        }
     return m.str();
 }
+
+mbpol_status ElecEngine::set_clusters(const int* cluster_of_particle, int ncl, double* cluster_energy, int stride) {
+    ElecImpl& I = *impl_;
+    I.ncl = 0;
+    I.cl_sink = ClusterSink();
+    I.cl_iters.clear();
+    I.cl_conv.clear();
+    I.cap = 0;
+    I.have_prev = false;
+    I.have_mprev = false;
+    I.hist_levels = 0;
+    if (ncl <= 0 || !cluster_of_particle) return MBPOL_OK;
+    if (I.pme) return mbpol_fail(MBPOL_ERR_STATE, "batched clusters need the NoCutoff electrostatics method");
+    std::vector<int> mcl(I.nmol), count(ncl, 0);
+    I.cl_nsites.assign(ncl, 0);
+    for (int m = 0; m < I.nmol; ++m) {
+        const int c = cluster_of_particle[I.K * m];
+        if (c < 0 || c >= ncl) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "cluster index out of range");
+        for (int a = 1; a < I.K; ++a)
+            if (cluster_of_particle[I.K * m + a] != c)
+                return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "the sites of one molecule are in different clusters");
+        mcl[m] = c;
+        ++count[c];
+        I.cl_nsites[c] += I.K;
+    }
+    I.max_cl_mol = 0;
+    for (int c = 0; c < ncl; ++c) I.max_cl_mol = std::max(I.max_cl_mol, count[c]);
+    MBPOL_CUDA_OK(I.d_mcl.ensure(I.nmol));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_mcl.p, mcl.data(), sizeof(int) * (size_t)I.nmol, cudaMemcpyHostToDevice));
+    MBPOL_CUDA_OK(I.d_cdone.ensure(ncl));
+    MBPOL_CUDA_OK(I.d_eps2c.ensure(ncl));
+    I.ncl = ncl;
+    I.cl_sink.wcl = I.d_mcl.p;
+    I.cl_sink.e = cluster_energy;
+    I.cl_sink.stride = stride;
+    return MBPOL_OK;
+}
+
+const std::vector<int>& ElecEngine::cluster_iterations() const { return impl_->cl_iters; }
 
 }  // namespace mbpol

@@ -2,6 +2,7 @@
 // permanent and induced fields, induced-dipole solver, PME, energy/forces).
 #pragma once
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 #include "../../include/mbpol_gb300.h"
 #include "mbpol_internal.cuh"
@@ -26,6 +27,22 @@ public:
     int iterations() const;
     long num_site_pairs() const;
     std::string convergence_message() const;
+    // learned initial guess (guess = 2); descriptors and collection refer to
+    // the last evaluation's geometry and converged dipoles
+    mbpol_status guess_descriptors(cudaStream_t st, float* host_out);
+    mbpol_status guess_collect(cudaStream_t st);
+    mbpol_status guess_train(cudaStream_t st, int steps, int batch, double lr, unsigned long long seed,
+                             double* loss);
+    mbpol_status guess_get_params(float* block);
+    mbpol_status guess_set_params(const float* block);
+    mbpol_status guess_loss_grad(cudaStream_t st, const float* X, const float* T, int n, double* loss, float* grad,
+                                 float* Y);
+    long guess_num_samples() const;
+    // batched independent clusters (NoCutoff only): cluster of every
+    // particle; per-cluster electrostatic energies go to
+    // cluster_energy[c * stride] (device).  ncl = 0 turns batching off.
+    mbpol_status set_clusters(const int* cluster_of_particle, int ncl, double* cluster_energy, int stride);
+    const std::vector<int>& cluster_iterations() const;
 
 private:
     ElecImpl* impl_;

@@ -1,0 +1,75 @@
+// Learned initial guess for the induced dipoles: per-water descriptors, a
+// 48-64-64-9 SiLU network with BF16 weights on the tensor cores (mma.sync,
+// FP32 accumulation), its training (forward, backward, Adam) on the GPU, and
+// the guess mu0 = mu_prev + (m_now - m_prev) (m the network's lab-frame
+// prediction), or m_now when there is no previous solve.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+namespace mbpol {
+
+namespace guess {
+constexpr int kFeat = 48;   // neighbourhood descriptors
+constexpr int kField = 9;   // permanent field at O, H1, H2 in the water's frame
+constexpr int kIn = 64;     // network input: descriptors, field, zero padding
+constexpr int kHidden = 64;
+constexpr int kOut = 9;
+// flat parameter vector: W1 [64][64], b1 [64], W2 [64][64], b2 [64], W3 [9][64], b3 [9]
+constexpr int kW1 = 0;
+constexpr int kB1 = kW1 + kHidden * kIn;
+constexpr int kW2 = kB1 + kHidden;
+constexpr int kB2 = kW2 + kHidden * kHidden;
+constexpr int kW3 = kB2 + kHidden;
+constexpr int kB3 = kW3 + kOut * kHidden;
+constexpr int kParams = kB3 + kOut;  // 8905
+// the parameter block handed across the ABI: kParams weights, then the
+// input standardisation (mean[64], 1/std[64])
+constexpr int kBlockFloats = kParams + 2 * kIn;
+constexpr float kOutScale = 1e-3f;  // e nm per network output unit
+}  // namespace guess
+
+struct GuessBuffers;
+
+// Owned by the electrostatics engine.  All arrays are device memory unless
+// named h_*.
+class GuessNet {
+public:
+    GuessNet();
+    ~GuessNet();
+    GuessNet(const GuessNet&) = delete;
+    GuessNet& operator=(const GuessNet&) = delete;
+
+    bool ready() const { return ready_; }
+    long num_samples() const { return nsamples_; }
+
+    // network inputs D [nmol][64] (48 descriptors from the electrostatics
+    // neighbour list, the permanent field E0 [sites][3] at O, H1, H2 in the
+    // water's frame, zeros) and frames F [nmol][9] of the current geometry
+    cudaError_t descriptors(cudaStream_t st, int nmol, int K, const float* off, const int* nb, const float* nbd,
+                            const int* nnb, int cap, const double* box, int periodic, const float* E0);
+    const float* d_desc() const;
+    const float* d_frames() const;
+    // append the current descriptors with the converged dipoles (FP64,
+    // [nsites][3]) as training targets
+    cudaError_t collect(cudaStream_t st, int nmol, int K, const double* mu_d);
+    // network prediction m [nsites][3] (lab frame, e nm) for the current
+    // descriptors
+    cudaError_t predict(cudaStream_t st, int nmol, int K, float* m_out);
+    // training on the collected samples; returns the mean loss of the last
+    // 10% of the steps
+    cudaError_t train(cudaStream_t st, int steps, int batch, double lr, unsigned long long seed, double* loss);
+    // loss, gradient and outputs for host data (n rows), no update
+    cudaError_t loss_grad(cudaStream_t st, const float* h_X, const float* h_T, int n, double* loss, float* h_grad,
+                          float* h_Y);
+    cudaError_t get_params(float* h_block) const;
+    cudaError_t set_params(const float* h_block);
+
+private:
+    GuessBuffers* b_;
+    bool ready_ = false;
+    long nsamples_ = 0;
+};
+
+}  // namespace mbpol

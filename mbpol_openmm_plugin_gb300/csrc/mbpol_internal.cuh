@@ -63,6 +63,18 @@ __device__ __forceinline__ void add_force(double* __restrict__ f, int i, double 
 }
 
 // Block-wide FP64 sum, then one atomic per block into *out.
+// Per-cluster energies for batched independent clusters: a unit's energy is
+// also added to e[cluster_of_water[w] * stride] (e offset by the term).
+// Empty (wcl null) for a single system.
+struct ClusterSink {
+    const int* wcl = nullptr;
+    double* e = nullptr;
+    int stride = 0;
+};
+__device__ __forceinline__ void cluster_energy(const ClusterSink& cs, int water, double e) {
+    if (cs.wcl && e != 0.0) atomicAdd(cs.e + (size_t)cs.wcl[water] * cs.stride, e);
+}
+
 template <int BLOCK>
 __device__ __forceinline__ void block_sum_atomic(double v, double* out) {
     __shared__ double red[BLOCK / 32];

@@ -9,16 +9,17 @@ namespace mbpol {
 // polyterms.cu
 void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245);
 void launch_onebody(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double* force,
-                    double* energy);
+                    double* energy, ClusterSink cs = ClusterSink());
 void launch_twobody_vars(cudaStream_t st, int npairs, const int2* pairs, const int4* waters, const double* pos,
                          Box box, float* X, int stride);
 void launch_twobody_forces(cudaStream_t st, int npairs, const int2* pairs, const int4* waters, const double* pos,
-                           Box box, const float* G, const float* E, int stride, double* force, double* energy);
+                           Box box, const float* G, const float* E, int stride, double* force, double* energy,
+                           ClusterSink cs = ClusterSink());
 void launch_threebody_vars(cudaStream_t st, int ntrip, const int4* trips, const int4* waters, const double* pos,
                            Box box, float* X, int stride);
 void launch_threebody_forces(cudaStream_t st, int ntrip, const int4* trips, const int4* waters,
                              const double* pos, Box box, const float* G, const float* E, int stride,
-                             double* force, double* energy);
+                             double* force, double* energy, ClusterSink cs = ClusterSink());
 
 // poly_df.cu
 cudaError_t poly_tables_upload(int device);
@@ -47,7 +48,8 @@ void launch_trimer_complete(cudaStream_t st, int nw, const int4* waters, const d
 // dispersion.cu
 void upload_dispersion_tables(const double* c6_4x4, const double* d6_4x4);
 void launch_dispersion(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, const int* full,
-                       const int* nfull, int cap_full, double rc, double* force, double* energy);
+                       const int* nfull, int cap_full, double rc, double* force, double* energy,
+                       ClusterSink cs = ClusterSink());
 
 // md.cu
 void launch_kick_drift(cudaStream_t st, int n, const double* invm, double* vel, double* pos, const double* force,

@@ -75,6 +75,34 @@ __device__ __forceinline__ void leaf_update(const PolyNode& L, float xl, float x
     acc(g, p, q);
 }
 
+// U leaves of one level-3 node: all loads first, then the updates in leaf
+// order (V3's summation order is unchanged), then the stores.
+template <int U>
+__device__ __forceinline__ void leaf_batch(const PolyNode* __restrict__ lv, const float* xs, const float* xq,
+                                           float* gh, float* gl, int t, const DF& P3, DF& V3) {
+    PolyNode L[U];
+    int o[U];
+    float x[U], xl[U];
+    DF g[U];
+    #pragma unroll
+    for (int u = 0; u < U; ++u) L[u] = lv[u];
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+        o[u] = L[u].var * kBlock + t;
+        x[u] = xs[o[u]];
+        xl[u] = xq[o[u]];
+        g[u].h = gh[o[u]];
+        g[u].l = gl[o[u]];
+    }
+    #pragma unroll
+    for (int u = 0; u < U; ++u) leaf_update(L[u], x[u], xl[u], P3, V3, g[u]);
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+        gh[o[u]] = g[u].h;
+        gl[o[u]] = g[u].l;
+    }
+}
+
 template <int NV>
 __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restrict__ l1, int n1,
                                                           const PolyNode* __restrict__ l2,
@@ -129,32 +157,11 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                         DF P3;
                         mul_df_f(P2, xk, P3.h, P3.l);
                         P3.l = __fmaf_rn(P2.h, xkl, P3.l);
-                        // four leaves at a time: their nodes and operands are
+                        // leaves in batches of four: their nodes and operands are
                         // loaded together, so the L2 latency of the node reads
-                        // overlaps (leaf variables of one node are distinct)
-                        for (; cl + 4 <= cend; cl += 4) {
-                            PolyNode L[4];
-                            int o[4];
-                            float x[4], xl[4];
-                            DF g[4];
-                            #pragma unroll
-                            for (int u = 0; u < 4; ++u) L[u] = lv[cl + u];
-                            #pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                o[u] = L[u].var * kBlock + t;
-                                x[u] = xs[o[u]];
-                                xl[u] = xq[o[u]];
-                                g[u].h = gh[o[u]];
-                                g[u].l = gl[o[u]];
-                            }
-                            #pragma unroll
-                            for (int u = 0; u < 4; ++u) leaf_update(L[u], x[u], xl[u], P3, V3, g[u]);
-                            #pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                gh[o[u]] = g[u].h;
-                                gl[o[u]] = g[u].l;
-                            }
-                        }
+                        // overlaps (leaf variables of one node are distinct;
+                        // batches of eight measured slower)
+                        for (; cl + 4 <= cend; cl += 4) leaf_batch<4>(lv + cl, xs, xq, gh, gl, t, P3, V3);
                         for (; cl < cend; ++cl) {
                             const PolyNode L = lv[cl];
                             const int o = L.var * kBlock + t;

@@ -28,7 +28,7 @@ struct OneBodyParams {
 __constant__ OneBodyParams c_1b;
 
 __global__ void onebody_kernel(int nw, const int4* __restrict__ waters, const double* __restrict__ pos,
-                               Box box, double* __restrict__ force, double* __restrict__ energy) {
+                               Box box, double* __restrict__ force, double* __restrict__ energy, ClusterSink cs) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     double e_out = 0.0;
     if (w < nw) {
@@ -92,6 +92,7 @@ __global__ void onebody_kernel(int nw, const int4* __restrict__ waters, const do
         add_force(force, wi.y, -fH1[0], -fH1[1], -fH1[2]);
         add_force(force, wi.z, -fH2[0], -fH2[1], -fH2[2]);
         add_force(force, wi.x, fH1[0] + fH2[0], fH1[1] + fH2[1], fH1[2] + fH2[2]);
+        cluster_energy(cs, w, e_out);
     }
     block_sum_atomic<128>(e_out, energy);
 }
@@ -196,7 +197,7 @@ __global__ void twobody_vars_kernel(int npairs, const int2* __restrict__ pairs, 
 __global__ void twobody_forces_kernel(int npairs, const int2* __restrict__ pairs, const int4* __restrict__ waters,
                                       const double* __restrict__ pos, Box box, const float* __restrict__ G,
                                       const float* __restrict__ E, int stride, double* __restrict__ force,
-                                      double* __restrict__ energy) {
+                                      double* __restrict__ energy, ClusterSink cs) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     double e_out = 0.0;
     if (p < npairs) {
@@ -263,6 +264,7 @@ __global__ void twobody_forces_kernel(int npairs, const int2* __restrict__ pairs
                 add_force(force, idx[i], f.x, f.y, f.z);
             }
             e_out = (double)sw * (double)Ep * kCalToJ;
+            cluster_energy(cs, pr.x, e_out);
         }
     }
     block_sum_atomic<128>(e_out, energy);
@@ -339,7 +341,7 @@ __device__ __forceinline__ float sw3(float r, float rf, float& g) {
 __global__ void threebody_forces_kernel(int ntrip, const int4* __restrict__ trips, const int4* __restrict__ waters,
                                         const double* __restrict__ pos, Box box, const float* __restrict__ G,
                                         const float* __restrict__ E, int stride, double* __restrict__ force,
-                                        double* __restrict__ energy) {
+                                        double* __restrict__ energy, ClusterSink cs) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     double e_out = 0.0;
     if (t < ntrip) {
@@ -379,6 +381,7 @@ __global__ void threebody_forces_kernel(int ntrip, const int4* __restrict__ trip
             #pragma unroll
             for (int i = 0; i < 9; ++i) add_force(force, idx[i], fr[i].x, fr[i].y, fr[i].z);
             e_out = (double)Ep * (double)sw * kCalToJ;
+            cluster_energy(cs, tr.x, e_out);
         }
     }
     block_sum_atomic<128>(e_out, energy);
@@ -467,10 +470,10 @@ void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245)
 }
 
 void launch_onebody(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, double* force,
-                    double* energy) {
+                    double* energy, ClusterSink cs) {
     if (nw <= 0) return;
     count_launch();
-    onebody_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, force, energy);
+    onebody_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, force, energy, cs);
 }
 
 void launch_twobody_vars(cudaStream_t st, int npairs, const int2* pairs, const int4* waters, const double* pos,
@@ -481,11 +484,12 @@ void launch_twobody_vars(cudaStream_t st, int npairs, const int2* pairs, const i
 }
 
 void launch_twobody_forces(cudaStream_t st, int npairs, const int2* pairs, const int4* waters, const double* pos,
-                           Box box, const float* G, const float* E, int stride, double* force, double* energy) {
+                           Box box, const float* G, const float* E, int stride, double* force, double* energy,
+                           ClusterSink cs) {
     if (npairs <= 0) return;
     count_launch();
     twobody_forces_kernel<<<(npairs + 127) / 128, 128, 0, st>>>(npairs, pairs, waters, pos, box, G, E, stride,
-                                                                 force, energy);
+                                                                 force, energy, cs);
 }
 
 void launch_threebody_vars(cudaStream_t st, int ntrip, const int4* trips, const int4* waters, const double* pos,
@@ -497,11 +501,11 @@ void launch_threebody_vars(cudaStream_t st, int ntrip, const int4* trips, const 
 
 void launch_threebody_forces(cudaStream_t st, int ntrip, const int4* trips, const int4* waters,
                              const double* pos, Box box, const float* G, const float* E, int stride,
-                             double* force, double* energy) {
+                             double* force, double* energy, ClusterSink cs) {
     if (ntrip <= 0) return;
     count_launch();
     threebody_forces_kernel<<<(ntrip + 127) / 128, 128, 0, st>>>(ntrip, trips, waters, pos, box, G, E, stride,
-                                                                  force, energy);
+                                                                  force, energy, cs);
 }
 
 }  // namespace mbpol

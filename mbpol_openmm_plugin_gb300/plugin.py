@@ -419,6 +419,84 @@ class Context:
         check(_capi.load().mbpol_get_counts(self._h, ptr(c)))
         return c
 
+    # ---- batched independent clusters (this library's addition): one
+    # context evaluates many water clusters that do not interact
+    def setClusters(self, cluster_of_particle):
+        """cluster_of_particle: (N,) cluster index of every particle, or None
+        to end batching.  All forces must be non-periodic."""
+        if self._h is None:
+            self._build()
+        if cluster_of_particle is None:
+            check(_capi.load().mbpol_set_clusters(self._h, None, 0))
+            self._ncl = 0
+            return
+        c = np.ascontiguousarray(cluster_of_particle, np.int32)
+        if c.size != self.system.getNumParticles():
+            raise ValueError("one cluster index per particle")
+        self._ncl = int(c.max()) + 1 if c.size else 0
+        check(_capi.load().mbpol_set_clusters(self._h, ptr(c), self._ncl))
+
+    def getClusterResults(self):
+        """(energies (nclusters, 5) kJ/mol in term order 1B, 2B, 3B,
+        electrostatics, dispersion; solver iterations (nclusters,)) of the
+        last evaluation."""
+        n = getattr(self, "_ncl", 0)
+        e = np.zeros((n, _capi.NUM_TERMS))
+        it = np.zeros(n, np.int32)
+        check(_capi.load().mbpol_get_cluster_results(self._h, ptr(e), ptr(it)))
+        return e, it
+
+    # ---- learned initial guess for the induced dipoles (guess = 2); this
+    # library's addition, no reference counterpart
+    def collectDipoleGuessSample(self):
+        """Append the last evaluation's descriptors and converged dipoles
+        (one sample per water) to the device-resident training set."""
+        check(_capi.load().mbpol_guess_collect(self._h))
+
+    def getNumDipoleGuessSamples(self):
+        n = ctypes.c_long()
+        check(_capi.load().mbpol_guess_num_samples(self._h, ctypes.byref(n)))
+        return n.value
+
+    def trainDipoleGuess(self, steps, batch=4096, learning_rate=2e-3, seed=1):
+        """Train the network on the GPU; returns the mean loss of the last
+        10% of the steps."""
+        loss = ctypes.c_double()
+        check(_capi.load().mbpol_guess_train(self._h, int(steps), int(batch), float(learning_rate), int(seed),
+                                             ctypes.byref(loss)))
+        return loss.value
+
+    def getDipoleGuessParameters(self):
+        b = np.zeros(_capi.GUESS_BLOCK_FLOATS, np.float32)
+        check(_capi.load().mbpol_guess_get_params(self._h, ptr(b)))
+        return b
+
+    def setDipoleGuessParameters(self, block):
+        b = np.ascontiguousarray(block, np.float32)
+        if b.size != _capi.GUESS_BLOCK_FLOATS:
+            raise ValueError("a parameter block has %d floats" % _capi.GUESS_BLOCK_FLOATS)
+        if self._h is None:
+            self._build()
+        check(_capi.load().mbpol_guess_set_params(self._h, ptr(b)))
+
+    def getDipoleGuessDescriptors(self):
+        nw = self.system.getNumParticles() // 4
+        d = np.zeros((nw, _capi.GUESS_INPUTS), np.float32)
+        check(_capi.load().mbpol_guess_descriptors(self._h, ptr(d)))
+        return d
+
+    def dipoleGuessLossGrad(self, X, T):
+        """Loss, gradient (8905) and outputs (n, 9) of the current network on
+        raw inputs X (n, 64) and targets T (n, 9); no update."""
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        n = X.shape[0]
+        g = np.zeros(_capi.GUESS_PARAMS, np.float32)
+        Y = np.zeros((n, 9), np.float32)
+        loss = ctypes.c_double()
+        check(_capi.load().mbpol_guess_loss_grad(self._h, ptr(X), ptr(T), n, ctypes.byref(loss), ptr(g), ptr(Y)))
+        return loss.value, g, Y
+
 
 def create_mbpol_system(ws, nonbonded_method="auto", terms=("onebody", "twobody", "threebody", "electrostatics",
                                                             "dispersion"), nonbonded_cutoff=0.9,

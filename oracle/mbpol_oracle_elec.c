@@ -353,6 +353,17 @@ static void o_recip(const OCtx* C, const OSpl* sp, int mode, const double* mu, c
 static void o_water_charge(OSite* O, OSite* H1, OSite* H2, OSite* M);
 #include "oracle_dms.h"
 
+/* fixed (permanent) field of the last orc_electrostatics call, FP64
+ * [n][3], before multiplication by the polarisabilities (the field the
+ * solver starts from; reference :361-420, :1342-1439) */
+static double* o_last_E0 = NULL;
+static int o_last_n = 0;
+int orc_last_fixed_field(int n, double* out) {
+    if (!o_last_E0 || n != o_last_n) return 1;
+    memcpy(out, o_last_E0, 3 * (size_t)n * sizeof(double));
+    return 0;
+}
+
 /* -------------------------------------------------------------- solver */
 int orc_electrostatics(int n, const double* pos, const double* box, int pme, double alpha, const int* grid,
                        double rc, double target_eps, int maxiter, const double* thole, int row_stride, double* f,
@@ -437,6 +448,11 @@ int orc_electrostatics(int n, const double* pos, const double* box, int pme, dou
         }
     for (int i = 0; i < n; ++i)
         for (int k = 0; k < 3; ++k) mu[3 * i + k] = C.s[i].pol * E0[3 * i + k];
+    /* keep the fixed field for orc_last_fixed_field */
+    free(o_last_E0);
+    o_last_E0 = (double*)malloc(3 * (size_t)n * sizeof(double));
+    memcpy(o_last_E0, E0, 3 * (size_t)n * sizeof(double));
+    o_last_n = n;
     tm[1] = o_now() - t0;
     /* SOR iterations */
     const double self = pme ? (4.0 / 3.0) * alpha * alpha * alpha / SQRT_PI : 0.0;

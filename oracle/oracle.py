@@ -100,6 +100,8 @@ def port():
     L.orc_dispersion.argtypes = [I, P, P, P, D, P]
     L.orc_electrostatics.restype = I
     L.orc_electrostatics.argtypes = [I, P, P, I, D, P, D, D, I, P, I, P, P, P, ctypes.POINTER(I), P]
+    L.orc_last_fixed_field.restype = I
+    L.orc_last_fixed_field.argtypes = [I, P]
     L.orc_set_onebody_tables.restype = None
     L.orc_set_onebody_tables.argtypes = [P, P]
     import numpy as np
@@ -160,6 +162,27 @@ def full_model(pos, box, alpha=0.0, grid=(0, 0, 0), eps=1e-8, maxiter=200, cut2=
     out["eelec"], out["felec"], out["iterations"], out["converged"], out["dipoles"] = e.value, f, it.value, rcode == 0, dip
     out["etotal"] = out["e1"] + out["e2"] + out["e3"] + out["edisp"] + out["eelec"]
     out["ftotal"] = out["f1"] + out["f2"] + out["f3"] + out["fdisp"] + out["felec"]
+    return out
+
+
+def fixed_field(pos, box=None, alpha=0.0, grid=(0, 0, 0), rc=0.9):
+    """Permanent field (n, 3) at every site (before the polarisabilities),
+    from one electrostatics evaluation of the port."""
+    import numpy as np
+    L = port()
+    pos = np.ascontiguousarray(pos, np.float64)
+    n = pos.shape[0]
+    b = None if box is None else np.ascontiguousarray(box, np.float64)
+    f = np.zeros((n, 3))
+    e = ctypes.c_double()
+    it = ctypes.c_int()
+    g = np.array(grid, np.int32)
+    th = np.array([0.4, 0.4, 0.055, 0.626, 0.055])
+    L.orc_electrostatics(n, _p(pos), _p(b), 1 if b is not None else 0, alpha, _p(g), rc, 1e-8, 1, _p(th), 1,
+                         _p(f), ctypes.byref(e), None, ctypes.byref(it), None)
+    out = np.zeros((n, 3))
+    if L.orc_last_fixed_field(n, _p(out)):
+        raise RuntimeError("no fixed field recorded")
     return out
 
 
