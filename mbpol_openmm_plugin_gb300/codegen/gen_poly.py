@@ -15,17 +15,16 @@ computes value and gradient in one pass with O(1) live state per level::
     g[v_d] += V_d * P_{d-1}               (reverse-mode contribution)
     E = V_root
 
-so a leaf costs 2 FMAs and an internal node 3 operations.  Outputs:
+Outputs:
 
-* ``csrc/gen/poly2b.ptx`` / ``poly3b.ptx`` — straight-line PTX kernels
-  evaluating the walk in double-float (FP32-pair) arithmetic on the FP32
-  pipe (coefficients are FFMA immediates, no coefficient memory traffic),
-  assembled by ptxas alone: nvcc's front end takes tens of minutes on a
-  function this long.  Plain FP32 is not enough: the monomial sum cancels by
-  a factor of ~1e4-1e5 (terms of 1e2-1e5 kcal/mol summing to ~1), so FP32
-  rounding leaves ~1e-3 relative error; the Dot2-style double-float walk
-  (Ogita, Rump, Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput.
-  26, 2005) brings it to the FP64 level at ~11x the FP32 operation count;
+* ``csrc/gen/poly2b_tables.inc`` / ``poly3b_tables.inc`` — the trie as
+  level arrays of nodes {coefficient as an FP32 (hi, lo) pair, variable,
+  end of children}, walked by the data-driven double-float kernel
+  (csrc/poly_df.cu).  Plain FP32 is not enough: the monomial sum cancels by
+  a factor of ~1e4-1e5, so the walk runs Dot2-style in double-float (Ogita,
+  Rump, Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26,
+  2005).  A straight-line generated kernel was measured too: nvcc did not
+  finish one seventh of the three-body trie in 30 minutes;
 * ``oracle/gen/poly2b_prog.h`` / ``poly3b_prog.h`` — the same walk as a
   table (level, variable, coefficient) interpreted in FP64 by the oracle port.
 """
@@ -111,305 +110,12 @@ def choose_perm(nvars, rows):
     return best[1]
 
 
-def fmt(c):
-    s = "%.9e" % c
-    return s + "f"
-
-
-def f32hex(c):
-    import struct
-    return "0f%08X" % struct.unpack(">I", struct.pack(">f", c))[0]
-
-
 def split_df(c):
     """c (FP64) -> (hi, lo) FP32 pair with hi + lo ~= c to ~48 bits."""
     import struct
     hi = struct.unpack(">f", struct.pack(">f", c))[0]
     lo = struct.unpack(">f", struct.pack(">f", c - hi))[0]
     return hi, lo
-
-
-def df_program(nvars, root, perm):
-    """The depth-first walk as a list of double-float operations.
-
-    Every value that accumulates (V per level, E, g) is a pair (s, c) of
-    FP32 numbers updated Dot2-style: s <- s + p with the exact rounding
-    error of the sum (TwoSum) and of the product (TwoProd by FMA) added into
-    c.  Products x*x are exact pairs; coefficients are (hi, lo) FP32 pairs.
-    Ops (operands are original variable indices):
-      ('p2', i, j)         P2 = x_i * x_j                  (exact pair)
-      ('p3', k)            P3 = P2 * x_k
-      ('set', lev, c)      V_lev = c
-      ('leaf', l, c)       V3 += c x_l ;  g_l += c P3
-      ('close3', k)        V2 += V3 x_k ; g_k += V3 P2
-      ('close2', j, i)     V1 += V2 x_j ; g_j += V2 x_i
-      ('close1', i)        E  += V1 x_i ; g_i += V1
-    """
-    inv = [0] * nvars
-    for v, label in enumerate(perm):
-        inv[label] = v
-    ops = []
-    for l1 in sorted(root["ch"]):
-        n1 = root["ch"][l1]
-        i = inv[l1]
-        ops.append(("set", 1, n1["c"]))
-        for l2 in sorted(n1["ch"]):
-            n2 = n1["ch"][l2]
-            j = inv[l2]
-            ops.append(("set", 2, n2["c"]))
-            if n2["ch"]:
-                ops.append(("p2", i, j))
-            for l3 in sorted(n2["ch"]):
-                n3 = n2["ch"][l3]
-                k = inv[l3]
-                ops.append(("set", 3, n3["c"]))
-                if n3["ch"]:
-                    ops.append(("p3", k))
-                for l4 in sorted(n3["ch"]):
-                    assert not n3["ch"][l4]["ch"]
-                    ops.append(("leaf", inv[l4], n3["ch"][l4]["c"]))
-                ops.append(("close3", k))
-            ops.append(("close2", j, i))
-        ops.append(("close1", i))
-    return ops
-
-
-def f32hex(c):
-    import struct
-    return "0f%08X" % struct.unpack(">I", struct.pack(">f", c))[0]
-
-
-def emit_ptx(name, nvars, ops, out_path, nmono):
-    """Write a standalone PTX kernel ``<name>_batch`` evaluating the walk in
-    double-float arithmetic on the FP32 pipe.
-
-    Layout: X and G are variable-major float arrays ([nvars][stride]),
-    E is [stride]; thread t of the grid-stride loop handles units t, t+grid, ...
-    Explicit .rn rounding keeps ptxas from fusing or reassociating the
-    error-free transformations."""
-    body = []
-    w = body.append
-
-    def two_sum_acc(sh, sl, p, q):
-        # (sh, sl) += p + q   with p the main term, q its low-order part
-        w("    add.rn.f32 %%ts, %s, %s;" % (sh, p))
-        w("    sub.rn.f32 %%tb, %%ts, %s;" % sh)
-        w("    sub.rn.f32 %t1, %ts, %tb;")
-        w("    sub.rn.f32 %%t1, %s, %%t1;" % sh)
-        w("    sub.rn.f32 %%t2, %s, %%tb;" % p)
-        w("    add.rn.f32 %t1, %t1, %t2;")
-        w("    mov.f32 %s, %%ts;" % sh)
-        w("    add.rn.f32 %s, %s, %%t1;" % (sl, sl))
-        w("    add.rn.f32 %s, %s, %s;" % (sl, sl, q))
-
-    def prod_df_f(ah, al, x):
-        # (p, q) = (ah + al) * x
-        w("    mul.rn.f32 %%p, %s, %s;" % (ah, x))
-        w("    neg.f32 %np, %p;")
-        w("    fma.rn.f32 %%q, %s, %s, %%np;" % (ah, x))
-        w("    fma.rn.f32 %%q, %s, %s, %%q;" % (al, x))
-
-    def prod_df_df(ah, al, bh, bl):
-        w("    mul.rn.f32 %%p, %s, %s;" % (ah, bh))
-        w("    neg.f32 %np, %p;")
-        w("    fma.rn.f32 %%q, %s, %s, %%np;" % (ah, bh))
-        w("    fma.rn.f32 %%q, %s, %s, %%q;" % (ah, bl))
-        w("    fma.rn.f32 %%q, %s, %s, %%q;" % (al, bh))
-
-    X = lambda v: "%%x%d" % v
-    for v in range(nvars):
-        w("    mov.f32 %%gh%d, 0f00000000;" % v)
-        w("    mov.f32 %%gl%d, 0f00000000;" % v)
-    w("    mov.f32 %Eh, 0f00000000;")
-    w("    mov.f32 %El, 0f00000000;")
-    for op in ops:
-        kind = op[0]
-        if kind == "set":
-            hi, lo = split_df(op[2])
-            w("    mov.f32 %%V%dh, %s;" % (op[1], f32hex(hi)))
-            w("    mov.f32 %%V%dl, %s;" % (op[1], f32hex(lo)))
-        elif kind == "p2":
-            w("    mul.rn.f32 %%P2h, %s, %s;" % (X(op[1]), X(op[2])))
-            w("    neg.f32 %np, %P2h;")
-            w("    fma.rn.f32 %%P2l, %s, %s, %%np;" % (X(op[1]), X(op[2])))
-        elif kind == "p3":
-            prod_df_f("%P2h", "%P2l", X(op[1]))
-            w("    mov.f32 %P3h, %p;")
-            w("    mov.f32 %P3l, %q;")
-        elif kind == "leaf":
-            l = op[1]
-            hi, lo = split_df(op[2])
-            H, L = f32hex(hi), f32hex(lo)
-            # V3 += c x_l
-            w("    mul.rn.f32 %%p, %s, %s;" % (X(l), H))
-            w("    neg.f32 %np, %p;")
-            w("    fma.rn.f32 %%q, %s, %s, %%np;" % (X(l), H))
-            w("    fma.rn.f32 %%q, %s, %s, %%q;" % (X(l), L))
-            two_sum_acc("%V3h", "%V3l", "%p", "%q")
-            # g_l += c P3
-            w("    mul.rn.f32 %%p, %%P3h, %s;" % H)
-            w("    neg.f32 %np, %p;")
-            w("    fma.rn.f32 %%q, %%P3h, %s, %%np;" % H)
-            w("    fma.rn.f32 %%q, %%P3l, %s, %%q;" % H)
-            w("    fma.rn.f32 %%q, %%P3h, %s, %%q;" % L)
-            two_sum_acc("%%gh%d" % l, "%%gl%d" % l, "%p", "%q")
-        elif kind == "close3":
-            k = op[1]
-            prod_df_f("%V3h", "%V3l", X(k))
-            two_sum_acc("%V2h", "%V2l", "%p", "%q")
-            prod_df_df("%V3h", "%V3l", "%P2h", "%P2l")
-            two_sum_acc("%%gh%d" % k, "%%gl%d" % k, "%p", "%q")
-        elif kind == "close2":
-            j, i = op[1], op[2]
-            prod_df_f("%V2h", "%V2l", X(j))
-            two_sum_acc("%V1h", "%V1l", "%p", "%q")
-            prod_df_f("%V2h", "%V2l", X(i))
-            two_sum_acc("%%gh%d" % j, "%%gl%d" % j, "%p", "%q")
-        elif kind == "close1":
-            i = op[1]
-            prod_df_f("%V1h", "%V1l", X(i))
-            two_sum_acc("%Eh", "%El", "%p", "%q")
-            two_sum_acc("%%gh%d" % i, "%%gl%d" % i, "%V1h", "%V1l")
-    head = """// Generated by mbpol_openmm_plugin_gb300/codegen/gen_poly.py from data/{name}_basis.txt
-// and data/{name}_coeffs.txt.  Do not edit.  {nmono} monomials; depth-first
-// trie walk computing value and gradient in double-float (FP32-pair)
-// arithmetic (scheme in gen_poly.py).
-// X, G: [{nvars}][stride] floats (variable-major); E: [stride] floats.
-.version 8.8
-.target sm_103a
-.address_size 64
-
-.visible .entry {name}_batch(
-    .param .u64 pX, .param .u64 pG, .param .u64 pE,
-    .param .u32 pN, .param .u32 pStride)
-.maxntid 128, 1, 1
-{{
-    .reg .f32 %x<{nvars}>;
-    .reg .f32 %gh<{nvars}>;
-    .reg .f32 %gl<{nvars}>;
-    .reg .f32 %Eh, %El, %P2h, %P2l, %P3h, %P3l, %V1h, %V1l, %V2h, %V2l, %V3h, %V3l;
-    .reg .f32 %p, %q, %np, %ts, %tb, %t1, %t2;
-    .reg .u32 %i, %n, %stride, %step, %t0, %tn;
-    .reg .u64 %X, %G, %Eb, %off, %rowb, %a;
-    .reg .pred %pr;
-    ld.param.u64 %X, [pX];
-    ld.param.u64 %G, [pG];
-    ld.param.u64 %Eb, [pE];
-    ld.param.u32 %n, [pN];
-    ld.param.u32 %stride, [pStride];
-    cvta.to.global.u64 %X, %X;
-    cvta.to.global.u64 %G, %G;
-    cvta.to.global.u64 %Eb, %Eb;
-    mov.u32 %t0, %ctaid.x;
-    mov.u32 %tn, %ntid.x;
-    mov.u32 %i, %tid.x;
-    mad.lo.u32 %i, %t0, %tn, %i;
-    mov.u32 %t0, %nctaid.x;
-    mul.lo.u32 %step, %t0, %tn;
-    mul.wide.u32 %rowb, %stride, 4;
-LOOP:
-    setp.ge.u32 %pr, %i, %n;
-    @%pr bra DONE;
-    mul.wide.u32 %off, %i, 4;
-""".format(name=name, nmono=nmono, nvars=nvars)
-    loads = []
-    for v in range(nvars):
-        loads.append("    add.u64 %a, %X, %off;" if v == 0 else "    add.u64 %a, %a, %rowb;")
-        loads.append("    ld.global.nc.f32 %%x%d, [%%a];" % v)
-    stores = []
-    for v in range(nvars):
-        stores.append("    add.u64 %a, %G, %off;" if v == 0 else "    add.u64 %a, %a, %rowb;")
-        stores.append("    add.rn.f32 %%gh%d, %%gh%d, %%gl%d;" % (v, v, v))
-        stores.append("    st.global.f32 [%%a], %%gh%d;" % v)
-    stores.append("    add.rn.f32 %Eh, %Eh, %El;")
-    stores.append("    add.u64 %a, %Eb, %off;")
-    stores.append("    st.global.f32 [%a], %Eh;")
-    tail = """    add.u32 %i, %i, %step;
-    bra.uni LOOP;
-DONE:
-    ret;
-}
-"""
-    with open(out_path, "w") as f:
-        f.write(head + "\n".join(loads) + "\n" + "\n".join(body) + "\n" + "\n".join(stores) + "\n" + tail)
-
-
-def emulate_df(ops, X):
-    """Numpy emulation (FP32 values, FMA as one rounding of an exact FP64
-    product-sum) of the emitted walk; X: (nvars, n).  Returns E, G (float64)."""
-    import numpy as np
-    f = np.float32
-
-    def fma(a, b, c):
-        return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(f)
-
-    n = X.shape[1]
-    x = X.astype(f)
-    z = lambda: np.zeros(n, f)
-    gh = [z() for _ in range(X.shape[0])]
-    gl = [z() for _ in range(X.shape[0])]
-    st = {k: z() for k in ("Eh", "El", "P2h", "P2l", "P3h", "P3l", "V1h", "V1l", "V2h", "V2l", "V3h", "V3l")}
-
-    def acc(hk, lk, p, q, store=None):
-        sh = st[hk] if store is None else store[0][store[1]]
-        ts = (sh + p).astype(f)
-        tb = (ts - sh).astype(f)
-        t1 = (sh - (ts - tb).astype(f)).astype(f)
-        t2 = (p - tb).astype(f)
-        e = (t1 + t2).astype(f)
-        if store is None:
-            st[hk] = ts
-            st[lk] = ((st[lk] + e).astype(f) + q).astype(f)
-        else:
-            store[0][store[1]] = ts
-            store[2][store[1]] = ((store[2][store[1]] + e).astype(f) + q).astype(f)
-
-    def pdf(ah, al, xv):
-        p = (ah * xv).astype(f)
-        q = fma(ah, xv, -p)
-        return p, fma(al, xv, q)
-
-    for op in ops:
-        kind = op[0]
-        if kind == "set":
-            hi, lo = split_df(op[2])
-            st["V%dh" % op[1]] = np.full(n, hi, f)
-            st["V%dl" % op[1]] = np.full(n, lo, f)
-        elif kind == "p2":
-            p = (x[op[1]] * x[op[2]]).astype(f)
-            st["P2h"], st["P2l"] = p, fma(x[op[1]], x[op[2]], -p)
-        elif kind == "p3":
-            st["P3h"], st["P3l"] = pdf(st["P2h"], st["P2l"], x[op[1]])
-        elif kind == "leaf":
-            l = op[1]
-            hi, lo = (np.full(n, v, f) for v in split_df(op[2]))
-            p = (x[l] * hi).astype(f)
-            q = fma(x[l], lo, fma(x[l], hi, -p))
-            acc("V3h", "V3l", p, q)
-            p = (st["P3h"] * hi).astype(f)
-            q = fma(st["P3h"], lo, fma(st["P3l"], hi, fma(st["P3h"], hi, -p)))
-            acc(None, None, p, q, store=(gh, l, gl))
-        elif kind == "close3":
-            k = op[1]
-            p, q = pdf(st["V3h"], st["V3l"], x[k])
-            acc("V2h", "V2l", p, q)
-            p = (st["V3h"] * st["P2h"]).astype(f)
-            q = fma(st["V3l"], st["P2h"], fma(st["V3h"], st["P2l"], fma(st["V3h"], st["P2h"], -p)))
-            acc(None, None, p, q, store=(gh, k, gl))
-        elif kind == "close2":
-            j, i = op[1], op[2]
-            p, q = pdf(st["V2h"], st["V2l"], x[j])
-            acc("V1h", "V1l", p, q)
-            p, q = pdf(st["V2h"], st["V2l"], x[i])
-            acc(None, None, p, q, store=(gh, j, gl))
-        elif kind == "close1":
-            i = op[1]
-            p, q = pdf(st["V1h"], st["V1l"], x[i])
-            acc("Eh", "El", p, q)
-            acc(None, None, st["V1h"], st["V1l"], store=(gh, i, gl))
-    E = (st["Eh"] + st["El"]).astype(f).astype(np.float64)
-    G = np.stack([(gh[v] + gl[v]).astype(f).astype(np.float64) for v in range(X.shape[0])])
-    return E, G
 
 
 def emit_tables(name, nvars, root, perm, out_path, nmono):

@@ -869,7 +869,7 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
 // field is stored once (mode 1) and later iterations evaluate only the field
 // of mu - anchor (mode 2), whose rounding noise is smaller by |mu - anchor|/|mu|.
 template <bool PME>
-__global__ void induced_update_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ damp,
+__global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ damp,
                                       const float* __restrict__ pol, const int* __restrict__ type,
                                       const int* __restrict__ nb, const float* __restrict__ nbd,
                                       const int* __restrict__ nnb, int cap, const float* __restrict__ E0,
@@ -878,7 +878,8 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
                                       double* __restrict__ eps2, int mode, float* __restrict__ Ebase,
                                       const float* __restrict__ anchor, const float* __restrict__ intra,
                                       const float* __restrict__ pcoef, const int* __restrict__ mcl,
-                                      const int* __restrict__ cdone, double* __restrict__ eps2c) {
+                                      const int* __restrict__ cdone, double* __restrict__ eps2c,
+                                      const int* __restrict__ polmask) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     double d2sum = 0.0;
@@ -907,14 +908,18 @@ __global__ void induced_update_kernel(int nmol, const float* __restrict__ off, c
         #pragma unroll
         for (int a = 0; a < kMaxK; ++a) E[a][0] = E[a][1] = E[a][2] = 0.f;
         const int n = min(nnb[A], cap);
+        // the next slot's neighbour index is read one iteration ahead, so the
+        // gathers that depend on it do not wait for its load
+        int Bn = lane < n ? nb[(size_t)A * cap + lane] : 0;
         for (int t = lane; t < n; t += 32) {
-            const int B = nb[(size_t)A * cap + t];
+            const int B = Bn;
+            if (t + 32 < n) Bn = nb[(size_t)A * cap + t + 32];
+            const int pmB = polmask[B];
             const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
             #pragma unroll
             for (int b = 0; b < kMaxK; ++b) {
-                if (b >= K) continue;
+                if (b >= K || !((pmB >> b) & 1)) continue;
                 const int jb = K * B + b;
-                if (pol[jb] == 0.f) continue;
                 const f3 mub = ld3(mu_in, jb);
                 const f3 offb = ld3(off, jb);
                 #pragma unroll
@@ -1414,7 +1419,7 @@ struct ElecImpl {
     std::vector<int> type;
     DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu2, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd,
         d_gfrac, d_reach, d_ebase, d_intra, d_pcoef;
-    DBuf<int> d_type, d_nb, d_nnb, d_gidx, d_flags;
+    DBuf<int> d_type, d_nb, d_nnb, d_gidx, d_flags, d_polmask;  // polmask: polarisable sites of a molecule, bit s
     DBuf<float4> d_opos;
     DBuf<double> d_eps2, d_mud, d_mud_prev;
     int cap = 0;
@@ -1516,6 +1521,14 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     MBPOL_CUDA_OK(cudaMemcpy(I.d_damp.p, I.damp.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     MBPOL_CUDA_OK(cudaMemcpy(I.d_pol.p, I.pol.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     MBPOL_CUDA_OK(cudaMemcpy(I.d_type.p, I.type.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    {
+        std::vector<int> mask(I.nmol, 0);
+        for (int m = 0; m < I.nmol; ++m)
+            for (int s = 0; s < I.K; ++s)
+                if (I.pol[I.K * m + s] != 0.f) mask[m] |= 1 << s;
+        MBPOL_CUDA_OK(I.d_polmask.ensure(I.nmol));
+        MBPOL_CUDA_OK(cudaMemcpy(I.d_polmask.p, mask.data(), sizeof(int) * I.nmol, cudaMemcpyHostToDevice));
+    }
     for (auto* b : {&I.d_off, &I.d_E0, &I.d_mu0, &I.d_mu1, &I.d_mu2, &I.d_mu_prev, &I.d_gfrac, &I.d_ebase})
         MBPOL_CUDA_OK(b->ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_q.ensure(n));
@@ -1787,7 +1800,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(
                 nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                 nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p, 0, I.d_ebase.p, nullptr, I.d_intra.p, I.d_pcoef.p,
-                I.d_mcl.p, I.d_cdone.p, I.d_eps2c.p);
+                I.d_mcl.p, I.d_cdone.p, I.d_eps2c.p, I.d_polmask.p);
             prof_end(st, K_ELEC_INDUCED);
             mu_in = mu_out;
             MBPOL_CUDA_OK(cudaMemcpyAsync(e2.data(), I.d_eps2c.p, sizeof(double) * ncl, cudaMemcpyDeviceToHost, st));
@@ -1857,13 +1870,15 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                                                                   I.d_phi_mu.p, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
                                                                   kmode, I.d_ebase.p, anchor, I.d_intra.p,
-                                                                  I.d_pcoef.p, nullptr, nullptr, nullptr);
+                                                                  I.d_pcoef.p, nullptr, nullptr, nullptr,
+                                                                  I.d_polmask.p);
         else
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                    I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                                                                    nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
                                                                    kmode, I.d_ebase.p, anchor, I.d_intra.p,
-                                                                  I.d_pcoef.p, nullptr, nullptr, nullptr);
+                                                                  I.d_pcoef.p, nullptr, nullptr, nullptr,
+                                                                  I.d_polmask.p);
         prof_end(st, K_ELEC_INDUCED);
         if (kmode == 1) anchor = mu_in;
         mode = kmode == 0 ? 0 : 2;
