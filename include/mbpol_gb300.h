@@ -77,7 +77,7 @@ typedef struct {
     int guess;                   /* initial dipole guess: 0 direct (alpha*E_fixed, as the reference),
                                     1 previous call's dipoles, 2 learned (network prediction plus the
                                     extrapolated residual of the last solves; 3 without a network),
-                                    3 polynomial extrapolation of the last (up to) three solves */
+                                    3 polynomial extrapolation of the last (up to) four solves */
 } mbpol_electrostatics_params;
 
 /* Fill p with the reference's defaults. */

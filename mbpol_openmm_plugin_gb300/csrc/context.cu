@@ -145,6 +145,10 @@ struct mbpol_context {
     unsigned long long md_step = 0;
     long solver_iterations_total = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // electrostatics run on their own stream, concurrently with the
+    // polynomial terms (independent work; both latency-bound)
+    cudaStream_t st_e = nullptr;
+    cudaEvent_t ev_pos = nullptr, ev_elec = nullptr;
 };
 
 namespace {
@@ -544,6 +548,9 @@ mbpol_status mbpol_context_create(int num_particles, int device, mbpol_context**
     ctx->N = num_particles;
     ctx->device = device;
     MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+    MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st_e, cudaStreamNonBlocking));
+    MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_pos, cudaEventDisableTiming));
+    MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_elec, cudaEventDisableTiming));
     MBPOL_CUDA_OK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
     MBPOL_CUDA_OK(ctx->d_pos.ensure(sizeof(double) * 3 * (size_t)num_particles));
     MBPOL_CUDA_OK(ctx->d_force.ensure(sizeof(double) * 3 * (size_t)num_particles));
@@ -561,9 +568,13 @@ mbpol_status mbpol_context_destroy(mbpol_context* ctx) {
     if (!ctx) return MBPOL_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->st);
+    if (ctx->st_e) cudaStreamSynchronize(ctx->st_e);
     ctx->elec.reset();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev_pos) cudaEventDestroy(ctx->ev_pos);
+    if (ctx->ev_elec) cudaEventDestroy(ctx->ev_elec);
+    if (ctx->st_e) cudaStreamDestroy(ctx->st_e);
     cudaStreamDestroy(ctx->st);
     delete ctx;
     return MBPOL_OK;
@@ -674,6 +685,9 @@ mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
         MBPOL_CUDA_OK(cudaMemsetAsync(ctx->d_cl_energy.p, 0, sizeof(double) * MBPOL_NUM_TERMS * (size_t)ctx->ncl,
                                       ctx->st));
     }
+    // positions (with M sites) and zeroed outputs are ready here: the
+    // electrostatics stream starts from this point, not after the terms below
+    MBPOL_CUDA_OK(cudaEventRecord(ctx->ev_pos, ctx->st));
     if ((mask & MBPOL_TERM_BIT(MBPOL_TERM_ONEBODY)) && ctx->t1.on) {
         const bool periodic = ctx->t1.method == MBPOL_ONEBODY_PERIODIC && ctx->box.periodic;
         launch_onebody(ctx->st, (int)ctx->t1.waters.size(), ctx->t1.d_waters.as<int4>(), ctx->d_pos.as<double>(),
@@ -689,14 +703,22 @@ mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
         s = run_dispersion(ctx, e + MBPOL_TERM_DISPERSION);
     ctx->shared_lists = false;
     if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS)) && ctx->elec) {
-        s = ctx->elec->compute(ctx->st, ctx->d_pos.as<double>(), ctx->box, ctx->d_force.as<double>(),
+        // the polynomial and dispersion kernels are queued on st; the
+        // electrostatics (whose solver loop waits on the host every
+        // iteration) run on st_e meanwhile, joined before the M-site
+        // projection.  Both accumulate forces with atomics.
+        MBPOL_CUDA_OK(cudaStreamWaitEvent(ctx->st_e, ctx->ev_pos, 0));
+        s = ctx->elec->compute(ctx->st_e, ctx->d_pos.as<double>(), ctx->box, ctx->d_force.as<double>(),
                                e + MBPOL_TERM_ELECTROSTATICS);
+        MBPOL_CUDA_OK(cudaEventRecord(ctx->ev_elec, ctx->st_e));
+        MBPOL_CUDA_OK(cudaStreamWaitEvent(ctx->st, ctx->ev_elec, 0));
         ctx->counts[2] = ctx->elec->num_site_pairs();
         ctx->counts[3] = ctx->elec->iterations();
         ctx->solver_iterations_total += ctx->elec->iterations();
     }
     if (s) {
         cudaStreamSynchronize(ctx->st);
+        cudaStreamSynchronize(ctx->st_e);
         return s;
     }
     launch_spread_vsites(ctx->st, nvs, ctx->d_vs_idx.as<int4>(), ctx->d_vs_w.as<double>(), ctx->d_force.as<double>());

@@ -116,15 +116,16 @@ struct Thole {
     bool damped;
 };
 
-__device__ __forceinline__ Thole thole(float r, float dampprod, float gamma) {
+// d6prod = (damp_i damp_j)^(1/6) as the product of the sites' sixth roots
+// (stored per site), so no powf per pair.
+__device__ __forceinline__ Thole thole(float r, float d6prod, float gamma) {
     Thole t;
-    t.damped = dampprod != 0.f;
+    t.damped = d6prod != 0.f;
     if (!t.damped) {
         t.e = 0.f; t.u4g = 0.f; t.u = 0.f;
         return t;
     }
-    const float damp = powf(dampprod, 1.f / 6.f);
-    t.u = r / damp;
+    t.u = r / d6prod;
     const float u2 = t.u * t.u;
     t.u4g = gamma * u2 * u2;
     t.e = expf(-t.u4g);
@@ -878,15 +879,20 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
                                       double* __restrict__ eps2, int mode, float* __restrict__ Ebase,
                                       const float* __restrict__ anchor, const float* __restrict__ intra,
                                       const float* __restrict__ pcoef, const int* __restrict__ mcl,
-                                      const int* __restrict__ cdone, double* __restrict__ eps2c,
-                                      const int* __restrict__ polmask) {
+                                      const int* __restrict__ cstate, double* __restrict__ eps2c,
+                                      const int* __restrict__ polmask, float* __restrict__ anchor_store,
+                                      float* __restrict__ Edir) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     double d2sum = 0.0;
-    // batched clusters (mcl set): each cluster converges on its own; a
-    // finished cluster keeps its dipoles (copied through, no field work)
+    // batched clusters (mcl set): each cluster converges on its own, with
+    // its own stage of the anchoring (cstate 0 plain, 1 anchoring, 2
+    // anchored); a finished cluster (cstate 3) keeps its dipoles (copied
+    // through, no field work).  At its anchoring iteration a cluster's
+    // dipoles are copied to anchor_store, which mode 2 then reads.
     const int cA = (mcl && A < nmol) ? mcl[A] : -1;
-    const bool frozen = cA >= 0 && cdone[cA] != 0;
+    const bool frozen = cA >= 0 && cstate[cA] >= 3;
+    if (cA >= 0 && !frozen) mode = cstate[cA];
     if (A < nmol && frozen && lane == 0) {
         for (int i = c_el.K * A; i < c_el.K * (A + 1); ++i)
             for (int k = 0; k < 3; ++k) mu_out[3 * i + k] = (float)mu_d[3 * i + k];
@@ -961,9 +967,19 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
                     E[a][1] += d.y * dur + mub.y * pf1;
                     E[a][2] += d.z * dur + mub.z * pf1;
                 }
+            // split form: the direct and intramolecular field only; the
+            // reciprocal part and the update follow in induced_finish_kernel
             #pragma unroll
             for (int a = 0; a < kMaxK; ++a) {
-                if (a >= K) continue;
+                if (!Edir || a >= K) continue;
+                const int i = K * A + a;
+                Edir[3 * i] = E[a][0];
+                Edir[3 * i + 1] = E[a][1];
+                Edir[3 * i + 2] = E[a][2];
+            }
+            #pragma unroll
+            for (int a = 0; a < kMaxK; ++a) {
+                if (Edir || a >= K) continue;
                 const int i = K * A + a;
                 const f3 mu = ld3(mu_in, i);
                 const double m0 = mu_d[3 * i], m1 = mu_d[3 * i + 1], m2 = mu_d[3 * i + 2];
@@ -979,6 +995,11 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
                     Ebase[3 * i] = ex;
                     Ebase[3 * i + 1] = ey;
                     Ebase[3 * i + 2] = ez;
+                    if (anchor_store) {
+                        anchor_store[3 * i] = mu_in[3 * i];
+                        anchor_store[3 * i + 1] = mu_in[3 * i + 1];
+                        anchor_store[3 * i + 2] = mu_in[3 * i + 2];
+                    }
                 } else if (mode == 2) {
                     ex += Ebase[3 * i];
                     ey += Ebase[3 * i + 1];
@@ -1017,6 +1038,112 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
     block_sum_atomic<128>(d2sum, eps2);
 }
 
+// Second half of a split solver iteration (PME, one system): per site, the
+// direct + intramolecular field from induced_update_kernel (Edir) plus the
+// self and reciprocal parts, the anchoring stages and the SOR update on the
+// FP64 dipoles, as the fused kernel does.  Splitting lets the PME pass of
+// the same dipoles run on another stream while the direct field is summed.
+__global__ void induced_finish_kernel(int n, const float* __restrict__ Edir, const float* __restrict__ phi_mu,
+                                      const float* __restrict__ E0, const float* __restrict__ pol,
+                                      const float* __restrict__ mu_in, float* __restrict__ mu_out,
+                                      double* __restrict__ mu_d, double* __restrict__ eps2, int mode,
+                                      float* __restrict__ Ebase, const float* __restrict__ anchor) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double d2 = 0.0;
+    if (i < n) {
+        const f3 mu = ld3(mu_in, i);
+        float ex = Edir[3 * i] + c_el.self_term * mu.x - c_el.scale[0] * phi_mu[4 * i + 1];
+        float ey = Edir[3 * i + 1] + c_el.self_term * mu.y - c_el.scale[1] * phi_mu[4 * i + 2];
+        float ez = Edir[3 * i + 2] + c_el.self_term * mu.z - c_el.scale[2] * phi_mu[4 * i + 3];
+        if (mode == 1) {
+            Ebase[3 * i] = ex;
+            Ebase[3 * i + 1] = ey;
+            Ebase[3 * i + 2] = ez;
+        } else if (mode == 2) {
+            ex += Ebase[3 * i];
+            ey += Ebase[3 * i + 1];
+            ez += Ebase[3 * i + 2];
+        }
+        const double m0 = mu_d[3 * i], m1 = mu_d[3 * i + 1], m2 = mu_d[3 * i + 2];
+        const float al = pol[i];
+        const double nx = (double)al * ((double)E0[3 * i] + ex);
+        const double ny = (double)al * ((double)E0[3 * i + 1] + ey);
+        const double nz = (double)al * ((double)E0[3 * i + 2] + ez);
+        const double dx = nx - m0, dy = ny - m1, dz = nz - m2;
+        const double u0 = m0 + kSOR * dx, u1 = m1 + kSOR * dy, u2 = m2 + kSOR * dz;
+        mu_d[3 * i] = u0;
+        mu_d[3 * i + 1] = u1;
+        mu_d[3 * i + 2] = u2;
+        if (mode == 0) {
+            mu_out[3 * i] = (float)u0;
+            mu_out[3 * i + 1] = (float)u1;
+            mu_out[3 * i + 2] = (float)u2;
+        } else {
+            const float* an = mode == 1 ? mu_in : anchor;
+            mu_out[3 * i] = (float)(u0 - (double)an[3 * i]);
+            mu_out[3 * i + 1] = (float)(u1 - (double)an[3 * i + 1]);
+            mu_out[3 * i + 2] = (float)(u2 - (double)an[3 * i + 2]);
+        }
+        d2 = dx * dx + dy * dy + dz * dz;
+    }
+    block_sum_atomic<128>(d2, eps2);
+}
+
+// Double-float (FP32 pair) helpers for the pair energies: FP64 arithmetic
+// runs at a small fraction of the FP32 rate on this part.
+struct DFe {
+    float h, l;
+};
+__device__ __forceinline__ void dfe_acc(DFe& a, float p, float q) {  // a += p + q (TwoSum on the leading part)
+    const float s = __fadd_rn(a.h, p);
+    const float bb = __fsub_rn(s, a.h);
+    const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    a.h = s;
+    a.l = __fadd_rn(a.l, __fadd_rn(e, q));
+}
+__device__ __forceinline__ DFe dfe_prod(float a, float b) {  // exact product
+    DFe r;
+    r.h = __fmul_rn(a, b);
+    r.l = __fmaf_rn(a, b, -r.h);
+    return r;
+}
+__device__ __forceinline__ DFe dfe_mul(const DFe& a, const DFe& b) {
+    DFe r;
+    r.h = __fmul_rn(a.h, b.h);
+    r.l = __fmaf_rn(a.h, b.h, -r.h);
+    r.l = __fmaf_rn(a.h, b.l, r.l);
+    r.l = __fmaf_rn(a.l, b.h, r.l);
+    return r;
+}
+__device__ __forceinline__ DFe dfe_mulf(const DFe& a, float b) {
+    DFe r;
+    r.h = __fmul_rn(a.h, b);
+    r.l = __fmaf_rn(a.h, b, -r.h);
+    r.l = __fmaf_rn(a.l, b, r.l);
+    return r;
+}
+__device__ __forceinline__ DFe dfe_dot(const f3& a, const f3& b) {  // a . b of FP32 vectors
+    DFe r = dfe_prod(a.x, b.x);
+    const DFe y = dfe_prod(a.y, b.y), z = dfe_prod(a.z, b.z);
+    dfe_acc(r, y.h, y.l);
+    dfe_acc(r, z.h, z.l);
+    return r;
+}
+// 1/|d| of an FP32 vector to ~1e-14: |d|^2 exactly as a double-float, then
+// one Newton step y (1 + (1 - r2 y^2)/2) on rsqrtf with the residual formed
+// in double-float.
+__device__ __forceinline__ DFe dfe_rinv(const f3& d) {
+    const DFe r2 = dfe_dot(d, d);
+    const float y = rsqrtf(r2.h);
+    DFe t = dfe_mulf(dfe_prod(y, y), r2.h);  // r2.h y^2
+    t.l = __fmaf_rn(y * y, r2.l, t.l);       // + r2.l y^2
+    const float h = __fadd_rn(__fsub_rn(1.f, t.h), -t.l);
+    DFe r;
+    r.h = y;
+    r.l = 0.5f * y * h;
+    return r;
+}
+
 // Energy and forces for molecule A (one warp): direct pairs over the full
 // list (force on A's sites, half the pair energy), intramolecular pairs, the
 // reciprocal and self parts, and the charge-derivative forces through the
@@ -1052,9 +1179,9 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
         float F[kMaxK][3], P[kMaxK];  // force on A's sites (before * f), potential (for dq terms)
         #pragma unroll
         for (int a = 0; a < kMaxK; ++a) F[a][0] = F[a][1] = F[a][2] = P[a] = 0.f;
-        // the energy is summed in FP64 from FP32 inputs (pair terms of tens of
-        // kJ/mol cancel to the total)
-        double e = 0.0;
+        // the pair energies (tens of kJ/mol each, cancelling to the total)
+        // are summed per lane in double-float, then in FP64 across the warp
+        DFe el = {0.f, 0.f};
         const int n = min(nnb[A], cap);
         const float gcc = c_el.thole[0], gcd = c_el.thole[1], gdd = c_el.thole[2];
         for (int t = lane; t < n; t += 32) {
@@ -1085,15 +1212,11 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                         const float s1CC = gl0 != 0.f || qb != 0.f ? s1_of(tCC, gcc) : 1.f;
                         const float s3CD = s3_of(tCD);
                         {
-                            const double rd = sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z);
-                            const double r1d = 1.0 / rd, r3d = r1d / (rd * rd);
-                            const double gl0d = (double)qA[a] * qb;
-                            const double glid = (double)qb * ((double)muA[a].x * d.x + (double)muA[a].y * d.y +
-                                                              (double)muA[a].z * d.z) -
-                                                (double)qA[a] * ((double)mub.x * d.x + (double)mub.y * d.y +
-                                                                 (double)mub.z * d.z);
-                            e += 0.5 * ((double)bn.b0 * gl0d + 0.5 * (double)bn.b1 * glid -
-                                        r1d * gl0d * (1.0 - (double)s1CC) - 0.5 * r3d * glid * (1.0 - (double)s3CD));
+                            // bn0 and bn1 are FP32 (~1e-7), which bounds each term; the
+                            // terms are formed in FP32 and summed in double-float
+                            const float pe = 0.5f * (bn.b0 * gl0 + 0.5f * bn.b1 * gli -
+                                                     rr1 * gl0 * (1.f - s1CC) - 0.5f * rr3 * gli * (1.f - s3CD));
+                            dfe_acc(el, pe, 0.f);
                         }
                         P[a] += qb * (bn.b0 - rr1 * (1.f - s1CC)) - sci4 * (bn.b1 - rr3 * (1.f - s3CD));
                         const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
@@ -1110,14 +1233,18 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                     } else {
                         const float s1CC = s1_of(tCC, gcc), s3CD = s3_of(tCD);
                         {
-                            const double rd = sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z);
-                            const double r1d = 1.0 / rd, r3d = r1d / (rd * rd);
-                            const double gl0d = (double)qA[a] * qb;
-                            const double glid = (double)qb * ((double)muA[a].x * d.x + (double)muA[a].y * d.y +
-                                                              (double)muA[a].z * d.z) -
-                                                (double)qA[a] * ((double)mub.x * d.x + (double)mub.y * d.y +
-                                                                 (double)mub.z * d.z);
-                            e += 0.5 * (r1d * gl0d * (double)s1CC + 0.5 * r3d * glid * (double)s3CD);
+                            // no cutoff: the charge-charge and charge-dipole terms of a
+                            // pair of neutral waters cancel to ~1e-3 of their size, so
+                            // 1/r, the products and the dot products are double-float
+                            const DFe r1 = dfe_rinv(d);
+                            const DFe r3 = dfe_mul(dfe_mul(r1, r1), r1);
+                            const DFe cc = dfe_mulf(dfe_mul(dfe_prod(qA[a], qb), r1), 0.5f * s1CC);
+                            DFe glid = dfe_mulf(dfe_dot(muA[a], d), qb);
+                            const DFe t2 = dfe_mulf(dfe_dot(mub, d), -qA[a]);
+                            dfe_acc(glid, t2.h, t2.l);
+                            const DFe cd = dfe_mulf(dfe_mul(glid, r3), 0.25f * s3CD);
+                            dfe_acc(el, cc.h, cc.l);
+                            dfe_acc(el, cd.h, cd.l);
                         }
                         const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
                         const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
@@ -1140,6 +1267,7 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                 }
             }
         }
+        double e = (double)el.h + (double)el.l;
         #pragma unroll
         for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
         #pragma unroll
@@ -1253,21 +1381,22 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
     block_sum_atomic<128>(e_out, energy);
 }
 
-// Starting dipoles from the history of solves (guess 2 and 3): with r_k the
-// residual mu - m of the k-th previous converged solve (m the network's
-// prediction, or 0 without a network), mu0 = m + P(r), P the polynomial
-// extrapolation through the available levels: r1; 2 r1 - r2; 3 r1 - 3 r2 + r3.
+// Starting dipoles from the history of solves (guess 2 and 3): the
+// polynomial extrapolation through the last (up to) kHist converged solves
+// r1 (newest) .. r4: r1; 2 r1 - r2; 3 r1 - 3 r2 + r3; 4 r1 - 6 r2 + 4 r3 - r4.
 // FP64 state and its FP32 copy.
-__global__ void extrapolated_guess_kernel(int n, const float* __restrict__ m, int levels,
-                                          const double* __restrict__ r1, const double* __restrict__ r2,
-                                          const double* __restrict__ r3, double* __restrict__ mu_d,
+constexpr int kHist = 4;
+__global__ void extrapolated_guess_kernel(int n, int levels, const double* __restrict__ r1,
+                                          const double* __restrict__ r2, const double* __restrict__ r3,
+                                          const double* __restrict__ r4, double* __restrict__ mu_d,
                                           float* __restrict__ mu_f) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double v = m ? (double)m[i] : 0.0;
-    if (levels == 1) v += r1[i];
-    else if (levels == 2) v += 2.0 * r1[i] - r2[i];
-    else if (levels >= 3) v += 3.0 * r1[i] - 3.0 * r2[i] + r3[i];
+    double v;
+    if (levels == 1) v = r1[i];
+    else if (levels == 2) v = 2.0 * r1[i] - r2[i];
+    else if (levels == 3) v = 3.0 * r1[i] - 3.0 * r2[i] + r3[i];
+    else v = 4.0 * r1[i] - 6.0 * r2[i] + 4.0 * r3[i] - r4[i];
     mu_d[i] = v;
     mu_f[i] = (float)v;
 }
@@ -1284,13 +1413,6 @@ __global__ void learned_guess_kernel(int n, const float* __restrict__ m, const f
     mu_f[i] = (float)v;
 }
 
-// residual mu - m of a converged solve, for the history
-__global__ void residual_kernel(int n, const double* __restrict__ mu, const float* __restrict__ m,
-                                double* __restrict__ r) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    r[i] = mu[i] - (m ? (double)m[i] : 0.0);
-}
 
 __global__ void narrow_kernel(int n, const double* __restrict__ a, float* __restrict__ b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1418,7 +1540,7 @@ struct ElecImpl {
     std::vector<float> q_static, damp, pol;
     std::vector<int> type;
     DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu2, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd,
-        d_gfrac, d_reach, d_ebase, d_intra, d_pcoef;
+        d_gfrac, d_reach, d_ebase, d_intra, d_pcoef, d_edir;
     DBuf<int> d_type, d_nb, d_nnb, d_gidx, d_flags, d_polmask;  // polmask: polarisable sites of a molecule, bit s
     DBuf<float4> d_opos;
     DBuf<double> d_eps2, d_mud, d_mud_prev;
@@ -1444,8 +1566,8 @@ struct ElecImpl {
     DBuf<float> d_mguess;
     DBuf<float> d_mprev;  // the network's prediction at the previous solve
     bool have_mprev = false;
-    // dipoles of the last (up to) three converged solves, a ring of three
-    // 3n planes (FP64)
+    // dipoles of the last (up to) kHist converged solves, a ring of 3n
+    // planes (FP64)
     DBuf<double> d_hist;
     int hist_levels = 0, hist_head = 0;
     bool evaluated = false;  // neighbour list, offsets and dipoles are current
@@ -1454,17 +1576,23 @@ struct ElecImpl {
     int ncl = 0, max_cl_mol = 0;
     std::vector<int> cl_nsites, cl_iters;
     std::vector<char> cl_conv;
-    DBuf<int> d_mcl, d_cdone;
+    DBuf<int> d_mcl, d_cstate;  // d_cstate: per-cluster solver stage (0 plain, 1 anchoring, 2 anchored, 3 done)
     DBuf<double> d_eps2c;
     ClusterSink cl_sink;
     Box last_box{};
     int mu_cur = 0;  // which buffer holds the current dipoles
+    // second stream for the solver's PME passes, ordered by two events
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_pme = nullptr;
 
     ~ElecImpl() {
         if (plans) {
             cufftDestroy(plan_f);
             cufftDestroy(plan_b);
         }
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_pme) cudaEventDestroy(ev_pme);
+        if (st2) cudaStreamDestroy(st2);
     }
 };
 
@@ -1509,7 +1637,9 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     I.type.resize(n);
     for (int i = 0; i < n; ++i) {
         I.q_static[i] = (float)charge[i];
-        I.damp[i] = (float)damping[i];
+        // sixth root of the damping factor: pair kernels use
+        // (damp_i damp_j)^(1/6) = damp_i^(1/6) damp_j^(1/6)
+        I.damp[i] = (float)std::pow(damping[i], 1.0 / 6.0);
         I.pol[i] = (float)polarity[i];
         I.type[i] = atom_type[i];
     }
@@ -1529,7 +1659,7 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
         MBPOL_CUDA_OK(I.d_polmask.ensure(I.nmol));
         MBPOL_CUDA_OK(cudaMemcpy(I.d_polmask.p, mask.data(), sizeof(int) * I.nmol, cudaMemcpyHostToDevice));
     }
-    for (auto* b : {&I.d_off, &I.d_E0, &I.d_mu0, &I.d_mu1, &I.d_mu2, &I.d_mu_prev, &I.d_gfrac, &I.d_ebase})
+    for (auto* b : {&I.d_off, &I.d_E0, &I.d_mu0, &I.d_mu1, &I.d_mu2, &I.d_mu_prev, &I.d_gfrac, &I.d_ebase, &I.d_edir})
         MBPOL_CUDA_OK(b->ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_q.ensure(n));
     MBPOL_CUDA_OK(I.d_dq.ensure(9 * (size_t)n));
@@ -1544,8 +1674,13 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     MBPOL_CUDA_OK(I.d_eps2.ensure(1));
     MBPOL_CUDA_OK(I.d_mud.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_mud_prev.ensure(3 * (size_t)n));
+    if (!I.st2) {
+        MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&I.st2, cudaStreamNonBlocking));
+        MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_in, cudaEventDisableTiming));
+        MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_pme, cudaEventDisableTiming));
+    }
     MBPOL_CUDA_OK(I.d_mguess.ensure(3 * (size_t)n));
-    MBPOL_CUDA_OK(I.d_hist.ensure(9 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_hist.ensure(3 * kHist * (size_t)n));
     MBPOL_CUDA_OK(I.d_mprev.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms, kDmsCoef, sizeof(kDmsCoef)));
     MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms_idx, kDmsIdx, sizeof(kDmsIdx)));
@@ -1744,11 +1879,10 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     const bool used_net = learned && !extrapolate;
     if (extrapolate) {
         const size_t plane = 3 * (size_t)n;
-        const double* r1 = I.d_hist.p + plane * I.hist_head;
-        const double* r2 = I.d_hist.p + plane * ((I.hist_head + 2) % 3);
-        const double* r3 = I.d_hist.p + plane * ((I.hist_head + 1) % 3);
+        const double* r[kHist];
+        for (int k = 0; k < kHist; ++k) r[k] = I.d_hist.p + plane * ((I.hist_head + kHist - k) % kHist);
         count_launch();
-        extrapolated_guess_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, nullptr, I.hist_levels, r1, r2, r3,
+        extrapolated_guess_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, I.hist_levels, r[0], r[1], r[2], r[3],
                                                                        I.d_mud.p, I.d_mu0.p);
     } else if (used_net) {
         const bool prev = I.have_prev && I.have_mprev;
@@ -1780,34 +1914,38 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         // epsilon (its own site count) and stops on its own; the others go on
         const int ncl = I.ncl;
         std::vector<double> cur(ncl, 1.0e+50), e2(ncl, 0.0);
-        std::vector<int> its(ncl, 0), cdone(ncl, 0);
+        std::vector<int> its(ncl, 0), cstate(ncl, 0);  // 0 plain, 1 anchoring, 2 anchored, 3 done
         std::vector<char> cconv(ncl, 0);
         int active = 0;
         for (int c = 0; c < ncl; ++c) {
             if (I.cl_nsites[c] > 0) {
                 ++active;
             } else {
-                cdone[c] = 1;
+                cstate[c] = 3;
                 cconv[c] = 1;
             }
         }
-        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_cdone.p, cdone.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, st));
+        float* anchor_buf = bufs[2];
         while (active > 0) {
+            // the anchoring switch per cluster, as for one system
+            for (int c = 0; c < ncl; ++c)
+                if (cstate[c] == 0 && cur[c] < switch_eps) cstate[c] = 1;
+            MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_cstate.p, cstate.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, st));
             float* mu_out = mu_in == bufs[0] ? bufs[1] : bufs[0];
             MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2c.p, 0, sizeof(double) * ncl, st));
             prof_begin(st, K_ELEC_INDUCED);
             count_launch();
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(
                 nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
-                nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p, 0, I.d_ebase.p, nullptr, I.d_intra.p, I.d_pcoef.p,
-                I.d_mcl.p, I.d_cdone.p, I.d_eps2c.p, I.d_polmask.p);
+                nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p, 0, I.d_ebase.p, anchor_buf, I.d_intra.p, I.d_pcoef.p,
+                I.d_mcl.p, I.d_cstate.p, I.d_eps2c.p, I.d_polmask.p, anchor_buf, nullptr);
             prof_end(st, K_ELEC_INDUCED);
             mu_in = mu_out;
             MBPOL_CUDA_OK(cudaMemcpyAsync(e2.data(), I.d_eps2c.p, sizeof(double) * ncl, cudaMemcpyDeviceToHost, st));
             MBPOL_CUDA_OK(cudaStreamSynchronize(st));
-            bool changed = false;
             for (int c = 0; c < ncl; ++c) {
-                if (cdone[c]) continue;
+                if (cstate[c] >= 3) continue;
+                if (cstate[c] == 1) cstate[c] = 2;
                 const double ec = kSOR * kDebye * sqrt(e2[c] / (double)I.cl_nsites[c]);
                 bool stop = false;
                 if (!std::isfinite(ec)) {
@@ -1821,16 +1959,10 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                 cur[c] = ec;
                 ++its[c];
                 if (stop) {
-                    cdone[c] = 1;
+                    cstate[c] = 3;
                     --active;
-                    changed = true;
                 }
             }
-            if (changed && active > 0)
-                MBPOL_CUDA_OK(
-                    cudaMemcpyAsync(I.d_cdone.p, cdone.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, st));
-            // the copy reads cdone before the next iteration's host update
-            MBPOL_CUDA_OK(cudaStreamSynchronize(st));
         }
         I.cl_iters = its;
         I.cl_conv = cconv;
@@ -1854,31 +1986,42 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                 break;
             }
         if (I.pme) {
-            prof_begin(st, K_ELEC_PME);
-            MBPOL_CUDA_OK(pme_spread(I, st, 1, mu_in, n, nreal));
-            mbpol_status s = pme_convolve(I, st, box);
+            // the reciprocal-space pass of mu_in runs on the second stream
+            // while the direct field of the same dipoles is summed here
+            MBPOL_CUDA_OK(cudaEventRecord(I.ev_in, st));
+            MBPOL_CUDA_OK(cudaStreamWaitEvent(I.st2, I.ev_in, 0));
+            prof_begin(I.st2, K_ELEC_PME);
+            MBPOL_CUDA_OK(pme_spread(I, I.st2, 1, mu_in, n, nreal));
+            mbpol_status s = pme_convolve(I, I.st2, box);
             if (s) return s;
             count_launch();
-            pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 4, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
-            prof_end(st, K_ELEC_PME);
+            pme_gather_kernel<<<(n + 127) / 128, 128, 0, I.st2>>>(n, 4, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p,
+                                                                   I.d_phi_mu.p);
+            prof_end(I.st2, K_ELEC_PME);
+            MBPOL_CUDA_OK(cudaEventRecord(I.ev_pme, I.st2));
         }
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2.p, 0, sizeof(double), st));
         prof_begin(st, K_ELEC_INDUCED);
         count_launch();
-        if (I.pme)
+        if (I.pme) {
             induced_update_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                                                                   I.d_phi_mu.p, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
                                                                   kmode, I.d_ebase.p, anchor, I.d_intra.p,
                                                                   I.d_pcoef.p, nullptr, nullptr, nullptr,
-                                                                  I.d_polmask.p);
-        else
+                                                                  I.d_polmask.p, nullptr, I.d_edir.p);
+            MBPOL_CUDA_OK(cudaStreamWaitEvent(st, I.ev_pme, 0));
+            count_launch();
+            induced_finish_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, I.d_edir.p, I.d_phi_mu.p, I.d_E0.p, I.d_pol.p,
+                                                                   mu_in, mu_out, I.d_mud.p, I.d_eps2.p, kmode,
+                                                                   I.d_ebase.p, anchor);
+        } else
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                    I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
                                                                    nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p,
                                                                    kmode, I.d_ebase.p, anchor, I.d_intra.p,
                                                                   I.d_pcoef.p, nullptr, nullptr, nullptr,
-                                                                  I.d_polmask.p);
+                                                                  I.d_polmask.p, nullptr, nullptr);
         prof_end(st, K_ELEC_INDUCED);
         if (kmode == 1) anchor = mu_in;
         mode = kmode == 0 ? 0 : 2;
@@ -1911,11 +2054,10 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mud_prev.p, I.d_mud.p, sizeof(double) * 3 * (size_t)n,
                                       cudaMemcpyDeviceToDevice, st));
         if (history) {
-            I.hist_head = (I.hist_head + 1) % 3;
-            count_launch();
-            residual_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, I.d_mud.p, nullptr,
-                                                                 I.d_hist.p + 3 * (size_t)n * I.hist_head);
-            I.hist_levels = std::min(I.hist_levels + 1, 3);
+            I.hist_head = (I.hist_head + 1) % kHist;
+            MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_hist.p + 3 * (size_t)n * I.hist_head, I.d_mud.p,
+                                          sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+            I.hist_levels = std::min(I.hist_levels + 1, kHist);
         }
         if (used_net)
             MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mprev.p, I.d_mguess.p, sizeof(float) * 3 * (size_t)n,
@@ -2061,7 +2203,7 @@ mbpol_status ElecEngine::set_clusters(const int* cluster_of_particle, int ncl, d
     for (int c = 0; c < ncl; ++c) I.max_cl_mol = std::max(I.max_cl_mol, count[c]);
     MBPOL_CUDA_OK(I.d_mcl.ensure(I.nmol));
     MBPOL_CUDA_OK(cudaMemcpy(I.d_mcl.p, mcl.data(), sizeof(int) * (size_t)I.nmol, cudaMemcpyHostToDevice));
-    MBPOL_CUDA_OK(I.d_cdone.ensure(ncl));
+    MBPOL_CUDA_OK(I.d_cstate.ensure(ncl));
     MBPOL_CUDA_OK(I.d_eps2c.ensure(ncl));
     I.ncl = ncl;
     I.cl_sink.wcl = I.d_mcl.p;

@@ -13,6 +13,7 @@
 //  * three-body: per trimer, 36 exp variables (FP64) -> poly_df.cu -> chain
 //    rule and the product switch in FP32.  Restates
 //    platforms/reference/src/MBPolReferenceThreeBodyForce.cpp:67-293.
+#include "dfmath.cuh"
 #include "mbpol_internal.cuh"
 #include "mbpol_kernels.h"
 
@@ -103,7 +104,8 @@ __global__ void onebody_kernel(int nw, const int4* __restrict__ waters, const do
 struct Var2 {
     unsigned char a, b, kind;
     float k, r0;
-    double kd;  // k in FP64 for the variable kernel
+    double kd;       // k in FP64
+    float kdh, kdl;  // k as a double-float, for the variable kernel
 };
 __constant__ Var2 c_v2[31];
 struct TwoBodyParams {
@@ -184,13 +186,23 @@ __global__ void twobody_vars_kernel(int npairs, const int2* __restrict__ pairs, 
         S[6 + 2 * m] = make_double3(inp.x + c.x * go, inp.y + c.y * go, inp.z + c.z * go);
         S[7 + 2 * m] = make_double3(inp.x - c.x * go, inp.y - c.y * go, inp.z - c.z * go);
     }
+    // as double-floats from here (the X sites are built in FP64 above)
+    dfm::df R[10][3];
+    #pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        R[i][0] = dfm::from_double(S[i].x);
+        R[i][1] = dfm::from_double(S[i].y);
+        R[i][2] = dfm::from_double(S[i].z);
+    }
     const int plane = 31 * stride;
     #pragma unroll 1
     for (int n = 0; n < 31; ++n) {
         const Var2 v = c_v2[n];
-        const double r = dnorm(dsub(S[v.a], S[v.b]));
-        const double e = exp((double)v.kd * ((double)v.r0 - r));
-        store_hl(X, n * stride + p, plane, v.kind ? e / r : e);
+        const dfm::df r = dfm::dist(R[v.a], R[v.b]);
+        dfm::df e = dfm::exp_df(dfm::mul(dfm::df{v.kdh, v.kdl}, dfm::sub(dfm::df{v.r0, 0.f}, r)));
+        if (v.kind) e = dfm::mul(e, dfm::recip(r));
+        X[n * stride + p] = e.h;
+        X[n * stride + p + plane] = e.l;
     }
 }
 
@@ -275,7 +287,8 @@ __global__ void twobody_forces_kernel(int npairs, const int2* __restrict__ pairs
 struct Var3 {
     unsigned char a, b;
     float k, d0;
-    double kd, dd;  // FP64 copies for the variable kernel
+    double kd, dd;                // FP64 copies
+    float kdh, kdl, ddh, ddl;     // the same as double-floats, for the variable kernel
 };
 __constant__ Var3 c_v3[36];
 __constant__ float c_3b_rf;  // switch outer radius (A)
@@ -318,12 +331,24 @@ __global__ void threebody_vars_kernel(int ntrip, const int4* __restrict__ trips,
     S[6] = image_to(S[0], load_pos(pos, wc.x), box);
     S[7] = image_to(S[6], load_pos(pos, wc.y), box);
     S[8] = image_to(S[6], load_pos(pos, wc.z), box);
+    // sites relative to the first O (Angstrom) as double-floats: the 36
+    // distances and exponentials then run on the FP32 pipe (FP64 is kept
+    // for the imaging only)
+    dfm::df R[9][3];
+    #pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        R[i][0] = dfm::from_double((S[i].x - S[0].x) * kNmToA);
+        R[i][1] = dfm::from_double((S[i].y - S[0].y) * kNmToA);
+        R[i][2] = dfm::from_double((S[i].z - S[0].z) * kNmToA);
+    }
     const int plane = 36 * stride;
     #pragma unroll 1
     for (int n = 0; n < 36; ++n) {
         const Var3 v = c_v3[n];
-        const double r = dnorm(dsub(S[v.a], S[v.b])) * kNmToA;
-        store_hl(X, n * stride + t, plane, exp(-v.kd * (r - v.dd)));
+        const dfm::df e = dfm::exp_df(
+            dfm::mul(dfm::df{-v.kdh, -v.kdl}, dfm::sub(dfm::dist(R[v.a], R[v.b]), dfm::df{v.ddh, v.ddl})));
+        X[n * stride + t] = e.h;
+        X[n * stride + t + plane] = e.l;
     }
 }
 
@@ -432,6 +457,10 @@ void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245)
         for (int q = 0; q < 8; ++q)
             if (v2[n].k == kf2[q]) v2d[n].kd = kd2[q];
     }
+    for (int n = 0; n < 31; ++n) {
+        v2d[n].kdh = (float)v2d[n].kd;
+        v2d[n].kdl = (float)(v2d[n].kd - (double)v2d[n].kdh);
+    }
     cudaMemcpyToSymbol(c_v2, v2d, sizeof(v2d));
     TwoBodyParams tp = {-9.721486914088159e-02f, 9.859272078406150e-02f, 4.5f, 6.5f};
     cudaMemcpyToSymbol(c_2b, &tp, sizeof(tp));
@@ -463,6 +492,12 @@ void upload_polyterm_constants(const double* c5z, const unsigned char* idx3x245)
                 v3d[n].kd = kd3[q];
                 v3d[n].dd = dd3[q];
             }
+    }
+    for (int n = 0; n < 36; ++n) {
+        v3d[n].kdh = (float)v3d[n].kd;
+        v3d[n].kdl = (float)(v3d[n].kd - (double)v3d[n].kdh);
+        v3d[n].ddh = (float)v3d[n].dd;
+        v3d[n].ddl = (float)(v3d[n].dd - (double)v3d[n].ddh);
     }
     cudaMemcpyToSymbol(c_v3, v3d, sizeof(v3d));
     const float rf = 4.5f;
