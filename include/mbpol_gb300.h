@@ -78,7 +78,18 @@ typedef struct {
                                     1 previous call's dipoles, 2 learned (network prediction plus the
                                     extrapolated residual of the last solves; 3 without a network),
                                     3 polynomial extrapolation of the last (up to) four solves */
+    int pme_fixed_field;         /* MBPOL_PME_FIELD_REFERENCE (default) or MBPOL_PME_FIELD_CONSISTENT;
+                                    no reference counterpart, see the enum below */
 } mbpol_electrostatics_params;
+
+/* Real-space Thole term of the PME permanent field.  The reference adds the
+ * damping correction (s3 - 1)/r^3 with the sign opposite to its energy
+ * expression (MBPolReferenceElectrostaticsForce.cpp:1377-1391 against
+ * :2609-2626), so under PME its forces are not the gradient of its energy
+ * (the induced dipoles are not stationary for that energy).  CONSISTENT
+ * takes bn1 - (1 - s3)/r^3, which makes forces and energy consistent;
+ * REFERENCE reproduces the reference's numbers.  NoCutoff is unaffected. */
+enum { MBPOL_PME_FIELD_REFERENCE = 0, MBPOL_PME_FIELD_CONSISTENT = 1 };
 
 /* Fill p with the reference's defaults. */
 void mbpol_electrostatics_params_default(mbpol_electrostatics_params* p);

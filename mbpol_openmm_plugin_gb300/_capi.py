@@ -57,6 +57,7 @@ class ElectrostaticsParams(ctypes.Structure):
         ("thole", ctypes.c_double * 5),
         ("include_charge_redistribution", ctypes.c_int),
         ("guess", ctypes.c_int),
+        ("pme_fixed_field", ctypes.c_int),
     ]
 
 

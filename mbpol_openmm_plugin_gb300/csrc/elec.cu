@@ -54,6 +54,7 @@ struct ElecConst {
     double box[3], inv[3];
     float boxf[3], invf[3];
     int periodic;         // per-site-pair minimum image (PME)
+    float fixed_thole_sign;  // +1 the reference's PME fixed-field Thole term, -1 the consistent one
 };
 __constant__ ElecConst c_el;
 
@@ -806,8 +807,10 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
                 float fac;
                 if (PME) {
                     const Bn bn = ewald_bn(r, r2);
+                    // reference :1377-1391 subtracts (s3 - 1)/r^3; the
+                    // gradient of its energy wants (1 - s3)/r^3
                     const float rr3 = (s3_of(th) - 1.f) / (r2 * r);
-                    fac = bn.b1 - rr3;
+                    fac = bn.b1 - c_el.fixed_thole_sign * rr3;
                 } else {
                     fac = s3_of(th) / (r2 * r);
                 }
@@ -826,7 +829,7 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
     }
     if (lane == 0) {
         if (PME) {
-            // intramolecular pairs: s3 = 2 (reference :1375-1377), within the cutoff
+            // intramolecular pairs: s3 = 2 (reference :1381-1384), within the cutoff
             #pragma unroll
             for (int a = 0; a < kMaxK; ++a)
                 #pragma unroll
@@ -1811,6 +1814,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         c.invf[d] = (float)c.inv[d];
     }
     c.periodic = I.pme ? 1 : 0;
+    c.fixed_thole_sign = I.prm.pme_fixed_field == MBPOL_PME_FIELD_CONSISTENT ? -1.f : 1.f;
     MBPOL_CUDA_OK(cudaMemcpyToSymbolAsync(c_el, &c, sizeof(c), 0, cudaMemcpyHostToDevice, st));
     const int redist = I.prm.include_charge_redistribution ? 1 : 0;
     count_launch();

@@ -28,7 +28,7 @@ void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, i
 // the two-body kernel on caller-supplied device tables (raise its dynamic
 // shared-memory limit once per device with poly2b_kernel_setup first)
 cudaError_t poly2b_kernel_setup();
-void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, int n1, const PolyNode* l2, const PolyNode* l3,
+void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, const PolyNode* l2, const PolyNode* l3,
                         const PolyNode* lv, const float* X, float* G, float* E, int n, int stride, int num_sms);
 
 // neighbor.cu

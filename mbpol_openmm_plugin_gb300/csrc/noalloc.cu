@@ -138,7 +138,7 @@ extern "C" mbpol_status mbpol_twobody_dimers_noalloc(const double* positions, co
     const int2* pairs = reinterpret_cast<const int2*>(dimers);
     const int4* w4 = reinterpret_cast<const int4*>(waters);
     launch_twobody_vars(st, num_dimers, pairs, w4, positions, box, d->x, kCap);
-    launch_poly2b_with(st, d->l1, POLY2B_N1, d->l2, d->l3, d->lv, d->x, d->g, d->e, num_dimers, kCap, d->num_sms);
+    launch_poly2b_with(st, d->l1, d->l2, d->l3, d->lv, d->x, d->g, d->e, num_dimers, kCap, d->num_sms);
     launch_twobody_forces(st, num_dimers, pairs, w4, positions, box, d->g, d->e, kCap, forces, energy);
     MBPOL_CUDA_OK(cudaGetLastError());
     return MBPOL_OK;

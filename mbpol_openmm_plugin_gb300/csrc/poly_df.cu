@@ -14,11 +14,14 @@
 // and TwoSum, errors collected in c; Ogita, Rump & Oishi, SIAM J. Sci.
 // Comput. 26 (2005)), which gives FP64-level results on the FP32 pipe.
 //
-// One thread per unit (dimer or trimer).  The variables x and the gradient
-// pairs (gh, gl) live in shared memory, [variable][thread], so every access
-// of a warp is one conflict-free wavefront; the trie tables are read with
-// warp-uniform addresses.  X: [2][nvars][stride] floats (FP64 variables as
+// Two threads per unit (dimer or trimer), each walking half of the trie.
+// The variables x ([variable][unit]) and the gradient pairs (gh, gl;
+// [variable][thread]) live in shared memory, so every access of a warp is one
+// conflict-free wavefront; the trie tables are read with warp-uniform
+// addresses.  X: [2][nvars][stride] floats (FP64 variables as
 // hi and lo planes); G: [nvars][stride]; E: [stride].
+#include <vector>
+
 #include "mbpol_internal.cuh"
 #include "poly_tables.h"
 
@@ -75,72 +78,120 @@ __device__ __forceinline__ void leaf_update(const PolyNode& L, float xl, float x
     acc(g, p, q);
 }
 
-// U leaves of one level-3 node: all loads first, then the updates in leaf
-// order (V3's summation order is unchanged), then the stores.
+// Shared-memory strides: the variables are shared by the two threads of a
+// unit ([variable][unit]), each thread has its own gradient pairs
+// ([variable][thread]).
+constexpr int kUnits = kBlock / 2;  // units per block
+constexpr int kXS = kUnits;         // variable plane stride
+constexpr int kGS = kBlock;         // gradient plane stride
+
+// U sibling nodes without children (leaves, or level-3 nodes without
+// leaves) under a parent with prefix product P: V += c x and g += c P for
+// each, with all loads first, then the updates in order (V's summation order
+// is unchanged), then the stores.  Siblings have distinct variables.  xs, xq
+// point at this thread's unit, gh, gl at this thread's gradient column.
 template <int U>
-__device__ __forceinline__ void leaf_batch(const PolyNode* __restrict__ lv, const float* xs, const float* xq,
-                                           float* gh, float* gl, int t, const DF& P3, DF& V3) {
-    PolyNode L[U];
-    int o[U];
+__device__ __forceinline__ void childless_batch(const PolyNode (&L)[U], const float* xs, const float* xq, float* gh,
+                                                float* gl, const DF& P, DF& V) {
     float x[U], xl[U];
     DF g[U];
     #pragma unroll
-    for (int u = 0; u < U; ++u) L[u] = lv[u];
-    #pragma unroll
     for (int u = 0; u < U; ++u) {
-        o[u] = L[u].var * kBlock + t;
-        x[u] = xs[o[u]];
-        xl[u] = xq[o[u]];
-        g[u].h = gh[o[u]];
-        g[u].l = gl[o[u]];
+        x[u] = xs[L[u].var * kXS];
+        xl[u] = xq[L[u].var * kXS];
+        g[u].h = gh[L[u].var * kGS];
+        g[u].l = gl[L[u].var * kGS];
     }
     #pragma unroll
-    for (int u = 0; u < U; ++u) leaf_update(L[u], x[u], xl[u], P3, V3, g[u]);
+    for (int u = 0; u < U; ++u) leaf_update(L[u], x[u], xl[u], P, V, g[u]);
     #pragma unroll
     for (int u = 0; u < U; ++u) {
-        gh[o[u]] = g[u].h;
-        gl[o[u]] = g[u].l;
+        gh[L[u].var * kGS] = g[u].h;
+        gl[L[u].var * kGS] = g[u].l;
     }
 }
 
+template <int U>
+__device__ __forceinline__ void leaf_batch(const PolyNode* __restrict__ lv, const float* xs, const float* xq,
+                                           float* gh, float* gl, const DF& P3, DF& V3) {
+    PolyNode L[U];
+    #pragma unroll
+    for (int u = 0; u < U; ++u) L[u] = lv[u];
+    childless_batch<U>(L, xs, xq, gh, gl, P3, V3);
+}
+
+// One half of the trie: level-1 nodes [a0, a1), level-2 nodes [c2_0, c2_1)
+// and the level-3 nodes and leaves under them, which start at c3_0 and
+// cl_0.  When the split falls inside the children of a level-1 node, both
+// halves visit that node and the second leaves out its coefficient
+// (skip_coef): E = sum_i x_i V_i and g_i += V_i are linear in V_i.
+struct WalkPart {
+    int a0, a1, c2_0, c2_1, c3_0, cl_0, skip_coef;
+};
+struct WalkSplit {
+    WalkPart part[2];
+};
+
+// Two threads per unit (dimer or trimer), each walking half of the trie:
+// the unit's variables are stored once for both, so a thread needs
+// NV * 12 bytes of shared memory instead of NV * 16, and an SM holds four
+// 128-thread blocks (16 warps) instead of three.  The two halves' energy and
+// gradient pairs are added at the end (double-float, fixed order).
 template <int NV>
-__global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restrict__ l1, int n1,
+__global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __restrict__ l1,
                                                           const PolyNode* __restrict__ l2,
                                                           const PolyNode* __restrict__ l3, int n3,
-                                                          const PolyNode* __restrict__ lv,
+                                                          const PolyNode* __restrict__ lv, const WalkSplit split,
                                                           const float* __restrict__ X, float* __restrict__ G,
                                                           float* __restrict__ E, int n, int stride) {
     extern __shared__ float smem[];
-    float* xs = smem;                  // [NV][kBlock]   variables, high part
-    float* xq = smem + NV * kBlock;    // [NV][kBlock]   variables, low part
-    float* gh = xq + NV * kBlock;      // [NV][kBlock]
-    float* gl = gh + NV * kBlock;      // [NV][kBlock]
+    float* xs_all = smem;                    // [NV][kUnits]  variables, high part
+    float* xq_all = xs_all + NV * kUnits;    // [NV][kUnits]  variables, low part
+    float* gh_all = xq_all + NV * kUnits;    // [NV][kBlock]
+    float* gl_all = gh_all + NV * kBlock;    // [NV][kBlock]
+    __shared__ float e_other[2][kUnits];     // the second half's energy pair
     const int t = threadIdx.x;
-    for (int base = blockIdx.x * kBlock; base < n; base += gridDim.x * kBlock) {
-        const int u = base + t;
+    const int half = t / kUnits;             // warp-uniform
+    const int tu = t % kUnits;
+    const WalkPart& P0 = split.part[0];
+    const WalkPart& P1 = split.part[1];
+    const WalkPart W = {half ? P1.a0 : P0.a0,     half ? P1.a1 : P0.a1,     half ? P1.c2_0 : P0.c2_0,
+                        half ? P1.c2_1 : P0.c2_1, half ? P1.c3_0 : P0.c3_0, half ? P1.cl_0 : P0.cl_0,
+                        half ? P1.skip_coef : P0.skip_coef};
+    const float* xs = xs_all + tu;
+    const float* xq = xq_all + tu;
+    float* gh = gh_all + t;
+    float* gl = gl_all + t;
+    for (int base = blockIdx.x * kUnits; base < n; base += gridDim.x * kUnits) {
+        const int u = base + tu;
         const bool live = u < n;
+        for (int v = half; v < NV; v += 2) {
+            xs_all[v * kXS + tu] = live ? X[(size_t)v * stride + u] : 0.f;
+            xq_all[v * kXS + tu] = live ? X[(size_t)(NV + v) * stride + u] : 0.f;
+        }
         #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            xs[v * kBlock + t] = live ? X[(size_t)v * stride + u] : 0.f;
-            xq[v * kBlock + t] = live ? X[(size_t)(NV + v) * stride + u] : 0.f;
-            gh[v * kBlock + t] = 0.f;
-            gl[v * kBlock + t] = 0.f;
+            gh[v * kGS] = 0.f;
+            gl[v * kGS] = 0.f;
         }
+        __syncthreads();
         DF Ev = {0.f, 0.f};
-        int c2 = 0, c3 = 0, cl = 0;
+        int c2 = W.c2_0, c3 = W.c3_0, cl = W.cl_0;
         // The next level-3 node is read one step ahead.  Children of a node
         // have distinct variables, so several leaves' gradient pairs can be
         // read before any of them is written back; a parent's own pair is
         // read only after its children's writes (a child may share its
         // variable).
-        PolyNode Cn = n3 > 0 ? l3[0] : PolyNode{0.f, 0.f, 0, 0};
-        for (int a = 0; a < n1; ++a) {
+        PolyNode Cn = c3 < n3 ? l3[c3] : PolyNode{0.f, 0.f, 0, 0};
+        for (int a = W.a0; a < W.a1; ++a) {
             const PolyNode A = l1[a];
-            const float xi = xs[A.var * kBlock + t], xil = xq[A.var * kBlock + t];
+            const float xi = xs[A.var * kXS], xil = xq[A.var * kXS];
             DF V1 = {A.hi, A.lo};
-            for (; c2 < A.end; ++c2) {
+            if (a == W.a0 && W.skip_coef) V1 = DF{0.f, 0.f};
+            const int e2 = min(A.end, W.c2_1);
+            for (; c2 < e2; ++c2) {
                 const PolyNode B = l2[c2];
-                const float xj = xs[B.var * kBlock + t], xjl = xq[B.var * kBlock + t];
+                const float xj = xs[B.var * kXS], xjl = xq[B.var * kXS];
                 DF V2 = {B.hi, B.lo};
                 DF P2;
                 P2.h = __fmul_rn(xi, xj);
@@ -149,8 +200,21 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                 P2.l = __fmaf_rn(xil, xj, P2.l);
                 for (; c3 < B.end; ++c3) {
                     const PolyNode C = Cn;
+                    if (NV == 31 && C.end == cl && c3 + 4 <= B.end) {
+                        // four level-3 nodes without leaves act as four leaves
+                        // of B (prefix product P2); taken for the two-body trie,
+                        // where 90% of the level-3 nodes have no leaves (in the
+                        // three-body trie the look-ahead loads measured slower)
+                        const PolyNode C4[4] = {C, l3[c3 + 1], l3[c3 + 2], l3[c3 + 3]};
+                        if (C4[1].end == cl && C4[2].end == cl && C4[3].end == cl) {
+                            childless_batch<4>(C4, xs, xq, gh, gl, P2, V2);
+                            c3 += 3;
+                            if (c3 + 1 < n3) Cn = l3[c3 + 1];
+                            continue;
+                        }
+                    }
                     if (c3 + 1 < n3) Cn = l3[c3 + 1];
-                    const float xk = xs[C.var * kBlock + t], xkl = xq[C.var * kBlock + t];
+                    const float xk = xs[C.var * kXS], xkl = xq[C.var * kXS];
                     DF V3 = {C.hi, C.lo};
                     const int cend = C.end;
                     if (cl < cend) {
@@ -161,14 +225,34 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                         // loaded together, so the L2 latency of the node reads
                         // overlaps (leaf variables of one node are distinct;
                         // batches of eight measured slower)
-                        for (; cl + 4 <= cend; cl += 4) leaf_batch<4>(lv + cl, xs, xq, gh, gl, t, P3, V3);
+                        if (NV == 31 && cl + 4 <= cend) {
+                            // two-body trie: the next batch's nodes are read
+                            // while this batch computes (in the three-body
+                            // trie this look-ahead measured slower)
+                            PolyNode Lc[4];
+                            #pragma unroll
+                            for (int w = 0; w < 4; ++w) Lc[w] = lv[cl + w];
+                            for (;;) {
+                                const bool more = cl + 8 <= cend;
+                                PolyNode Ln[4];
+                                if (more) {
+                                    #pragma unroll
+                                    for (int w = 0; w < 4; ++w) Ln[w] = lv[cl + 4 + w];
+                                }
+                                childless_batch<4>(Lc, xs, xq, gh, gl, P3, V3);
+                                cl += 4;
+                                if (!more) break;
+                                #pragma unroll
+                                for (int w = 0; w < 4; ++w) Lc[w] = Ln[w];
+                            }
+                        }
+                        for (; cl + 4 <= cend; cl += 4) leaf_batch<4>(lv + cl, xs, xq, gh, gl, P3, V3);
                         for (; cl < cend; ++cl) {
                             const PolyNode L = lv[cl];
-                            const int o = L.var * kBlock + t;
-                            DF g = {gh[o], gl[o]};
-                            leaf_update(L, xs[o], xq[o], P3, V3, g);
-                            gh[o] = g.h;
-                            gl[o] = g.l;
+                            DF g = {gh[L.var * kGS], gl[L.var * kGS]};
+                            leaf_update(L, xs[L.var * kXS], xq[L.var * kXS], P3, V3, g);
+                            gh[L.var * kGS] = g.h;
+                            gl[L.var * kGS] = g.l;
                         }
                     }
                     float p, q;
@@ -176,11 +260,10 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                     q = __fmaf_rn(V3.h, xkl, q);
                     acc(V2, p, q);
                     mul_df_df(V3, P2, p, q);
-                    const int o = C.var * kBlock + t;
-                    DF g = {gh[o], gl[o]};
+                    DF g = {gh[C.var * kGS], gl[C.var * kGS]};
                     acc(g, p, q);
-                    gh[o] = g.h;
-                    gl[o] = g.l;
+                    gh[C.var * kGS] = g.h;
+                    gl[C.var * kGS] = g.l;
                 }
                 float p, q;
                 mul_df_f(V2, xj, p, q);
@@ -188,28 +271,97 @@ __global__ void __launch_bounds__(kBlock) poly_df_kernel(const PolyNode* __restr
                 acc(V1, p, q);
                 mul_df_f(V2, xi, p, q);
                 q = __fmaf_rn(V2.h, xil, q);
-                const int o = B.var * kBlock + t;
-                DF g = {gh[o], gl[o]};
+                DF g = {gh[B.var * kGS], gl[B.var * kGS]};
                 acc(g, p, q);
-                gh[o] = g.h;
-                gl[o] = g.l;
+                gh[B.var * kGS] = g.h;
+                gl[B.var * kGS] = g.l;
             }
             float p, q;
             mul_df_f(V1, xi, p, q);
             q = __fmaf_rn(V1.h, xil, q);
             acc(Ev, p, q);
-            const int o = A.var * kBlock + t;
-            DF g = {gh[o], gl[o]};
+            DF g = {gh[A.var * kGS], gl[A.var * kGS]};
             acc(g, V1.h, V1.l);
-            gh[o] = g.h;
-            gl[o] = g.l;
+            gh[A.var * kGS] = g.h;
+            gl[A.var * kGS] = g.l;
         }
+        if (half) {
+            e_other[0][tu] = Ev.h;
+            e_other[1][tu] = Ev.l;
+        }
+        __syncthreads();
         if (live) {
-            #pragma unroll
-            for (int v = 0; v < NV; ++v) G[(size_t)v * stride + u] = __fadd_rn(gh[v * kBlock + t], gl[v * kBlock + t]);
-            E[u] = __fadd_rn(Ev.h, Ev.l);
+            // first half's pair + second half's pair, variables split
+            // between the two threads of the unit
+            for (int v = half; v < NV; v += 2) {
+                DF g = {gh_all[v * kGS + tu], gl_all[v * kGS + tu]};
+                acc(g, gh_all[v * kGS + kUnits + tu], gl_all[v * kGS + kUnits + tu]);
+                G[(size_t)v * stride + u] = __fadd_rn(g.h, g.l);
+            }
+            if (!half) {
+                acc(Ev, e_other[0][tu], e_other[1][tu]);
+                E[u] = __fadd_rn(Ev.h, Ev.l);
+            }
         }
+        __syncthreads();
     }
+}
+
+// Split of a trie into two halves of about equal work (level-3 nodes and
+// leaves, weighted by their instruction counts), at a level-2 node.
+WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, const PolyNode* l3) {
+    std::vector<double> w(n2);
+    double total = 0.0;
+    int c3 = 0, cl = 0;
+    for (int j = 0; j < n2; ++j) {
+        double wj = 0.0;
+        for (; c3 < l2[j].end; ++c3) {
+            const int nl = l3[c3].end - cl;
+            wj += nl > 0 ? 12.0 + 7.0 * nl : 8.0;
+            cl = l3[c3].end;
+        }
+        w[j] = wj;
+        total += wj;
+    }
+    int m = 0;
+    double pre = 0.0;
+    while (m < n2 && pre + w[m] <= 0.5 * total) pre += w[m++];
+    if (m == 0) m = 1;  // both halves non-empty (n2 >= 2 for both tries)
+    int am = 0;
+    while (am < n1 && l1[am].end <= m) ++am;
+    const int first = am == 0 ? 0 : l1[am - 1].end;
+    const int c3m = l2[m - 1].end;
+    const int clm = c3m == 0 ? 0 : l3[c3m - 1].end;
+    WalkSplit s;
+    if (first == m) {
+        s.part[0] = WalkPart{0, am, 0, m, 0, 0, 0};
+        s.part[1] = WalkPart{am, n1, m, n2, c3m, clm, 0};
+    } else {
+        s.part[0] = WalkPart{0, am + 1, 0, m, 0, 0, 0};
+        s.part[1] = WalkPart{am, n1, m, n2, c3m, clm, 1};
+    }
+    return s;
+}
+
+const WalkSplit& split2() {
+    static const WalkSplit s = make_split(poly2b_l1, POLY2B_N1, poly2b_l2, POLY2B_N2, poly2b_l3);
+    return s;
+}
+const WalkSplit& split3() {
+    static const WalkSplit s = make_split(poly3b_l1, POLY3B_N1, poly3b_l2, POLY3B_N2, poly3b_l3);
+    return s;
+}
+
+template <int NV>
+constexpr int walk_smem() {
+    return NV * (2 * kUnits + 2 * kBlock) * (int)sizeof(float);
+}
+
+template <int NV>
+int walk_blocks(int n, int num_sms) {
+    int blocks = (n + kUnits - 1) / kUnits;
+    if (blocks > num_sms * 4) blocks = num_sms * 4;
+    return blocks;
 }
 
 template <int NV>
@@ -231,6 +383,10 @@ cudaError_t upload(const PolyNode* src, size_t n, PolyNode** dst) {
 
 }  // namespace
 
+cudaError_t poly2b_kernel_setup() {
+    return cudaFuncSetAttribute(poly_df_kernel<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, walk_smem<31>());
+}
+
 cudaError_t poly_tables_upload(int device) {
     if (g_dev_uploaded == device) return cudaSuccess;
     cudaError_t e;
@@ -241,44 +397,30 @@ cudaError_t poly_tables_upload(int device) {
         return e;
     g_t2.n1 = POLY2B_N1;
     g_t3.n1 = POLY3B_N1;
-    const int sm2 = 4 * 31 * kBlock * (int)sizeof(float), sm3 = 4 * 36 * kBlock * (int)sizeof(float);
-    if ((e = cudaFuncSetAttribute(poly_df_kernel<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm2))) return e;
-    if ((e = cudaFuncSetAttribute(poly_df_kernel<36>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm3))) return e;
+    if ((e = poly2b_kernel_setup())) return e;
+    if ((e = cudaFuncSetAttribute(poly_df_kernel<36>, cudaFuncAttributeMaxDynamicSharedMemorySize, walk_smem<36>())))
+        return e;
     g_dev_uploaded = device;
     return cudaSuccess;
 }
 
-void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms) {
-    if (n <= 0) return;
-    int blocks = (n + kBlock - 1) / kBlock;
-    if (blocks > num_sms * 4) blocks = num_sms * 4;
-    count_launch();
-    poly_df_kernel<31><<<blocks, kBlock, 4 * 31 * kBlock * sizeof(float), st>>>(g_t2.l1, g_t2.n1, g_t2.l2, g_t2.l3,
-                                                                                POLY2B_N3, g_t2.lv, X, G, E, n, stride);
-}
-
-cudaError_t poly2b_kernel_setup() {
-    return cudaFuncSetAttribute(poly_df_kernel<31>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                4 * 31 * kBlock * (int)sizeof(float));
-}
-
-void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, int n1, const PolyNode* l2, const PolyNode* l3,
+void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, const PolyNode* l2, const PolyNode* l3,
                         const PolyNode* lv, const float* X, float* G, float* E, int n, int stride, int num_sms) {
     if (n <= 0) return;
-    int blocks = (n + kBlock - 1) / kBlock;
-    if (blocks > num_sms * 4) blocks = num_sms * 4;
     count_launch();
-    poly_df_kernel<31><<<blocks, kBlock, 4 * 31 * kBlock * sizeof(float), st>>>(l1, n1, l2, l3, POLY2B_N3, lv, X, G, E, n,
-                                                                                stride);
+    poly_df_kernel<31><<<walk_blocks<31>(n, num_sms), kBlock, walk_smem<31>(), st>>>(l1, l2, l3, POLY2B_N3, lv,
+                                                                                     split2(), X, G, E, n, stride);
+}
+
+void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms) {
+    launch_poly2b_with(st, g_t2.l1, g_t2.l2, g_t2.l3, g_t2.lv, X, G, E, n, stride, num_sms);
 }
 
 void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms) {
     if (n <= 0) return;
-    int blocks = (n + kBlock - 1) / kBlock;
-    if (blocks > num_sms * 4) blocks = num_sms * 4;
     count_launch();
-    poly_df_kernel<36><<<blocks, kBlock, 4 * 36 * kBlock * sizeof(float), st>>>(g_t3.l1, g_t3.n1, g_t3.l2, g_t3.l3,
-                                                                                POLY3B_N3, g_t3.lv, X, G, E, n, stride);
+    poly_df_kernel<36><<<walk_blocks<36>(n, num_sms), kBlock, walk_smem<36>(), st>>>(
+        g_t3.l1, g_t3.l2, g_t3.l3, POLY3B_N3, g_t3.lv, split3(), X, G, E, n, stride);
 }
 
 }  // namespace mbpol

@@ -164,6 +164,7 @@ class MBPolElectrostaticsForce:
         self._thole = list(MBPOL_THOLE)
         self._redist = True
         self._guess = 0
+        self._pme_field = 0
         self._group = 0
 
     def addElectrostatics(self, charge, moleculeIndex, atomType, dampingFactor, polarity):
@@ -242,6 +243,17 @@ class MBPolElectrostaticsForce:
     def getInducedDipoleGuess(self):
         return self._guess
 
+    # Thole term of the PME permanent field: the reference's sign (default)
+    # or the one whose forces are the gradient of the energy; no reference
+    # counterpart (MBPolReferenceElectrostaticsForce.cpp:1377-1391)
+    ReferencePmeField, ConsistentPmeField = 0, 1
+
+    def setPmeFixedField(self, m):
+        self._pme_field = int(m)
+
+    def getPmeFixedField(self):
+        return self._pme_field
+
     def setForceGroup(self, g):
         self._group = int(g)
 
@@ -266,6 +278,7 @@ class MBPolElectrostaticsForce:
             p.thole[k] = self._thole[k]
         p.include_charge_redistribution = 1 if self._redist else 0
         p.guess = self._guess
+        p.pme_fixed_field = self._pme_field
         return p
 
 
@@ -501,7 +514,7 @@ class Context:
 def create_mbpol_system(ws, nonbonded_method="auto", terms=("onebody", "twobody", "threebody", "electrostatics",
                                                             "dispersion"), nonbonded_cutoff=0.9,
                         ewald_alpha=0.0, pme_grid=None, ewald_tol=1e-5, target_epsilon=1e-8, max_iterations=200,
-                        trimer_rule=0, guess=0):
+                        trimer_rule=0, guess=0, pme_fixed_field=0):
     """Build the MB-pol System for a WaterSystem as ForceField('mbpol.xml')
     does (python/mbpol.py:65-76, 138-150, 211-223, 288-326 and the <Script>
     of python/mbpol.xml): per water O, H1, H2, M with the M virtual site."""
@@ -546,6 +559,7 @@ def create_mbpol_system(ws, nonbonded_method="auto", terms=("onebody", "twobody"
         f.setMutualInducedTargetEpsilon(target_epsilon)
         f.setMutualInducedMaxIterations(max_iterations)
         f.setInducedDipoleGuess(guess)
+        f.setPmeFixedField(pme_fixed_field)
         if periodic:
             f.setEwaldErrorTolerance(ewald_tol)
             if ewald_alpha:

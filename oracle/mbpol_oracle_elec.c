@@ -364,6 +364,13 @@ int orc_last_fixed_field(int n, double* out) {
     return 0;
 }
 
+/* PME fixed-field Thole sign: 1 the reference's (s3 - 1)/r^3 subtraction
+ * (MBPolReferenceElectrostaticsForce.cpp:1377-1391), -1 the form whose
+ * forces are the gradient of the energy, bn1 - (1 - s3)/r^3 (the same
+ * damping as the energy, :2609-2626).  Intramolecular pairs are unaffected. */
+static double o_fixed_thole_sign = 1.0;
+void orc_set_pme_fixed_field(int consistent) { o_fixed_thole_sign = consistent ? -1.0 : 1.0; }
+
 /* -------------------------------------------------------------- solver */
 int orc_electrostatics(int n, const double* pos, const double* box, int pme, double alpha, const int* grid,
                        double rc, double target_eps, int maxiter, const double* thole, int row_stride, double* f,
@@ -437,7 +444,7 @@ int orc_electrostatics(int n, const double* pos, const double* box, int pme, dou
                 double bn[4];
                 o_bn(alpha, r, bn);
                 const double s3 = same ? 2.0 : o_scale(&C, a, b, r, 3, TCC);
-                fac = bn[1] - (s3 - 1.0) / (r2 * r);
+                fac = bn[1] - (same ? 1.0 : o_fixed_thole_sign) * (s3 - 1.0) / (r2 * r);
             } else {
                 fac = o_scale(&C, a, b, r, 3, TCC) / (r2 * r);
             }

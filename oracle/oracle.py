@@ -69,9 +69,9 @@ def build_port(force=False):
     """Compile oracle/mbpol_oracle.c into oracle/_port (gcc, plain C)."""
     src = os.path.join(HERE, "mbpol_oracle.c")
     os.makedirs(PORT_DIR, exist_ok=True)
-    if not force and os.path.exists(PORT_LIB) and os.path.getmtime(PORT_LIB) >= os.path.getmtime(src):
-        return PORT_LIB
     srcs = [src, os.path.join(HERE, "mbpol_oracle_elec.c")]
+    if not force and os.path.exists(PORT_LIB) and os.path.getmtime(PORT_LIB) >= max(map(os.path.getmtime, srcs)):
+        return PORT_LIB
     subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-I", os.path.join(HERE, "gen"),
                            "-I", HERE] + srcs + ["-o", PORT_LIB, "-lm"])
     return PORT_LIB
@@ -104,6 +104,8 @@ def port():
     L.orc_last_fixed_field.argtypes = [I, P]
     L.orc_set_onebody_tables.restype = None
     L.orc_set_onebody_tables.argtypes = [P, P]
+    L.orc_set_pme_fixed_field.restype = None
+    L.orc_set_pme_fixed_field.argtypes = [I]
     import numpy as np
     rows = [ln.split() for ln in open(os.path.join(os.path.dirname(HERE), "mbpol_openmm_plugin_gb300", "data",
                                                  "onebody_tables.txt")) if not ln.startswith(("#", "n "))]
@@ -163,6 +165,13 @@ def full_model(pos, box, alpha=0.0, grid=(0, 0, 0), eps=1e-8, maxiter=200, cut2=
     out["etotal"] = out["e1"] + out["e2"] + out["e3"] + out["edisp"] + out["eelec"]
     out["ftotal"] = out["f1"] + out["f2"] + out["f3"] + out["fdisp"] + out["felec"]
     return out
+
+
+def set_pme_fixed_field(consistent):
+    """PME fixed-field Thole term of the port: False the reference's sign
+    (MBPolReferenceElectrostaticsForce.cpp:1377-1391, the default), True the
+    sign that makes forces the gradient of the energy.  Process-wide."""
+    port().orc_set_pme_fixed_field(1 if consistent else 0)
 
 
 def fixed_field(pos, box=None, alpha=0.0, grid=(0, 0, 0), rc=0.9):
