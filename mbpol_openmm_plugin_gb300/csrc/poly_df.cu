@@ -15,10 +15,10 @@
 // Comput. 26 (2005)), which gives FP64-level results on the FP32 pipe.
 //
 // Two threads per unit (dimer or trimer), each walking half of the trie.
-// The variables x ([variable][unit]) and the gradient pairs (gh, gl;
-// [variable][thread]) live in shared memory, so every access of a warp is one
-// conflict-free wavefront; the trie tables are read with warp-uniform
-// addresses.  X: [2][nvars][stride] floats (FP64 variables as
+// The variables x ([variable][unit]) and the gradient ([variable][thread])
+// live in shared memory as (hi, lo) float2 pairs, so every access of a warp
+// is one conflict-free 8-byte load or store; the trie tables are read with
+// warp-uniform addresses.  X: [2][nvars][stride] floats (FP64 variables as
 // hi and lo planes); G: [nvars][stride]; E: [stride].
 #include <vector>
 
@@ -88,36 +88,35 @@ constexpr int kGS = kBlock;         // gradient plane stride
 // U sibling nodes without children (leaves, or level-3 nodes without
 // leaves) under a parent with prefix product P: V += c x and g += c P for
 // each, with all loads first, then the updates in order (V's summation order
-// is unchanged), then the stores.  Siblings have distinct variables.  xs, xq
-// point at this thread's unit, gh, gl at this thread's gradient column.
+// is unchanged), then the stores.  Siblings have distinct variables.  xv
+// points at this thread's unit, gv at this thread's gradient column; both
+// hold (hi, lo) pairs, one 8-byte access each.
 template <int U>
-__device__ __forceinline__ void childless_batch(const PolyNode (&L)[U], const float* xs, const float* xq, float* gh,
-                                                float* gl, const DF& P, DF& V) {
-    float x[U], xl[U];
-    DF g[U];
+__device__ __forceinline__ void childless_batch(const PolyNode (&L)[U], const float2* xv, float2* gv, const DF& P,
+                                                DF& V) {
+    float2 x[U], g[U];
     #pragma unroll
     for (int u = 0; u < U; ++u) {
-        x[u] = xs[L[u].var * kXS];
-        xl[u] = xq[L[u].var * kXS];
-        g[u].h = gh[L[u].var * kGS];
-        g[u].l = gl[L[u].var * kGS];
+        x[u] = xv[L[u].var * kXS];
+        g[u] = gv[L[u].var * kGS];
     }
-    #pragma unroll
-    for (int u = 0; u < U; ++u) leaf_update(L[u], x[u], xl[u], P, V, g[u]);
     #pragma unroll
     for (int u = 0; u < U; ++u) {
-        gh[L[u].var * kGS] = g[u].h;
-        gl[L[u].var * kGS] = g[u].l;
+        DF gu = {g[u].x, g[u].y};
+        leaf_update(L[u], x[u].x, x[u].y, P, V, gu);
+        g[u] = make_float2(gu.h, gu.l);
     }
+    #pragma unroll
+    for (int u = 0; u < U; ++u) gv[L[u].var * kGS] = g[u];
 }
 
 template <int U>
-__device__ __forceinline__ void leaf_batch(const PolyNode* __restrict__ lv, const float* xs, const float* xq,
-                                           float* gh, float* gl, const DF& P3, DF& V3) {
+__device__ __forceinline__ void leaf_batch(const PolyNode* __restrict__ lv, const float2* xv, float2* gv,
+                                           const DF& P3, DF& V3) {
     PolyNode L[U];
     #pragma unroll
     for (int u = 0; u < U; ++u) L[u] = lv[u];
-    childless_batch<U>(L, xs, xq, gh, gl, P3, V3);
+    childless_batch<U>(L, xv, gv, P3, V3);
 }
 
 // One half of the trie: level-1 nodes [a0, a1), level-2 nodes [c2_0, c2_1)
@@ -144,11 +143,9 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
                                                           const PolyNode* __restrict__ lv, const WalkSplit split,
                                                           const float* __restrict__ X, float* __restrict__ G,
                                                           float* __restrict__ E, int n, int stride) {
-    extern __shared__ float smem[];
-    float* xs_all = smem;                    // [NV][kUnits]  variables, high part
-    float* xq_all = xs_all + NV * kUnits;    // [NV][kUnits]  variables, low part
-    float* gh_all = xq_all + NV * kUnits;    // [NV][kBlock]
-    float* gl_all = gh_all + NV * kBlock;    // [NV][kBlock]
+    extern __shared__ float2 smem2[];
+    float2* xv_all = smem2;                  // [NV][kUnits]  variables (hi, lo)
+    float2* gv_all = xv_all + NV * kUnits;   // [NV][kBlock]  gradient pairs
     __shared__ float e_other[2][kUnits];     // the second half's energy pair
     const int t = threadIdx.x;
     const int half = t / kUnits;             // warp-uniform
@@ -158,22 +155,16 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
     const WalkPart W = {half ? P1.a0 : P0.a0,     half ? P1.a1 : P0.a1,     half ? P1.c2_0 : P0.c2_0,
                         half ? P1.c2_1 : P0.c2_1, half ? P1.c3_0 : P0.c3_0, half ? P1.cl_0 : P0.cl_0,
                         half ? P1.skip_coef : P0.skip_coef};
-    const float* xs = xs_all + tu;
-    const float* xq = xq_all + tu;
-    float* gh = gh_all + t;
-    float* gl = gl_all + t;
+    const float2* xv = xv_all + tu;
+    float2* gv = gv_all + t;
     for (int base = blockIdx.x * kUnits; base < n; base += gridDim.x * kUnits) {
         const int u = base + tu;
         const bool live = u < n;
-        for (int v = half; v < NV; v += 2) {
-            xs_all[v * kXS + tu] = live ? X[(size_t)v * stride + u] : 0.f;
-            xq_all[v * kXS + tu] = live ? X[(size_t)(NV + v) * stride + u] : 0.f;
-        }
+        for (int v = half; v < NV; v += 2)
+            xv_all[v * kXS + tu] = live ? make_float2(X[(size_t)v * stride + u], X[(size_t)(NV + v) * stride + u])
+                                        : make_float2(0.f, 0.f);
         #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            gh[v * kGS] = 0.f;
-            gl[v * kGS] = 0.f;
-        }
+        for (int v = 0; v < NV; ++v) gv[v * kGS] = make_float2(0.f, 0.f);
         __syncthreads();
         DF Ev = {0.f, 0.f};
         int c2 = W.c2_0, c3 = W.c3_0, cl = W.cl_0;
@@ -185,13 +176,15 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
         PolyNode Cn = c3 < n3 ? l3[c3] : PolyNode{0.f, 0.f, 0, 0};
         for (int a = W.a0; a < W.a1; ++a) {
             const PolyNode A = l1[a];
-            const float xi = xs[A.var * kXS], xil = xq[A.var * kXS];
+            const float2 xa = xv[A.var * kXS];
+            const float xi = xa.x, xil = xa.y;
             DF V1 = {A.hi, A.lo};
             if (a == W.a0 && W.skip_coef) V1 = DF{0.f, 0.f};
             const int e2 = min(A.end, W.c2_1);
             for (; c2 < e2; ++c2) {
                 const PolyNode B = l2[c2];
-                const float xj = xs[B.var * kXS], xjl = xq[B.var * kXS];
+                const float2 xb = xv[B.var * kXS];
+                const float xj = xb.x, xjl = xb.y;
                 DF V2 = {B.hi, B.lo};
                 DF P2;
                 P2.h = __fmul_rn(xi, xj);
@@ -207,14 +200,15 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
                         // three-body trie the look-ahead loads measured slower)
                         const PolyNode C4[4] = {C, l3[c3 + 1], l3[c3 + 2], l3[c3 + 3]};
                         if (C4[1].end == cl && C4[2].end == cl && C4[3].end == cl) {
-                            childless_batch<4>(C4, xs, xq, gh, gl, P2, V2);
+                            childless_batch<4>(C4, xv, gv, P2, V2);
                             c3 += 3;
                             if (c3 + 1 < n3) Cn = l3[c3 + 1];
                             continue;
                         }
                     }
                     if (c3 + 1 < n3) Cn = l3[c3 + 1];
-                    const float xk = xs[C.var * kXS], xkl = xq[C.var * kXS];
+                    const float2 xc = xv[C.var * kXS];
+                    const float xk = xc.x, xkl = xc.y;
                     DF V3 = {C.hi, C.lo};
                     const int cend = C.end;
                     if (cl < cend) {
@@ -239,20 +233,20 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
                                     #pragma unroll
                                     for (int w = 0; w < 4; ++w) Ln[w] = lv[cl + 4 + w];
                                 }
-                                childless_batch<4>(Lc, xs, xq, gh, gl, P3, V3);
+                                childless_batch<4>(Lc, xv, gv, P3, V3);
                                 cl += 4;
                                 if (!more) break;
                                 #pragma unroll
                                 for (int w = 0; w < 4; ++w) Lc[w] = Ln[w];
                             }
                         }
-                        for (; cl + 4 <= cend; cl += 4) leaf_batch<4>(lv + cl, xs, xq, gh, gl, P3, V3);
+                        for (; cl + 4 <= cend; cl += 4) leaf_batch<4>(lv + cl, xv, gv, P3, V3);
                         for (; cl < cend; ++cl) {
                             const PolyNode L = lv[cl];
-                            DF g = {gh[L.var * kGS], gl[L.var * kGS]};
-                            leaf_update(L, xs[L.var * kXS], xq[L.var * kXS], P3, V3, g);
-                            gh[L.var * kGS] = g.h;
-                            gl[L.var * kGS] = g.l;
+                            const float2 xl = xv[L.var * kXS], g0 = gv[L.var * kGS];
+                            DF g = {g0.x, g0.y};
+                            leaf_update(L, xl.x, xl.y, P3, V3, g);
+                            gv[L.var * kGS] = make_float2(g.h, g.l);
                         }
                     }
                     float p, q;
@@ -260,10 +254,10 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
                     q = __fmaf_rn(V3.h, xkl, q);
                     acc(V2, p, q);
                     mul_df_df(V3, P2, p, q);
-                    DF g = {gh[C.var * kGS], gl[C.var * kGS]};
+                    const float2 g0 = gv[C.var * kGS];
+                    DF g = {g0.x, g0.y};
                     acc(g, p, q);
-                    gh[C.var * kGS] = g.h;
-                    gl[C.var * kGS] = g.l;
+                    gv[C.var * kGS] = make_float2(g.h, g.l);
                 }
                 float p, q;
                 mul_df_f(V2, xj, p, q);
@@ -271,19 +265,19 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
                 acc(V1, p, q);
                 mul_df_f(V2, xi, p, q);
                 q = __fmaf_rn(V2.h, xil, q);
-                DF g = {gh[B.var * kGS], gl[B.var * kGS]};
+                const float2 g0 = gv[B.var * kGS];
+                DF g = {g0.x, g0.y};
                 acc(g, p, q);
-                gh[B.var * kGS] = g.h;
-                gl[B.var * kGS] = g.l;
+                gv[B.var * kGS] = make_float2(g.h, g.l);
             }
             float p, q;
             mul_df_f(V1, xi, p, q);
             q = __fmaf_rn(V1.h, xil, q);
             acc(Ev, p, q);
-            DF g = {gh[A.var * kGS], gl[A.var * kGS]};
+            const float2 g0 = gv[A.var * kGS];
+            DF g = {g0.x, g0.y};
             acc(g, V1.h, V1.l);
-            gh[A.var * kGS] = g.h;
-            gl[A.var * kGS] = g.l;
+            gv[A.var * kGS] = make_float2(g.h, g.l);
         }
         if (half) {
             e_other[0][tu] = Ev.h;
@@ -294,8 +288,9 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
             // first half's pair + second half's pair, variables split
             // between the two threads of the unit
             for (int v = half; v < NV; v += 2) {
-                DF g = {gh_all[v * kGS + tu], gl_all[v * kGS + tu]};
-                acc(g, gh_all[v * kGS + kUnits + tu], gl_all[v * kGS + kUnits + tu]);
+                const float2 g0 = gv_all[v * kGS + tu], g1 = gv_all[v * kGS + kUnits + tu];
+                DF g = {g0.x, g0.y};
+                acc(g, g1.x, g1.y);
                 G[(size_t)v * stride + u] = __fadd_rn(g.h, g.l);
             }
             if (!half) {
@@ -307,9 +302,12 @@ __global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __re
     }
 }
 
-// Split of a trie into two halves of about equal work (level-3 nodes and
-// leaves, weighted by their instruction counts), at a level-2 node.
-WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, const PolyNode* l3) {
+// Split of a trie at a level-2 node, the first half taking `frac` of the
+// modelled work (level-3 nodes and leaves weighted by their instruction
+// counts).  The model undercounts the second half's per-node overhead: the
+// fastest splits measured on GB300 (box4096, sweeps of frac) give the first
+// half 54% of the three-body and 57% of the two-body modelled work.
+WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, const PolyNode* l3, double frac) {
     std::vector<double> w(n2);
     double total = 0.0;
     int c3 = 0, cl = 0;
@@ -325,7 +323,7 @@ WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, con
     }
     int m = 0;
     double pre = 0.0;
-    while (m < n2 && pre + w[m] <= 0.5 * total) pre += w[m++];
+    while (m < n2 && pre + w[m] <= frac * total) pre += w[m++];
     if (m == 0) m = 1;  // both halves non-empty (n2 >= 2 for both tries)
     int am = 0;
     while (am < n1 && l1[am].end <= m) ++am;
@@ -344,11 +342,11 @@ WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, con
 }
 
 const WalkSplit& split2() {
-    static const WalkSplit s = make_split(poly2b_l1, POLY2B_N1, poly2b_l2, POLY2B_N2, poly2b_l3);
+    static const WalkSplit s = make_split(poly2b_l1, POLY2B_N1, poly2b_l2, POLY2B_N2, poly2b_l3, 0.57);
     return s;
 }
 const WalkSplit& split3() {
-    static const WalkSplit s = make_split(poly3b_l1, POLY3B_N1, poly3b_l2, POLY3B_N2, poly3b_l3);
+    static const WalkSplit s = make_split(poly3b_l1, POLY3B_N1, poly3b_l2, POLY3B_N2, poly3b_l3, 0.54);
     return s;
 }
 
