@@ -96,13 +96,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_workload(name, seed, guess):
+def build_workload(name, seed, guess, model="reference"):
+    """model "reference": the reference's trimer rule and PME permanent field
+    (parity); "physical": every trimer with a nonzero switch and the
+    consistent PME field, for which forces are -dE/dx."""
     import mbpol_openmm_plugin_gb300 as mb
     from mbpol_openmm_plugin_gb300 import systems
     ws = systems.workload(name, seed)
     alpha, grid = mb.pme_parameters(ws.box, 0.9, 1e-5)
+    phys = 1 if model == "physical" else 0
     sysm = mb.create_mbpol_system(ws, ewald_alpha=alpha, pme_grid=grid, ewald_tol=1e-5, target_epsilon=1e-8,
-                                  guess=guess)
+                                  guess=guess, trimer_rule=phys, pme_fixed_field=phys)
     return ws, sysm, alpha, grid
 
 
@@ -123,7 +127,7 @@ ALGO_FLOP_PER_UNIT = {"poly2b": 31200, "poly3b": 112600}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # each walk on box4096, measured with ncu --set full, and the units that launch
 # processed; the traffic of a launch is scaled by its unit count.
-NCU_TRAFFIC = {"poly3b": (53.078e6 + 2.419e6, 181889), "poly2b": (16.481e6, 65434)}
+NCU_TRAFFIC = {"poly3b": (53.173e6 + 2.374e6, 181889), "poly2b": (16.451e6, 65434)}
 
 
 def fp32_ops_per_unit(name):
@@ -150,6 +154,10 @@ def guess_params(args):
     workload (trained by mbpol_openmm_plugin_gb300.train_guess on 2000 NVT
     frames of the same box), else one trained here on a short trajectory."""
     path = GUESS_WEIGHTS % args.workload
+    if not os.path.exists(path) and args.workload.startswith("box"):
+        # a bulk box of the same density: the 4096-water box's network (its
+        # inputs are per-molecule and local, plus the permanent field)
+        path = GUESS_WEIGHTS % "box4096"
     if os.path.exists(path):
         return np.load(path), "committed (%s)" % os.path.relpath(path, ROOT)
     out = os.path.join("/tmp", "dipole_guess_%s_%d.npy" % (args.workload, os.getpid()))
@@ -163,7 +171,7 @@ def timed_md(args, guess, params=None, profile=False):
     import mbpol_openmm_plugin_gb300 as mb
     from mbpol_openmm_plugin_gb300 import _capi
     lib = _capi.load()
-    ws, sysm, alpha, grid = build_workload(args.workload, args.seed, GUESS_MODE[guess])
+    ws, sysm, alpha, grid = build_workload(args.workload, args.seed, GUESS_MODE[guess], args.model)
     ctx = mb.Context(sysm)
     ctx.setPositions(ws.positions)
     ctx._build()
@@ -216,7 +224,7 @@ def run_ours(args):
     # comparison arms first (same initial state), the headline arm last
     others = {}
     for g in ("plain", "extrapolation", "learned"):
-        if g == args.guess:
+        if g == args.guess or args.no_comparison:
             continue
         rr = timed_md(args, g, params if g == "learned" else None)
         others[g] = {"ns_per_day": ns_per_day(rr["step_s"]), "ms_per_step": rr["step_s"] * 1e3,
@@ -231,6 +239,9 @@ def run_ours(args):
     value = ns_per_day(step_s)
     solver_it = r["iterations"]
     en = r["energies"]
+
+    # NVE energy conservation after the timed region (device-resident state)
+    drift = nve_drift(lib, h, args.drift_steps, pos.shape[0] // 4) if args.drift_steps > 0 else None
 
     # e2e: public API with host buffers, host-side velocity Verlet
     hpos = np.zeros_like(pos)
@@ -251,10 +262,12 @@ def run_ours(args):
     e2e_s = (time.perf_counter() - t0) / args.steps
     n = pos.shape[0]
 
-    # roofline of the dominant kernel (by measured time)
-    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    # roofline of the dominant kernel: the three-body walk, first in the ncu
+    # launch list (the electrostatics timers span multi-kernel passes that
+    # overlap each other and the walks, so they are not kernel durations)
+    dom = "poly3b"
     roof = None
-    if dom in ("poly3b", "poly2b") and kern[dom]["launches"]:
+    if kern[dom]["launches"]:
         units = int(counts[1] if dom == "poly3b" else counts[0])
         per_launch_ms = kern[dom]["total_ms"] / kern[dom]["launches"]
         algo = ALGO_FLOP_PER_UNIT[dom]
@@ -280,6 +293,7 @@ def run_ours(args):
         "config": {"workload": args.workload, "waters": n // 4, "box_nm": float(ws.box[0]), "pme_alpha": alpha,
                    "pme_grid": grid, "cutoff_nm": 0.9, "ewald_tol": 1e-5, "target_epsilon_D": 1e-8,
                    "dt_fs": 0.2, "guess": args.guess, "guess_parameters": params_src, "seed": args.seed,
+                   "model": args.model,
                    "l2": "no flush: inputs larger than L2 (per-step trimer and pair variable/gradient planes "
                          "%.0f MB, PME grids %.0f MB, against 129 MB of L2)" % (
                              (int(counts[1]) * 36 * 3 + int(counts[0]) * 31 * 3) * 4 / 1e6,
@@ -296,9 +310,75 @@ def run_ours(args):
         "roofline": roof,
         "energies_kJ_mol": {"1b": en[0], "2b": en[1], "3b": en[2], "elec": en[3], "disp": en[4], "kinetic": en[5]},
     }
+    if drift is not None:
+        out["nve_drift"] = drift
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, sample=True)
     return out
+
+
+def nve_drift(lib, h, nsteps, nwaters, block=10):
+    """Total energy (potential + kinetic) every `block` NVE steps after the
+    timed region; linear drift per ns and the fluctuation about the fit."""
+    from mbpol_openmm_plugin_gb300 import _capi
+    ms = ctypes.c_double()
+    iters = ctypes.c_long()
+    en = np.zeros(6)
+    E = []
+    for _ in range(max(nsteps // block, 2)):
+        _capi.check(lib.mbpol_md_run(h, block, DT_PS, 0.0, 0.0, 0, ctypes.byref(ms), _capi.ptr(en),
+                                     ctypes.byref(iters)))
+        E.append(float(en.sum()))
+    t = np.arange(1, len(E) + 1) * block * DT_PS * 1e-3  # ns
+    fit = np.polyfit(t, E, 1)
+    return {"steps": block * len(E), "kJ_mol_per_ns": float(fit[0]), "kJ_mol_per_ns_per_water": float(fit[0]) / nwaters,
+            "fluctuation_kJ_mol": float(np.std(np.asarray(E) - np.polyval(fit, t))),
+            "total_energy_first_last": [E[0], E[-1]]}
+
+
+def run_clusters(args):
+    """Batched independent clusters: one context evaluates all clusters of
+    systems.batched_clusters (4096 clusters of 2-64 waters) per call, every
+    kernel launched once over all of them.  A step is one evaluation of the
+    whole batch through mbpol_compute (host buffers)."""
+    import mbpol_openmm_plugin_gb300 as mb
+    from mbpol_openmm_plugin_gb300 import _capi, systems
+    lib = _capi.load()
+    ws = systems.batched_clusters(seed=args.seed)
+    ncl = int(ws.cluster_of_water.max()) + 1
+    sysm = mb.create_mbpol_system(ws, target_epsilon=1e-8, guess=GUESS_MODE[args.guess] if args.guess != "learned" else 0)
+    ctx = mb.Context(sysm)
+    ctx.setPositions(ws.positions)
+    ctx.setClusters(np.repeat(ws.cluster_of_water, 4))
+    h = ctx._h
+    n = ws.positions.shape[0]
+    pos = np.ascontiguousarray(ws.positions, np.float64)
+    e5 = np.zeros(5)
+    forces = np.zeros((n, 3))
+    for _ in range(args.warmup):
+        _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), None))
+        _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
+    ts = []
+    for _ in range(args.steps):
+        forces[:] = 0.0
+        t0 = time.perf_counter()
+        _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), None))
+        _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
+        ts.append(time.perf_counter() - t0)
+    E, its = ctx.getClusterResults()
+    c = ctx.getCounts()
+    step_s = float(np.mean(ts))
+    return {"metric": "batched cluster evaluations/s (4096 clusters of 2-64 waters)", "value": ncl / step_s,
+            "unit": "clusters/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "replicas", "vs_baseline": None,
+            "dtype": "fp32+double-float polynomials, fp64 accumulation", "data": "synthetic (seeded clusters)",
+            "config": {"workload": "clusters", "clusters": ncl, "waters": int(ws.num_waters),
+                       "target_epsilon_D": 1e-8, "guess": "alpha*E (reference)" if args.guess == "learned" else args.guess,
+                       "seed": args.seed},
+            "e2e": {"value": ncl / step_s, "unit": "clusters/s", "h2d_bytes_per_step": int(n * 24),
+                    "d2h_bytes_per_step": int(n * 24 + 40)},
+            "solver_iterations": {"mean": float(its.mean()), "max": int(its.max())},
+            "counts": {"pairs_2b": int(c[0]), "trimers": int(c[1])}}
 
 
 def cpu_baseline(args, sample=True):
@@ -323,6 +403,10 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-comparison", action="store_true", help="time the --guess arm only")
+    ap.add_argument("--drift-steps", type=int, default=0, help="NVE steps after the timed region for the drift")
+    ap.add_argument("--model", default="reference", choices=["reference", "physical"],
+                    help="physical: complete trimers and the consistent PME field (energy-conserving)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
@@ -343,7 +427,7 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.gpus > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
-    out = run_ours(args)
+    out = run_clusters(args) if args.workload == "clusters" else run_ours(args)
     if rank == 0:
         print(json.dumps(out))
 

@@ -171,6 +171,17 @@ mbpol_status mbpol_get_induced_dipoles(mbpol_context* ctx, double* dipoles, int*
  * [2] electrostatics site pairs within the cutoff, [3] solver iterations. */
 mbpol_status mbpol_get_counts(mbpol_context* ctx, long* counts4);
 
+/* Electrostatic potential (kJ/mol/e) at num_points points (xyz, nm):
+ * MBPolElectrostaticsForce::getElectrostaticPotential
+ * (openmmapi/include/openmm/MBPolElectrostaticsForce.h:267;
+ * MBPolReferenceKernels.cpp:261-283).  Evaluates the electrostatics at the
+ * current positions (charges, converged induced dipoles), then sums
+ * q/r - mu.(r_i - g)/r^3 over all particles, minimum-imaged under PME and
+ * unscreened, as the reference.  Fails with MBPOL_ERR_NOT_CONVERGED as the
+ * reference throws; not available with batched clusters. */
+mbpol_status mbpol_get_electrostatic_potential(mbpol_context* ctx, int num_points, const double* points,
+                                               double* potential);
+
 /* Kernel timing with CUDA events on the launching stream (process-wide).
  * Kernel ids: 0 two-body polynomial, 1 three-body polynomial, 2 fixed field,
  * 3 induced field + solver update, 4 PME dipole pass (spread, FFT,

@@ -150,6 +150,15 @@ public:
     void setIncludeChargeRedistribution(bool b) { p_.include_charge_redistribution = b ? 1 : 0; }
     bool getIncludeChargeRedistribution() const { return p_.include_charge_redistribution != 0; }
     void setInducedDipoleGuess(int g) { p_.guess = g; }
+    /* MBPOL_PME_FIELD_REFERENCE (default) or MBPOL_PME_FIELD_CONSISTENT; no
+     * reference counterpart (see mbpol_gb300.h) */
+    void setPmeFixedField(int m) { p_.pme_fixed_field = m; }
+    int getPmeFixedField() const { return p_.pme_fixed_field; }
+    /* MBPolElectrostaticsForce.h:267: potential (kJ/mol/e) at the points of
+     * inputGrid (nm) from the context's current positions (defined after
+     * Context below) */
+    void getElectrostaticPotential(const std::vector<Vec3>& inputGrid, class Context& context,
+                                   std::vector<double>& outputElectrostaticPotential) const;
     int term() const override { return MBPOL_TERM_ELECTROSTATICS; }
 
     mbpol_electrostatics_params p_;
@@ -265,6 +274,16 @@ private:
     Vec3 box_{0, 0, 0};
     bool periodic_ = false;
 };
+
+inline void MBPolElectrostaticsForce::getElectrostaticPotential(const std::vector<Vec3>& inputGrid, Context& context,
+                                                                std::vector<double>& outputElectrostaticPotential) const {
+    std::vector<double> flat(3 * inputGrid.size());
+    for (size_t i = 0; i < inputGrid.size(); ++i)
+        for (int k = 0; k < 3; ++k) flat[3 * i + k] = inputGrid[i][k];
+    outputElectrostaticPotential.assign(inputGrid.size(), 0.0);
+    mbpol_check(mbpol_get_electrostatic_potential(context.handle(), (int)inputGrid.size(), flat.data(),
+                                                  outputElectrostaticPotential.data()));
+}
 
 }  // namespace MBPolPlugin
 

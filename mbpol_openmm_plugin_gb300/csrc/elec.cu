@@ -1534,6 +1534,71 @@ struct DBuf {
     }
 };
 
+// FP64 site charges for the electrostatic potential: the charges of
+// elec_prepare_kernel (redistribution from the raw positions, as the
+// reference) kept in FP64.
+__global__ void site_charges_kernel(int nmol, const double* __restrict__ pos, int redist,
+                                    const double* __restrict__ q_static, double* __restrict__ qd) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmol) return;
+    const int K = c_el.K, s0 = K * m;
+    if (redist) {
+        double qq[4], dd[4][3][3];
+        water_charges(load_pos(pos, s0), load_pos(pos, s0 + 1), load_pos(pos, s0 + 2), qq, dd);
+        for (int s = 0; s < 4; ++s) qd[s0 + s] = qq[s];
+    } else {
+        for (int s = 0; s < K; ++s) qd[s0 + s] = q_static[s0 + s];
+    }
+}
+
+// Electrostatic potential at probe points (reference
+// calculateElectrostaticPotential, MBPolReferenceElectrostaticsForce.cpp:
+// 1023-1085): phi(g) = 138.9354558456 * sum_i [q_i / r - mu_i . d / r^3] with
+// d = r_i - g, minimum-imaged under PME (getPeriodicDelta, :1234-1239), over
+// every site, unscreened.  One thread per point, the sites staged through
+// shared memory in tiles; FP64 throughout (an analysis call, not part of a
+// step).
+constexpr int kPotTile = 128;
+__global__ void __launch_bounds__(kPotTile) potential_kernel(int n, const double* __restrict__ pos,
+                                                             const double* __restrict__ qd,
+                                                             const double* __restrict__ mud, int npts,
+                                                             const double* __restrict__ pts,
+                                                             double* __restrict__ out) {
+    __shared__ double sr[3][kPotTile], sq[kPotTile], sm[3][kPotTile];
+    const int t = threadIdx.x;
+    const int p = blockIdx.x * kPotTile + t;
+    const bool live = p < npts;
+    double g[3] = {0.0, 0.0, 0.0};
+    if (live)
+        for (int k = 0; k < 3; ++k) g[k] = pts[3 * (size_t)p + k];
+    double acc = 0.0;
+    for (int base = 0; base < n; base += kPotTile) {
+        const int i = base + t;
+        __syncthreads();
+        if (i < n) {
+            for (int k = 0; k < 3; ++k) {
+                sr[k][t] = pos[3 * (size_t)i + k];
+                sm[k][t] = mud[3 * (size_t)i + k];
+            }
+            sq[t] = qd[i];
+        }
+        __syncthreads();
+        const int cnt = min(kPotTile, n - base);
+        if (!live) continue;
+        for (int j = 0; j < cnt; ++j) {
+            double d[3];
+            for (int k = 0; k < 3; ++k) {
+                d[k] = sr[k][j] - g[k];
+                if (c_el.periodic) d[k] -= floor(d[k] * c_el.inv[k] + 0.5) * c_el.box[k];
+            }
+            const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            const double rinv = 1.0 / sqrt(r2);
+            acc += sq[j] * rinv - (sm[0][j] * d[0] + sm[1][j] * d[1] + sm[2][j] * d[2]) * (rinv * rinv * rinv);
+        }
+    }
+    if (live) out[p] = acc * kElectric;
+}
+
 }  // namespace
 
 struct ElecImpl {
@@ -1541,6 +1606,8 @@ struct ElecImpl {
     mbpol_electrostatics_params prm{};
     bool pme = false;
     std::vector<float> q_static, damp, pol;
+    std::vector<double> q_static64;  // the caller's charges, for the potential
+    DBuf<double> d_qs64, d_qd, d_pts, d_pot;
     std::vector<int> type;
     DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu2, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd,
         d_gfrac, d_reach, d_ebase, d_intra, d_pcoef, d_edir;
@@ -1635,11 +1702,13 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     I.K = K;
     I.nmol = n / K;
     I.q_static.resize(n);
+    I.q_static64.resize(n);
     I.damp.resize(n);
     I.pol.resize(n);
     I.type.resize(n);
     for (int i = 0; i < n; ++i) {
         I.q_static[i] = (float)charge[i];
+        I.q_static64[i] = charge[i];
         // sixth root of the damping factor: pair kernels use
         // (damp_i damp_j)^(1/6) = damp_i^(1/6) damp_j^(1/6)
         I.damp[i] = (float)std::pow(damping[i], 1.0 / 6.0);
@@ -2105,6 +2174,32 @@ mbpol_status ElecEngine::get_dipoles(cudaStream_t st, double* dipoles, int* iter
         for (size_t i = 0; i < h.size(); ++i) dipoles[i] = h[i];
     if (iterations) *iterations = I.iterations;
     if (epsilon) *epsilon = I.epsilon;
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::potential(cudaStream_t st, const double* pos, int npts, const double* points,
+                                   double* potential) {
+    ElecImpl& I = *impl_;
+    if (!I.evaluated) return mbpol_fail(MBPOL_ERR_STATE, "no electrostatics evaluation yet");
+    if (npts <= 0) return MBPOL_OK;
+    const int n = I.N;
+    MBPOL_CUDA_OK(I.d_qd.ensure(n));
+    if (!I.prm.include_charge_redistribution) {
+        MBPOL_CUDA_OK(I.d_qs64.ensure(n));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_qs64.p, I.q_static64.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    }
+    MBPOL_CUDA_OK(I.d_pts.ensure(3 * (size_t)npts));
+    MBPOL_CUDA_OK(I.d_pot.ensure(npts));
+    MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_pts.p, points, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, st));
+    count_launch();
+    site_charges_kernel<<<(I.nmol + 127) / 128, 128, 0, st>>>(I.nmol, pos, I.prm.include_charge_redistribution ? 1 : 0,
+                                                              I.d_qs64.p, I.d_qd.p);
+    count_launch();
+    potential_kernel<<<(npts + kPotTile - 1) / kPotTile, kPotTile, 0, st>>>(n, pos, I.d_qd.p, I.d_mud.p, npts,
+                                                                          I.d_pts.p, I.d_pot.p);
+    MBPOL_CUDA_OK(cudaGetLastError());
+    MBPOL_CUDA_OK(cudaMemcpyAsync(potential, I.d_pot.p, sizeof(double) * npts, cudaMemcpyDeviceToHost, st));
+    MBPOL_CUDA_OK(cudaStreamSynchronize(st));
     return MBPOL_OK;
 }
 

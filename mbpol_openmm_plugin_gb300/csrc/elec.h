@@ -23,6 +23,9 @@ public:
     // Adds forces (kJ/mol/nm) into force and the energy (kJ/mol) into *energy (device pointers).
     mbpol_status compute(cudaStream_t st, const double* pos, const Box& box, double* force, double* energy);
     mbpol_status get_dipoles(cudaStream_t st, double* dipoles, int* iterations, double* epsilon);
+    // electrostatic potential (kJ/mol/e) at npts host points (nm) from the
+    // last evaluation's charges and induced dipoles; pos: device positions
+    mbpol_status potential(cudaStream_t st, const double* pos, int npts, const double* points, double* potential);
     bool converged() const;
     int iterations() const;
     long num_site_pairs() const;

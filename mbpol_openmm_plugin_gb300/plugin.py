@@ -263,6 +263,23 @@ class MBPolElectrostaticsForce:
     def updateParametersInContext(self, context):
         context._invalidate()
 
+    def getElectrostaticPotential(self, inputGrid, context, outputElectrostaticPotential=None):
+        """MBPolElectrostaticsForce.h:267: potential (kJ/mol/e) at the points
+        of inputGrid (nm) from the charges and converged induced dipoles at
+        the context's current positions.  Returns the values; when a list is
+        passed as outputElectrostaticPotential it is filled as well."""
+        pts = as_c(np.asarray(inputGrid, float).reshape(-1, 3), np.float64)
+        if context._h is None:
+            context._build()
+        lib = _capi.load()
+        box = None if context._box is None else as_c(context._box, np.float64)
+        check(lib.mbpol_set_positions(context._h, ptr(context._pos), ptr(box)))
+        out = np.zeros(pts.shape[0])
+        check(lib.mbpol_get_electrostatic_potential(context._h, pts.shape[0], ptr(pts), ptr(out)))
+        if outputElectrostaticPotential is not None:
+            outputElectrostaticPotential[:] = out.tolist()
+        return out
+
     def _params(self):
         p = _capi.ElectrostaticsParams()
         _capi.load().mbpol_electrostatics_params_default(ctypes.byref(p))

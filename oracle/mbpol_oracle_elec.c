@@ -371,6 +371,35 @@ int orc_last_fixed_field(int n, double* out) {
 static double o_fixed_thole_sign = 1.0;
 void orc_set_pme_fixed_field(int consistent) { o_fixed_thole_sign = consistent ? -1.0 : 1.0; }
 
+/* positions, charges (after redistribution) and converged induced dipoles
+ * of the last orc_electrostatics call: [n][7] = r[3], q, mu[3] */
+static double* o_last_state = NULL;
+static int o_last_state_n = 0, o_last_pme = 0;
+static double o_last_box[3];
+
+/* Electrostatic potential at npts points from the last orc_electrostatics
+ * call (MBPolReferenceElectrostaticsForce.cpp:1023-1085): for every point g
+ * the sum over all sites of q/r - mu.(r_i - g)/r^3 with d = r_i - g
+ * minimum-imaged under PME, times 138.9354558456 (kJ/mol/e). */
+int orc_electrostatic_potential(int npts, const double* points, double* out) {
+    if (!o_last_state) return 1;
+    for (int p = 0; p < npts; ++p) {
+        double acc = 0.0;
+        for (int i = 0; i < o_last_state_n; ++i) {
+            const double* S = o_last_state + 7 * i;
+            double d[3];
+            for (int k = 0; k < 3; ++k) {
+                d[k] = S[k] - points[3 * p + k];
+                if (o_last_pme) d[k] -= floor(d[k] / o_last_box[k] + 0.5) * o_last_box[k];
+            }
+            const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2], r = sqrt(r2);
+            acc += S[3] / r - (S[4] * d[0] + S[5] * d[1] + S[6] * d[2]) / (r2 * r);
+        }
+        out[p] = acc * ELECTRIC;
+    }
+    return 0;
+}
+
 /* -------------------------------------------------------------- solver */
 int orc_electrostatics(int n, const double* pos, const double* box, int pme, double alpha, const int* grid,
                        double rc, double target_eps, int maxiter, const double* thole, int row_stride, double* f,
@@ -608,6 +637,17 @@ int orc_electrostatics(int n, const double* pos, const double* box, int pme, dou
     *energy = e * ELECTRIC;
     if (iters) *iters = it;
     if (dip_out) memcpy(dip_out, mu, sizeof(double) * 3 * (size_t)n);
+    /* the state the electrostatic potential is evaluated from */
+    free(o_last_state);
+    o_last_state = (double*)malloc(7 * (size_t)n * sizeof(double));
+    for (int i = 0; i < n; ++i) {
+        memcpy(o_last_state + 7 * i, C.s[i].r, 24);
+        o_last_state[7 * i + 3] = C.s[i].q;
+        memcpy(o_last_state + 7 * i + 4, mu + 3 * i, 24);
+    }
+    o_last_state_n = n;
+    o_last_pme = pme;
+    if (pme) memcpy(o_last_box, box, 24);
     free(C.s);
     free(E0);
     free(Ei);

@@ -194,4 +194,47 @@ int ref_electrostatics(int ns, const double* pos, const double* charge, const in
     return 0;
 }
 
+/* MBPolElectrostaticsForce::getElectrostaticPotential: the reference kernel
+ * (MBPolReferenceKernels.cpp:261-283) calls calculateElectrostaticPotential
+ * (MBPolReferenceElectrostaticsForce.cpp:1048-1085): setup (charges with
+ * redistribution, converged induced dipoles), then for every grid point the
+ * sum over all particles of q/r - mu.(r_i - g)/r^3 (minimum image under PME),
+ * times 138.9354558456. */
+int ref_electrostatic_potential(int ns, const double* pos, const double* charge, const int* mol, const int* type,
+                                const double* damp, const double* pol, const double* thole5, int pme, double cutoff,
+                                double alpha, const int* grid, const double* box, double target_eps, int maxiter,
+                                int charge_redist, int npts, const double* points, double* potential, char* err,
+                                int errlen) {
+    std::vector<RealVec> p = load_positions(ns, pos), g = load_positions(npts, points);
+    std::vector<double> q(charge, charge + ns), d(damp, damp + ns), a(pol, pol + ns), th((size_t)ns, 0.0);
+    std::vector<int> m(mol, mol + ns), t(type, type + ns);
+    std::vector<double> thole(thole5, thole5 + 5), out;
+    try {
+        MBPolReferenceElectrostaticsForce* force = nullptr;
+        if (pme) {
+            PmeProbe* pp = new PmeProbe();
+            pp->setAlphaEwald(alpha);
+            pp->setCutoffDistance(cutoff);
+            std::vector<int> gd(grid, grid + 3);
+            pp->setPmeGridDimensions(gd);
+            RealVec b(box[0], box[1], box[2]);
+            pp->setPeriodicBoxSize(b);
+            force = pp;
+        } else {
+            force = new NonPmeProbe();
+        }
+        force->setMutualInducedDipoleTargetEpsilon(target_eps);
+        force->setMaximumMutualInducedDipoleIterations(maxiter);
+        force->setIncludeChargeRedistribution(charge_redist != 0);
+        force->setTholeParameters(thole);
+        force->calculateElectrostaticPotential(p, q, m, t, th, d, a, g, out);
+        for (int i = 0; i < npts; ++i) potential[i] = out[(size_t)i];
+        delete force;
+    } catch (const std::exception& ex) {
+        set_err(err, errlen, ex.what());
+        return 1;
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -13,7 +13,7 @@ Sources:
 Dispersion has no plugin code in the reference (python/mbpol.xml:37-108 builds
 an OpenMM CustomNonbondedForce); its values come from the C oracle port.
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference] [elec|pdb|potential]
 """
 import ctypes
 import json
@@ -65,6 +65,9 @@ def lib():
     L.ref_threebody.argtypes = [I, P, I, P, P, D, P, P, P, ctypes.c_long]
     L.ref_electrostatics.restype = I
     L.ref_electrostatics.argtypes = [I, P, P, P, P, P, P, P, I, D, D, P, P, D, I, I, P, P, P, P, ctypes.c_char_p, I]
+    L.ref_electrostatic_potential.restype = I
+    L.ref_electrostatic_potential.argtypes = [I, P, P, P, P, P, P, P, I, D, D, P, P, D, I, I, I, P, P,
+                                              ctypes.c_char_p, I]
     return L
 
 
@@ -276,12 +279,65 @@ def main_elec():
         print(name, seed, "Eelec %.6f kJ/mol  iterations %d  alpha %.4f grid %s" % (e, it, alpha, grid))
 
 
+def potential_points(pos, box, npts, rng, dmin=0.12):
+    """Seeded probe points at least dmin nm from every site: in the box, or
+    within 0.4 nm of the cluster's extent."""
+    lo, hi = (np.zeros(3), np.asarray(box, float)) if box is not None else (pos.min(0) - 0.4, pos.max(0) + 0.4)
+    out = []
+    while len(out) < npts:
+        g = lo + (hi - lo) * rng.random(3)
+        d = pos - g
+        if box is not None:
+            d -= box * np.round(d / box)
+        if np.sqrt((d * d).sum(1)).min() >= dmin:
+            out.append(g)
+    return np.array(out)
+
+
+def main_potential():
+    """getElectrostaticPotential (MBPolReferenceKernels.cpp:261-283) of the
+    compiled reference on seeded probe points."""
+    L = lib()
+    sys.path.insert(0, ROOT)
+    from mbpol_openmm_plugin_gb300.plugin import pme_parameters
+    for name, seed in (("cluster14", 0), ("box256", 0)):
+        ws = systems.workload(name, seed)
+        pos = place_m(ws.positions)
+        n = pos.shape[0]
+        pts = potential_points(pos, ws.box, 64, np.random.default_rng(1000 + seed))
+        if ws.box is None:
+            alpha, grid, b = 0.0, [0, 0, 0], np.zeros(3)
+        else:
+            alpha, grid = pme_parameters(ws.box, 0.9, 1e-5)
+            b = np.asarray(ws.box, float)
+        typ = np.tile([0, 1, 1, 2], n // 4).astype(np.int32)
+        q = np.tile([-5.1966000e-01, 2.5983000e-01, 2.5983000e-01, 0.0], n // 4)
+        damp = np.tile([0.00131, 0.000294, 0.000294, 0.00131], n // 4)
+        pol = np.tile([0.00131, 0.000294, 0.000294, 0.0], n // 4)
+        mol = np.repeat(np.arange(n // 4), 4).astype(np.int32)
+        out = np.zeros(len(pts))
+        err = ctypes.create_string_buffer(512)
+        rc = L.ref_electrostatic_potential(n, p(np.ascontiguousarray(pos)), p(q), p(mol), p(typ), p(damp), p(pol),
+                                           p(np.array(THOLE)), 0 if ws.box is None else 1, 0.9, alpha,
+                                           p(np.array(grid, np.int32)), p(b), 1e-8, 200, 1, len(pts),
+                                           p(np.ascontiguousarray(pts)), p(out), err, 512)
+        if rc:
+            raise RuntimeError(err.value.decode())
+        np.savez_compressed(os.path.join(HERE, "potential_%s_seed%d.npz" % (name, seed)), positions=pos,
+                            box=b, periodic=ws.box is not None, alpha=alpha, grid=np.array(grid), points=pts,
+                            potential=out)
+        print(name, seed, "potential range %.4f .. %.4f kJ/mol/e" % (out.min(), out.max()))
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "elec":
         main_elec()
+    elif len(sys.argv) > 2 and sys.argv[2] == "potential":
+        main_potential()
     elif len(sys.argv) > 2 and sys.argv[2] == "pdb":
         main_pdb()
     else:
         main()
         main_elec()
         main_pdb()
+        main_potential()

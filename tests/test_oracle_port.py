@@ -74,3 +74,15 @@ def test_port_water3_virtual_site_known_answer():
     r = oracle.full_model(pos, None, eps=1e-7)
     assert abs(r["eelec"] / 4.184 - k["expected_energy_kcal"]) < 1e-4
     assert rel_rms(r["felec"], np.array(k["oracle_forces_kJ_nm"])) < 1e-8
+
+
+@pytest.mark.parametrize("name", ["potential_cluster14_seed0", "potential_box256_seed0"])
+def test_port_electrostatic_potential(name):
+    """getElectrostaticPotential (MBPolReferenceElectrostaticsForce.cpp:1023-1085)
+    against the compiled reference on seeded probe points."""
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    periodic = bool(d["periodic"])
+    out = oracle.electrostatic_potential(d["positions"], d["points"], d["box"] if periodic else None,
+                                         float(d["alpha"]), tuple(int(v) for v in d["grid"]))
+    ref = d["potential"]
+    assert np.max(np.abs(out - ref)) <= 1e-8 * np.max(np.abs(ref))
