@@ -285,6 +285,31 @@ def run_ours(args):
                 "peak_kind": "nominal FP32 FMA rate at the median sampled SM clock (152 SM x 128 lanes x 2); "
                              "the measured-peaks file has no FP32 figure",
                 "launch_ms": per_launch_ms}
+    # memory-bound electrostatics kernels against the measured HBM copy rate
+    # (algorithmic bytes as in the reference's operation counts: pair index
+    # 4 B + cached pair coefficients 8 B per polarisable site pair within the
+    # cutoff, 36 B per polarisable site; PME pass: 125 grid updates of 4 B per
+    # site, 8 B per grid point for the FFT input and output, 16 B for the
+    # convolution).  Both timers run concurrently with the polynomial walks,
+    # so the fractions are lower bounds.
+    hbm = measured_hbm_gbs()
+    nsites = 3 * (n // 4)
+    secondary = {}
+    if kern["elec_direct_field"]["launches"] and counts[2] > 0:
+        t = kern["elec_direct_field"]["total_ms"] / kern["elec_direct_field"]["launches"] * 1e-3
+        b = 12 * int(counts[2]) + 36 * nsites
+        secondary["induced_direct_field"] = {
+            "bound": "hbm", "achieved": b / t / 1e9, "peak": hbm[0], "unit": "GB/s", "frac": b / t / 1e9 / hbm[0],
+            "traffic": None, "work": "%d polarisable site pairs x 12 B + %d sites x 36 B" % (int(counts[2]), nsites),
+            "launch_ms": t * 1e3, "peak_kind": hbm[1]}
+    if grid and kern["elec_pme_dipoles"]["launches"]:
+        t = kern["elec_pme_dipoles"]["total_ms"] / kern["elec_pme_dipoles"]["launches"] * 1e-3
+        G = grid[0] * grid[1] * grid[2]
+        b = nsites * 125 * 4 + 24 * G
+        secondary["pme_dipole_pass"] = {
+            "bound": "hbm", "achieved": b / t / 1e9, "peak": hbm[0], "unit": "GB/s", "frac": b / t / 1e9 / hbm[0],
+            "traffic": None, "work": "%d sites x 125 x 4 B + %d grid points x 24 B (spread, cuFFT, gather)" % (nsites, G),
+            "launch_ms": t * 1e3, "peak_kind": hbm[1]}
     out = {
         "metric": "ns/day @4096 H2O PME, learned-guess vs plain GPU at <=1e-4 rel RMS force err",
         "value": value, "unit": "ns/day", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -304,10 +329,12 @@ def run_ours(args):
         "solver_iterations_per_step": solver_it,
         "guess_comparison": dict(others, **{args.guess: {"ns_per_day": value, "ms_per_step": step_s * 1e3,
                                                          "solver_iterations_per_step": solver_it}}),
-        "counts": {"pairs_2b": int(counts[0]), "trimers": int(counts[1])},
+        "counts": {"pairs_2b": int(counts[0]), "trimers": int(counts[1]), "elec_site_pairs": int(counts[2]),
+                   "pme_grid_points": int(grid[0] * grid[1] * grid[2]) if grid else 0},
         "kernels_ms_per_step": {k: v["total_ms"] / args.steps for k, v in kern.items()},
         "clocks": clocks,
         "roofline": roof,
+        "roofline_memory_kernels": secondary,
         "energies_kJ_mol": {"1b": en[0], "2b": en[1], "3b": en[2], "elec": en[3], "disp": en[4], "kinetic": en[5]},
     }
     if drift is not None:
@@ -315,6 +342,16 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, sample=True)
     return out
+
+
+def measured_hbm_gbs():
+    """(GB/s, source): the HBM copy rate of MEASURED_PEAKS.json, else the
+    fallback figure of one earlier GB300 measurement."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured HBM copy rate (MEASURED_PEAKS.json)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback HBM copy rate"
 
 
 def nve_drift(lib, h, nsteps, nwaters, block=10):

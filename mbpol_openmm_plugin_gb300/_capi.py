@@ -36,7 +36,8 @@ GUESS_BLOCK_FLOATS = 9033  # MBPOL_GUESS_BLOCK_FLOATS
 GUESS_PARAMS = 8905
 GUESS_INPUTS = 64
 NOALLOC_MAX_DIMERS = 65536  # MBPOL_NOALLOC_MAX_DIMERS
-KERNELS = ["poly2b", "poly3b", "elec_fixed_field", "elec_induced_update", "elec_pme_dipoles", "elec_energy_forces"]
+KERNELS = ["poly2b", "poly3b", "elec_fixed_field", "elec_induced_update", "elec_pme_dipoles", "elec_energy_forces",
+           "elec_direct_field"]
 
 
 class MBPolError(RuntimeError):

@@ -721,7 +721,7 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
                                    const float* __restrict__ nbd, const int* __restrict__ nnb, int cap,
                                    const float* __restrict__ phi_fix, float* __restrict__ E0,
                                    float* __restrict__ mu_out, float* __restrict__ intra,
-                                   float* __restrict__ pcoef) {
+                                   float* __restrict__ pcoef, unsigned long long* __restrict__ npair) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (A >= nmol) return;
@@ -758,6 +758,7 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
     for (int a = 0; a < kMaxK; ++a) E[a][0] = E[a][1] = E[a][2] = 0.f;
     const int n = min(nnb[A], cap);
     const float gcc = c_el.thole[0];
+    unsigned npol = 0;  // polarisable site pairs within the cutoff
     for (int t = lane; t < n; t += 32) {
         const int B = nb[(size_t)A * cap + t];
         const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
@@ -776,6 +777,7 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
                 const float r2 = dot(d, d);
                 float pf1 = 0.f, pf2 = 0.f;
                 if (!PME || r2 <= c_el.rc2) {
+                    ++npol;
                     const float r = sqrtf(r2);
                     const Thole th = thole(r, MA.damp[a] * MB.damp[b], c_el.thole[2]);
                     if (PME) {
@@ -827,6 +829,8 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
         E[a][1] = warp_sum(E[a][1]);
         E[a][2] = warp_sum(E[a][2]);
     }
+    npol = __reduce_add_sync(0xffffffffu, npol);
+    if (lane == 0 && npair) atomicAdd(npair, (unsigned long long)npol);
     if (lane == 0) {
         if (PME) {
             // intramolecular pairs: s3 = 2 (reference :1381-1384), within the cutoff
@@ -1635,7 +1639,6 @@ struct ElecImpl {
     bool converged = true;
     int iterations = 0;
     double epsilon = 0.0;
-    long npairs = 0;
     bool have_prev = false;
     // learned guess (guess = 2)
     GuessNet net;
@@ -1661,7 +1664,13 @@ struct ElecImpl {
     cudaStream_t st2 = nullptr;
     cudaEvent_t ev_in = nullptr, ev_pme = nullptr;
 
+    // polarisable site pairs within the cutoff, counted in both directions by
+    // the fixed-field kernel
+    DBuf<unsigned long long> d_npair;
+    unsigned long long* h_npair = nullptr;
+
     ~ElecImpl() {
+        if (h_npair) cudaFreeHost(h_npair);
         if (plans) {
             cufftDestroy(plan_f);
             cufftDestroy(plan_b);
@@ -1915,6 +1924,9 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         I.cap *= 2;
     }
     MBPOL_CUDA_OK(I.d_pcoef.ensure((size_t)nmol * kMaxK * kMaxK * 2 * I.cap));
+    MBPOL_CUDA_OK(I.d_npair.ensure(1));
+    if (!I.h_npair) MBPOL_CUDA_OK(cudaMallocHost(&I.h_npair, sizeof(unsigned long long)));
+    MBPOL_CUDA_OK(cudaMemsetAsync(I.d_npair.p, 0, sizeof(unsigned long long), st));
     const int wblocks = (nmol * 32 + 127) / 128;
     const size_t nreal = I.pme ? (size_t)I.grid[0] * I.grid[1] * I.grid[2] : 0;
     // fixed field
@@ -1929,15 +1941,18 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         count_launch();
         fixed_field_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                            I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_phi_fix.p,
-                                                           I.d_E0.p, I.d_mu0.p, I.d_intra.p, I.d_pcoef.p);
+                                                           I.d_E0.p, I.d_mu0.p, I.d_intra.p, I.d_pcoef.p,
+                                                           I.d_npair.p);
         prof_end(st, K_ELEC_FIXED);
     } else {
         count_launch();
         fixed_field_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p,
                                                             I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
                                                             nullptr, I.d_E0.p, I.d_mu0.p, I.d_intra.p,
-                                                            I.d_pcoef.p);
+                                                            I.d_pcoef.p, I.d_npair.p);
     }
+    // directed pair count -> host (pinned), read after the solver's first wait
+    MBPOL_CUDA_OK(cudaMemcpyAsync(I.h_npair, I.d_npair.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     // d_mu0 holds float(mu) of the starting dipoles (alpha*E0 from the
     // fixed-field kernel, or the previous call's dipoles)
     float* bufs[3] = {I.d_mu0.p, I.d_mu1.p, I.d_mu2.p};
@@ -2087,6 +2102,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2.p, 0, sizeof(double), st));
         prof_begin(st, K_ELEC_INDUCED);
         count_launch();
+        prof_begin(st, K_ELEC_FIELD);
         if (I.pme) {
             induced_update_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                   I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
@@ -2094,6 +2110,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                                                                   kmode, I.d_ebase.p, anchor, I.d_intra.p,
                                                                   I.d_pcoef.p, nullptr, nullptr, nullptr,
                                                                   I.d_polmask.p, nullptr, I.d_edir.p);
+            prof_end(st, K_ELEC_FIELD);
             MBPOL_CUDA_OK(cudaStreamWaitEvent(st, I.ev_pme, 0));
             count_launch();
             induced_finish_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, I.d_edir.p, I.d_phi_mu.p, I.d_E0.p, I.d_pol.p,
@@ -2106,6 +2123,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                                                                    kmode, I.d_ebase.p, anchor, I.d_intra.p,
                                                                   I.d_pcoef.p, nullptr, nullptr, nullptr,
                                                                   I.d_polmask.p, nullptr, nullptr);
+        if (!I.pme) prof_end(st, K_ELEC_FIELD);
         prof_end(st, K_ELEC_INDUCED);
         if (kmode == 1) anchor = mu_in;
         mode = kmode == 0 ? 0 : 2;
@@ -2273,7 +2291,7 @@ long ElecEngine::guess_num_samples() const { return impl_->net.num_samples(); }
 
 bool ElecEngine::converged() const { return impl_->converged; }
 int ElecEngine::iterations() const { return impl_->iterations; }
-long ElecEngine::num_site_pairs() const { return impl_->npairs; }
+long ElecEngine::num_site_pairs() const { return impl_->h_npair ? (long)(*impl_->h_npair / 2) : 0; }
 std::string ElecEngine::convergence_message() const {
     std::ostringstream m;
     m << "Induced dipoles did not converge:  iterations=" << impl_->iterations << " eps=" << impl_->epsilon;

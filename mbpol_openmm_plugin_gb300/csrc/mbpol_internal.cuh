@@ -21,7 +21,7 @@ namespace mbpol {
 
 // Per-kernel CUDA-event timing (enabled with mbpol_profile_enable): ids of
 // the timed kernels.
-enum KernelId { K_POLY2B = 0, K_POLY3B, K_ELEC_FIXED, K_ELEC_INDUCED, K_ELEC_PME, K_ELEC_FORCES, K_NUM };
+enum KernelId { K_POLY2B = 0, K_POLY3B, K_ELEC_FIXED, K_ELEC_INDUCED, K_ELEC_PME, K_ELEC_FORCES, K_ELEC_FIELD, K_NUM };
 void prof_begin(cudaStream_t st, int id);
 // Number of kernels this library has launched (cuFFT's own launches excluded).
 void count_launch();
