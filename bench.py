@@ -396,12 +396,20 @@ def run_clusters(args):
         _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), None))
         _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
     ts = []
+    lib.mbpol_profile_enable(1)
     for _ in range(args.steps):
         forces[:] = 0.0
         t0 = time.perf_counter()
         _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), None))
         _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
         ts.append(time.perf_counter() - t0)
+    kern = {}
+    for kid, kname in enumerate(_capi.KERNELS):
+        t = ctypes.c_double()
+        nl = ctypes.c_long()
+        lib.mbpol_profile_read(kid, ctypes.byref(t), ctypes.byref(nl))
+        kern[kname] = t.value / args.steps
+    lib.mbpol_profile_enable(0)
     E, its = ctx.getClusterResults()
     c = ctx.getCounts()
     step_s = float(np.mean(ts))
@@ -415,6 +423,7 @@ def run_clusters(args):
             "e2e": {"value": ncl / step_s, "unit": "clusters/s", "h2d_bytes_per_step": int(n * 24),
                     "d2h_bytes_per_step": int(n * 24 + 40)},
             "solver_iterations": {"mean": float(its.mean()), "max": int(its.max())},
+            "kernels_ms_per_step": kern,
             "counts": {"pairs_2b": int(c[0]), "trimers": int(c[1])}}
 
 

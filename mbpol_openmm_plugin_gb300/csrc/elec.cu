@@ -1544,6 +1544,53 @@ struct DBuf {
     }
 };
 
+// Convergence control of the batched-cluster solver on the device: after
+// each iteration, for every cluster still running, the host loop's rules of
+// the single-system solver (reference convergeInduceDipoles :557-616):
+// cstate 1 -> 2 after the anchoring iteration; epsilon from the cluster's
+// own sum of squared changes and site count; stop on convergence, on an
+// increase or at the iteration limit; then the anchoring switch for the
+// next iteration.  One block; it sets the condition of the graph's while
+// loop (more clusters to run, and a bound on the loop's length).
+constexpr int kCtlThreads = 1024;
+__global__ void __launch_bounds__(kCtlThreads) cluster_control_kernel(
+    int ncl, const double* __restrict__ eps2c, const int* __restrict__ nsites, double* __restrict__ cur,
+    int* __restrict__ its, int* __restrict__ cstate, int* __restrict__ cconv, double target, int max_it,
+    double switch_eps, int* __restrict__ rounds, cudaGraphConditionalHandle loop) {
+    __shared__ int s_active[kCtlThreads / 32];
+    int active = 0;
+    for (int c = threadIdx.x; c < ncl; c += kCtlThreads) {
+        int st = cstate[c];
+        if (st >= 3) continue;
+        if (st == 1) st = 2;
+        const double ec = kSOR * kDebye * sqrt(eps2c[c] / (double)nsites[c]);
+        bool stop = false;
+        if (!isfinite(ec)) {
+            stop = true;
+        } else if (ec < target) {
+            cconv[c] = 1;
+            stop = true;
+        } else if (cur[c] < ec || its[c] >= max_it) {
+            stop = true;
+        }
+        cur[c] = ec;
+        its[c] += 1;
+        if (stop) st = 3;
+        else if (st == 0 && ec < switch_eps) st = 1;
+        cstate[c] = st;
+        if (st < 3) ++active;
+    }
+    active = __reduce_add_sync(0xffffffffu, active);
+    if ((threadIdx.x & 31) == 0) s_active[threadIdx.x >> 5] = active;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int total = 0;
+        for (int w = 0; w < kCtlThreads / 32; ++w) total += s_active[w];
+        const int r = ++(*rounds);
+        cudaGraphSetConditional(loop, (total > 0 && r <= max_it + 2) ? 1u : 0u);
+    }
+}
+
 // FP64 site charges for the electrostatic potential: the charges of
 // elec_prepare_kernel (redistribution from the raw positions, as the
 // reference) kept in FP64.
@@ -1657,6 +1704,14 @@ struct ElecImpl {
     std::vector<char> cl_conv;
     DBuf<int> d_mcl, d_cstate;  // d_cstate: per-cluster solver stage (0 plain, 1 anchoring, 2 anchored, 3 done)
     DBuf<double> d_eps2c;
+    // the batched solver as one graph launch: a while node whose body runs
+    // two iterations (ping-pong buffers), each followed by the control kernel
+    DBuf<int> d_cl_nsites, d_cl_its, d_cl_conv, d_rounds;
+    DBuf<double> d_cl_cur;
+    cudaStream_t st_cap = nullptr;
+    cudaGraph_t cl_graph = nullptr;
+    cudaGraphExec_t cl_exec = nullptr;
+    std::vector<uintptr_t> cl_graph_key;
     ClusterSink cl_sink;
     Box last_box{};
     int mu_cur = 0;  // which buffer holds the current dipoles
@@ -1670,6 +1725,9 @@ struct ElecImpl {
     unsigned long long* h_npair = nullptr;
 
     ~ElecImpl() {
+        if (cl_exec) cudaGraphExecDestroy(cl_exec);
+        if (cl_graph) cudaGraphDestroy(cl_graph);
+        if (st_cap) cudaStreamDestroy(st_cap);
         if (h_npair) cudaFreeHost(h_npair);
         if (plans) {
             cufftDestroy(plan_f);
@@ -1871,6 +1929,74 @@ static mbpol_status pme_convolve(ElecImpl& I, cudaStream_t st, const Box& box) {
     return MBPOL_OK;
 }
 
+namespace {
+
+uintptr_t key_bits(double v) {
+    uint64_t u;
+    std::memcpy(&u, &v, sizeof u);
+    return (uintptr_t)u;
+}
+
+// The batched-cluster solver as one graph: a while node whose body runs two
+// iterations (buffers a -> b, then b -> a), each a zeroing of the
+// per-cluster sums, the field + update kernel and the control kernel, which
+// decides on the device whether the loop goes on.  Rebuilt when a buffer,
+// size or solver parameter it captured changes.
+mbpol_status cluster_solver_graph(ElecImpl& I, int nmol, int wblocks, float* buf_a, float* buf_b, float* anchor_buf,
+                                  double switch_eps) {
+    const std::vector<uintptr_t> key = {
+        (uintptr_t)nmol, (uintptr_t)wblocks, (uintptr_t)I.cap, (uintptr_t)I.ncl, (uintptr_t)buf_a, (uintptr_t)buf_b,
+        (uintptr_t)anchor_buf, (uintptr_t)I.d_off.p, (uintptr_t)I.d_damp.p, (uintptr_t)I.d_pol.p,
+        (uintptr_t)I.d_type.p, (uintptr_t)I.d_nb.p, (uintptr_t)I.d_nbd.p, (uintptr_t)I.d_nnb.p, (uintptr_t)I.d_E0.p,
+        (uintptr_t)I.d_mud.p, (uintptr_t)I.d_eps2.p, (uintptr_t)I.d_ebase.p, (uintptr_t)I.d_intra.p,
+        (uintptr_t)I.d_pcoef.p, (uintptr_t)I.d_mcl.p, (uintptr_t)I.d_cstate.p, (uintptr_t)I.d_eps2c.p,
+        (uintptr_t)I.d_polmask.p, (uintptr_t)I.d_cl_nsites.p, (uintptr_t)I.d_cl_cur.p, (uintptr_t)I.d_cl_its.p,
+        (uintptr_t)I.d_cl_conv.p, (uintptr_t)I.d_rounds.p, key_bits(I.prm.target_epsilon),
+        (uintptr_t)I.prm.max_iterations, key_bits(switch_eps)};
+    if (I.cl_exec && key == I.cl_graph_key) return MBPOL_OK;
+    if (I.cl_exec) cudaGraphExecDestroy(I.cl_exec);
+    if (I.cl_graph) cudaGraphDestroy(I.cl_graph);
+    I.cl_exec = nullptr;
+    I.cl_graph = nullptr;
+    I.cl_graph_key.clear();
+    if (!I.st_cap) MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&I.st_cap, cudaStreamNonBlocking));
+    MBPOL_CUDA_OK(cudaGraphCreate(&I.cl_graph, 0));
+    cudaGraphConditionalHandle loop;
+    MBPOL_CUDA_OK(cudaGraphConditionalHandleCreate(&loop, I.cl_graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    MBPOL_CUDA_OK(cudaGraphAddNode(&node, I.cl_graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t sc = I.st_cap;
+    MBPOL_CUDA_OK(cudaStreamBeginCaptureToGraph(sc, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    for (int half = 0; half < 2; ++half) {
+        const float* mu_in = half ? buf_b : buf_a;
+        float* mu_out = half ? buf_a : buf_b;
+        cudaMemsetAsync(I.d_eps2c.p, 0, sizeof(double) * I.ncl, sc);
+        induced_update_kernel<false><<<wblocks, 128, 0, sc>>>(
+            nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
+            nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p, 0, I.d_ebase.p, anchor_buf, I.d_intra.p, I.d_pcoef.p,
+            I.d_mcl.p, I.d_cstate.p, I.d_eps2c.p, I.d_polmask.p, anchor_buf, nullptr);
+        cluster_control_kernel<<<1, kCtlThreads, 0, sc>>>(I.ncl, I.d_eps2c.p, I.d_cl_nsites.p, I.d_cl_cur.p,
+                                                           I.d_cl_its.p, I.d_cstate.p, I.d_cl_conv.p,
+                                                           I.prm.target_epsilon, I.prm.max_iterations, switch_eps,
+                                                           I.d_rounds.p, loop);
+    }
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(sc, &captured);
+    MBPOL_CUDA_OK(ce);
+    MBPOL_CUDA_OK(cudaGetLastError());
+    MBPOL_CUDA_OK(cudaGraphInstantiate(&I.cl_exec, I.cl_graph, 0));
+    I.cl_graph_key = key;
+    return MBPOL_OK;
+}
+
+}  // namespace
+
 mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& box, double* force, double* energy) {
     ElecImpl& I = *impl_;
     const int n = I.N, K = I.K, nmol = I.nmol;
@@ -2010,61 +2136,35 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     int mode = 0;
     if (I.ncl > 0) {
         // batched clusters: each cluster runs the reference's loop on its own
-        // epsilon (its own site count) and stops on its own; the others go on
+        // epsilon (its own site count) and stops on its own while the others
+        // go on; the whole loop is one graph launch, its control on the device
         const int ncl = I.ncl;
-        std::vector<double> cur(ncl, 1.0e+50), e2(ncl, 0.0);
-        std::vector<int> its(ncl, 0), cstate(ncl, 0);  // 0 plain, 1 anchoring, 2 anchored, 3 done
-        std::vector<char> cconv(ncl, 0);
-        int active = 0;
-        for (int c = 0; c < ncl; ++c) {
-            if (I.cl_nsites[c] > 0) {
-                ++active;
-            } else {
+        std::vector<int> cstate(ncl, 0), cconv(ncl, 0), its(ncl, 0);
+        std::vector<double> cur(ncl, 1.0e+50);
+        for (int c = 0; c < ncl; ++c)
+            if (I.cl_nsites[c] == 0) {
                 cstate[c] = 3;
                 cconv[c] = 1;
             }
-        }
-        float* anchor_buf = bufs[2];
-        while (active > 0) {
-            // the anchoring switch per cluster, as for one system
-            for (int c = 0; c < ncl; ++c)
-                if (cstate[c] == 0 && cur[c] < switch_eps) cstate[c] = 1;
-            MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_cstate.p, cstate.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, st));
-            float* mu_out = mu_in == bufs[0] ? bufs[1] : bufs[0];
-            MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2c.p, 0, sizeof(double) * ncl, st));
-            prof_begin(st, K_ELEC_INDUCED);
-            count_launch();
-            induced_update_kernel<false><<<wblocks, 128, 0, st>>>(
-                nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
-                nullptr, mu_in, mu_out, I.d_mud.p, I.d_eps2.p, 0, I.d_ebase.p, anchor_buf, I.d_intra.p, I.d_pcoef.p,
-                I.d_mcl.p, I.d_cstate.p, I.d_eps2c.p, I.d_polmask.p, anchor_buf, nullptr);
-            prof_end(st, K_ELEC_INDUCED);
-            mu_in = mu_out;
-            MBPOL_CUDA_OK(cudaMemcpyAsync(e2.data(), I.d_eps2c.p, sizeof(double) * ncl, cudaMemcpyDeviceToHost, st));
-            MBPOL_CUDA_OK(cudaStreamSynchronize(st));
-            for (int c = 0; c < ncl; ++c) {
-                if (cstate[c] >= 3) continue;
-                if (cstate[c] == 1) cstate[c] = 2;
-                const double ec = kSOR * kDebye * sqrt(e2[c] / (double)I.cl_nsites[c]);
-                bool stop = false;
-                if (!std::isfinite(ec)) {
-                    stop = true;
-                } else if (ec < I.prm.target_epsilon) {
-                    cconv[c] = 1;
-                    stop = true;
-                } else if (cur[c] < ec || its[c] >= I.prm.max_iterations) {
-                    stop = true;
-                }
-                cur[c] = ec;
-                ++its[c];
-                if (stop) {
-                    cstate[c] = 3;
-                    --active;
-                }
-            }
-        }
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_cstate.p, cstate.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_cl_conv.p, cconv.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_cl_cur.p, cur.data(), sizeof(double) * ncl, cudaMemcpyHostToDevice, st));
+        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_cl_its.p, 0, sizeof(int) * ncl, st));
+        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_rounds.p, 0, sizeof(int), st));
+        mbpol_status gs = cluster_solver_graph(I, nmol, wblocks, bufs[0], bufs[1], bufs[2], switch_eps);
+        if (gs) return gs;
+        prof_begin(st, K_ELEC_INDUCED);
+        MBPOL_CUDA_OK(cudaGraphLaunch(I.cl_exec, st));
+        prof_end(st, K_ELEC_INDUCED);
+        int rounds = 0;
+        MBPOL_CUDA_OK(cudaMemcpyAsync(its.data(), I.d_cl_its.p, sizeof(int) * ncl, cudaMemcpyDeviceToHost, st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(cconv.data(), I.d_cl_conv.p, sizeof(int) * ncl, cudaMemcpyDeviceToHost, st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(cur.data(), I.d_cl_cur.p, sizeof(double) * ncl, cudaMemcpyDeviceToHost, st));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(&rounds, I.d_rounds.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+        for (int r = 0; r < 2 * rounds; ++r) count_launch();  // field + control kernels per iteration
         I.cl_iters = its;
-        I.cl_conv = cconv;
+        I.cl_conv.assign(cconv.begin(), cconv.end());
         it = 0;
         conv = true;
         current = 0.0;
@@ -2333,6 +2433,12 @@ mbpol_status ElecEngine::set_clusters(const int* cluster_of_particle, int ncl, d
     MBPOL_CUDA_OK(cudaMemcpy(I.d_mcl.p, mcl.data(), sizeof(int) * (size_t)I.nmol, cudaMemcpyHostToDevice));
     MBPOL_CUDA_OK(I.d_cstate.ensure(ncl));
     MBPOL_CUDA_OK(I.d_eps2c.ensure(ncl));
+    MBPOL_CUDA_OK(I.d_cl_nsites.ensure(ncl));
+    MBPOL_CUDA_OK(I.d_cl_its.ensure(ncl));
+    MBPOL_CUDA_OK(I.d_cl_conv.ensure(ncl));
+    MBPOL_CUDA_OK(I.d_cl_cur.ensure(ncl));
+    MBPOL_CUDA_OK(I.d_rounds.ensure(1));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_cl_nsites.p, I.cl_nsites.data(), sizeof(int) * (size_t)ncl, cudaMemcpyHostToDevice));
     I.ncl = ncl;
     I.cl_sink.wcl = I.d_mcl.p;
     I.cl_sink.e = cluster_energy;
