@@ -93,8 +93,10 @@ struct WaterTerm {
     int rule = 0;
     std::vector<int4> waters;
     DevBuf d_waters;
-    // batched clusters: cluster of each water of this term's list
-    DevBuf d_cluster;
+    // batched clusters: cluster of each water of this term's list, the
+    // waters of each cluster (ascending) and their offsets
+    DevBuf d_cluster, d_cl_members, d_cl_start;
+    CandidateSet cl_candidates;
     int max_cluster = 0;
 };
 
@@ -128,6 +130,7 @@ struct mbpol_context {
     // FP32 O positions for the neighbour prefilter; lists built by one
     // shared pass for the two-body, three-body and dispersion terms
     DevBuf opos;
+    DevBuf cells;  // cell binning scratch of the O-O lists
     bool shared_lists = false;
     // batched independent clusters (cluster of every particle)
     int ncl = 0;
@@ -189,8 +192,17 @@ mbpol_status check_box(const mbpol_context* ctx, double cutoff) {
     return MBPOL_OK;
 }
 
-const int* term_clusters(const mbpol_context* ctx, const WaterTerm& t) {
-    return ctx->ncl > 0 ? t.d_cluster.as<int>() : nullptr;
+const CandidateSet* term_clusters(const mbpol_context* ctx, const WaterTerm& t) {
+    return ctx->ncl > 0 ? &t.cl_candidates : nullptr;
+}
+
+// Device scratch for the cell binning of n waters at list radius r (null
+// when the box has no cell grid, or on allocation failure: then all pairs
+// are scanned).
+int* cell_scratch(mbpol_context* ctx, int n, const Box& box, double r) {
+    const size_t ints = cell_scratch_ints(n, box, r);
+    if (ints == 0 || ctx->cells.ensure(sizeof(int) * ints) != cudaSuccess) return nullptr;
+    return ctx->cells.as<int>();
 }
 
 ClusterSink term_sink(mbpol_context* ctx, const WaterTerm& t, int term) {
@@ -226,6 +238,18 @@ mbpol_status apply_clusters(mbpol_context* ctx) {
             for (int c = 0; c < ncl; ++c) t->max_cluster = std::max(t->max_cluster, count[c]);
             MBPOL_CUDA_OK(t->d_cluster.ensure(sizeof(int) * (size_t)nw));
             MBPOL_CUDA_OK(cudaMemcpy(t->d_cluster.p, wc.data(), sizeof(int) * nw, cudaMemcpyHostToDevice));
+            std::vector<int> members, start;
+            cluster_members(wc.data(), nw, ncl, members, start);
+            MBPOL_CUDA_OK(t->d_cl_members.ensure(sizeof(int) * members.size()));
+            MBPOL_CUDA_OK(t->d_cl_start.ensure(sizeof(int) * start.size()));
+            MBPOL_CUDA_OK(cudaMemcpy(t->d_cl_members.p, members.data(), sizeof(int) * members.size(),
+                                     cudaMemcpyHostToDevice));
+            MBPOL_CUDA_OK(cudaMemcpy(t->d_cl_start.p, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+            t->cl_candidates = CandidateSet();
+            t->cl_candidates.mode = 1;
+            t->cl_candidates.members = t->d_cl_members.as<int>();
+            t->cl_candidates.start = t->d_cl_start.as<int>();
+            t->cl_candidates.group = t->d_cluster.as<int>();
         }
     }
     ctx->cap_full_d = 0;
@@ -248,9 +272,11 @@ mbpol_status twobody_list(mbpol_context* ctx, const Box& box, double rc, int* np
         if (ctx->cap2 == 0) ctx->cap2 = nw * 24 + 64;
         MBPOL_CUDA_OK(ctx->p2.ensure(sizeof(int2) * (size_t)ctx->cap2));
         MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
-        launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(),
-                             box, -1.0, -1.0, rc, 0, 0, nullptr, nullptr, nullptr, nullptr, ctx->p2.as<int2>(),
-                             ctx->cap2, cnt, cnt + 1, term_clusters(ctx, t));
+        mbpol_status ns = launch_mol_neighbors(
+            ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(), box, -1.0, -1.0, rc,
+            0, 0, nullptr, nullptr, nullptr, nullptr, ctx->p2.as<int2>(), ctx->cap2, cnt, cnt + 1,
+            term_clusters(ctx, t), cell_scratch(ctx, nw, box, rc));
+        if (ns) return ns;
         int h[2];
         MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
@@ -312,19 +338,21 @@ mbpol_status threebody_list(mbpol_context* ctx, const Box& box, double rc, int* 
         MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
         if (!complete) {
             MBPOL_CUDA_OK(ctx->lower3.ensure(sizeof(int) * (size_t)nw * ctx->cap_lower3));
-            launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
-                                 ctx->opos.as<float4>(), box, -1.0, rc, -1.0, 0, ctx->cap_lower3, nullptr, nullptr,
-                                 ctx->lower3.as<int>(), ctx->nlower3.as<int>(), nullptr, 0, cnt, cnt + 1,
-                                 term_clusters(ctx, t));
+            mbpol_status ns = launch_mol_neighbors(
+                ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(), box, -1.0, rc,
+                -1.0, 0, ctx->cap_lower3, nullptr, nullptr, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), nullptr, 0,
+                cnt, cnt + 1, term_clusters(ctx, t), cell_scratch(ctx, nw, box, rc));
+            if (ns) return ns;
             launch_trimer_count(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
                                 ctx->count3.as<int>(), ctx->offs3.as<int>());
         } else {
             MBPOL_CUDA_OK(ctx->full3.ensure(sizeof(int) * (size_t)nw * ctx->cap_full3));
             MBPOL_CUDA_OK(ctx->nfull3.ensure(sizeof(int) * (size_t)nw));
-            launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
-                                 ctx->opos.as<float4>(), box, rc, -1.0, -1.0, ctx->cap_full3, 0, ctx->full3.as<int>(),
-                                 ctx->nfull3.as<int>(), nullptr, nullptr, nullptr, 0, cnt, cnt + 1,
-                                 term_clusters(ctx, t));
+            mbpol_status ns = launch_mol_neighbors(
+                ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(), box, rc, -1.0,
+                -1.0, ctx->cap_full3, 0, ctx->full3.as<int>(), ctx->nfull3.as<int>(), nullptr, nullptr, nullptr, 0, cnt,
+                cnt + 1, term_clusters(ctx, t), cell_scratch(ctx, nw, box, rc));
+            if (ns) return ns;
             launch_trimer_complete(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
                                    ctx->full3.as<int>(), ctx->nfull3.as<int>(), ctx->cap_full3,
                                    ctx->count3.as<int>(), ctx->offs3.as<int>(), 0, nullptr, false);
@@ -406,10 +434,11 @@ mbpol_status dispersion_list(mbpol_context* ctx, const Box& box) {
         MBPOL_CUDA_OK(ctx->full_d.ensure(sizeof(int) * (size_t)nw * ctx->cap_full_d));
         MBPOL_CUDA_OK(ctx->nfull_d.ensure(sizeof(int) * (size_t)nw));
         MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
-        launch_mol_neighbors(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(),
-                             box, rlist, -1.0, -1.0, ctx->cap_full_d, 0, ctx->full_d.as<int>(),
-                             ctx->nfull_d.as<int>(), nullptr, nullptr, nullptr, 0, cnt, cnt + 1,
-                             term_clusters(ctx, t));
+        mbpol_status ns = launch_mol_neighbors(
+            ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(), box, rlist, -1.0,
+            -1.0, ctx->cap_full_d, 0, ctx->full_d.as<int>(), ctx->nfull_d.as<int>(), nullptr, nullptr, nullptr, 0, cnt,
+            cnt + 1, term_clusters(ctx, t), cell_scratch(ctx, nw, box, rlist));
+        if (ns) return ns;
         int h[2];
         MBPOL_CUDA_OK(cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
@@ -488,10 +517,13 @@ mbpol_status build_shared_lists(mbpol_context* ctx, unsigned mask, bool* built) 
         MBPOL_CUDA_OK(ctx->lower3.ensure(sizeof(int) * (size_t)nw * ctx->cap_lower3));
         MBPOL_CUDA_OK(ctx->full_d.ensure(sizeof(int) * (size_t)nw * ctx->cap_full_d));
         MBPOL_CUDA_OK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), ctx->st));
-        launch_mol_neighbors(ctx->st, nw, t2.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(),
-                             box, dispersion_list_radius(td), t3.cutoff, t2.cutoff, ctx->cap_full_d,
-                             ctx->cap_lower3, ctx->full_d.as<int>(), ctx->nfull_d.as<int>(), ctx->lower3.as<int>(),
-                             ctx->nlower3.as<int>(), ctx->p2.as<int2>(), ctx->cap2, cnt, cnt + 1, nullptr);
+        const double rmax = std::max(dispersion_list_radius(td), std::max(t3.cutoff, t2.cutoff));
+        mbpol_status ns = launch_mol_neighbors(
+            ctx->st, nw, t2.d_waters.as<int4>(), ctx->d_pos.as<double>(), ctx->opos.as<float4>(), box,
+            dispersion_list_radius(td), t3.cutoff, t2.cutoff, ctx->cap_full_d, ctx->cap_lower3, ctx->full_d.as<int>(),
+            ctx->nfull_d.as<int>(), ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->p2.as<int2>(), ctx->cap2, cnt,
+            cnt + 1, nullptr, cell_scratch(ctx, nw, box, rmax));
+        if (ns) return ns;
         launch_trimer_count(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
                             ctx->count3.as<int>(), ctx->offs3.as<int>());
         int h[3];

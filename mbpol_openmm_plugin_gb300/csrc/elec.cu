@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "elec.h"
+#include "mbpol_kernels.h"
 #include "guess.h"
 
 namespace mbpol {
@@ -42,6 +43,10 @@ constexpr double kSqrtPi = 1.77245385091;
 constexpr double kElectric = 138.9354558456;  // reference _electric (:52)
 constexpr double kDebye = 48.033324;          // reference _debye (:60)
 constexpr double kSOR = 0.55;                 // reference _polarSOR (:59)
+
+// largest distance of a molecule's sites from its first site that the cell
+// grid of the electrostatics list allows for (water: O-H ~0.1 nm)
+constexpr float kCellReach = 0.15f;
 
 struct ElecConst {
     float thole[5];       // TCC, TCD, TDD, TDDOH, TDDHH
@@ -409,7 +414,7 @@ __global__ void elec_prepare_kernel(int nmol, const double* __restrict__ pos, in
 __global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, const float4* __restrict__ opos,
                                       int periodic, double rc, const float* __restrict__ reach, int cap,
                                       int* __restrict__ nb, float* __restrict__ nbd, int* __restrict__ nnb,
-                                      int* __restrict__ overflow, const int* __restrict__ cluster) {
+                                      int* __restrict__ overflow, const CandidateSet cs) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= nmol) return;
@@ -418,13 +423,14 @@ __global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, 
     const float4 fi = opos[i];
     const float ai = fmaxf(fabsf(fi.x), fmaxf(fabsf(fi.y), fabsf(fi.z)));
     const float rci = (float)rc + reach[i];
-    const int ci = cluster ? cluster[i] : 0;
+    // cells are sized for molecules whose sites lie within kCellReach of
+    // their first site; a larger one makes the host scan all pairs instead
+    if (cs.mode == 2 && lane == 0 && reach[i] > kCellReach) atomicOr(overflow, 2);
     int n = 0;
-    for (int base = 0; base < nmol; base += 32) {
-        const int j = base + lane;
+    for_candidates(cs, nmol, i, lane, [&](const int j) {
         bool in = false;
         double dx = 0, dy = 0, dz = 0;
-        if (j < nmol && j != i && (!cluster || cluster[j] == ci)) {
+        if (j >= 0 && j != i) {
             // FP32 prefilter, padded well above its error (2^-24 of each
             // coordinate): the list only has to contain every molecule pair
             // with a site pair within the cutoff, which the pair kernels test
@@ -461,7 +467,7 @@ __global__ void elec_neighbors_kernel(int nmol, const double* __restrict__ pos, 
             }
         }
         n += __popc(msk);
-    }
+    });
     if (lane == 0) {
         nnb[i] = n;
         if (n > cap) atomicOr(overflow, 1);
@@ -1703,6 +1709,11 @@ struct ElecImpl {
     std::vector<int> cl_nsites, cl_iters;
     std::vector<char> cl_conv;
     DBuf<int> d_mcl, d_cstate;  // d_cstate: per-cluster solver stage (0 plain, 1 anchoring, 2 anchored, 3 done)
+    // neighbour candidates: molecules of each cluster (batched clusters), and
+    // the cell-binning scratch of periodic boxes
+    DBuf<int> d_cl_members, d_cl_start, d_cells;
+    CandidateSet cl_candidates;
+    bool cells_ok = true;
     DBuf<double> d_eps2c;
     // the batched solver as one graph launch: a while node whose body runs
     // two iterations (ping-pong buffers), each followed by the control kernel
@@ -2034,18 +2045,40 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     // neighbour list
     const double rcut = I.pme ? I.prm.cutoff : 1e30;
     if (I.cap == 0) I.cap = I.pme ? 256 : ((((I.ncl > 0 ? I.max_cl_mol : nmol)) + 31) / 32) * 32;
+    // candidates: the molecule's cluster, or the cells around it (edges >=
+    // the cutoff plus twice kCellReach), else all molecules
+    CandidateSet cands;
+    Box cbox = box;
+    cbox.periodic = box.periodic && I.pme;
+    if (I.ncl > 0) {
+        cands = I.cl_candidates;
+    } else if (I.cells_ok) {
+        const double rcell = rcut + 2.0 * kCellReach;
+        const size_t ints = cell_scratch_ints(nmol, cbox, rcell);
+        if (ints) {
+            MBPOL_CUDA_OK(I.d_cells.ensure(ints));
+            mbpol_status cs = launch_cell_binning(st, nmol, I.d_opos.p, cbox, rcell, I.d_cells.p, &cands);
+            if (cs) return cs;
+        }
+    }
     for (int attempt = 0;; ++attempt) {
         MBPOL_CUDA_OK(I.d_nb.ensure((size_t)nmol * I.cap));
         MBPOL_CUDA_OK(I.d_nbd.ensure((size_t)nmol * I.cap * 3));
         MBPOL_CUDA_OK(cudaMemsetAsync(I.d_flags.p, 0, sizeof(int), st));
         count_launch();
         elec_neighbors_kernel<<<(nmol * 32 + 127) / 128, 128, 0, st>>>(
-            nmol, pos, I.d_opos.p, box.periodic && I.pme, rcut, I.d_reach.p, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p,
-            I.d_flags.p, I.ncl > 0 ? I.d_mcl.p : nullptr);
+            nmol, pos, I.d_opos.p, cbox.periodic, rcut, I.d_reach.p, I.cap, I.d_nb.p, I.d_nbd.p, I.d_nnb.p,
+            I.d_flags.p, cands);
         int ovf = 0;
         MBPOL_CUDA_OK(cudaMemcpyAsync(&ovf, I.d_flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(st));
         if (!ovf) break;
+        if (ovf & 2) {
+            // a molecule reaches beyond kCellReach: scan all pairs from now on
+            I.cells_ok = false;
+            cands = CandidateSet();
+            continue;
+        }
         if (attempt > 6) return mbpol_fail(MBPOL_ERR_CAPACITY, "electrostatics neighbour capacity");
         I.cap *= 2;
     }
@@ -2439,6 +2472,17 @@ mbpol_status ElecEngine::set_clusters(const int* cluster_of_particle, int ncl, d
     MBPOL_CUDA_OK(I.d_cl_cur.ensure(ncl));
     MBPOL_CUDA_OK(I.d_rounds.ensure(1));
     MBPOL_CUDA_OK(cudaMemcpy(I.d_cl_nsites.p, I.cl_nsites.data(), sizeof(int) * (size_t)ncl, cudaMemcpyHostToDevice));
+    std::vector<int> members, start;
+    cluster_members(mcl.data(), I.nmol, ncl, members, start);
+    MBPOL_CUDA_OK(I.d_cl_members.ensure(members.size()));
+    MBPOL_CUDA_OK(I.d_cl_start.ensure(start.size()));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_cl_members.p, members.data(), sizeof(int) * members.size(), cudaMemcpyHostToDevice));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_cl_start.p, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+    I.cl_candidates = CandidateSet();
+    I.cl_candidates.mode = 1;
+    I.cl_candidates.members = I.d_cl_members.p;
+    I.cl_candidates.start = I.d_cl_start.p;
+    I.cl_candidates.group = I.d_mcl.p;
     I.ncl = ncl;
     I.cl_sink.wcl = I.d_mcl.p;
     I.cl_sink.e = cluster_energy;

@@ -62,6 +62,60 @@ __device__ __forceinline__ void add_force(double* __restrict__ f, int i, double 
     atomicAdd(f + 3 * i + 2, fz);
 }
 
+// Neighbour candidates of molecule i when a warp builds i's list: all
+// molecules (mode 0), the members of i's cluster (mode 1; batched
+// independent clusters), or the molecules of the 27 cells around i's cell
+// (mode 2; periodic boxes with at least 3 cells per dimension whose edges
+// are at least the largest list radius).  Members are ascending within a
+// cluster and within a cell, and cells are visited in a fixed order, so the
+// lists are the same from run to run.
+struct CandidateSet {
+    int mode = 0;
+    const int* members = nullptr;  // molecules grouped by cluster / cell
+    const int* start = nullptr;    // offset of each group in members, and the end
+    const int* group = nullptr;    // cluster / cell of each molecule
+    int nc[3] = {0, 0, 0};         // cells per dimension (mode 2)
+};
+
+// body(j) is called by all 32 lanes of the warp together for each chunk of
+// candidates; j = -1 on lanes without one (and j may equal i).
+template <class F>
+__device__ __forceinline__ void for_candidates(const CandidateSet& cs, int n, int i, int lane, F&& body) {
+    if (cs.mode == 0) {
+        for (int base = 0; base < n; base += 32) body(base + lane < n ? base + lane : -1);
+        return;
+    }
+    if (cs.mode == 1) {
+        const int g = cs.group[i];
+        const int s0 = cs.start[g], s1 = cs.start[g + 1];
+        for (int k = s0; k < s1; k += 32) body(k + lane < s1 ? cs.members[k + lane] : -1);
+        return;
+    }
+    const int c = cs.group[i];
+    const int cz = c % cs.nc[2], cy = (c / cs.nc[2]) % cs.nc[1], cx = c / (cs.nc[1] * cs.nc[2]);
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+                const int x = (cx + dx + cs.nc[0]) % cs.nc[0];
+                const int y = (cy + dy + cs.nc[1]) % cs.nc[1];
+                const int z = (cz + dz + cs.nc[2]) % cs.nc[2];
+                const int cc = (x * cs.nc[1] + y) * cs.nc[2] + z;
+                const int s0 = cs.start[cc], s1 = cs.start[cc + 1];
+                for (int k = s0; k < s1; k += 32) body(k + lane < s1 ? cs.members[k + lane] : -1);
+            }
+}
+
+// Cells per dimension of a periodic box for list radius r (edges >= r plus a
+// margin for the FP32 positions the cells are assigned from); false when a
+// dimension would have fewer than 3 cells (or the box is not periodic).
+bool cell_grid_dims(const Box& box, double r, int nc[3]);
+// Device ints the cell binning of n molecules needs (0 when no grid).
+size_t cell_scratch_ints(int n, const Box& box, double r);
+// launch_cell_binning (mbpol_kernels.h) bins n molecules by their FP32 O
+// positions (wrapped into the box) into that grid, in scratch of
+// cell_scratch_ints ints, and gives the mode-2 candidate set over it (mode 0
+// when there is no grid).
+
 // Block-wide FP64 sum, then one atomic per block into *out.
 // Per-cluster energies for batched independent clusters: a unit's energy is
 // also added to e[cluster_of_water[w] * stride] (e offset by the term).

@@ -1,8 +1,14 @@
 // Host-side launchers of the MB-pol kernels (internal to the library).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/mbpol_gb300.h"
 #include "mbpol_internal.cuh"
 #include "poly_tables.h"
+
+mbpol_status mbpol_fail_cuda(cudaError_t e, const char* what);
 
 namespace mbpol {
 
@@ -33,10 +39,17 @@ void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, const PolyNode* l2,
 
 // neighbor.cu
 // opos: scratch of nw float4 (FP32 O positions for the distance prefilter)
-void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, float4* opos, Box box,
-                          double r_full, double r_3b, double r_2b, int cap_full, int cap_lower, int* full,
-                          int* nfull, int* lower, int* nlower, int2* pairs, int cap_pairs, int* npairs,
-                          int* overflow, const int* cluster);
+// clusters: mode-1 candidate set of batched clusters, or null; cell_scratch:
+// cell_scratch_ints(nw, box, max radius) device ints (may be null: no cells)
+mbpol_status launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, float4* opos,
+                                  Box box, double r_full, double r_3b, double r_2b, int cap_full, int cap_lower,
+                                  int* full, int* nfull, int* lower, int* nlower, int2* pairs, int cap_pairs,
+                                  int* npairs, int* overflow, const CandidateSet* clusters, int* cell_scratch);
+mbpol_status launch_cell_binning(cudaStream_t st, int n, const float4* opos, const Box& box, double r, int* scratch,
+                                 CandidateSet* out);
+// members of each cluster, ascending, and their offsets (host: molecule
+// cluster indices in [0, ncl)); the mode-1 candidate set's arrays
+void cluster_members(const int* cluster_of, int n, int ncl, std::vector<int>& members, std::vector<int>& start);
 void launch_trimer_count(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower, int* count,
                          int* offs);
 void launch_trimer_fill(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower,

@@ -1,8 +1,11 @@
 // O-O neighbour structures for the many-body terms.
 //
-//  * mol_neighbors_kernel: one warp per water i scans all waters j (tiles of
-//    32, ballot-compacted appends; distances prefiltered in FP32 and settled
-//    in FP64 near each threshold) and records
+//  * mol_neighbors_kernel: one warp per water i scans the candidate waters j
+//    (tiles of 32, ballot-compacted appends; distances prefiltered in FP32
+//    and settled in FP64 near each threshold): the 27 cells around i's cell
+//    in periodic boxes with at least 3 cells per dimension (cell binning by
+//    counting sort, members ascending within a cell), the waters of i's
+//    cluster for batched clusters, else all waters.  It records
 //      - full[i][*]   j != i with d(i,j) <= r_full   (electrostatics, dispersion)
 //      - lower[i][*]  j <  i with d(i,j) <= r_3b     (three-body chain rule)
 //      - pairs        (i,j), j > i, d <= r_2b        (two-body half list)
@@ -80,7 +83,7 @@ __global__ void mol_neighbors_kernel(int nw, const int4* __restrict__ waters, co
                                      double r_2b2, int cap_full, int cap_lower, int* __restrict__ full,
                                      int* __restrict__ nfull, int* __restrict__ lower, int* __restrict__ nlower,
                                      int2* __restrict__ pairs, int cap_pairs, int* __restrict__ npairs,
-                                     int* __restrict__ overflow, const int* __restrict__ cluster) {
+                                     int* __restrict__ overflow, const CandidateSet cs) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nw) return;
@@ -92,12 +95,10 @@ __global__ void mol_neighbors_kernel(int nw, const int4* __restrict__ waters, co
     const float ix = (float)box.inv[0], iy = (float)box.inv[1], iz = (float)box.inv[2];
     const float rf = full ? (float)sqrt(r_full2) : 0.f, r3 = lower ? (float)sqrt(r_3b2) : 0.f,
                 r2 = pairs ? (float)sqrt(r_2b2) : 0.f;
-    const int ci = cluster ? cluster[i] : 0;
     int nf = 0, nl = 0;
-    for (int base = 0; base < nw; base += 32) {
-        const int j = base + lane;
+    for_candidates(cs, nw, i, lane, [&](const int j) {
         bool in_full = false, in_lower = false, in_pair = false;
-        if (j < nw && j != i && (!cluster || cluster[j] == ci)) {
+        if (j >= 0 && j != i) {
             const float4 fj = opos[j];
             float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
             if (box.periodic) {
@@ -135,7 +136,7 @@ __global__ void mol_neighbors_kernel(int nw, const int4* __restrict__ waters, co
                 if (slot < cap_pairs) pairs[slot] = make_int2(i, j);
             }
         }
-    }
+    });
     if (lane == 0) {
         if (nfull) nfull[i] = nf;
         if (nlower) nlower[i] = nl;
@@ -229,19 +230,122 @@ __global__ void trimer_complete_kernel(int nw, const int4* __restrict__ waters, 
     if (count) count[v] = cnt;
 }
 
-void launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, float4* opos, Box box,
-                          double r_full, double r_3b, double r_2b, int cap_full, int cap_lower, int* full,
-                          int* nfull, int* lower, int* nlower, int2* pairs, int cap_pairs, int* npairs,
-                          int* overflow, const int* cluster) {
-    if (nw <= 0) return;
+// ---------------------------------------------------------------- cells
+bool cell_grid_dims(const Box& box, double r, int nc[3]) {
+    if (!box.periodic || !(r > 0.0)) return false;
+    const double edge = r * (1.0 + 1e-5) + 1e-4;
+    long total = 1;
+    for (int d = 0; d < 3; ++d) {
+        nc[d] = (int)floor(box.L[d] / edge);
+        if (nc[d] < 3) return false;
+        if (nc[d] > 1024) nc[d] = 1024;  // larger cells stay correct
+        total *= nc[d];
+    }
+    return total <= (1L << 27);
+}
+
+size_t cell_scratch_ints(int n, const Box& box, double r) {
+    int nc[3];
+    if (n <= 0 || !cell_grid_dims(box, r, nc)) return 0;
+    return 3 * (size_t)n + 3 * ((size_t)nc[0] * nc[1] * nc[2] + 1);
+}
+
+__global__ void cell_assign_kernel(int n, const float4* __restrict__ opos, float sx, float sy, float sz, int ncx,
+                                   int ncy, int ncz, int* __restrict__ cell_of, int* __restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = opos[i];
+    const int x = min(max((int)(p.x * sx), 0), ncx - 1);
+    const int y = min(max((int)(p.y * sy), 0), ncy - 1);
+    const int z = min(max((int)(p.z * sz), 0), ncz - 1);
+    const int c = (x * ncy + y) * ncz + z;
+    cell_of[i] = c;
+    atomicAdd(count + c, 1);
+}
+
+__global__ void cell_scatter_kernel(int n, const int* __restrict__ cell_of, const int* __restrict__ start,
+                                    int* __restrict__ fill, int* __restrict__ unsorted) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cell_of[i];
+    unsorted[start[c] + atomicAdd(fill + c, 1)] = i;
+}
+
+// each molecule's place in its cell is its rank among the cell's members,
+// so members are ascending whatever order the scatter's atomics took
+__global__ void cell_rank_kernel(int n, const int* __restrict__ cell_of, const int* __restrict__ start,
+                                 const int* __restrict__ unsorted, int* __restrict__ sorted) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cell_of[i];
+    int r = 0;
+    for (int k = start[c]; k < start[c + 1]; ++k) r += unsorted[k] < i;
+    sorted[start[c] + r] = i;
+}
+
+mbpol_status launch_cell_binning(cudaStream_t st, int n, const float4* opos, const Box& box, double r, int* scratch,
+                                 CandidateSet* out) {
+    *out = CandidateSet();
+    int nc[3];
+    if (n <= 0 || !scratch || !cell_grid_dims(box, r, nc)) return MBPOL_OK;
+    const int ncell = nc[0] * nc[1] * nc[2];
+    int* cell_of = scratch;
+    int* unsorted = cell_of + n;
+    int* sorted = unsorted + n;
+    int* count = sorted + n;
+    int* start = count + (ncell + 1);
+    int* fill = start + (ncell + 1);
+    MBPOL_CUDA_OK(cudaMemsetAsync(count, 0, sizeof(int) * (size_t)(ncell + 1), st));
+    MBPOL_CUDA_OK(cudaMemsetAsync(fill, 0, sizeof(int) * (size_t)(ncell + 1), st));
+    const int blocks = (n + 255) / 256;
+    count_launch();
+    cell_assign_kernel<<<blocks, 256, 0, st>>>(n, opos, (float)(nc[0] * box.inv[0]), (float)(nc[1] * box.inv[1]),
+                                               (float)(nc[2] * box.inv[2]), nc[0], nc[1], nc[2], cell_of, count);
+    count_launch();
+    scan_kernel<<<1, 1024, 0, st>>>(ncell, count, start);
+    count_launch();
+    cell_scatter_kernel<<<blocks, 256, 0, st>>>(n, cell_of, start, fill, unsorted);
+    count_launch();
+    cell_rank_kernel<<<blocks, 256, 0, st>>>(n, cell_of, start, unsorted, sorted);
+    out->mode = 2;
+    out->members = sorted;
+    out->start = start;
+    out->group = cell_of;
+    for (int d = 0; d < 3; ++d) out->nc[d] = nc[d];
+    return MBPOL_OK;
+}
+
+void cluster_members(const int* cluster_of, int n, int ncl, std::vector<int>& members, std::vector<int>& start) {
+    start.assign((size_t)ncl + 1, 0);
+    for (int i = 0; i < n; ++i) ++start[(size_t)cluster_of[i] + 1];
+    for (int c = 0; c < ncl; ++c) start[(size_t)c + 1] += start[(size_t)c];
+    members.assign((size_t)n, 0);
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int i = 0; i < n; ++i) members[(size_t)fill[(size_t)cluster_of[i]]++] = i;
+}
+
+mbpol_status launch_mol_neighbors(cudaStream_t st, int nw, const int4* waters, const double* pos, float4* opos,
+                                  Box box, double r_full, double r_3b, double r_2b, int cap_full, int cap_lower,
+                                  int* full, int* nfull, int* lower, int* nlower, int2* pairs, int cap_pairs,
+                                  int* npairs, int* overflow, const CandidateSet* clusters, int* cell_scratch) {
+    if (nw <= 0) return MBPOL_OK;
     count_launch();
     o_positions_kernel<<<(nw + 127) / 128, 128, 0, st>>>(nw, waters, pos, box, opos);
+    CandidateSet cs;
+    if (clusters) {
+        cs = *clusters;
+    } else {
+        const double r = fmax(r_full, fmax(r_3b, r_2b));
+        mbpol_status s = launch_cell_binning(st, nw, opos, box, r, cell_scratch, &cs);
+        if (s) return s;
+    }
     const int threads = 256;
     const int blocks = (nw * 32 + threads - 1) / threads;
     count_launch();
     mol_neighbors_kernel<<<blocks, threads, 0, st>>>(nw, waters, pos, opos, box, r_full * r_full, r_3b * r_3b,
                                                      r_2b * r_2b, cap_full, cap_lower, full, nfull, lower, nlower,
-                                                     pairs, cap_pairs, npairs, overflow, cluster);
+                                                     pairs, cap_pairs, npairs, overflow, cs);
+    return MBPOL_OK;
 }
 
 void launch_trimer_count(cudaStream_t st, int nw, const int* lower, const int* nlower, int cap_lower, int* count,
