@@ -524,17 +524,17 @@ __device__ __forceinline__ void bspline5(float w, float th[5], float d1[5], floa
 // so the grid, and the solver, are deterministic.  FP32 atomics left a
 // run-to-run noise floor of ~1e-8 D in the dipole convergence measure.
 constexpr double kGridFix = 1099511627776.0;  // 2^40
+// One warp per site: lane l < 25 takes the grid column (x, y) = (l / 5,
+// l % 5) of the 5x5x5 stencil and its 5 z points.  The fixed-point atomics
+// make the grid independent of the order of the updates; v * 2^40 is exact
+// in FP32 and converts to the same integer as in FP64.
+constexpr float kGridFixF = 1099511627776.0f;  // 2^40
 __global__ void pme_spread_kernel(int nsite, int mode, const float* __restrict__ q, const float* __restrict__ mu,
                                   const int* __restrict__ gidx, const float* __restrict__ gfrac,
                                   unsigned long long* __restrict__ grid) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsite) return;
-    float tx[5], ty[5], tz[5], dx[5], dy[5], dz[5], sx[5];
-    bspline5(gfrac[3 * i], tx, dx, sx);
-    bspline5(gfrac[3 * i + 1], ty, dy, sx);
-    bspline5(gfrac[3 * i + 2], tz, dz, sx);
-    const int Nx = c_el.grid[0], Ny = c_el.grid[1], Nz = c_el.grid[2];
-    const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= nsite || lane >= 25) return;
     float c0 = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
     if (mode == 0) {
         c0 = q[i];
@@ -545,24 +545,39 @@ __global__ void pme_spread_kernel(int nsite, int mode, const float* __restrict__
         mz = mu[3 * i + 2] * c_el.scale[2];
         if (mx == 0.f && my == 0.f && mz == 0.f) return;
     }
-    for (int a = 0; a < 5; ++a) {
-        int x = gx + a;
-        if (x >= Nx) x -= Nx;
-        for (int b = 0; b < 5; ++b) {
-            int y = gy + b;
-            if (y >= Ny) y -= Ny;
-            const float txy = tx[a] * ty[b];
-            const float wA = mode == 0 ? c0 * txy : mx * dx[a] * ty[b];
-            const float wB = mode == 0 ? 0.f : my * tx[a] * dy[b];
-            const float wC = mode == 0 ? 0.f : mz * txy;
-            unsigned long long* row = grid + ((size_t)x * Ny + y) * Nz;
-            for (int c = 0; c < 5; ++c) {
-                int z = gz + c;
-                if (z >= Nz) z -= Nz;
-                const float v = mode == 0 ? wA * tz[c] : (wA + wB) * tz[c] + wC * dz[c];
-                atomicAdd(row + z, (unsigned long long)__double2ll_rn((double)v * kGridFix));
-            }
+    float tx[5], ty[5], tz[5], dx[5], dy[5], dz[5], sx[5];
+    bspline5(gfrac[3 * i], tx, dx, sx);
+    bspline5(gfrac[3 * i + 1], ty, dy, sx);
+    bspline5(gfrac[3 * i + 2], tz, dz, sx);
+    const int Nx = c_el.grid[0], Ny = c_el.grid[1], Nz = c_el.grid[2];
+    const int a = lane / 5, b = lane % 5;
+    int x = gidx[3 * i] + a, y = gidx[3 * i + 1] + b;
+    if (x >= Nx) x -= Nx;
+    if (y >= Ny) y -= Ny;
+    const int gz = gidx[3 * i + 2];
+    float txa = 0.f, dxa = 0.f, tyb = 0.f, dyb = 0.f;
+    #pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        if (k == a) {
+            txa = tx[k];
+            dxa = dx[k];
         }
+        if (k == b) {
+            tyb = ty[k];
+            dyb = dy[k];
+        }
+    }
+    const float txy = txa * tyb;
+    const float wA = mode == 0 ? c0 * txy : mx * dxa * tyb;
+    const float wB = mode == 0 ? 0.f : my * txa * dyb;
+    const float wC = mode == 0 ? 0.f : mz * txy;
+    unsigned long long* row = grid + ((size_t)x * Ny + y) * Nz;
+    #pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        int z = gz + c;
+        if (z >= Nz) z -= Nz;
+        const float v = mode == 0 ? wA * tz[c] : (wA + wB) * tz[c] + wC * dz[c];
+        atomicAdd(row + z, (unsigned long long)__float2ll_rn(v * kGridFixF));
     }
 }
 
@@ -616,49 +631,71 @@ __global__ void pme_scale_kernel(long total, cufftComplex* __restrict__ g, const
 
 // Gather phi and derivatives (grid units) at every site: ncomp 4 (phi, dx,
 // dy, dz) or 10 (+ xx, yy, zz, xy, xz, yz).
+// One warp per site: lane l < 25 sums its grid column (x, y) = (l / 5, l % 5)
+// over z with the spline weights; the 25 partial sums of each component are
+// added by a fixed shuffle tree (the same order every call).
 __global__ void pme_gather_kernel(int nsite, int ncomp, const float* __restrict__ grid,
                                   const int* __restrict__ gidx, const float* __restrict__ gfrac,
                                   float* __restrict__ phi) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (i >= nsite) return;
-    float tx[5], ty[5], tz[5], dx[5], dy[5], dz[5], ex[5], ey[5], ez[5];
-    bspline5(gfrac[3 * i], tx, dx, ex);
-    bspline5(gfrac[3 * i + 1], ty, dy, ey);
-    bspline5(gfrac[3 * i + 2], tz, dz, ez);
-    const int Nx = c_el.grid[0], Ny = c_el.grid[1], Nz = c_el.grid[2];
-    const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
     float p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int a = 0; a < 5; ++a) {
-        int x = gx + a;
+    if (lane < 25) {
+        float tx[5], ty[5], tz[5], dx[5], dy[5], dz[5], ex[5], ey[5], ez[5];
+        bspline5(gfrac[3 * i], tx, dx, ex);
+        bspline5(gfrac[3 * i + 1], ty, dy, ey);
+        bspline5(gfrac[3 * i + 2], tz, dz, ez);
+        const int Nx = c_el.grid[0], Ny = c_el.grid[1], Nz = c_el.grid[2];
+        const int a = lane / 5, b = lane % 5;
+        int x = gidx[3 * i] + a, y = gidx[3 * i + 1] + b;
         if (x >= Nx) x -= Nx;
-        for (int b = 0; b < 5; ++b) {
-            int y = gy + b;
-            if (y >= Ny) y -= Ny;
-            const float* row = grid + ((size_t)x * Ny + y) * Nz;
-            float t0 = 0.f, t1 = 0.f, t2 = 0.f;
-            for (int c = 0; c < 5; ++c) {
-                int z = gz + c;
-                if (z >= Nz) z -= Nz;
-                const float v = row[z];
-                t0 += v * tz[c];
-                t1 += v * dz[c];
-                t2 += v * ez[c];
+        if (y >= Ny) y -= Ny;
+        const int gz = gidx[3 * i + 2];
+        float txa = 0.f, dxa = 0.f, exa = 0.f, tyb = 0.f, dyb = 0.f, eyb = 0.f;
+        #pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            if (k == a) {
+                txa = tx[k];
+                dxa = dx[k];
+                exa = ex[k];
             }
-            p[0] += tx[a] * ty[b] * t0;
-            p[1] += dx[a] * ty[b] * t0;
-            p[2] += tx[a] * dy[b] * t0;
-            p[3] += tx[a] * ty[b] * t1;
-            if (ncomp == 10) {
-                p[4] += ex[a] * ty[b] * t0;
-                p[5] += tx[a] * ey[b] * t0;
-                p[6] += tx[a] * ty[b] * t2;
-                p[7] += dx[a] * dy[b] * t0;
-                p[8] += dx[a] * ty[b] * t1;
-                p[9] += tx[a] * dy[b] * t1;
+            if (k == b) {
+                tyb = ty[k];
+                dyb = dy[k];
+                eyb = ey[k];
             }
         }
+        const float* row = grid + ((size_t)x * Ny + y) * Nz;
+        float t0 = 0.f, t1 = 0.f, t2 = 0.f;
+        #pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            int z = gz + c;
+            if (z >= Nz) z -= Nz;
+            const float v = row[z];
+            t0 += v * tz[c];
+            t1 += v * dz[c];
+            t2 += v * ez[c];
+        }
+        p[0] = txa * tyb * t0;
+        p[1] = dxa * tyb * t0;
+        p[2] = txa * dyb * t0;
+        p[3] = txa * tyb * t1;
+        p[4] = exa * tyb * t0;
+        p[5] = txa * eyb * t0;
+        p[6] = txa * tyb * t2;
+        p[7] = dxa * dyb * t0;
+        p[8] = dxa * tyb * t1;
+        p[9] = txa * dyb * t1;
     }
-    for (int k = 0; k < ncomp; ++k) phi[(size_t)ncomp * i + k] = p[k];
+    #pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        if (k >= ncomp) break;
+        float v = p[k];
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) phi[(size_t)ncomp * i + k] = v;
+    }
 }
 
 // ------------------------------------------------------------ pair kernels
@@ -1906,7 +1943,7 @@ static mbpol_status pme_setup(ElecImpl& I, const Box& box) {
 // spread (fixed point) and convert to the FP32 grid d_grid
 static cudaError_t pme_spread(ElecImpl& I, cudaStream_t st, int mode, const float* mu, int n, size_t nreal) {
     count_launch();
-    pme_spread_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, mode, I.d_q.p, mu, I.d_gidx.p, I.d_gfrac.p, I.d_gridq.p);
+    pme_spread_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(n, mode, I.d_q.p, mu, I.d_gidx.p, I.d_gfrac.p, I.d_gridq.p);
     count_launch();
     pme_fix_to_float_kernel<<<(int)std::min<size_t>((nreal + 255) / 256, 152 * 16), 256, 0, st>>>(
         (long)nreal, I.d_gridq.p, I.d_grid.p);
@@ -2095,7 +2132,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         if (s) return s;
         MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_gridfix.p, I.d_grid.p, sizeof(float) * nreal, cudaMemcpyDeviceToDevice, st));
         count_launch();
-        pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 10, I.d_gridfix.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_fix.p);
+        pme_gather_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(n, 10, I.d_gridfix.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_fix.p);
         prof_begin(st, K_ELEC_FIXED);
         count_launch();
         fixed_field_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
@@ -2227,7 +2264,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
             mbpol_status s = pme_convolve(I, I.st2, box);
             if (s) return s;
             count_launch();
-            pme_gather_kernel<<<(n + 127) / 128, 128, 0, I.st2>>>(n, 4, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p,
+            pme_gather_kernel<<<(n * 32 + 127) / 128, 128, 0, I.st2>>>(n, 4, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p,
                                                                    I.d_phi_mu.p);
             prof_end(I.st2, K_ELEC_PME);
             MBPOL_CUDA_OK(cudaEventRecord(I.ev_pme, I.st2));
@@ -2308,7 +2345,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         mbpol_status s = pme_convolve(I, st, box);
         if (s) return s;
         count_launch();
-        pme_gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, 10, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
+        pme_gather_kernel<<<(n * 32 + 127) / 128, 128, 0, st>>>(n, 10, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p, I.d_phi_mu.p);
         prof_begin(st, K_ELEC_FORCES);
         count_launch();
         energy_force_kernel<true><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_q.p, I.d_dq.p, I.d_damp.p, I.d_type.p,
