@@ -75,9 +75,10 @@ typedef struct {
     double thole[5];             /* TCC, TCD, TDD, TDDOH, TDDHH; default {0.4,0.4,0.055,0.626,0.055} */
     int include_charge_redistribution; /* default 1                                              */
     int guess;                   /* initial dipole guess: 0 direct (alpha*E_fixed, as the reference),
-                                    1 previous call's dipoles, 2 learned (network prediction plus the
-                                    extrapolated residual of the last solves; 3 without a network),
-                                    3 polynomial extrapolation of the last (up to) four solves */
+                                    1 previous call's dipoles, 2 learned (the network on a cold start,
+                                    then polynomial extrapolation, then the learned linear predictor
+                                    once MBPOL_GUESS_HISTORY solves exist), 3 polynomial extrapolation
+                                    of the last (up to) four solves */
     int pme_fixed_field;         /* MBPOL_PME_FIELD_REFERENCE (default) or MBPOL_PME_FIELD_CONSISTENT;
                                     no reference counterpart, see the enum below */
 } mbpol_electrostatics_params;
@@ -246,6 +247,17 @@ mbpol_status mbpol_guess_descriptors(mbpol_context* ctx, float* out);
  * data X [n][64] (raw inputs), T [n][9] (targets), without an update. */
 mbpol_status mbpol_guess_loss_grad(mbpol_context* ctx, const float* X, const float* T, int n, double* loss,
                                    float* grad, float* Y);
+/* The learned linear predictor used by guess 2 once MBPOL_GUESS_HISTORY
+ * solves exist: mu = X0 + sum_j a_j nabla^j X0 over backward differences of
+ * orders 1..MBPOL_GUESS_PREDICTOR_ORDER, a_j refitted by least squares on
+ * the last MBPOL_GUESS_PREDICTOR_WINDOW steps before every solve.  On host
+ * history [MBPOL_GUESS_HISTORY][n3] (newest first): the coefficients
+ * [MBPOL_GUESS_PREDICTOR_ORDER] and the prediction [n3]. */
+#define MBPOL_GUESS_PREDICTOR_ORDER 7
+#define MBPOL_GUESS_PREDICTOR_WINDOW 4
+#define MBPOL_GUESS_HISTORY 12
+mbpol_status mbpol_guess_fit_predictor(mbpol_context* ctx, const double* history, int n3, double* coef,
+                                       double* prediction);
 
 /* ---- Two-body term without device allocation ---------------------------
  * No reference counterpart: the reference evaluates the two-body term only

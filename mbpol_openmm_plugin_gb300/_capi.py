@@ -29,10 +29,12 @@ EXPORTED = [
     "mbpol_profile_enable", "mbpol_profile_read", "mbpol_launch_count", "mbpol_status_string", "mbpol_last_error",
     "mbpol_twobody_dimers_noalloc",
     "mbpol_guess_collect", "mbpol_guess_num_samples", "mbpol_guess_train", "mbpol_guess_get_params",
-    "mbpol_guess_set_params", "mbpol_guess_descriptors", "mbpol_guess_loss_grad",
+    "mbpol_guess_set_params", "mbpol_guess_descriptors", "mbpol_guess_loss_grad", "mbpol_guess_fit_predictor",
     "mbpol_set_clusters", "mbpol_get_cluster_results",
 ]
 GUESS_BLOCK_FLOATS = 9033  # MBPOL_GUESS_BLOCK_FLOATS
+GUESS_PREDICTOR_ORDER = 7  # MBPOL_GUESS_PREDICTOR_ORDER
+GUESS_HISTORY = 12  # MBPOL_GUESS_HISTORY
 GUESS_PARAMS = 8905
 GUESS_INPUTS = 64
 NOALLOC_MAX_DIMERS = 65536  # MBPOL_NOALLOC_MAX_DIMERS
@@ -95,6 +97,7 @@ def load(path=None):
         "mbpol_get_induced_dipoles": (I, [P, P, ctypes.POINTER(I), ctypes.POINTER(D)]),
         "mbpol_get_counts": (I, [P, P]),
         "mbpol_get_electrostatic_potential": (I, [P, I, P, P]),
+        "mbpol_guess_fit_predictor": (I, [P, P, I, P, P]),
         "mbpol_profile_enable": (I, [I]),
         "mbpol_launch_count": (ctypes.c_ulonglong, []),
         "mbpol_profile_read": (I, [I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_long)]),

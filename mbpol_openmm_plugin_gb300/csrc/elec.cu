@@ -1438,8 +1438,8 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
 // iterations on the 4096-water box at 0.2 fs (22.1 per step, against 26.9
 // for L = 3, 23.4 for L = 5 and 25.3 for L = 6; least-squares cubic fits
 // through 5-8 solves: 23.2-27.5).
-constexpr int kHist = 4;         // solves kept
-constexpr int kExtrapolate = 4;  // largest L used
+constexpr int kHist = guess::kPredHistory;  // solves kept (the learned predictor's history)
+constexpr int kExtrapolate = 4;             // largest L used
 struct HistRing {
     const double* r[kHist];
     double c[kHist];
@@ -1738,6 +1738,7 @@ struct ElecImpl {
     // dipoles of the last (up to) kHist converged solves, a ring of 3n
     // planes (FP64)
     DBuf<double> d_hist;
+    DBuf<double> d_pred;  // the predictor's partial sums, then its coefficients
     int hist_levels = 0, hist_head = 0;
     bool evaluated = false;  // neighbour list, offsets and dipoles are current
     // batched independent clusters (NoCutoff): molecule -> cluster, per-
@@ -1766,6 +1767,11 @@ struct ElecImpl {
     // second stream for the solver's PME passes, ordered by two events
     cudaStream_t st2 = nullptr;
     cudaEvent_t ev_in = nullptr, ev_pme = nullptr;
+    // the learned predictor is fitted on the second stream right after a
+    // solve enters the history (beside the energy/force kernel); the next
+    // evaluation waits for ev_fit before it applies the coefficients
+    cudaEvent_t ev_hist = nullptr, ev_fit = nullptr;
+    bool pred_fitted = false;
 
     // polarisable site pairs within the cutoff, counted in both directions by
     // the fixed-field kernel
@@ -1782,6 +1788,8 @@ struct ElecImpl {
             cufftDestroy(plan_b);
         }
         if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_hist) cudaEventDestroy(ev_hist);
+        if (ev_fit) cudaEventDestroy(ev_fit);
         if (ev_pme) cudaEventDestroy(ev_pme);
         if (st2) cudaStreamDestroy(st2);
     }
@@ -1871,6 +1879,8 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
         MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&I.st2, cudaStreamNonBlocking));
         MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_in, cudaEventDisableTiming));
         MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_pme, cudaEventDisableTiming));
+        MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_hist, cudaEventDisableTiming));
+        MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_fit, cudaEventDisableTiming));
     }
     MBPOL_CUDA_OK(I.d_mguess.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_hist.ensure(3 * kHist * (size_t)n));
@@ -2161,13 +2171,27 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
     const bool learned = I.prm.guess == 2 && I.net.ready() && (I.K == 3 || I.K == 4);
     const bool history = I.prm.guess >= 2;
     const bool extrapolate = history && (I.hist_levels >= 2 || (I.prm.guess == 3 && I.hist_levels >= 1));
+    // guess 2 with a full history: the learned linear predictor, refitted on
+    // the last steps (predictor.cu)
+    const bool predictor = I.prm.guess == 2 && I.hist_levels >= guess::kPredHistory;
     if (learned && !extrapolate) {
         MBPOL_CUDA_OK(I.net.descriptors(st, nmol, I.K, I.d_off.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, box.L,
                                         box.periodic && I.pme, I.d_E0.p));
         MBPOL_CUDA_OK(I.net.predict(st, nmol, I.K, I.d_mguess.p));
     }
     const bool used_net = learned && !extrapolate;
-    if (extrapolate) {
+    if (predictor) {
+        PredictorRing ring{};
+        for (int k = 0; k < guess::kPredHistory; ++k)
+            ring.r[k] = I.d_hist.p + 3 * (size_t)n * ((I.hist_head + kHist - k) % kHist);
+        MBPOL_CUDA_OK(I.d_pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredOrder));
+        double* coef = I.d_pred.p + (size_t)predictor_partial_blocks() * guess::kPredStats;
+        if (I.pred_fitted)
+            MBPOL_CUDA_OK(cudaStreamWaitEvent(st, I.ev_fit, 0));  // fitted after the last solve
+        else
+            MBPOL_CUDA_OK(predictor_fit(st, 3 * n, ring, I.d_pred.p, coef));
+        MBPOL_CUDA_OK(predictor_apply(st, 3 * n, ring, coef, I.d_mud.p, I.d_mu0.p));
+    } else if (extrapolate) {
         const size_t plane = 3 * (size_t)n;
         HistRing h{};
         h.levels = std::min(I.hist_levels, kExtrapolate);
@@ -2331,6 +2355,23 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
                                           sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, st));
             I.hist_levels = std::min(I.hist_levels + 1, kHist);
         }
+        // the next evaluation's predictor, fitted now beside the energy and
+        // forces (the ring is not written again before that evaluation's
+        // start, which waits for the fit)
+        I.pred_fitted = false;
+        if (history && I.prm.guess == 2 && I.hist_levels >= guess::kPredHistory) {
+            PredictorRing ring{};
+            for (int k = 0; k < guess::kPredHistory; ++k)
+                ring.r[k] = I.d_hist.p + 3 * (size_t)n * ((I.hist_head + kHist - k) % kHist);
+            MBPOL_CUDA_OK(
+                I.d_pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredOrder));
+            MBPOL_CUDA_OK(cudaEventRecord(I.ev_hist, st));
+            MBPOL_CUDA_OK(cudaStreamWaitEvent(I.st2, I.ev_hist, 0));
+            MBPOL_CUDA_OK(predictor_fit(I.st2, 3 * n, ring, I.d_pred.p,
+                                        I.d_pred.p + (size_t)predictor_partial_blocks() * guess::kPredStats));
+            MBPOL_CUDA_OK(cudaEventRecord(I.ev_fit, I.st2));
+            I.pred_fitted = true;
+        }
         if (used_net)
             MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mprev.p, I.d_mguess.p, sizeof(float) * 3 * (size_t)n,
                                           cudaMemcpyDeviceToDevice, st));
@@ -2399,6 +2440,31 @@ mbpol_status ElecEngine::potential(cudaStream_t st, const double* pos, int npts,
     MBPOL_CUDA_OK(cudaGetLastError());
     MBPOL_CUDA_OK(cudaMemcpyAsync(potential, I.d_pot.p, sizeof(double) * npts, cudaMemcpyDeviceToHost, st));
     MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::guess_fit_predictor(cudaStream_t st, const double* history, int n3, double* coef,
+                                             double* prediction) {
+    ElecImpl& I = *impl_;
+    if (!history || n3 <= 0) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad argument");
+    DBuf<double> h, pred, out;
+    DBuf<float> outf;
+    MBPOL_CUDA_OK(h.ensure((size_t)guess::kPredHistory * n3));
+    MBPOL_CUDA_OK(pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredOrder));
+    MBPOL_CUDA_OK(out.ensure(n3));
+    MBPOL_CUDA_OK(outf.ensure(n3));
+    MBPOL_CUDA_OK(cudaMemcpyAsync(h.p, history, sizeof(double) * guess::kPredHistory * (size_t)n3,
+                                  cudaMemcpyHostToDevice, st));
+    PredictorRing ring{};
+    for (int k = 0; k < guess::kPredHistory; ++k) ring.r[k] = h.p + (size_t)k * n3;
+    double* c = pred.p + (size_t)predictor_partial_blocks() * guess::kPredStats;
+    MBPOL_CUDA_OK(predictor_fit(st, n3, ring, pred.p, c));
+    MBPOL_CUDA_OK(predictor_apply(st, n3, ring, c, out.p, outf.p));
+    if (coef) MBPOL_CUDA_OK(cudaMemcpyAsync(coef, c, sizeof(double) * guess::kPredOrder, cudaMemcpyDeviceToHost, st));
+    if (prediction)
+        MBPOL_CUDA_OK(cudaMemcpyAsync(prediction, out.p, sizeof(double) * (size_t)n3, cudaMemcpyDeviceToHost, st));
+    MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+    (void)I;
     return MBPOL_OK;
 }
 

@@ -41,6 +41,10 @@ public:
     mbpol_status guess_loss_grad(cudaStream_t st, const float* X, const float* T, int n, double* loss, float* grad,
                                  float* Y);
     long guess_num_samples() const;
+    // the learned linear predictor on host history [kPredHistory][n3]
+    // (newest first): its coefficients [kPredOrder] and prediction [n3]
+    mbpol_status guess_fit_predictor(cudaStream_t st, const double* history, int n3, double* coef,
+                                     double* prediction);
     // batched independent clusters (NoCutoff only): cluster of every
     // particle; per-cluster electrostatic energies go to
     // cluster_energy[c * stride] (device).  ncl = 0 turns batching off.

@@ -1,8 +1,12 @@
-// Learned initial guess for the induced dipoles: per-water descriptors, a
-// 48-64-64-9 SiLU network with BF16 weights on the tensor cores (mma.sync,
-// FP32 accumulation), its training (forward, backward, Adam) on the GPU, and
-// the guess mu0 = mu_prev + (m_now - m_prev) (m the network's lab-frame
-// prediction), or m_now when there is no previous solve.
+// Learned initial guess for the induced dipoles.
+//  (1) Cold starts: per-water descriptors, a 64-64-64-9 SiLU network with
+//      BF16 weights on the tensor cores (mma.sync, FP32 accumulation), its
+//      training (forward, backward, Adam) on the GPU, and the guess
+//      mu0 = mu_prev + (m_now - m_prev) (m the network's lab-frame
+//      prediction), or m_now when there is no previous solve.
+//  (2) Trajectories: a linear predictor over the last solves whose
+//      coefficients are refitted by least squares before every solve
+//      (predictor.cu).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -28,7 +32,25 @@ constexpr int kParams = kB3 + kOut;  // 8905
 // input standardisation (mean[64], 1/std[64])
 constexpr int kBlockFloats = kParams + 2 * kIn;
 constexpr float kOutScale = 1e-3f;  // e nm per network output unit
+// learned linear predictor over the history of solves (predictor.cu)
+constexpr int kPredOrder = 7;    // backward differences in the model
+constexpr int kPredWindow = 4;   // past steps it is fitted on
+constexpr int kPredHistory = kPredOrder + 1 + kPredWindow;  // solves it needs
+constexpr int kPredStats = kPredOrder * (kPredOrder + 1) / 2 + kPredOrder;
 }  // namespace guess
+
+// Converged dipoles [3n] of past solves, r[0] the newest.
+struct PredictorRing {
+    const double* r[guess::kPredHistory];
+};
+// Fits the predictor's coefficients (d_coef[kPredOrder], device) on the
+// history; d_partials holds predictor_partial_blocks() x kPredStats doubles.
+int predictor_partial_blocks();
+cudaError_t predictor_fit(cudaStream_t st, int n3, const PredictorRing& ring, double* d_partials, double* d_coef);
+// Starting dipoles from the history and the coefficients (FP64 state and
+// its FP32 copy).
+cudaError_t predictor_apply(cudaStream_t st, int n3, const PredictorRing& ring, const double* d_coef, double* mu_d,
+                            float* mu_f);
 
 struct GuessBuffers;
 

@@ -189,3 +189,53 @@ def init_params(seed):
         "b3": np.zeros(NOUT),
     }
     return {k: v.astype(np.float32) for k, v in p.items()}
+
+
+# ------------------------------------------------- learned linear predictor
+PRED_ORDER = 7    # backward differences in the model
+PRED_WINDOW = 4   # past steps it is fitted on
+PRED_HISTORY = PRED_ORDER + 1 + PRED_WINDOW
+
+
+def backward_differences(x):
+    """nabla^1 .. nabla^J of the sequence x[0 .. J] (x[0] the newest; rows
+    of any trailing shape), by repeated differencing."""
+    t = np.array(x, dtype=np.float64)
+    out = []
+    for j in range(1, t.shape[0]):
+        t = t[:-1] - t[1:]
+        out.append(t[0])
+    return np.array(out)
+
+
+def predictor_fit(history, stride=None):
+    """Coefficients a_1..a_J of mu = X0 + sum_j a_j nabla^j X0, fitted by
+    least squares on the last PRED_WINDOW steps: X_w - X_{w+1} from the
+    differences at X_{w+1}.  history: [PRED_HISTORY, n3], newest first.
+    Normal equations scaled by their diagonal, vanishing columns left out,
+    ridge 1e-6 on the scaled system, as the CUDA kernel (which solves the
+    scaled system in FP32; here FP64)."""
+    h = np.asarray(history, np.float64)
+    if stride is None:  # the CUDA kernel's subsample: about 8k components
+        stride = h.shape[1] // 8192 if h.shape[1] > 8192 else 1
+    h = h[:, ::stride]
+    J = PRED_ORDER
+    G = np.zeros((J, J))
+    b = np.zeros(J)
+    for w in range(PRED_WINDOW):
+        D = backward_differences(h[w + 1:w + 2 + J])  # [J, m]
+        y = h[w] - h[w + 1]
+        G += D @ D.T
+        b += D @ y
+    gmax = np.max(np.diag(G))
+    keep = (np.diag(G) > 1e-24 * gmax) & (np.diag(G) > 0)
+    sc = np.where(keep, 1.0 / np.sqrt(np.where(keep, np.diag(G), 1.0)), 0.0)
+    Gs = np.where(np.outer(keep, keep), G * np.outer(sc, sc), np.eye(J)) + 1e-6 * np.eye(J)
+    bs = np.where(keep, b * sc, 0.0)
+    return np.linalg.solve(Gs, bs) * sc
+
+
+def predictor_apply(history, a):
+    h = np.asarray(history, np.float64)
+    D = backward_differences(h[:PRED_ORDER + 1])
+    return h[0] + np.tensordot(a, D, axes=1)

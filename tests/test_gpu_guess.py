@@ -166,3 +166,69 @@ def test_trained_network_cuts_solver_iterations():
           "previous-step %.1f, learned %.1f" % (loss, cold["alphaE"], cold["learned"], md["plain"], md["learned"]))
     assert cold["learned"] <= cold["alphaE"] - 3
     assert md["learned"] <= md["plain"] - 5
+
+
+def test_predictor_fit_matches_oracle():
+    """The learned linear predictor's least-squares fit and prediction
+    (predictor.cu: FP64 normal equations, FP32 solve of the scaled system)
+    against the oracle (FP64 throughout) on 12 consecutive converged solves
+    of an MD run of the 4096-water box (tests/golden/make_dipole_history.py):
+    coefficients within 2e-3, the predicted change within 1e-3 of its size,
+    and a prediction closer to the next solve than the 4-point polynomial
+    extrapolation."""
+    import ctypes
+    from mbpol_openmm_plugin_gb300 import _capi
+    lib = _capi.load()
+    d = np.load(os.path.join(GOLDEN, "elec_cluster14_seed0.npz"))
+    ctx = _context(d["positions"], None)
+    f = np.load(os.path.join(GOLDEN, "dipole_history_box4096.npz"))
+    hist = np.ascontiguousarray(f["history"])
+    n3 = hist.shape[1]
+    coef = np.zeros(dg.PRED_ORDER)
+    pred = np.zeros(n3)
+    _capi.check(lib.mbpol_guess_fit_predictor(ctx._h, _capi.ptr(hist), n3, _capi.ptr(coef), _capi.ptr(pred)))
+    a_ref = dg.predictor_fit(hist)
+    p_ref = dg.predictor_apply(hist, a_ref)
+    p4 = dg.predictor_apply(hist, np.array([1.0, 1.0, 1.0, 0, 0, 0, 0]))
+    err, err4 = np.sqrt(np.mean((pred - f["next"]) ** 2)), np.sqrt(np.mean((p4 - f["next"]) ** 2))
+    print("coefficients", np.round(coef, 6), "oracle", np.round(a_ref, 6), "| error %.3e, 4-point %.3e" % (err, err4))
+    assert np.max(np.abs(coef - a_ref)) <= 2e-3 * max(1.0, np.max(np.abs(a_ref)))
+    step = np.max(np.abs(p_ref - hist[0]))
+    assert np.max(np.abs(pred - p_ref)) <= 1e-3 * step
+    assert err < err4
+
+
+def test_learned_predictor_cuts_md_iterations():
+    """MD on the 256-water PME box from the same state: guess 2 (without a
+    network: extrapolation, then the learned predictor once 12 solves exist)
+    against guess 3 (4-point polynomial extrapolation), iterations per step
+    over steps 16-40 at the same 1e-8 D threshold."""
+    import ctypes
+    from mbpol_openmm_plugin_gb300 import _capi
+    lib = _capi.load()
+    ws = systems.workload("box256", 2)
+    alpha, grid = mb.pme_parameters(ws.box, 0.9, 1e-5)
+    masses = None
+    its = {}
+    for name, guess in (("extrapolation", 3), ("learned", 2)):
+        s = mb.create_mbpol_system(ws, target_epsilon=1e-8, ewald_alpha=alpha, pme_grid=grid, guess=guess)
+        c = mb.Context(s)
+        c.setPositions(ws.positions)
+        c._build()
+        masses = np.ascontiguousarray(s.masses, np.float64)
+        rng = np.random.default_rng(4)
+        vel = np.zeros((masses.size, 3))
+        live = masses > 0
+        vel[live] = rng.normal(size=(int(live.sum()), 3)) * np.sqrt(2.494 / masses[live])[:, None]
+        box = np.ascontiguousarray(ws.box, np.float64)
+        _capi.check(lib.mbpol_set_positions(c._h, _capi.ptr(np.ascontiguousarray(ws.positions)), _capi.ptr(box)))
+        _capi.check(lib.mbpol_set_masses(c._h, _capi.ptr(masses)))
+        _capi.check(lib.mbpol_set_velocities(c._h, _capi.ptr(vel)))
+        ms, it, en = ctypes.c_double(), ctypes.c_long(), np.zeros(6)
+        _capi.check(lib.mbpol_md_run(c._h, 16, 0.0002, 0.0, 0.0, 0, ctypes.byref(ms), _capi.ptr(en),
+                                     ctypes.byref(it)))
+        _capi.check(lib.mbpol_md_run(c._h, 24, 0.0002, 0.0, 0.0, 0, ctypes.byref(ms), _capi.ptr(en),
+                                     ctypes.byref(it)))
+        its[name] = it.value / 24.0
+    print("MD iterations/step: extrapolation %.2f, learned predictor %.2f" % (its["extrapolation"], its["learned"]))
+    assert its["learned"] <= its["extrapolation"] - 0.5

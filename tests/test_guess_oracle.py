@@ -88,3 +88,37 @@ def test_bf16_network_close_to_exact():
     assert np.linalg.norm(y1 - y0) <= 2e-2 * np.linalg.norm(y0)
     for k in g0:
         assert np.linalg.norm(g1[k] - g0[k]) <= 5e-2 * np.linalg.norm(g0[k]), k
+
+
+def _oscillation_history(n3=600, steps=None, seed=0, noise=0.0):
+    """Superposed slow oscillations sampled at unit steps, newest first."""
+    steps = steps or dg.PRED_HISTORY + 1
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=(4, n3)) * 1e-2
+    w = np.array([0.03, 0.05, 0.08, 0.13])
+    ph = rng.uniform(0, 2 * np.pi, size=(4, n3))
+    t = np.arange(steps)[::-1].astype(float)  # newest first
+    X = np.einsum("mn,tmn->tn", A, np.cos(w[None, :, None] * t[:, None, None] + ph[None]))
+    return X + noise * rng.normal(size=X.shape)
+
+
+def test_predictor_exact_on_polynomial_history():
+    """A cubic trajectory: the higher differences vanish, their columns are
+    left out, and the prediction is the cubic's continuation (to the 1e-6
+    ridge on the scaled normal equations)."""
+    t = np.arange(dg.PRED_HISTORY + 1)[::-1].astype(float)
+    c = np.random.default_rng(1).normal(size=(4, 50))
+    X = c[0] + np.outer(t, c[1]) + np.outer(t ** 2, c[2]) * 1e-2 + np.outer(t ** 3, c[3]) * 1e-4
+    a = dg.predictor_fit(X[1:])
+    p = dg.predictor_apply(X[1:], a)
+    assert np.max(np.abs(p - X[0])) <= 1e-6 * np.max(np.abs(X))
+
+
+def test_predictor_beats_polynomial_extrapolation():
+    """On smooth oscillations the fitted predictor is closer to the next
+    value than the 4-point polynomial extrapolation (its a = 1, 1, 1, 0...)."""
+    X = _oscillation_history()
+    hist = X[1:]
+    p = dg.predictor_apply(hist, dg.predictor_fit(hist))
+    p4 = dg.predictor_apply(hist, np.array([1.0, 1.0, 1.0, 0, 0, 0, 0]))
+    assert np.sqrt(np.mean((p - X[0]) ** 2)) < 0.5 * np.sqrt(np.mean((p4 - X[0]) ** 2))
