@@ -248,16 +248,20 @@ mbpol_status mbpol_guess_descriptors(mbpol_context* ctx, float* out);
 mbpol_status mbpol_guess_loss_grad(mbpol_context* ctx, const float* X, const float* T, int n, double* loss,
                                    float* grad, float* Y);
 /* The learned linear predictor used by guess 2 once MBPOL_GUESS_HISTORY
- * solves exist: mu = X0 + sum_j a_j nabla^j X0 over backward differences of
- * orders 1..MBPOL_GUESS_PREDICTOR_ORDER, a_j refitted by least squares on
- * the last MBPOL_GUESS_PREDICTOR_WINDOW steps before every solve.  On host
- * history [MBPOL_GUESS_HISTORY][n3] (newest first): the coefficients
+ * solves exist: mu = P(X) + g (F_new - P(F)), P(Y) = Y0 + sum_j a_j nabla^j Y0
+ * over backward differences of orders 1..MBPOL_GUESS_PREDICTOR_ORDER, F =
+ * alpha E0 (polarisability times permanent field) of each step, g =
+ * MBPOL_GUESS_FIELD_GAIN; the a are refitted on the dipoles by least squares
+ * over the last MBPOL_GUESS_PREDICTOR_WINDOW steps before every solve.  On
+ * host history [MBPOL_GUESS_HISTORY][n3] of dipoles and of alpha E0 (newest
+ * first) and alpha E0 of the new geometry [n3]: the coefficients
  * [MBPOL_GUESS_PREDICTOR_ORDER] and the prediction [n3]. */
+#define MBPOL_GUESS_FIELD_GAIN 2.4
 #define MBPOL_GUESS_PREDICTOR_ORDER 7
 #define MBPOL_GUESS_PREDICTOR_WINDOW 4
 #define MBPOL_GUESS_HISTORY 12
-mbpol_status mbpol_guess_fit_predictor(mbpol_context* ctx, const double* history, int n3, double* coef,
-                                       double* prediction);
+mbpol_status mbpol_guess_fit_predictor(mbpol_context* ctx, const double* history, const double* field,
+                                       const double* field_now, int n3, double* coef, double* prediction);
 
 /* ---- Two-body term without device allocation ---------------------------
  * No reference counterpart: the reference evaluates the two-body term only

@@ -97,7 +97,7 @@ def load(path=None):
         "mbpol_get_induced_dipoles": (I, [P, P, ctypes.POINTER(I), ctypes.POINTER(D)]),
         "mbpol_get_counts": (I, [P, P]),
         "mbpol_get_electrostatic_potential": (I, [P, I, P, P]),
-        "mbpol_guess_fit_predictor": (I, [P, P, I, P, P]),
+        "mbpol_guess_fit_predictor": (I, [P, P, P, P, I, P, P]),
         "mbpol_profile_enable": (I, [I]),
         "mbpol_launch_count": (ctypes.c_ulonglong, []),
         "mbpol_profile_read": (I, [I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_long)]),

@@ -980,10 +980,10 @@ mbpol_status mbpol_guess_loss_grad(mbpol_context* ctx, const float* X, const flo
     return s ? s : ctx->elec->guess_loss_grad(ctx->st, X, T, n, loss, grad, Y);
 }
 
-mbpol_status mbpol_guess_fit_predictor(mbpol_context* ctx, const double* history, int n3, double* coef,
-                                       double* prediction) {
+mbpol_status mbpol_guess_fit_predictor(mbpol_context* ctx, const double* history, const double* field,
+                                       const double* field_now, int n3, double* coef, double* prediction) {
     mbpol_status s = need_elec(ctx);
-    return s ? s : ctx->elec->guess_fit_predictor(ctx->st, history, n3, coef, prediction);
+    return s ? s : ctx->elec->guess_fit_predictor(ctx->st, history, field, field_now, n3, coef, prediction);
 }
 
 // ---- batched independent clusters (no reference counterpart as one call)

@@ -1739,6 +1739,7 @@ struct ElecImpl {
     // planes (FP64)
     DBuf<double> d_hist;
     DBuf<double> d_pred;  // the predictor's partial sums, then its coefficients
+    DBuf<double> d_fhist, d_fnow;  // alpha E0 of the solves in d_hist, and of the current geometry
     int hist_levels = 0, hist_head = 0;
     bool evaluated = false;  // neighbour list, offsets and dipoles are current
     // batched independent clusters (NoCutoff): molecule -> cluster, per-
@@ -1884,6 +1885,8 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
     }
     MBPOL_CUDA_OK(I.d_mguess.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_hist.ensure(3 * kHist * (size_t)n));
+    MBPOL_CUDA_OK(I.d_fhist.ensure(3 * kHist * (size_t)n));
+    MBPOL_CUDA_OK(I.d_fnow.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_mprev.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms, kDmsCoef, sizeof(kDmsCoef)));
     MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms_idx, kDmsIdx, sizeof(kDmsIdx)));
@@ -2180,17 +2183,22 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         MBPOL_CUDA_OK(I.net.predict(st, nmol, I.K, I.d_mguess.p));
     }
     const bool used_net = learned && !extrapolate;
+    if (history) MBPOL_CUDA_OK(scaled_field(st, 3 * n, I.d_E0.p, I.d_pol.p, I.d_fnow.p));
     if (predictor) {
         PredictorRing ring{};
-        for (int k = 0; k < guess::kPredHistory; ++k)
-            ring.r[k] = I.d_hist.p + 3 * (size_t)n * ((I.hist_head + kHist - k) % kHist);
-        MBPOL_CUDA_OK(I.d_pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredOrder));
+        for (int k = 0; k < guess::kPredHistory; ++k) {
+            const size_t slot = 3 * (size_t)n * ((I.hist_head + kHist - k) % kHist);
+            ring.r[k] = I.d_hist.p + slot;
+            ring.f[k] = I.d_fhist.p + slot;
+        }
+        MBPOL_CUDA_OK(
+            I.d_pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredRegressors));
         double* coef = I.d_pred.p + (size_t)predictor_partial_blocks() * guess::kPredStats;
         if (I.pred_fitted)
             MBPOL_CUDA_OK(cudaStreamWaitEvent(st, I.ev_fit, 0));  // fitted after the last solve
         else
             MBPOL_CUDA_OK(predictor_fit(st, 3 * n, ring, I.d_pred.p, coef));
-        MBPOL_CUDA_OK(predictor_apply(st, 3 * n, ring, coef, I.d_mud.p, I.d_mu0.p));
+        MBPOL_CUDA_OK(predictor_apply(st, 3 * n, ring, I.d_fnow.p, coef, I.d_mud.p, I.d_mu0.p));
     } else if (extrapolate) {
         const size_t plane = 3 * (size_t)n;
         HistRing h{};
@@ -2353,6 +2361,8 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
             I.hist_head = (I.hist_head + 1) % kHist;
             MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_hist.p + 3 * (size_t)n * I.hist_head, I.d_mud.p,
                                           sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+            MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_fhist.p + 3 * (size_t)n * I.hist_head, I.d_fnow.p,
+                                          sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, st));
             I.hist_levels = std::min(I.hist_levels + 1, kHist);
         }
         // the next evaluation's predictor, fitted now beside the energy and
@@ -2361,10 +2371,13 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         I.pred_fitted = false;
         if (history && I.prm.guess == 2 && I.hist_levels >= guess::kPredHistory) {
             PredictorRing ring{};
-            for (int k = 0; k < guess::kPredHistory; ++k)
-                ring.r[k] = I.d_hist.p + 3 * (size_t)n * ((I.hist_head + kHist - k) % kHist);
+            for (int k = 0; k < guess::kPredHistory; ++k) {
+                const size_t slot = 3 * (size_t)n * ((I.hist_head + kHist - k) % kHist);
+                ring.r[k] = I.d_hist.p + slot;
+                ring.f[k] = I.d_fhist.p + slot;
+            }
             MBPOL_CUDA_OK(
-                I.d_pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredOrder));
+                I.d_pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredRegressors));
             MBPOL_CUDA_OK(cudaEventRecord(I.ev_hist, st));
             MBPOL_CUDA_OK(cudaStreamWaitEvent(I.st2, I.ev_hist, 0));
             MBPOL_CUDA_OK(predictor_fit(I.st2, 3 * n, ring, I.d_pred.p,
@@ -2443,28 +2456,35 @@ mbpol_status ElecEngine::potential(cudaStream_t st, const double* pos, int npts,
     return MBPOL_OK;
 }
 
-mbpol_status ElecEngine::guess_fit_predictor(cudaStream_t st, const double* history, int n3, double* coef,
-                                             double* prediction) {
-    ElecImpl& I = *impl_;
-    if (!history || n3 <= 0) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad argument");
-    DBuf<double> h, pred, out;
+mbpol_status ElecEngine::guess_fit_predictor(cudaStream_t st, const double* history, const double* field,
+                                             const double* field_now, int n3, double* coef, double* prediction) {
+    if (!history || !field || !field_now || n3 <= 0) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad argument");
+    DBuf<double> h, fh, fn, pred, out;
     DBuf<float> outf;
-    MBPOL_CUDA_OK(h.ensure((size_t)guess::kPredHistory * n3));
-    MBPOL_CUDA_OK(pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredOrder));
+    const size_t hn = (size_t)guess::kPredHistory * n3;
+    MBPOL_CUDA_OK(h.ensure(hn));
+    MBPOL_CUDA_OK(fh.ensure(hn));
+    MBPOL_CUDA_OK(fn.ensure(n3));
+    MBPOL_CUDA_OK(pred.ensure((size_t)predictor_partial_blocks() * guess::kPredStats + guess::kPredRegressors));
     MBPOL_CUDA_OK(out.ensure(n3));
     MBPOL_CUDA_OK(outf.ensure(n3));
-    MBPOL_CUDA_OK(cudaMemcpyAsync(h.p, history, sizeof(double) * guess::kPredHistory * (size_t)n3,
-                                  cudaMemcpyHostToDevice, st));
+    MBPOL_CUDA_OK(cudaMemcpyAsync(h.p, history, sizeof(double) * hn, cudaMemcpyHostToDevice, st));
+    MBPOL_CUDA_OK(cudaMemcpyAsync(fh.p, field, sizeof(double) * hn, cudaMemcpyHostToDevice, st));
+    MBPOL_CUDA_OK(cudaMemcpyAsync(fn.p, field_now, sizeof(double) * (size_t)n3, cudaMemcpyHostToDevice, st));
     PredictorRing ring{};
-    for (int k = 0; k < guess::kPredHistory; ++k) ring.r[k] = h.p + (size_t)k * n3;
+    for (int k = 0; k < guess::kPredHistory; ++k) {
+        ring.r[k] = h.p + (size_t)k * n3;
+        ring.f[k] = fh.p + (size_t)k * n3;
+    }
     double* c = pred.p + (size_t)predictor_partial_blocks() * guess::kPredStats;
     MBPOL_CUDA_OK(predictor_fit(st, n3, ring, pred.p, c));
-    MBPOL_CUDA_OK(predictor_apply(st, n3, ring, c, out.p, outf.p));
-    if (coef) MBPOL_CUDA_OK(cudaMemcpyAsync(coef, c, sizeof(double) * guess::kPredOrder, cudaMemcpyDeviceToHost, st));
+    MBPOL_CUDA_OK(predictor_apply(st, n3, ring, fn.p, c, out.p, outf.p));
+    if (coef)
+        MBPOL_CUDA_OK(
+            cudaMemcpyAsync(coef, c, sizeof(double) * guess::kPredRegressors, cudaMemcpyDeviceToHost, st));
     if (prediction)
         MBPOL_CUDA_OK(cudaMemcpyAsync(prediction, out.p, sizeof(double) * (size_t)n3, cudaMemcpyDeviceToHost, st));
     MBPOL_CUDA_OK(cudaStreamSynchronize(st));
-    (void)I;
     return MBPOL_OK;
 }
 

@@ -42,9 +42,10 @@ public:
                                  float* Y);
     long guess_num_samples() const;
     // the learned linear predictor on host history [kPredHistory][n3]
-    // (newest first): its coefficients [kPredOrder] and prediction [n3]
-    mbpol_status guess_fit_predictor(cudaStream_t st, const double* history, int n3, double* coef,
-                                     double* prediction);
+    // (newest first) of dipoles and of alpha E0, with alpha E0 of the new
+    // geometry: its coefficients [kPredRegressors] and prediction [n3]
+    mbpol_status guess_fit_predictor(cudaStream_t st, const double* history, const double* field,
+                                     const double* field_now, int n3, double* coef, double* prediction);
     // batched independent clusters (NoCutoff only): cluster of every
     // particle; per-cluster electrostatic energies go to
     // cluster_energy[c * stride] (device).  ncl = 0 turns batching off.

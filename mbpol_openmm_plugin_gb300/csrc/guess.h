@@ -33,24 +33,35 @@ constexpr int kParams = kB3 + kOut;  // 8905
 constexpr int kBlockFloats = kParams + 2 * kIn;
 constexpr float kOutScale = 1e-3f;  // e nm per network output unit
 // learned linear predictor over the history of solves (predictor.cu)
-constexpr int kPredOrder = 7;    // backward differences in the model
+constexpr int kPredOrder = 7;    // backward differences of the dipoles in the model
+constexpr int kPredRegressors = kPredOrder;  // fitted coefficients
 constexpr int kPredWindow = 4;   // past steps it is fitted on
 constexpr int kPredHistory = kPredOrder + 1 + kPredWindow;  // solves it needs
-constexpr int kPredStats = kPredOrder * (kPredOrder + 1) / 2 + kPredOrder;
+constexpr int kPredStats = kPredRegressors * (kPredRegressors + 1) / 2 + kPredRegressors;
+// weight of the unpredicted permanent-field change: the mean response of
+// the induced dipoles to it, 1 / (1 - alpha T), for liquid water; the
+// 4096-water box at 0.2 fs gave 18.0, 16.8, 15.9, 15.7, 15.9 and 16.6
+// solver iterations per step for 1.0, 1.6, 2.0, 2.5, 2.8 and 3.2
+constexpr double kFieldGain = 2.4;
 }  // namespace guess
 
-// Converged dipoles [3n] of past solves, r[0] the newest.
+// Converged dipoles [3n] of past solves, r[0] the newest, and the
+// polarisability times the permanent field (alpha E0) of the same steps.
 struct PredictorRing {
     const double* r[guess::kPredHistory];
+    const double* f[guess::kPredHistory];
 };
-// Fits the predictor's coefficients (d_coef[kPredOrder], device) on the
-// history; d_partials holds predictor_partial_blocks() x kPredStats doubles.
+// Fits the predictor's coefficients (d_coef[kPredRegressors], device) on the
+// dipole history; d_partials holds predictor_partial_blocks() x kPredStats
+// doubles.
 int predictor_partial_blocks();
 cudaError_t predictor_fit(cudaStream_t st, int n3, const PredictorRing& ring, double* d_partials, double* d_coef);
-// Starting dipoles from the history and the coefficients (FP64 state and
-// its FP32 copy).
-cudaError_t predictor_apply(cudaStream_t st, int n3, const PredictorRing& ring, const double* d_coef, double* mu_d,
-                            float* mu_f);
+// Starting dipoles (FP64 state and its FP32 copy) from the history, the
+// coefficients and alpha E0 of the new geometry (f_now).
+cudaError_t predictor_apply(cudaStream_t st, int n3, const PredictorRing& ring, const double* f_now,
+                            const double* d_coef, double* mu_d, float* mu_f);
+// alpha E0 per dipole component, in FP64 (pol per site, E0 [sites][3]).
+cudaError_t scaled_field(cudaStream_t st, int n3, const float* E0, const float* pol, double* out);
 
 struct GuessBuffers;
 

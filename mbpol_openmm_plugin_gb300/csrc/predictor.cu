@@ -1,22 +1,31 @@
 // Learned linear predictor of the induced dipoles from the history of
 // converged solves (guess = 2 once the history is long enough).
 //
-// With X_0 the newest converged dipoles and X_k those k steps older, the
-// starting dipoles of the next solve are
-//     mu = X_0 + sum_{j=1..J} a_j nabla^j X_0,
-//     nabla^j X_b = sum_{i=0..j} (-1)^i C(j, i) X_{b+i}   (backward differences),
-// J = kPredOrder.  a_j = 1 for j <= 3 and 0 above is the 4-point polynomial
-// extrapolation; here the a_j are refitted before every solve by least
-// squares on the last kPredWindow steps of the trajectory: each of those
-// solves X_w (w = 0 .. W-1) is predicted from the solves before it,
+// With X_0 the newest converged dipoles, X_k those k steps older, F_k =
+// alpha E0 of the same steps (polarisability times permanent field) and
+// F_new that of the geometry about to be solved, the starting dipoles are
+//     mu = P(X) + g (F_new - P(F)),
+//     P(Y) = Y_0 + sum_{j=1..J} a_j nabla^j Y_0,
+//     nabla^j Y_b = sum_{i=0..j} (-1)^i C(j, i) Y_{b+i}   (backward differences),
+// J = kPredOrder.  a = (1, 1, 1, 0, ...) is the 4-point polynomial
+// extrapolation.  The a are refitted before every solve by least squares on
+// the last kPredWindow steps of the dipoles: each of those solves X_w
+// (w = 0 .. W-1) is predicted from the steps before it,
 //     minimise sum_w || X_w - X_{w+1} - sum_j a_j nabla^j X_{w+1} ||^2,
-// over (a subsample of) all dipole components.  The backward differences
-// are nearly orthogonal with geometrically falling norms, so the normal
-// equations, scaled by their diagonal, are well conditioned; they are
-// formed in FP64 (the high differences cancel to ~1e-10 of mu) with a
-// fixed-order reduction and solved by an FP32 Cholesky on the device.  Columns that
-// vanish (a history that is exactly polynomial) are left out; a system that
-// is not positive definite falls back to the polynomial coefficients.
+// over (a subsample of) all dipole components.  The second term feeds in
+// the part of the permanent field's change that the history does not
+// predict (the field of the new geometry is known before the solve), with
+// the weight g = kFieldGain, the mean response of the dipoles to it.  (A
+// fitted weight came out smaller and worse: the FP32 field's rounding
+// noise, amplified by the extrapolation, biases a least-squares weight
+// towards zero.)
+// The backward differences are nearly orthogonal with geometrically falling
+// norms, so the normal equations, scaled by their diagonal, are well
+// conditioned; they are formed in FP64 (the high differences cancel to
+// ~1e-10 of mu) with a fixed-order reduction and solved by an FP32 Cholesky
+// on the device.  Columns that vanish (a history that is exactly
+// polynomial) are left out; a system that is not positive definite falls
+// back to the polynomial coefficients.
 #include "guess.h"
 #include "mbpol_internal.cuh"
 
@@ -25,6 +34,7 @@ namespace mbpol {
 namespace {
 
 constexpr int kJ = guess::kPredOrder;
+constexpr int kR = guess::kPredRegressors;
 constexpr int kW = guess::kPredWindow;
 constexpr int kStats = guess::kPredStats;  // upper triangle of G, then b
 constexpr int kGramThreads = 128;
@@ -55,18 +65,18 @@ __global__ void __launch_bounds__(kGramThreads) predictor_gram_kernel(int n3, in
         for (int k = 0; k < guess::kPredHistory; ++k) x[k] = ring.r[k][e];
         #pragma unroll
         for (int w = 0; w < kW; ++w) {
-            double base[kJ + 1], d[kJ];
+            double base[kJ + 1], d[kR];
             #pragma unroll
             for (int i = 0; i <= kJ; ++i) base[i] = x[w + 1 + i];
             backward_differences(base, d);
             const double y = x[w] - x[w + 1];
             int k = 0;
             #pragma unroll
-            for (int i = 0; i < kJ; ++i)
+            for (int i = 0; i < kR; ++i)
                 #pragma unroll
-                for (int j = i; j < kJ; ++j) S[k++] += d[i] * d[j];
+                for (int j = i; j < kR; ++j) S[k++] += d[i] * d[j];
             #pragma unroll
-            for (int i = 0; i < kJ; ++i) S[k++] += d[i] * y;
+            for (int i = 0; i < kR; ++i) S[k++] += d[i] * y;
         }
     }
     // block sum in a fixed order: warps by shuffles, then warp 0 over warps
@@ -101,34 +111,34 @@ __global__ void predictor_solve_kernel(int nblocks, const double* __restrict__ p
     }
     __syncthreads();
     if (threadIdx.x != 0) return;
-    float G[kJ][kJ], b[kJ], sc[kJ];
-    bool keep[kJ];
+    float G[kR][kR], b[kR], sc[kR];
+    bool keep[kR];
     double gmax = 0.0;
     #pragma unroll
-    for (int i = 0; i < kJ; ++i) {
-        const int d = i * kJ - i * (i - 1) / 2;  // G[i][i] in the packed upper triangle
+    for (int i = 0; i < kR; ++i) {
+        const int d = i * kR - i * (i - 1) / 2;  // G[i][i] in the packed upper triangle
         gmax = fmax(gmax, S[d]);
     }
     // diagonal scaling; a column whose norm vanishes against the largest is
     // left out (its coefficient 0)
     #pragma unroll
-    for (int i = 0; i < kJ; ++i) {
-        const double gii = S[i * kJ - i * (i - 1) / 2];
+    for (int i = 0; i < kR; ++i) {
+        const double gii = S[i * kR - i * (i - 1) / 2];
         keep[i] = gii > 1e-24 * gmax && gii > 0.0;
         sc[i] = keep[i] ? rsqrtf((float)gii) : 0.f;
     }
     int k = 0;
     #pragma unroll
-    for (int i = 0; i < kJ; ++i)
+    for (int i = 0; i < kR; ++i)
         #pragma unroll
-        for (int j = i; j < kJ; ++j) {
+        for (int j = i; j < kR; ++j) {
             const float g = (keep[i] && keep[j]) ? (float)S[k] * sc[i] * sc[j] : (i == j ? 1.f : 0.f);
             G[i][j] = g;
             G[j][i] = g;
             ++k;
         }
     #pragma unroll
-    for (int i = 0; i < kJ; ++i) {
+    for (int i = 0; i < kR; ++i) {
         b[i] = keep[i] ? (float)S[k] * sc[i] : 0.f;
         ++k;
         G[i][i] += 1e-6f;
@@ -136,7 +146,7 @@ __global__ void predictor_solve_kernel(int nblocks, const double* __restrict__ p
     // Cholesky G = L L^T in place (lower triangle)
     bool ok = gmax > 0.0;
     #pragma unroll
-    for (int j = 0; j < kJ; ++j) {
+    for (int j = 0; j < kR; ++j) {
         float s = G[j][j];
         #pragma unroll
         for (int p = 0; p < j; ++p) s -= G[j][p] * G[j][p];
@@ -144,47 +154,62 @@ __global__ void predictor_solve_kernel(int nblocks, const double* __restrict__ p
         const float l = sqrtf(fmaxf(s, 1e-30f)), il = 1.f / l;
         G[j][j] = l;
         #pragma unroll
-        for (int i = j + 1; i < kJ; ++i) {
+        for (int i = j + 1; i < kR; ++i) {
             float t = G[i][j];
             #pragma unroll
             for (int p = 0; p < j; ++p) t -= G[i][p] * G[j][p];
             G[i][j] = t * il;
         }
     }
-    float a[kJ], z[kJ];
+    float a[kR], z[kR];
     #pragma unroll
-    for (int i = 0; i < kJ; ++i) {
+    for (int i = 0; i < kR; ++i) {
         float t = b[i];
         #pragma unroll
         for (int p = 0; p < i; ++p) t -= G[i][p] * z[p];
         z[i] = t / G[i][i];
     }
     #pragma unroll
-    for (int i = kJ - 1; i >= 0; --i) {
+    for (int i = kR - 1; i >= 0; --i) {
         float t = z[i];
         #pragma unroll
-        for (int p = i + 1; p < kJ; ++p) t -= G[p][i] * a[p];
+        for (int p = i + 1; p < kR; ++p) t -= G[p][i] * a[p];
         a[i] = t / G[i][i];
     }
     #pragma unroll
-    for (int i = 0; i < kJ; ++i) ok = ok && isfinite(a[i] * sc[i]);
+    for (int i = 0; i < kR; ++i) ok = ok && isfinite(a[i] * sc[i]);
     #pragma unroll
-    for (int i = 0; i < kJ; ++i) coef[i] = ok ? (double)(a[i] * sc[i]) : (i < 3 ? 1.0 : 0.0);
+    for (int i = 0; i < kR; ++i) coef[i] = ok ? (double)(a[i] * sc[i]) : (i < 3 ? 1.0 : 0.0);  // fallback: 4-point
 }
 
-__global__ void predictor_apply_kernel(int n3, const PredictorRing ring, const double* __restrict__ coef,
-                                       double* __restrict__ mu_d, float* __restrict__ mu_f) {
+__global__ void predictor_apply_kernel(int n3, const PredictorRing ring, const double* __restrict__ f_now,
+                                       const double* __restrict__ coef, double* __restrict__ mu_d,
+                                       float* __restrict__ mu_f) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n3) return;
-    double x[kJ + 1], d[kJ];
+    double x[kJ + 1], d[kJ], fx[kJ + 1], fd[kJ];
     #pragma unroll
-    for (int i = 0; i <= kJ; ++i) x[i] = ring.r[i][e];
+    for (int i = 0; i <= kJ; ++i) {
+        x[i] = ring.r[i][e];
+        fx[i] = ring.f[i][e];
+    }
     backward_differences(x, d);
-    double v = x[0];
+    backward_differences(fx, fd);
+    double v = x[0], pf = fx[0];
     #pragma unroll
-    for (int j = 0; j < kJ; ++j) v += coef[j] * d[j];
+    for (int j = 0; j < kJ; ++j) {
+        v += coef[j] * d[j];
+        pf += coef[j] * fd[j];
+    }
+    v += guess::kFieldGain * (f_now[e] - pf);
     mu_d[e] = v;
     mu_f[e] = (float)v;
+}
+
+__global__ void scaled_field_kernel(int n3, const float* __restrict__ E0, const float* __restrict__ pol,
+                                    double* __restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n3) out[e] = (double)pol[e / 3] * (double)E0[e];
 }
 
 }  // namespace
@@ -202,10 +227,16 @@ cudaError_t predictor_fit(cudaStream_t st, int n3, const PredictorRing& ring, do
     return cudaGetLastError();
 }
 
-cudaError_t predictor_apply(cudaStream_t st, int n3, const PredictorRing& ring, const double* d_coef, double* mu_d,
-                            float* mu_f) {
+cudaError_t predictor_apply(cudaStream_t st, int n3, const PredictorRing& ring, const double* f_now,
+                            const double* d_coef, double* mu_d, float* mu_f) {
     count_launch();
-    predictor_apply_kernel<<<(n3 + 255) / 256, 256, 0, st>>>(n3, ring, d_coef, mu_d, mu_f);
+    predictor_apply_kernel<<<(n3 + 255) / 256, 256, 0, st>>>(n3, ring, f_now, d_coef, mu_d, mu_f);
+    return cudaGetLastError();
+}
+
+cudaError_t scaled_field(cudaStream_t st, int n3, const float* E0, const float* pol, double* out) {
+    count_launch();
+    scaled_field_kernel<<<(n3 + 255) / 256, 256, 0, st>>>(n3, E0, pol, out);
     return cudaGetLastError();
 }
 

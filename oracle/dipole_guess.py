@@ -192,9 +192,11 @@ def init_params(seed):
 
 
 # ------------------------------------------------- learned linear predictor
-PRED_ORDER = 7    # backward differences in the model
+PRED_ORDER = 7    # backward differences of the dipoles in the model
+PRED_REGRESSORS = PRED_ORDER
 PRED_WINDOW = 4   # past steps it is fitted on
 PRED_HISTORY = PRED_ORDER + 1 + PRED_WINDOW
+FIELD_GAIN = 2.4  # weight of the unpredicted permanent-field change
 
 
 def backward_differences(x):
@@ -209,12 +211,12 @@ def backward_differences(x):
 
 
 def predictor_fit(history, stride=None):
-    """Coefficients a_1..a_J of mu = X0 + sum_j a_j nabla^j X0, fitted by
-    least squares on the last PRED_WINDOW steps: X_w - X_{w+1} from the
-    differences at X_{w+1}.  history: [PRED_HISTORY, n3], newest first.
-    Normal equations scaled by their diagonal, vanishing columns left out,
-    ridge 1e-6 on the scaled system, as the CUDA kernel (which solves the
-    scaled system in FP32; here FP64)."""
+    """Coefficients a_1..a_J of P(Y) = Y0 + sum_j a_j nabla^j Y0, fitted by
+    least squares on the last PRED_WINDOW steps of the dipoles: X_w - X_{w+1}
+    from the differences at X_{w+1}.  history: [PRED_HISTORY, n3], newest
+    first.  Normal equations scaled by their diagonal, vanishing columns left
+    out, ridge 1e-6 on the scaled system, as the CUDA kernel (which solves
+    the scaled system in FP32; here FP64)."""
     h = np.asarray(history, np.float64)
     if stride is None:  # the CUDA kernel's subsample: about 8k components
         stride = h.shape[1] // 8192 if h.shape[1] > 8192 else 1
@@ -223,7 +225,7 @@ def predictor_fit(history, stride=None):
     G = np.zeros((J, J))
     b = np.zeros(J)
     for w in range(PRED_WINDOW):
-        D = backward_differences(h[w + 1:w + 2 + J])  # [J, m]
+        D = backward_differences(h[w + 1:w + 2 + J])
         y = h[w] - h[w + 1]
         G += D @ D.T
         b += D @ y
@@ -235,7 +237,9 @@ def predictor_fit(history, stride=None):
     return np.linalg.solve(Gs, bs) * sc
 
 
-def predictor_apply(history, a):
+def predictor_apply(history, field, field_now, a, gain=FIELD_GAIN):
+    """mu = P(X) + gain (F_new - P(F)) with P(Y) = Y0 + sum_j a_j nabla^j Y0."""
     h = np.asarray(history, np.float64)
-    D = backward_differences(h[:PRED_ORDER + 1])
-    return h[0] + np.tensordot(a, D, axes=1)
+    f = np.asarray(field, np.float64)
+    P = lambda y: y[0] + np.tensordot(a, backward_differences(y[:PRED_ORDER + 1]), axes=1)  # noqa: E731
+    return P(h) + gain * (np.asarray(field_now, np.float64) - P(f))

@@ -90,7 +90,7 @@ def test_bf16_network_close_to_exact():
         assert np.linalg.norm(g1[k] - g0[k]) <= 5e-2 * np.linalg.norm(g0[k]), k
 
 
-def _oscillation_history(n3=600, steps=None, seed=0, noise=0.0):
+def _oscillation_history(n3=600, steps=None, seed=0):
     """Superposed slow oscillations sampled at unit steps, newest first."""
     steps = steps or dg.PRED_HISTORY + 1
     rng = np.random.default_rng(seed)
@@ -98,27 +98,40 @@ def _oscillation_history(n3=600, steps=None, seed=0, noise=0.0):
     w = np.array([0.03, 0.05, 0.08, 0.13])
     ph = rng.uniform(0, 2 * np.pi, size=(4, n3))
     t = np.arange(steps)[::-1].astype(float)  # newest first
-    X = np.einsum("mn,tmn->tn", A, np.cos(w[None, :, None] * t[:, None, None] + ph[None]))
-    return X + noise * rng.normal(size=X.shape)
+    return np.einsum("mn,tmn->tn", A, np.cos(w[None, :, None] * t[:, None, None] + ph[None]))
 
 
 def test_predictor_exact_on_polynomial_history():
-    """A cubic trajectory: the higher differences vanish, their columns are
-    left out, and the prediction is the cubic's continuation (to the 1e-6
-    ridge on the scaled normal equations)."""
+    """A cubic trajectory without a field: the higher differences vanish,
+    are left out, and the prediction is the cubic's continuation (to the
+    1e-6 ridge on the scaled normal equations)."""
     t = np.arange(dg.PRED_HISTORY + 1)[::-1].astype(float)
     c = np.random.default_rng(1).normal(size=(4, 50))
     X = c[0] + np.outer(t, c[1]) + np.outer(t ** 2, c[2]) * 1e-2 + np.outer(t ** 3, c[3]) * 1e-4
+    F = np.zeros_like(X)
     a = dg.predictor_fit(X[1:])
-    p = dg.predictor_apply(X[1:], a)
+    p = dg.predictor_apply(X[1:], F[1:], F[0], a)
     assert np.max(np.abs(p - X[0])) <= 1e-6 * np.max(np.abs(X))
 
 
 def test_predictor_beats_polynomial_extrapolation():
     """On smooth oscillations the fitted predictor is closer to the next
-    value than the 4-point polynomial extrapolation (its a = 1, 1, 1, 0...)."""
+    value than the 4-point polynomial extrapolation (a = 1, 1, 1, 0, ...)."""
     X = _oscillation_history()
+    F = np.zeros_like(X)
     hist = X[1:]
-    p = dg.predictor_apply(hist, dg.predictor_fit(hist))
-    p4 = dg.predictor_apply(hist, np.array([1.0, 1.0, 1.0, 0, 0, 0, 0]))
+    p = dg.predictor_apply(hist, F[1:], F[0], dg.predictor_fit(hist))
+    p4 = dg.predictor_apply(hist, F[1:], F[0], np.array([1.0, 1.0, 1.0, 0, 0, 0, 0]))
     assert np.sqrt(np.mean((p - X[0]) ** 2)) < 0.5 * np.sqrt(np.mean((p4 - X[0]) ** 2))
+
+
+def test_predictor_field_term():
+    """Dipoles that respond with the field gain to an unpredictable field
+    change at the new step: the field term adds exactly that response."""
+    X = _oscillation_history(seed=2)
+    F = 0.3 * _oscillation_history(seed=3)
+    a = dg.predictor_fit(X[1:])
+    kick = 1e-4 * np.random.default_rng(4).normal(size=X.shape[1])
+    p0 = dg.predictor_apply(X[1:], F[1:], F[0], a)
+    p1 = dg.predictor_apply(X[1:], F[1:], F[0] + kick, a)
+    assert np.allclose(p1 - p0, dg.FIELD_GAIN * kick, rtol=1e-10, atol=1e-15)
