@@ -1,0 +1,82 @@
+"""GPU: size-independent properties at the benchmark sizes, where the FP64
+oracle is too slow to run: the 4096- and 32768-water boxes (configurations
+C3 and C4).
+
+  * Newton's third law: every term's forces sum to zero (the polynomial
+    terms and dispersion to the rounding of their FP32 per-unit force
+    arithmetic, <= 1e-7 of the summed force magnitudes; PME electrostatics
+    to its interpolation error, <= 1e-4).
+  * Translation by a non-lattice vector in the periodic box: the energy of
+    each term is unchanged (1e-9 relative for the short-range terms, 1e-6
+    for electrostatics, whose PME grid is not translation invariant).
+  * Relabelling the waters: each term's energy is unchanged (1e-9 relative
+    short-range, 1e-7 electrostatics: FP32 sums in another order) and the
+    forces follow the particles (1e-5 relative RMS: each unit's FP32 force
+    arithmetic runs with its waters in another order).  With the complete
+    trimer rule: the reference's chain rule depends on the water order
+    (I > J > K), so relabelling changes its set of trimers.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+import mbpol_openmm_plugin_gb300 as mb
+from mbpol_openmm_plugin_gb300 import systems
+
+pytestmark = pytest.mark.gpu
+ELEC = 3  # energy slots and force order: one-, two-, three-body, electrostatics, dispersion
+
+
+def _evaluate(ws, positions, trimer_rule=0):
+    alpha, grid = mb.pme_parameters(ws.box, 0.9, 1e-5)
+    s = mb.create_mbpol_system(ws, target_epsilon=1e-8, ewald_alpha=alpha, pme_grid=grid, trimer_rule=trimer_rule)
+    ctx = mb.Context(s)
+    out = []
+    for term in range(5):
+        for f in s.forces:
+            f.setForceGroup(0)
+        s.forces[term].setForceGroup(1)
+        ctx.setPositions(positions)
+        st = ctx.getState(groups=1 << 1)
+        out.append((st.getPotentialEnergy(), st.getForces()))
+    return out
+
+
+@pytest.fixture(scope="module", params=["box4096", "box32768"])
+def box(request):
+    ws = systems.workload(request.param, 0)
+    return ws, _evaluate(ws, ws.positions)
+
+
+def test_forces_sum_to_zero(box):
+    ws, res = box
+    for term, (e, f) in enumerate(res):
+        total = np.abs(f.sum(0)).max()
+        scale = np.abs(f).sum()
+        print(ws.name, "term", term, "E %.6f |sum F| %.3e / sum |F| %.3e" % (e, total, scale))
+        assert total <= (1e-4 if term == ELEC else 1e-7) * scale
+
+
+def test_translation_invariance(box):
+    ws, res = box
+    shifted = ws.positions + np.array([0.1234, -0.4567, 0.789])
+    res2 = _evaluate(ws, shifted)
+    for term in range(5):
+        e, e2 = res[term][0], res2[term][0]
+        print(ws.name, "term", term, "E %.8f shifted %.8f rel %.2e" % (e, e2, abs(e2 - e) / abs(e)))
+        assert abs(e2 - e) <= (1e-6 if term == ELEC else 1e-9) * abs(e)
+
+
+def test_relabelling_invariance(box):
+    ws, _ = box
+    res = _evaluate(ws, ws.positions, trimer_rule=1)
+    nw = ws.num_waters
+    perm = np.random.default_rng(9).permutation(nw)
+    idx = (4 * perm[:, None] + np.arange(4)[None]).reshape(-1)
+    ws2 = systems.WaterSystem(ws.positions[idx], ws.box, 0, ws.name + "-relabelled")
+    res2 = _evaluate(ws2, ws2.positions, trimer_rule=1)
+    for term in range(5):
+        (e, f), (e2, f2) = res[term], res2[term]
+        print(ws.name, "term", term, "E rel %.2e F relrms %.2e" % (abs(e2 - e) / abs(e), rel_rms(f2, f[idx])))
+        assert abs(e2 - e) <= (1e-7 if term == ELEC else 1e-9) * abs(e)
+        assert rel_rms(f2, f[idx]) <= 1e-5
