@@ -136,8 +136,13 @@ struct WalkSplit {
 // NV * 12 bytes of shared memory instead of NV * 16, and an SM holds four
 // 128-thread blocks (16 warps) instead of three.  The two halves' energy and
 // gradient pairs are added at the end (double-float, fixed order).
+// Shared memory holds four blocks per SM; the registers are capped as for
+// six (80 per thread) so that a quarter of the register file stays free for
+// the electrostatics kernels of the other stream, which then run beside the
+// walk (4096-water box: 14.0 against 14.2 ms per MD step; a cap of 72 made
+// the walk slower than the overlap gains).
 template <int NV>
-__global__ void __launch_bounds__(kBlock, 4) poly_df_kernel(const PolyNode* __restrict__ l1,
+__global__ void __launch_bounds__(kBlock, 6) poly_df_kernel(const PolyNode* __restrict__ l1,
                                                           const PolyNode* __restrict__ l2,
                                                           const PolyNode* __restrict__ l3, int n3,
                                                           const PolyNode* __restrict__ lv, const WalkSplit split,
