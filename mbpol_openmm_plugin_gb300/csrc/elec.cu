@@ -999,41 +999,47 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
             E[a][1] = warp_sum(E[a][1]);
             E[a][2] = warp_sum(E[a][2]);
         }
-        if (lane == 0) {
+        // one lane per site a of the molecule (the sites' updates are
+        // independent): its intramolecular field, then the split form's
+        // store or the fused update
+        const int a = lane;
+        if (a < K) {
+            float ea[3] = {0.f, 0.f, 0.f};
+            f3 offa = mk(0.f, 0.f, 0.f);
+            #pragma unroll
+            for (int aa = 0; aa < kMaxK; ++aa)
+                if (aa == a) {
+                    ea[0] = E[aa][0];
+                    ea[1] = E[aa][1];
+                    ea[2] = E[aa][2];
+                    offa = offA[aa];
+                }
             // intramolecular pairs: coefficients of this geometry from the
             // fixed-field pass
             const float* pin = intra + (size_t)2 * kMaxIntra * A;
             #pragma unroll
-            for (int a = 0; a < kMaxK; ++a)
-                #pragma unroll
-                for (int b = 0; b < kMaxK; ++b) {
-                    if (a >= K || b >= K || a == b) continue;
-                    const int p = intra_pair(a, b, K);
-                    const float pf1 = pin[2 * p], pf2 = pin[2 * p + 1];
-                    const f3 mub = ld3(mu_in, K * A + b);
-                    const f3 d = offA[b] - offA[a];
-                    const float dur = dot(mub, d) * pf2;
-                    E[a][0] += d.x * dur + mub.x * pf1;
-                    E[a][1] += d.y * dur + mub.y * pf1;
-                    E[a][2] += d.z * dur + mub.z * pf1;
-                }
-            // split form: the direct and intramolecular field only; the
-            // reciprocal part and the update follow in induced_finish_kernel
-            #pragma unroll
-            for (int a = 0; a < kMaxK; ++a) {
-                if (!Edir || a >= K) continue;
-                const int i = K * A + a;
-                Edir[3 * i] = E[a][0];
-                Edir[3 * i + 1] = E[a][1];
-                Edir[3 * i + 2] = E[a][2];
+            for (int b = 0; b < kMaxK; ++b) {
+                if (b >= K || a == b) continue;
+                const int p = intra_pair(a, b, K);
+                const float pf1 = pin[2 * p], pf2 = pin[2 * p + 1];
+                const f3 mub = ld3(mu_in, K * A + b);
+                const f3 d = offA[b] - offa;
+                const float dur = dot(mub, d) * pf2;
+                ea[0] += d.x * dur + mub.x * pf1;
+                ea[1] += d.y * dur + mub.y * pf1;
+                ea[2] += d.z * dur + mub.z * pf1;
             }
-            #pragma unroll
-            for (int a = 0; a < kMaxK; ++a) {
-                if (Edir || a >= K) continue;
-                const int i = K * A + a;
+            const int i = K * A + a;
+            if (Edir) {
+                // split form: the direct and intramolecular field only; the
+                // reciprocal part and the update follow in induced_finish_kernel
+                Edir[3 * i] = ea[0];
+                Edir[3 * i + 1] = ea[1];
+                Edir[3 * i + 2] = ea[2];
+            } else {
                 const f3 mu = ld3(mu_in, i);
                 const double m0 = mu_d[3 * i], m1 = mu_d[3 * i + 1], m2 = mu_d[3 * i + 2];
-                float ex = E[a][0], ey = E[a][1], ez = E[a][2];
+                float ex = ea[0], ey = ea[1], ez = ea[2];
                 if (PME) {
                     ex += c_el.self_term * mu.x - c_el.scale[0] * phi_mu[4 * i + 1];
                     ey += c_el.self_term * mu.y - c_el.scale[1] * phi_mu[4 * i + 2];
@@ -1082,6 +1088,8 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
         }
     }
     if (mcl) {
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d2sum += __shfl_xor_sync(0xffffffffu, d2sum, o);
         if (cA >= 0 && !frozen && lane == 0) atomicAdd(eps2c + cA, d2sum);
         d2sum = 0.0;
     }
