@@ -207,6 +207,16 @@ def timed_md(args, guess, params=None, profile=False):
     r["energies"] = en.copy()
     if profile:
         r["clocks"] = sampler.stop()
+    if args.avg_steps > 0:
+        # the metric's iteration average: >= 1000 further steps of the same
+        # trajectory (after the equilibration and the timed steps)
+        msl, itl, enl = ctypes.c_double(), ctypes.c_long(), np.zeros(6)
+        _capi.check(lib.mbpol_md_run(h, args.avg_steps, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(msl),
+                                     _capi.ptr(enl), ctypes.byref(itl)))
+        r["long_run"] = {"steps": args.avg_steps, "ms_per_step": msl.value / args.avg_steps,
+                         "ns_per_day": ns_per_day(msl.value / 1e3 / args.avg_steps),
+                         "solver_iterations_per_step": itl.value / args.avg_steps}
+    if profile:
         # per-kernel CUDA-event timers on K further steps (the events add
         # launches, so the timed steps above run without them)
         lib.mbpol_profile_enable(1)
@@ -236,6 +246,8 @@ def run_ours(args):
         rr = timed_md(args, g, params if g == "learned" else None)
         others[g] = {"ns_per_day": ns_per_day(rr["step_s"]), "ms_per_step": rr["step_s"] * 1e3,
                      "solver_iterations_per_step": rr["iterations"]}
+        if "long_run" in rr:
+            others[g]["long_run"] = rr["long_run"]
         del rr
     r = timed_md(args, args.guess, params, profile=True)
     ctx, ws, sysm, alpha, grid = r["ctx"], r["ws"], r["sysm"], r["alpha"], r["grid"]
@@ -334,8 +346,10 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(pos.nbytes + 5 * 8)},
         "gpu_launches": launches,
         "solver_iterations_per_step": solver_it,
-        "guess_comparison": dict(others, **{args.guess: {"ns_per_day": value, "ms_per_step": step_s * 1e3,
-                                                         "solver_iterations_per_step": solver_it}}),
+        "guess_comparison": dict(others, **{args.guess: dict({"ns_per_day": value, "ms_per_step": step_s * 1e3,
+                                                              "solver_iterations_per_step": solver_it},
+                                                             **({"long_run": r["long_run"]} if "long_run" in r
+                                                                else {}))}),
         "counts": {"pairs_2b": int(counts[0]), "trimers": int(counts[1]), "elec_site_pairs": int(counts[2]),
                    "pme_grid_points": int(grid[0] * grid[1] * grid[2]) if grid else 0},
         "kernels_ms_per_step": {k: v["total_ms"] / args.steps for k, v in kern.items()},
@@ -346,9 +360,34 @@ def run_ours(args):
     }
     if drift is not None:
         out["nve_drift"] = drift
+    if not args.no_accuracy:
+        out["accuracy"] = accuracy_check()
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, sample=True)
     return out
+
+
+def accuracy_check():
+    """The acceptance bar of the metric (total forces <= 1e-4 relative RMS,
+    energy <= 1e-6 relative) on the largest reference fixture: the
+    reference's 256-water PME box (python/tests/pdb_files/water256.pdb),
+    whose FP64 energy and forces from the reference's own code are committed
+    under tests/golden.  Same settings as the timed box: PME, 1e-8 D."""
+    import mbpol_openmm_plugin_gb300 as mb
+    from mbpol_openmm_plugin_gb300 import systems
+    d = np.load(os.path.join(ROOT, "tests", "golden", "pdb_water256_pme.npz"))
+    ws = systems.WaterSystem(d["positions"], d["box"], 0, "water256_pme")
+    s = mb.create_mbpol_system(ws, target_epsilon=1e-8, ewald_alpha=float(d["alpha"]),
+                               pme_grid=[int(v) for v in d["grid"]])
+    ctx = mb.Context(s)
+    ctx.setPositions(d["positions"])
+    st = ctx.getState()
+    e, eref = st.getPotentialEnergy(), float(d["etotal"])
+    f, fref = np.asarray(st.getForces()), np.asarray(d["ftotal"])
+    ferr = float(np.sqrt(np.sum((f - fref) ** 2) / np.sum(fref ** 2)))
+    return {"workload": "water256 PME (reference fixture, FP64 reference outputs)",
+            "energy_rel": abs(e - eref) / abs(eref), "force_rel_rms": ferr,
+            "passes": bool(abs(e - eref) <= 1e-6 * abs(eref) and ferr <= 1e-4)}
 
 
 def measured_hbm_gbs():
@@ -458,7 +497,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-comparison", action="store_true", help="time the --guess arm only")
     ap.add_argument("--drift-steps", type=int, default=0, help="NVE steps after the timed region for the drift")
-    ap.add_argument("--equilibrate", type=int, default=16,
+    ap.add_argument("--avg-steps", type=int, default=1000,
+                    help="MD steps after the timed ones over which iterations/step are averaged (0: none)")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the reference-fixture accuracy check")
+    ap.add_argument("--equilibrate", type=int, default=200,
                     help="untimed MD steps before the warm-up (trajectory start, every arm)")
     ap.add_argument("--model", default="reference", choices=["reference", "physical"],
                     help="physical: complete trimers and the consistent PME field (energy-conserving)")
