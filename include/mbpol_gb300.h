@@ -183,6 +183,18 @@ mbpol_status mbpol_get_counts(mbpol_context* ctx, long* counts4);
 mbpol_status mbpol_get_electrostatic_potential(mbpol_context* ctx, int num_points, const double* points,
                                                double* potential);
 
+/* System multipole moments: the reference's getSystemElectrostaticsMoments
+ * (openmmapi/include/openmm/mbpolKernels.h:121; MBPolReferenceKernels.cpp:
+ * 285-303, MBPolReferenceElectrostaticsForce.cpp:923-1021).  Evaluates the
+ * electrostatics at the current positions, then, about the centre of mass
+ * of masses[num_particles] (none when they sum to 0), moments[13] = net
+ * charge (e), dipole x y z (Debye), the traceless quadrupole
+ * xx xy xz yx yy yz zx zy zz (the reference's units: e nm^2 x 300 x 4.80321
+ * / 2).  Positions as stored, not wrapped.  Fails with
+ * MBPOL_ERR_NOT_CONVERGED as the reference throws; not available with
+ * batched clusters. */
+mbpol_status mbpol_get_system_multipole_moments(mbpol_context* ctx, const double* masses, double* moments);
+
 /* Kernel timing with CUDA events on the launching stream (process-wide).
  * Kernel ids: 0 two-body polynomial, 1 three-body polynomial, 2 fixed field,
  * 3 induced field + solver update, 4 PME dipole pass (spread, FFT,

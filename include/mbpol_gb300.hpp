@@ -159,6 +159,10 @@ public:
      * Context below) */
     void getElectrostaticPotential(const std::vector<Vec3>& inputGrid, class Context& context,
                                    std::vector<double>& outputElectrostaticPotential) const;
+    /* mbpolKernels.h:121 getSystemElectrostaticsMoments: charge, dipole
+     * (Debye) and traceless quadrupole about the System's centre of mass,
+     * 13 values (defined after Context below) */
+    void getSystemElectrostaticsMoments(class Context& context, std::vector<double>& outputMoments) const;
     int term() const override { return MBPOL_TERM_ELECTROSTATICS; }
 
     mbpol_electrostatics_params p_;
@@ -173,6 +177,7 @@ public:
         return (int)masses_.size() - 1;
     }
     int getNumParticles() const { return (int)masses_.size(); }
+    double getParticleMass(int i) const { return masses_.at((size_t)i); }
     /* ThreeParticleAverageSite */
     void setVirtualSite(int index, int p1, int p2, int p3, double w1, double w2, double w3) {
         vs_.push_back({index, p1, p2, p3, w1, w2, w3});
@@ -243,6 +248,7 @@ public:
         return st;
     }
     mbpol_context* handle() { return h_; }
+    const System& getSystem() const { return sys_; }
 
 private:
     void add(const Force& f) {
@@ -283,6 +289,15 @@ inline void MBPolElectrostaticsForce::getElectrostaticPotential(const std::vecto
     outputElectrostaticPotential.assign(inputGrid.size(), 0.0);
     mbpol_check(mbpol_get_electrostatic_potential(context.handle(), (int)inputGrid.size(), flat.data(),
                                                   outputElectrostaticPotential.data()));
+}
+
+inline void MBPolElectrostaticsForce::getSystemElectrostaticsMoments(Context& context,
+                                                                     std::vector<double>& outputMoments) const {
+    const System& sys = context.getSystem();
+    std::vector<double> m((size_t)sys.getNumParticles());
+    for (int i = 0; i < sys.getNumParticles(); ++i) m[(size_t)i] = sys.getParticleMass(i);
+    outputMoments.assign(13, 0.0);
+    mbpol_check(mbpol_get_system_multipole_moments(context.handle(), m.data(), outputMoments.data()));
 }
 
 }  // namespace MBPolPlugin

@@ -26,6 +26,7 @@ EXPORTED = [
     "mbpol_add_threebody_force", "mbpol_add_electrostatics_force", "mbpol_add_dispersion_force",
     "mbpol_set_positions", "mbpol_compute", "mbpol_set_masses", "mbpol_set_velocities", "mbpol_md_run",
     "mbpol_get_state", "mbpol_get_induced_dipoles", "mbpol_get_counts", "mbpol_get_electrostatic_potential",
+    "mbpol_get_system_multipole_moments",
     "mbpol_profile_enable", "mbpol_profile_read", "mbpol_launch_count", "mbpol_status_string", "mbpol_last_error",
     "mbpol_twobody_dimers_noalloc",
     "mbpol_guess_collect", "mbpol_guess_num_samples", "mbpol_guess_train", "mbpol_guess_get_params",
@@ -97,6 +98,7 @@ def load(path=None):
         "mbpol_get_induced_dipoles": (I, [P, P, ctypes.POINTER(I), ctypes.POINTER(D)]),
         "mbpol_get_counts": (I, [P, P]),
         "mbpol_get_electrostatic_potential": (I, [P, I, P, P]),
+        "mbpol_get_system_multipole_moments": (I, [P, P, P]),
         "mbpol_guess_fit_predictor": (I, [P, P, P, P, I, P, P]),
         "mbpol_profile_enable": (I, [I]),
         "mbpol_launch_count": (ctypes.c_ulonglong, []),

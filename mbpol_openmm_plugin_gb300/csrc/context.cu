@@ -885,6 +885,20 @@ mbpol_status mbpol_get_electrostatic_potential(mbpol_context* ctx, int num_point
     return ctx->elec->potential(ctx->st, ctx->d_pos.as<double>(), num_points, points, potential);
 }
 
+mbpol_status mbpol_get_system_multipole_moments(mbpol_context* ctx, const double* masses, double* moments) {
+    if (!ctx || !masses || !moments) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+    if (!ctx->elec) return mbpol_fail(MBPOL_ERR_STATE, "no electrostatics force");
+    if (!ctx->have_pos) return mbpol_fail(MBPOL_ERR_STATE, "positions have not been set");
+    if (ctx->ncl > 0) return mbpol_fail(MBPOL_ERR_STATE, "the moments are not defined for batched clusters");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    // the reference's setup: charges and converged induced dipoles at the
+    // current positions (MBPolReferenceElectrostaticsForce.cpp:936-941)
+    ctx->forces_valid = false;
+    mbpol_status s = compute_device(ctx, MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS));
+    if (s) return s;
+    return ctx->elec->moments(ctx->st, ctx->d_pos.as<double>(), masses, moments);
+}
+
 mbpol_status mbpol_get_counts(mbpol_context* ctx, long* c) {
     if (!ctx || !c) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
     for (int k = 0; k < 4; ++k) c[k] = ctx->counts[k];

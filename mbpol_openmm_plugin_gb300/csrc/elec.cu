@@ -1707,6 +1707,110 @@ __global__ void __launch_bounds__(kPotTile) potential_kernel(int n, const double
     if (live) out[p] = acc * kElectric;
 }
 
+// System multipole moments (reference
+// calculateMBPolSystemElectrostaticsMoments,
+// MBPolReferenceElectrostaticsForce.cpp:923-1021): net charge, dipole and
+// traceless quadrupole of the site charges and converged induced dipoles
+// about the centre of mass, positions as stored (not wrapped).  Two passes
+// of FP64 sums over sites (centre of mass, then the moments), each summed
+// per block in a fixed order and then over blocks by one thread, so the
+// result is the same from run to run.
+constexpr int kMomBlocks = 64, kMomThreads = 256;
+
+template <int NS>
+__device__ __forceinline__ void moment_block_sums(double (&v)[NS], double* __restrict__ out) {
+    __shared__ double red[kMomThreads / 32][NS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    #pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        double x = v[k];
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp][k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NS) {
+        double x = 0.0;
+        for (int w = 0; w < kMomThreads / 32; ++w) x += red[w][threadIdx.x];
+        out[threadIdx.x] = x;
+    }
+}
+
+__global__ void __launch_bounds__(kMomThreads) moments_com_kernel(int n, const double* __restrict__ pos,
+                                                                  const double* __restrict__ mass,
+                                                                  double* __restrict__ part) {
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int i = blockIdx.x * kMomThreads + threadIdx.x; i < n; i += kMomBlocks * kMomThreads) {
+        const double m = mass[i];
+        v[0] += m;
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) v[1 + k] += pos[3 * (size_t)i + k] * m;
+    }
+    moment_block_sums<4>(v, part + 4 * blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kMomThreads) moments_kernel(int n, const double* __restrict__ pos,
+                                                              const double* __restrict__ qd,
+                                                              const double* __restrict__ mud,
+                                                              const double* __restrict__ pcom,
+                                                              double* __restrict__ part) {
+    __shared__ double com[3];
+    if (threadIdx.x == 0) {
+        double mt = 0.0, c[3] = {0.0, 0.0, 0.0};
+        for (int b = 0; b < kMomBlocks; ++b) {
+            mt += pcom[4 * b];
+            for (int k = 0; k < 3; ++k) c[k] += pcom[4 * b + 1 + k];
+        }
+        for (int k = 0; k < 3; ++k) com[k] = mt > 0.0 ? c[k] * (1.0 / mt) : 0.0;
+    }
+    __syncthreads();
+    // q, dipole x y z, Q xx xy xz yy yz zz
+    double v[10];
+    #pragma unroll
+    for (int k = 0; k < 10; ++k) v[k] = 0.0;
+    for (int i = blockIdx.x * kMomThreads + threadIdx.x; i < n; i += kMomBlocks * kMomThreads) {
+        double r[3], mu[3];
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            r[k] = pos[3 * (size_t)i + k] - com[k];
+            mu[k] = mud[3 * (size_t)i + k];
+        }
+        const double q = qd[i];
+        v[0] += q;
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) v[1 + k] += r[k] * q + mu[k];
+        v[4] += r[0] * r[0] * q + 2.0 * r[0] * mu[0];
+        v[5] += r[0] * r[1] * q + r[0] * mu[1] + r[1] * mu[0];
+        v[6] += r[0] * r[2] * q + r[0] * mu[2] + r[2] * mu[0];
+        v[7] += r[1] * r[1] * q + 2.0 * r[1] * mu[1];
+        v[8] += r[1] * r[2] * q + r[1] * mu[2] + r[2] * mu[1];
+        v[9] += r[2] * r[2] * q + 2.0 * r[2] * mu[2];
+    }
+    moment_block_sums<10>(v, part + 10 * blockIdx.x);
+}
+
+// out: charge (e), dipole (Debye), traceless quadrupole row by row (the
+// reference's units: e nm x 10 x 4.80321, e nm^2 x 100 x 3 x 4.80321)
+__global__ void moments_final_kernel(const double* __restrict__ part, double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double v[10];
+    for (int k = 0; k < 10; ++k) v[k] = 0.0;
+    for (int b = 0; b < kMomBlocks; ++b)
+        for (int k = 0; k < 10; ++k) v[k] += part[10 * b + k];
+    const double debye = 4.80321, tr = (v[4] + v[7] + v[9]) / 3.0, qs = 0.5 * 100.0 * 3.0 * debye;
+    out[0] = v[0];
+    for (int k = 0; k < 3; ++k) out[1 + k] = v[1 + k] * 10.0 * debye;
+    out[4] = (v[4] - tr) * qs;
+    out[5] = v[5] * qs;
+    out[6] = v[6] * qs;
+    out[7] = v[5] * qs;
+    out[8] = (v[7] - tr) * qs;
+    out[9] = v[8] * qs;
+    out[10] = v[6] * qs;
+    out[11] = v[8] * qs;
+    out[12] = (v[9] - tr) * qs;
+}
+
 }  // namespace
 
 struct ElecImpl {
@@ -1715,7 +1819,7 @@ struct ElecImpl {
     bool pme = false;
     std::vector<float> q_static, damp, pol;
     std::vector<double> q_static64;  // the caller's charges, for the potential
-    DBuf<double> d_qs64, d_qd, d_pts, d_pot;
+    DBuf<double> d_qs64, d_qd, d_pts, d_pot, d_mass, d_mom;
     std::vector<int> type;
     DBuf<float> d_qs, d_damp, d_pol, d_off, d_q, d_dq, d_E0, d_mu0, d_mu1, d_mu2, d_mu_prev, d_phi_fix, d_phi_mu, d_nbd,
         d_gfrac, d_reach, d_ebase, d_intra, d_pcoef, d_edir;
@@ -2460,6 +2564,36 @@ mbpol_status ElecEngine::potential(cudaStream_t st, const double* pos, int npts,
                                                                           I.d_pts.p, I.d_pot.p);
     MBPOL_CUDA_OK(cudaGetLastError());
     MBPOL_CUDA_OK(cudaMemcpyAsync(potential, I.d_pot.p, sizeof(double) * npts, cudaMemcpyDeviceToHost, st));
+    MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+    return MBPOL_OK;
+}
+
+mbpol_status ElecEngine::moments(cudaStream_t st, const double* pos, const double* masses, double* out) {
+    ElecImpl& I = *impl_;
+    if (!I.evaluated) return mbpol_fail(MBPOL_ERR_STATE, "no electrostatics evaluation yet");
+    const int n = I.N;
+    MBPOL_CUDA_OK(I.d_qd.ensure(n));
+    if (!I.prm.include_charge_redistribution) {
+        MBPOL_CUDA_OK(I.d_qs64.ensure(n));
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_qs64.p, I.q_static64.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    }
+    MBPOL_CUDA_OK(I.d_mass.ensure(n));
+    MBPOL_CUDA_OK(I.d_mom.ensure(14 * (size_t)kMomBlocks + 13));
+    MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mass.p, masses, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    double* pcom = I.d_mom.p;
+    double* part = pcom + 4 * kMomBlocks;
+    double* res = part + 10 * kMomBlocks;
+    count_launch();
+    site_charges_kernel<<<(I.nmol + 127) / 128, 128, 0, st>>>(I.nmol, pos, I.prm.include_charge_redistribution ? 1 : 0,
+                                                              I.d_qs64.p, I.d_qd.p);
+    count_launch();
+    moments_com_kernel<<<kMomBlocks, kMomThreads, 0, st>>>(n, pos, I.d_mass.p, pcom);
+    count_launch();
+    moments_kernel<<<kMomBlocks, kMomThreads, 0, st>>>(n, pos, I.d_qd.p, I.d_mud.p, pcom, part);
+    count_launch();
+    moments_final_kernel<<<1, 32, 0, st>>>(part, res);
+    MBPOL_CUDA_OK(cudaGetLastError());
+    MBPOL_CUDA_OK(cudaMemcpyAsync(out, res, sizeof(double) * 13, cudaMemcpyDeviceToHost, st));
     MBPOL_CUDA_OK(cudaStreamSynchronize(st));
     return MBPOL_OK;
 }

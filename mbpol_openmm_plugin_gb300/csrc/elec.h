@@ -26,6 +26,9 @@ public:
     // electrostatic potential (kJ/mol/e) at npts host points (nm) from the
     // last evaluation's charges and induced dipoles; pos: device positions
     mbpol_status potential(cudaStream_t st, const double* pos, int npts, const double* points, double* potential);
+    // system multipole moments (13 values) of the last evaluation's charges
+    // and induced dipoles about the centre of mass of the host masses
+    mbpol_status moments(cudaStream_t st, const double* pos, const double* masses, double* out13);
     bool converged() const;
     int iterations() const;
     long num_site_pairs() const;

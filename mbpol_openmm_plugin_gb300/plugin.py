@@ -280,6 +280,26 @@ class MBPolElectrostaticsForce:
             outputElectrostaticPotential[:] = out.tolist()
         return out
 
+    def getSystemElectrostaticsMoments(self, context, outputElectrostaticsMoments=None):
+        """mbpolKernels.h:121 (MBPolReferenceElectrostaticsForce.cpp:923-1021):
+        the 13 system moments of the charges and converged induced dipoles
+        at the context's current positions, about the System's centre of
+        mass: net charge (e), dipole (Debye), traceless quadrupole
+        xx xy xz yx yy yz zx zy zz (e nm^2 x 300 x 4.80321 / 2).  Returns
+        the values; a list passed as outputElectrostaticsMoments is filled
+        as well."""
+        if context._h is None:
+            context._build()
+        lib = _capi.load()
+        box = None if context._box is None else as_c(context._box, np.float64)
+        check(lib.mbpol_set_positions(context._h, ptr(context._pos), ptr(box)))
+        masses = as_c(context.system.masses, np.float64)
+        out = np.zeros(13)
+        check(lib.mbpol_get_system_multipole_moments(context._h, ptr(masses), ptr(out)))
+        if outputElectrostaticsMoments is not None:
+            outputElectrostaticsMoments[:] = out.tolist()
+        return out
+
     def _params(self):
         p = _capi.ElectrostaticsParams()
         _capi.load().mbpol_electrostatics_params_default(ctypes.byref(p))

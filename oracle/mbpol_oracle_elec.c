@@ -400,6 +400,44 @@ int orc_electrostatic_potential(int npts, const double* points, double* out) {
     return 0;
 }
 
+/* System multipole moments from the last orc_electrostatics call
+ * (calculateMBPolSystemElectrostaticsMoments,
+ * MBPolReferenceElectrostaticsForce.cpp:923-1021), about the centre of mass
+ * of `mass` (none when the total mass is 0): out[0] net charge (e),
+ * out[1..3] dipole (Debye: e nm x 10 x 4.80321), out[4..12] the traceless
+ * quadrupole 0.5 (Q_ab - delta_ab tr/3) row by row, Q_ab = sum q r_a r_b +
+ * r_a mu_b + r_b mu_a, in e nm^2 x 100 x 3 x 4.80321. */
+int orc_system_moments(const double* mass, double* out) {
+    if (!o_last_state) return 1;
+    const int n = o_last_state_n;
+    double mt = 0.0, com[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < n; ++i) {
+        mt += mass[i];
+        for (int k = 0; k < 3; ++k) com[k] += o_last_state[7 * i + k] * mass[i];
+    }
+    if (mt > 0.0)
+        for (int k = 0; k < 3; ++k) com[k] *= 1.0 / mt;
+    double q = 0.0, dp[3] = {0.0, 0.0, 0.0}, Q[3][3] = {{0.0}};
+    for (int i = 0; i < n; ++i) {
+        const double* S = o_last_state + 7 * i;
+        double r[3];
+        for (int k = 0; k < 3; ++k) r[k] = S[k] - com[k];
+        q += S[3];
+        for (int k = 0; k < 3; ++k) dp[k] += r[k] * S[3] + S[4 + k];
+        for (int a = 0; a < 3; ++a)
+            for (int b = a; b < 3; ++b) Q[a][b] += r[a] * r[b] * S[3] + r[a] * S[4 + b] + r[b] * S[4 + a];
+    }
+    const double debye = 4.80321, tr = (Q[0][0] + Q[1][1] + Q[2][2]) / 3.0;
+    out[0] = q;
+    for (int k = 0; k < 3; ++k) out[1 + k] = dp[k] * 10.0 * debye;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            const double v = a <= b ? Q[a][b] : Q[b][a];
+            out[4 + 3 * a + b] = 0.5 * (v - (a == b ? tr : 0.0)) * 100.0 * 3.0 * debye;
+        }
+    return 0;
+}
+
 /* -------------------------------------------------------------- solver */
 int orc_electrostatics(int n, const double* pos, const double* box, int pme, double alpha, const int* grid,
                        double rc, double target_eps, int maxiter, const double* thole, int row_stride, double* f,

@@ -106,6 +106,8 @@ def port():
     L.orc_set_onebody_tables.argtypes = [P, P]
     L.orc_electrostatic_potential.restype = I
     L.orc_electrostatic_potential.argtypes = [I, P, P]
+    L.orc_system_moments.restype = I
+    L.orc_system_moments.argtypes = [P, P]
     L.orc_set_pme_fixed_field.restype = None
     L.orc_set_pme_fixed_field.argtypes = [I]
     import numpy as np
@@ -195,6 +197,30 @@ def electrostatic_potential(pos, points, box=None, alpha=0.0, grid=(0, 0, 0), ep
         raise RuntimeError("induced dipoles did not converge")
     out = np.zeros(pts.shape[0])
     if L.orc_electrostatic_potential(pts.shape[0], _p(pts), _p(out)):
+        raise RuntimeError("no electrostatics state")
+    return out
+
+
+def system_moments(pos, masses, box=None, alpha=0.0, grid=(0, 0, 0), eps=1e-8, rc=0.9):
+    """getSystemElectrostaticsMoments of the port: one electrostatics solve,
+    then the 13 moments (charge, dipole in Debye, traceless quadrupole) about
+    the centre of mass of `masses`."""
+    import numpy as np
+    L = port()
+    pos = np.ascontiguousarray(pos, np.float64)
+    n = pos.shape[0]
+    b = None if box is None else np.ascontiguousarray(box, np.float64)
+    f = np.zeros((n, 3))
+    e = ctypes.c_double()
+    it = ctypes.c_int()
+    g = np.array(grid, np.int32)
+    th = np.array([0.4, 0.4, 0.055, 0.626, 0.055])
+    if L.orc_electrostatics(n, _p(pos), _p(b), 1 if b is not None else 0, alpha, _p(g), rc, eps, 200, _p(th), 1,
+                            _p(f), ctypes.byref(e), None, ctypes.byref(it), None):
+        raise RuntimeError("induced dipoles did not converge")
+    out = np.zeros(13)
+    m = np.ascontiguousarray(masses, np.float64)
+    if L.orc_system_moments(_p(m), _p(out)):
         raise RuntimeError("no electrostatics state")
     return out
 

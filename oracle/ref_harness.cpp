@@ -237,4 +237,46 @@ int ref_electrostatic_potential(int ns, const double* pos, const double* charge,
     return 0;
 }
 
+/* System multipole moments (calculateMBPolSystemElectrostaticsMoments,
+ * MBPolReferenceElectrostaticsForce.cpp:923-1021): the same setup as the
+ * potential (charges with redistribution, converged induced dipoles), then
+ * charge, dipole (Debye) and traceless quadrupole about the centre of mass
+ * of `mass`, 13 values. */
+int ref_system_moments(int ns, const double* pos, const double* charge, const int* mol, const int* type,
+                       const double* damp, const double* pol, const double* thole5, int pme, double cutoff,
+                       double alpha, const int* grid, const double* box, double target_eps, int maxiter,
+                       int charge_redist, const double* mass, double* moments, char* err, int errlen) {
+    std::vector<RealVec> p = load_positions(ns, pos);
+    std::vector<double> q(charge, charge + ns), d(damp, damp + ns), a(pol, pol + ns), th((size_t)ns, 0.0);
+    std::vector<double> m8(mass, mass + ns);
+    std::vector<int> m(mol, mol + ns), t(type, type + ns);
+    std::vector<double> thole(thole5, thole5 + 5), out;
+    try {
+        MBPolReferenceElectrostaticsForce* force = nullptr;
+        if (pme) {
+            PmeProbe* pp = new PmeProbe();
+            pp->setAlphaEwald(alpha);
+            pp->setCutoffDistance(cutoff);
+            std::vector<int> gd(grid, grid + 3);
+            pp->setPmeGridDimensions(gd);
+            RealVec b(box[0], box[1], box[2]);
+            pp->setPeriodicBoxSize(b);
+            force = pp;
+        } else {
+            force = new NonPmeProbe();
+        }
+        force->setMutualInducedDipoleTargetEpsilon(target_eps);
+        force->setMaximumMutualInducedDipoleIterations(maxiter);
+        force->setIncludeChargeRedistribution(charge_redist != 0);
+        force->setTholeParameters(thole);
+        force->calculateMBPolSystemElectrostaticsMoments(m8, p, q, m, t, th, d, a, out);
+        for (int i = 0; i < 13; ++i) moments[i] = out[(size_t)i];
+        delete force;
+    } catch (const std::exception& ex) {
+        set_err(err, errlen, ex.what());
+        return 1;
+    }
+    return 0;
+}
+
 }  // extern "C"

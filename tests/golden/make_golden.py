@@ -13,7 +13,7 @@ Sources:
 Dispersion has no plugin code in the reference (python/mbpol.xml:37-108 builds
 an OpenMM CustomNonbondedForce); its values come from the C oracle port.
 
-    python tests/golden/make_golden.py [/path/to/reference] [elec|pdb|potential]
+    python tests/golden/make_golden.py [/path/to/reference] [elec|pdb|potential|moments]
 """
 import ctypes
 import json
@@ -68,6 +68,8 @@ def lib():
     L.ref_electrostatic_potential.restype = I
     L.ref_electrostatic_potential.argtypes = [I, P, P, P, P, P, P, P, I, D, D, P, P, D, I, I, I, P, P,
                                               ctypes.c_char_p, I]
+    L.ref_system_moments.restype = I
+    L.ref_system_moments.argtypes = [I, P, P, P, P, P, P, P, I, D, D, P, P, D, I, I, P, P, ctypes.c_char_p, I]
     return L
 
 
@@ -329,6 +331,41 @@ def main_potential():
         print(name, seed, "potential range %.4f .. %.4f kJ/mol/e" % (out.min(), out.max()))
 
 
+def main_moments():
+    """getSystemElectrostaticsMoments (MBPolReferenceKernels.cpp:285-303,
+    MBPolReferenceElectrostaticsForce.cpp:923-1021) of the compiled
+    reference, with the mbpol.xml masses (python/mbpol.xml:3-5)."""
+    L = lib()
+    sys.path.insert(0, ROOT)
+    from mbpol_openmm_plugin_gb300.plugin import pme_parameters
+    for name, seed in (("cluster14", 0), ("box256", 0)):
+        ws = systems.workload(name, seed)
+        pos = place_m(ws.positions)
+        n = pos.shape[0]
+        if ws.box is None:
+            alpha, grid, b = 0.0, [0, 0, 0], np.zeros(3)
+        else:
+            alpha, grid = pme_parameters(ws.box, 0.9, 1e-5)
+            b = np.asarray(ws.box, float)
+        typ = np.tile([0, 1, 1, 2], n // 4).astype(np.int32)
+        q = np.tile([-5.1966000e-01, 2.5983000e-01, 2.5983000e-01, 0.0], n // 4)
+        damp = np.tile([0.00131, 0.000294, 0.000294, 0.00131], n // 4)
+        pol = np.tile([0.00131, 0.000294, 0.000294, 0.0], n // 4)
+        mol = np.repeat(np.arange(n // 4), 4).astype(np.int32)
+        mass = np.tile([15.99943, 1.007947, 1.007947, 0.0], n // 4)
+        out = np.zeros(13)
+        err = ctypes.create_string_buffer(512)
+        rc = L.ref_system_moments(n, p(np.ascontiguousarray(pos)), p(q), p(mol), p(typ), p(damp), p(pol),
+                                  p(np.array(THOLE)), 0 if ws.box is None else 1, 0.9, alpha,
+                                  p(np.array(grid, np.int32)), p(b), 1e-8, 200, 1, p(mass), p(out), err, 512)
+        if rc:
+            raise RuntimeError(err.value.decode())
+        np.savez_compressed(os.path.join(HERE, "moments_%s_seed%d.npz" % (name, seed)), positions=pos,
+                            box=b, periodic=ws.box is not None, alpha=alpha, grid=np.array(grid), masses=mass,
+                            moments=out)
+        print(name, seed, "moments", np.array2string(out, precision=5))
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "elec":
         main_elec()
@@ -336,8 +373,11 @@ if __name__ == "__main__":
         main_potential()
     elif len(sys.argv) > 2 and sys.argv[2] == "pdb":
         main_pdb()
+    elif len(sys.argv) > 2 and sys.argv[2] == "moments":
+        main_moments()
     else:
         main()
         main_elec()
         main_pdb()
         main_potential()
+        main_moments()
