@@ -136,6 +136,14 @@ mbpol_status mbpol_add_electrostatics_force(mbpol_context* ctx, const mbpol_elec
 mbpol_status mbpol_add_dispersion_force(mbpol_context* ctx, int num_waters, const int* waters, int method,
                                         double cutoff, const double* c6, const double* d6);
 
+/* Chloride ions (class Cl of the tables) in the dispersion term, after
+ * mbpol_add_dispersion_force: each ion interacts with the O and H sites of
+ * every water and with the other ions, site distances within the cutoff, as
+ * the CustomNonbondedForce of python/mbpol.xml:37-108 does for a Cl residue
+ * (its exclusions: same residue, M sites).  Not available with batched
+ * clusters. */
+mbpol_status mbpol_add_dispersion_ions(mbpol_context* ctx, int num_ions, const int* particles);
+
 /* Positions (3*num_particles, nm) and the rectangular box (3 lengths, nm),
  * or box = NULL for a non-periodic system.  Virtual sites are placed from
  * their parents on the device before each evaluation. */

@@ -24,6 +24,7 @@ EXPORTED = [
     "mbpol_electrostatics_params_default", "mbpol_context_create", "mbpol_context_destroy",
     "mbpol_add_average3_site", "mbpol_add_onebody_force", "mbpol_add_twobody_force",
     "mbpol_add_threebody_force", "mbpol_add_electrostatics_force", "mbpol_add_dispersion_force",
+    "mbpol_add_dispersion_ions",
     "mbpol_set_positions", "mbpol_compute", "mbpol_set_masses", "mbpol_set_velocities", "mbpol_md_run",
     "mbpol_get_state", "mbpol_get_induced_dipoles", "mbpol_get_counts", "mbpol_get_electrostatic_potential",
     "mbpol_get_system_multipole_moments",
@@ -89,6 +90,7 @@ def load(path=None):
         "mbpol_add_threebody_force": (I, [P, I, P, I, D, I]),
         "mbpol_add_electrostatics_force": (I, [P, ctypes.POINTER(ElectrostaticsParams), P, P, P, P, P]),
         "mbpol_add_dispersion_force": (I, [P, I, P, I, D, P, P]),
+        "mbpol_add_dispersion_ions": (I, [P, I, P]),
         "mbpol_set_positions": (I, [P, P, P]),
         "mbpol_compute": (I, [P, ctypes.c_uint, P, P]),
         "mbpol_set_masses": (I, [P, P]),

@@ -138,6 +138,8 @@ struct mbpol_context {
     bool cl_dirty = false;
     DevBuf d_cl_energy;  // [ncl][MBPOL_NUM_TERMS]
     double disp_c6[16], disp_d6[16];
+    std::vector<int> disp_ions;  // chloride ions of the dispersion term
+    DevBuf d_disp_ions;
     // electrostatics
     std::unique_ptr<ElecEngine> elec;
     int num_sms = 0;
@@ -454,7 +456,8 @@ mbpol_status dispersion_list(mbpol_context* ctx, const Box& box) {
 mbpol_status run_dispersion(mbpol_context* ctx, double* energy) {
     WaterTerm& t = ctx->tdisp;
     const int nw = (int)t.waters.size();
-    if (nw < 2) return MBPOL_OK;
+    const int nion = (int)ctx->disp_ions.size();
+    if (nw < 2 && nion == 0) return MBPOL_OK;
     const bool periodic = t.method == MBPOL_CUTOFF_PERIODIC;
     if (periodic) {
         mbpol_status s = check_box(ctx, t.cutoff);
@@ -462,15 +465,19 @@ mbpol_status run_dispersion(mbpol_context* ctx, double* energy) {
     }
     const Box box = term_box(ctx, periodic);
     const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
-    if (ctx->cap_full_d == 0)
-        ctx->cap_full_d = t.method == MBPOL_NOCUTOFF ? (((ctx->ncl > 0 ? t.max_cluster : nw) + 31) / 32) * 32 : 256;
-    if (!ctx->shared_lists) {
-        mbpol_status s = dispersion_list(ctx, box);
-        if (s) return s;
+    if (nw >= 2) {
+        if (ctx->cap_full_d == 0)
+            ctx->cap_full_d = t.method == MBPOL_NOCUTOFF ? (((ctx->ncl > 0 ? t.max_cluster : nw) + 31) / 32) * 32 : 256;
+        if (!ctx->shared_lists) {
+            mbpol_status s = dispersion_list(ctx, box);
+            if (s) return s;
+        }
+        launch_dispersion(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, ctx->full_d.as<int>(),
+                          ctx->nfull_d.as<int>(), ctx->cap_full_d, rc, ctx->d_force.as<double>(), energy,
+                          term_sink(ctx, t, MBPOL_TERM_DISPERSION));
     }
-    launch_dispersion(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, ctx->full_d.as<int>(),
-                      ctx->nfull_d.as<int>(), ctx->cap_full_d, rc, ctx->d_force.as<double>(), energy,
-                      term_sink(ctx, t, MBPOL_TERM_DISPERSION));
+    launch_dispersion_ions(ctx->st, nion, ctx->d_disp_ions.as<int>(), nw, t.d_waters.as<int4>(),
+                           ctx->d_pos.as<double>(), box, rc, ctx->d_force.as<double>(), energy);
     return MBPOL_OK;
 }
 
@@ -654,6 +661,26 @@ mbpol_status mbpol_add_dispersion_force(mbpol_context* ctx, int nw, const int* w
     return set_term(ctx, ctx->tdisp, nw, w, method, cutoff, 0);
 }
 
+mbpol_status mbpol_add_dispersion_ions(mbpol_context* ctx, int num_ions, const int* particles) {
+    if (!ctx || num_ions < 0 || (num_ions > 0 && !particles))
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad ion list");
+    if (!ctx->tdisp.on) return mbpol_fail(MBPOL_ERR_STATE, "add the dispersion force first");
+    std::vector<int> ions(particles, particles + num_ions);
+    for (int p : ions)
+        if (p < 0 || p >= ctx->N) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "ion particle index out of range");
+    for (const int4& w : ctx->tdisp.waters)
+        for (int p : ions)
+            if (p == w.x || p == w.y || p == w.z)
+                return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "an ion particle is also a water atom");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    ctx->disp_ions.insert(ctx->disp_ions.end(), ions.begin(), ions.end());
+    MBPOL_CUDA_OK(ctx->d_disp_ions.ensure(sizeof(int) * std::max<size_t>(ctx->disp_ions.size(), 1)));
+    if (!ctx->disp_ions.empty())
+        MBPOL_CUDA_OK(cudaMemcpy(ctx->d_disp_ions.p, ctx->disp_ions.data(), sizeof(int) * ctx->disp_ions.size(),
+                                 cudaMemcpyHostToDevice));
+    return MBPOL_OK;
+}
+
 mbpol_status mbpol_add_electrostatics_force(mbpol_context* ctx, const mbpol_electrostatics_params* p,
                                             const double* charge, const int* molecule, const int* atom_type,
                                             const double* damping, const double* polarity) {
@@ -714,6 +741,7 @@ mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
         for (const WaterTerm* t : {&ctx->t1, &ctx->t2, &ctx->t3, &ctx->tdisp})
             if (t->on && (t->method == MBPOL_CUTOFF_PERIODIC || (t == &ctx->t1 && t->method == MBPOL_ONEBODY_PERIODIC)))
                 return mbpol_fail(MBPOL_ERR_STATE, "batched clusters need non-periodic methods");
+        if (!ctx->disp_ions.empty()) return mbpol_fail(MBPOL_ERR_STATE, "batched clusters of waters only (no ions)");
         MBPOL_CUDA_OK(cudaMemsetAsync(ctx->d_cl_energy.p, 0, sizeof(double) * MBPOL_NUM_TERMS * (size_t)ctx->ncl,
                                       ctx->st));
     }

@@ -7,7 +7,7 @@
 // PME, no switching, no long-range correction).
 //
 // One thread per (water i, neighbour slot); only j > i is evaluated so each
-// water pair is visited once.  FP32 pair arithmetic from FP64 minimum-image
+// water pair is visited once.  Chloride ions: dispersion_ions_kernel.  FP32 pair arithmetic from FP64 minimum-image
 // differences; FP64 force atomics and energy reduction.
 #include "mbpol_internal.cuh"
 #include "mbpol_kernels.h"
@@ -82,6 +82,71 @@ __global__ void dispersion_kernel(int nw, const int4* __restrict__ waters, const
         }
     }
     block_sum_atomic<128>(e_out, energy);
+}
+
+// Chloride ions (class CL = 3 of the tables, python/mbpol.xml:52-83): one
+// thread per (ion, partner) with the partners the O, H1, H2 sites of every
+// water, then the other ions (j > i); the same damped -C6 tt6 / r^6 with
+// site distances within the cutoff.  Few ions per system, so the partners
+// are not listed.
+__global__ void dispersion_ions_kernel(int nion, const int* __restrict__ ions, int nw, const int4* __restrict__ waters,
+                                       const double* __restrict__ pos, Box box, float rc2, double* __restrict__ force,
+                                       double* __restrict__ energy) {
+    const int np = 3 * nw + nion;
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    double e_out = 0.0;
+    if (gid < (long)nion * np) {
+        const int i = (int)(gid / np), j = (int)(gid - (long)i * np);
+        int pj = -1, cls = 0;
+        if (j < 3 * nw) {
+            const int4 w = waters[j / 3];
+            const int a = j % 3;
+            pj = a == 0 ? w.x : (a == 1 ? w.y : w.z);
+            cls = a == 0 ? 0 : 1;
+        } else if (j - 3 * nw > i) {
+            pj = ions[j - 3 * nw];
+            cls = 3;
+        }
+        const int pi = ions[i];
+        const float c6 = pj >= 0 ? c_disp_c6[3 * 4 + cls] : 0.f;
+        if (c6 != 0.f) {
+            const double3 a = load_pos(pos, pi), b = load_pos(pos, pj);
+            double dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+            if (box.periodic) {
+                dx = min_image(dx, box.L[0], box.inv[0]);
+                dy = min_image(dy, box.L[1], box.inv[1]);
+                dz = min_image(dz, box.L[2], box.inv[2]);
+            }
+            const f3 d = mk((float)dx, (float)dy, (float)dz);
+            const float r2 = dot(d, d);
+            if (r2 <= rc2) {
+                const float d6 = c_disp_d6[3 * 4 + cls];
+                const float r = sqrtf(r2), x = d6 * r, ex = expf(-x);
+                const float s6 = 1.f + x * (1.f + x * (0.5f + x * (1.f / 6.f + x * (1.f / 24.f + x * (1.f / 120.f + x * (1.f / 720.f))))));
+                const float tt = 1.f - ex * s6;
+                float x6 = x * x * x;
+                x6 *= x6;
+                const float dtt = d6 * ex * x6 * (1.f / 720.f);
+                const float ir2 = 1.f / r2, ir6 = ir2 * ir2 * ir2;
+                const float dEdr = -c6 * (dtt * ir6 - 6.f * tt * ir6 / r);
+                const f3 f = d * (-dEdr / r);
+                add_force(force, pj, f.x, f.y, f.z);
+                add_force(force, pi, -f.x, -f.y, -f.z);
+                e_out = -c6 * tt * ir6;
+            }
+        }
+    }
+    block_sum_atomic<128>(e_out, energy);
+}
+
+void launch_dispersion_ions(cudaStream_t st, int nion, const int* ions, int nw, const int4* waters,
+                            const double* pos, Box box, double rc, double* force, double* energy) {
+    if (nion <= 0) return;
+    const long total = (long)nion * (3 * (long)nw + nion);
+    const float rc2 = rc > 1e15 ? 3.0e38f : (float)(rc * rc);
+    count_launch();
+    dispersion_ions_kernel<<<(int)((total + 127) / 128), 128, 0, st>>>(nion, ions, nw, waters, pos, box, rc2, force,
+                                                                        energy);
 }
 
 void upload_dispersion_tables(const double* c6_4x4, const double* d6_4x4) {

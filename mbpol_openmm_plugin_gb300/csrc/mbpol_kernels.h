@@ -63,6 +63,9 @@ void upload_dispersion_tables(const double* c6_4x4, const double* d6_4x4);
 void launch_dispersion(cudaStream_t st, int nw, const int4* waters, const double* pos, Box box, const int* full,
                        const int* nfull, int cap_full, double rc, double* force, double* energy,
                        ClusterSink cs = ClusterSink());
+// chloride ions (particle indices) against the water sites and each other
+void launch_dispersion_ions(cudaStream_t st, int nion, const int* ions, int nw, const int4* waters,
+                            const double* pos, Box box, double rc, double* force, double* energy);
 
 // md.cu
 void launch_kick_drift(cudaStream_t st, int n, const double* invm, double* vel, double* pos, const double* force,

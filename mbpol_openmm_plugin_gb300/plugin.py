@@ -144,6 +144,17 @@ class MBPolDispersionForce(_CutoffWaterForce):
         super().__init__(0.9)
         self.c6 = DISP_C6.copy()
         self.d6 = DISP_D6.copy()
+        self._ions = []
+
+    def addIon(self, particleIndex):
+        """A chloride ion (class Cl of the tables, python/mbpol.xml:52-83):
+        it interacts with the O and H sites of every water and with the
+        other ions, as the xml's CustomNonbondedForce does for a Cl residue."""
+        self._ions.append(int(particleIndex))
+        return len(self._ions) - 1
+
+    def getNumIons(self):
+        return len(self._ions)
 
 
 class MBPolElectrostaticsForce:
@@ -431,6 +442,9 @@ class Context:
                 c6 = as_c(f.c6, np.float64)
                 d6 = as_c(f.d6, np.float64)
                 check(lib.mbpol_add_dispersion_force(h, nw, ptr(w), f._method, f._cutoff, ptr(c6), ptr(d6)))
+                if f._ions:
+                    ions = as_c(f._ions, np.int32)
+                    check(lib.mbpol_add_dispersion_ions(h, len(f._ions), ptr(ions)))
             else:
                 raise TypeError("unsupported force %r" % (f,))
 

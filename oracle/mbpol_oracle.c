@@ -456,3 +456,52 @@ double orc_dispersion(int nw, const int* w, const double* pos, const double* box
                 }
     return e;
 }
+
+/* Dispersion of chloride ions (class CL, python/mbpol.xml:52-83): every ion
+ * with the O and H sites of every water and with every other ion (C6 Cl-Cl
+ * = 0 in the table), site distances within rc (minimum image with a box);
+ * the same damped -C6 tt6 / r^6 as the water pairs.  Returns the energy
+ * (kJ/mol) and adds the forces into f. */
+double orc_dispersion_ions(int nw, const int* w, int nion, const int* ions, const double* pos, const double* box,
+                           double rc, double* f) {
+    /* [class of the partner: O, H, CL] against CL */
+    static const double C6[3] = {0.00456078851, 0.00085979832, 0.0};
+    static const double D6[3] = {1.638868407461115e+02, 5.778854012725382e+01, 0.0};
+    double e = 0.0;
+    for (int i = 0; i < nion; ++i) {
+        const int pi = ions[i];
+        for (int j = 0; j < 3 * nw + nion; ++j) {
+            int pj, c;
+            if (j < 3 * nw) {
+                pj = w[j];
+                c = j % 3 ? 1 : 0;
+            } else {
+                if (j - 3 * nw <= i) continue;
+                pj = ions[j - 3 * nw];
+                c = 2;
+            }
+            if (C6[c] == 0.0) continue;
+            double d[3];
+            for (int k = 0; k < 3; ++k) {
+                d[k] = pos[3 * pj + k] - pos[3 * pi + k];
+                if (box) d[k] = mimg(d[k], box[k]);
+            }
+            const double r2 = dot3(d, d);
+            if (r2 > rc * rc) continue;
+            const double r = sqrt(r2), x = D6[c] * r;
+            double s = 1.0, t = 1.0;
+            for (int n = 1; n <= 6; ++n) {
+                t *= x / n;
+                s += t;
+            }
+            const double tt = 1.0 - exp(-x) * s, dtt = D6[c] * exp(-x) * pow(x, 6) / 720.0;
+            e += -C6[c] * tt / pow(r, 6);
+            const double dEdr = -C6[c] * (dtt / pow(r, 6) - 6.0 * tt / pow(r, 7));
+            for (int k = 0; k < 3; ++k) {
+                f[3 * pj + k] += -dEdr * d[k] / r;
+                f[3 * pi + k] -= -dEdr * d[k] / r;
+            }
+        }
+    }
+    return e;
+}

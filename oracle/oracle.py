@@ -98,6 +98,8 @@ def port():
     L.orc_threebody.argtypes = [I, P, P, P, D, ctypes.c_long, P, LP, LP]
     L.orc_dispersion.restype = D
     L.orc_dispersion.argtypes = [I, P, P, P, D, P]
+    L.orc_dispersion_ions.restype = D
+    L.orc_dispersion_ions.argtypes = [I, P, I, P, P, P, D, P]
     L.orc_electrostatics.restype = I
     L.orc_electrostatics.argtypes = [I, P, P, I, D, P, D, D, I, P, I, P, P, P, ctypes.POINTER(I), P]
     L.orc_last_fixed_field.restype = I
@@ -223,6 +225,21 @@ def system_moments(pos, masses, box=None, alpha=0.0, grid=(0, 0, 0), eps=1e-8, r
     if L.orc_system_moments(_p(m), _p(out)):
         raise RuntimeError("no electrostatics state")
     return out
+
+
+def dispersion(pos, waters, ions=(), box=None, rc=1e30):
+    """Dispersion energy (kJ/mol) and forces of the port: the water pairs
+    (O, H sites) and the chloride ions' pairs (python/mbpol.xml:37-108)."""
+    import numpy as np
+    L = port()
+    pos = np.ascontiguousarray(pos, np.float64)
+    w = np.ascontiguousarray(waters, np.int32)
+    ions = np.ascontiguousarray(ions, np.int32)
+    b = None if box is None else np.ascontiguousarray(box, np.float64)
+    f = np.zeros_like(pos)
+    e = L.orc_dispersion(w.shape[0], _p(w), _p(pos), _p(b), rc, _p(f))
+    e += L.orc_dispersion_ions(w.shape[0], _p(w), ions.shape[0], _p(ions), _p(pos), _p(b), rc, _p(f))
+    return e, f
 
 
 def fixed_field(pos, box=None, alpha=0.0, grid=(0, 0, 0), rc=0.9):

@@ -13,7 +13,7 @@ Sources:
 Dispersion has no plugin code in the reference (python/mbpol.xml:37-108 builds
 an OpenMM CustomNonbondedForce); its values come from the C oracle port.
 
-    python tests/golden/make_golden.py [/path/to/reference] [elec|pdb|potential|moments]
+    python tests/golden/make_golden.py [/path/to/reference] [elec|pdb|potential|moments|dispersion]
 """
 import ctypes
 import json
@@ -331,6 +331,29 @@ def main_potential():
         print(name, seed, "potential range %.4f .. %.4f kJ/mol/e" % (out.min(), out.max()))
 
 
+def main_dispersion():
+    """Dispersion known answers of the reference's own tests
+    (python/tests/TestCustomDispersion.py:14-47, 49-83: water3.pdb and
+    water_and_ion.pdb, CutoffNonPeriodic at 1000 nm, -6.84471477 and
+    -1.306598 kcal/mol, asserted there to 0.01) with the oracle's energy and
+    forces (the reference builds this term from python/mbpol.xml:37-108 as an
+    OpenMM CustomNonbondedForce, which is not available here)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    pdbdir = os.path.join(REF, "python", "tests", "pdb_files")
+    for name, fn, expected in (("water3", "water3.pdb", -6.84471477),
+                               ("water_and_ion", "water_and_ion.pdb", -1.306598)):
+        pos = read_pdb(os.path.join(pdbdir, fn))
+        nw = pos.shape[0] // 4
+        pos = place_m(pos)
+        waters = np.stack([4 * np.arange(nw), 4 * np.arange(nw) + 1, 4 * np.arange(nw) + 2], 1).astype(np.int32)
+        ions = np.arange(4 * nw, pos.shape[0], dtype=np.int32)
+        e, f = oracle.dispersion(pos, waters, ions, None, 1e3)
+        np.savez_compressed(os.path.join(HERE, "disp_%s.npz" % name), positions=pos, waters=waters, ions=ions,
+                            edisp=e, fdisp=f, expected_kcal=expected, expected_tol_kcal=0.01)
+        print("%-14s dispersion %.8f kcal/mol (reference test expects %.8f)" % (name, e / 4.184, expected))
+
+
 def main_moments():
     """getSystemElectrostaticsMoments (MBPolReferenceKernels.cpp:285-303,
     MBPolReferenceElectrostaticsForce.cpp:923-1021) of the compiled
@@ -375,9 +398,12 @@ if __name__ == "__main__":
         main_pdb()
     elif len(sys.argv) > 2 and sys.argv[2] == "moments":
         main_moments()
+    elif len(sys.argv) > 2 and sys.argv[2] == "dispersion":
+        main_dispersion()
     else:
         main()
         main_elec()
         main_pdb()
         main_potential()
         main_moments()
+        main_dispersion()

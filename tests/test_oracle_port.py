@@ -99,3 +99,32 @@ def test_port_system_moments(name):
                                 tuple(int(v) for v in d["grid"]))
     ref = d["moments"]
     assert np.max(np.abs(out - ref)) <= 1e-10 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("name", ["disp_water3", "disp_water_and_ion"])
+def test_port_dispersion_known_answers(name):
+    """Dispersion (python/mbpol.xml:37-108, chloride included) against the
+    reference's own known answers (python/tests/TestCustomDispersion.py:14,
+    50), at that test's tolerance of 0.01 kcal/mol."""
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    e, f = oracle.dispersion(d["positions"], d["waters"], d["ions"], None, 1e3)
+    assert abs(e / 4.184 - float(d["expected_kcal"])) <= float(d["expected_tol_kcal"])
+    assert abs(e - float(d["edisp"])) <= 1e-12 * abs(e)
+    assert np.allclose(f, d["fdisp"], rtol=0, atol=1e-12)
+
+
+def test_port_dispersion_ion_forces_match_finite_differences():
+    """The port's chloride forces are minus the gradient of its energy
+    (central differences on every coordinate of the water-and-ion case)."""
+    d = np.load(os.path.join(GOLDEN, "disp_water_and_ion.npz"))
+    pos = d["positions"].copy()
+    e0, f = oracle.dispersion(pos, d["waters"], d["ions"], None, 1e3)
+    h = 1e-6
+    for i in (0, 1, 2, 4):
+        for k in range(3):
+            p = pos.copy()
+            p[i, k] += h
+            ep, _ = oracle.dispersion(p, d["waters"], d["ions"], None, 1e3)
+            p[i, k] -= 2 * h
+            em, _ = oracle.dispersion(p, d["waters"], d["ions"], None, 1e3)
+            assert abs(-(ep - em) / (2 * h) - f[i, k]) <= 1e-6 * np.abs(f).max()
