@@ -7,3 +7,6 @@ from .plugin import (  # noqa: F401
     ThreeParticleAverageSite, System, Context, State, create_mbpol_system, pme_parameters,
 )
 from ._capi import MBPolError  # noqa: F401
+from .forcefield import (  # noqa: F401
+    ForceField, PDBFile, CMMotionRemover, NoCutoff, CutoffNonPeriodic, CutoffPeriodic, PME,
+)

@@ -362,6 +362,18 @@ class System:
         self.forces.append(f)
         return len(self.forces) - 1
 
+    def getNumForces(self):
+        return len(self.forces)
+
+    def getForce(self, i):
+        return self.forces[i]
+
+    def removeForce(self, i):
+        del self.forces[i]
+
+    def getParticleMass(self, i):
+        return self.masses[i]
+
     def setDefaultPeriodicBoxVectors(self, a, b, c):
         self.box = np.array([a[0], b[1], c[2]], float)
 
@@ -417,6 +429,8 @@ class Context:
         for idx, vs in sorted(self.system.vsites.items()):
             check(lib.mbpol_add_average3_site(h, idx, *vs.particles, *vs.weights))
         for f in self.system.forces:
+            if getattr(f, "_no_kernel", False):  # e.g. the centre-of-mass motion remover
+                continue
             if isinstance(f, MBPolElectrostaticsForce):
                 if f.getNumElectrostatics() != n:
                     raise _capi.MBPolError(1, "MBPolElectrostaticsForce must have exactly as many particles as the System")
@@ -462,6 +476,8 @@ class Context:
         check(lib.mbpol_set_positions(self._h, ptr(self._pos), ptr(box)))
         mask = 0
         for f in self.system.forces:
+            if getattr(f, "_no_kernel", False):
+                continue
             g = f.getForceGroup()
             if groups is None or (int(groups) >> g) & 1:
                 mask |= 1 << TERM_OF[type(f)]
