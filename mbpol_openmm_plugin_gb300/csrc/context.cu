@@ -154,6 +154,10 @@ struct mbpol_context {
     // polynomial terms (independent work; both latency-bound)
     cudaStream_t st_e = nullptr;
     cudaEvent_t ev_pos = nullptr, ev_elec = nullptr;
+    // the one-body term (FP64, few threads) and the dispersion (latency
+    // bound) run on a third stream beside the lists and the walks
+    cudaStream_t st_a = nullptr;
+    cudaEvent_t ev_lists = nullptr, ev_aux = nullptr;
 };
 
 namespace {
@@ -292,7 +296,12 @@ mbpol_status twobody_list(mbpol_context* ctx, const Box& box, double rc, int* np
     return mbpol_fail(MBPOL_ERR_CAPACITY, "two-body pair list capacity");
 }
 
-mbpol_status run_twobody(mbpol_context* ctx, double* energy) {
+// Each term runs in two phases: the list phase builds its neighbour list on
+// ctx->st (host synchronisations for the list sizes), the launch phase
+// queues its kernels on `ls` without synchronising.  All list phases run
+// before any launch phase, so no host wait queues behind a walk and the
+// electrostatics stream starts while the walks run.
+mbpol_status run_twobody(mbpol_context* ctx, double* energy, cudaStream_t ls, bool list_phase) {
     WaterTerm& t = ctx->t2;
     const int nw = (int)t.waters.size();
     if (nw < 2) return MBPOL_OK;
@@ -303,24 +312,26 @@ mbpol_status run_twobody(mbpol_context* ctx, double* energy) {
     }
     const Box box = term_box(ctx, periodic);
     const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
-    int np = 0;
-    if (ctx->shared_lists) {
-        np = (int)ctx->counts[0];
-    } else {
-        mbpol_status s = twobody_list(ctx, box, rc, &np);
-        if (s) return s;
+    if (list_phase) {
+        if (!ctx->shared_lists) {
+            int np = 0;
+            mbpol_status s = twobody_list(ctx, box, rc, &np);
+            if (s) return s;
+            ctx->counts[0] = np;
+        }
+        return MBPOL_OK;
     }
-    ctx->counts[0] = np;
+    const int np = (int)ctx->counts[0];
     const int stride = ctx->cap2;
     MBPOL_CUDA_OK(ctx->x2.ensure(sizeof(float) * 2 * 31 * (size_t)stride));
     MBPOL_CUDA_OK(ctx->g2.ensure(sizeof(float) * 31 * (size_t)stride));
     MBPOL_CUDA_OK(ctx->e2.ensure(sizeof(float) * (size_t)stride));
-    launch_twobody_vars(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
+    launch_twobody_vars(ls, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
                         ctx->x2.as<float>(), stride);
-    prof_begin(ctx->st, K_POLY2B);
-    launch_poly2b(ctx->st, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride, ctx->num_sms);
-    prof_end(ctx->st, K_POLY2B);
-    launch_twobody_forces(ctx->st, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
+    prof_begin(ls, K_POLY2B);
+    launch_poly2b(ls, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride, ctx->num_sms);
+    prof_end(ls, K_POLY2B);
+    launch_twobody_forces(ls, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
                           ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy,
                           term_sink(ctx, t, MBPOL_TERM_TWOBODY));
     return MBPOL_OK;
@@ -374,7 +385,7 @@ mbpol_status threebody_list(mbpol_context* ctx, const Box& box, double rc, int* 
     return mbpol_fail(MBPOL_ERR_CAPACITY, "three-body neighbour capacity");
 }
 
-mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
+mbpol_status run_threebody(mbpol_context* ctx, double* energy, cudaStream_t ls, bool list_phase) {
     WaterTerm& t = ctx->t3;
     const int nw = (int)t.waters.size();
     if (nw < 3) return MBPOL_OK;
@@ -386,14 +397,16 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
     const Box box = term_box(ctx, periodic);
     const double rc = t.method == MBPOL_NOCUTOFF ? 1e30 : t.cutoff;
     const bool complete = t.rule == MBPOL_TRIMER_COMPLETE;
-    int ntrip = 0;
-    if (ctx->shared_lists) {
-        ntrip = (int)ctx->counts[1];
-    } else {
-        mbpol_status s = threebody_list(ctx, box, rc, &ntrip);
-        if (s) return s;
+    if (list_phase) {
+        if (!ctx->shared_lists) {
+            int ntrip = 0;
+            mbpol_status s = threebody_list(ctx, box, rc, &ntrip);
+            if (s) return s;
+            ctx->counts[1] = ntrip;
+        }
+        return MBPOL_OK;
     }
-    ctx->counts[1] = ntrip;
+    const int ntrip = (int)ctx->counts[1];
     if (ntrip > ctx->cap3) ctx->cap3 = ntrip + ntrip / 4 + 64;
     const int stride = ctx->cap3;
     MBPOL_CUDA_OK(ctx->trips3.ensure(sizeof(int4) * (size_t)stride));
@@ -401,19 +414,19 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy) {
     MBPOL_CUDA_OK(ctx->g3.ensure(sizeof(float) * 36 * (size_t)stride));
     MBPOL_CUDA_OK(ctx->e3.ensure(sizeof(float) * (size_t)stride));
     if (!complete)
-        launch_trimer_fill(ctx->st, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
+        launch_trimer_fill(ls, nw, ctx->lower3.as<int>(), ctx->nlower3.as<int>(), ctx->cap_lower3,
                            ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>());
     else
-        launch_trimer_complete(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
+        launch_trimer_complete(ls, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, rc,
                                ctx->full3.as<int>(), ctx->nfull3.as<int>(), ctx->cap_full3, nullptr,
                                ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>(), true);
-    launch_threebody_vars(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+    launch_threebody_vars(ls, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                           box, ctx->x3.as<float>(), stride);
-    prof_begin(ctx->st, K_POLY3B);
-    launch_poly3b(ctx->st, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
+    prof_begin(ls, K_POLY3B);
+    launch_poly3b(ls, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
                   ctx->num_sms);
-    prof_end(ctx->st, K_POLY3B);
-    launch_threebody_forces(ctx->st, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+    prof_end(ls, K_POLY3B);
+    launch_threebody_forces(ls, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                             box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride, ctx->d_force.as<double>(), energy,
                             term_sink(ctx, t, MBPOL_TERM_THREEBODY));
     return MBPOL_OK;
@@ -453,7 +466,7 @@ mbpol_status dispersion_list(mbpol_context* ctx, const Box& box) {
     return mbpol_fail(MBPOL_ERR_CAPACITY, "dispersion neighbour capacity");
 }
 
-mbpol_status run_dispersion(mbpol_context* ctx, double* energy) {
+mbpol_status run_dispersion(mbpol_context* ctx, double* energy, cudaStream_t ls, bool list_phase) {
     WaterTerm& t = ctx->tdisp;
     const int nw = (int)t.waters.size();
     const int nion = (int)ctx->disp_ions.size();
@@ -468,15 +481,19 @@ mbpol_status run_dispersion(mbpol_context* ctx, double* energy) {
     if (nw >= 2) {
         if (ctx->cap_full_d == 0)
             ctx->cap_full_d = t.method == MBPOL_NOCUTOFF ? (((ctx->ncl > 0 ? t.max_cluster : nw) + 31) / 32) * 32 : 256;
-        if (!ctx->shared_lists) {
-            mbpol_status s = dispersion_list(ctx, box);
-            if (s) return s;
+        if (list_phase) {
+            if (!ctx->shared_lists) {
+                mbpol_status s = dispersion_list(ctx, box);
+                if (s) return s;
+            }
+            return MBPOL_OK;
         }
-        launch_dispersion(ctx->st, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, ctx->full_d.as<int>(),
+        launch_dispersion(ls, nw, t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box, ctx->full_d.as<int>(),
                           ctx->nfull_d.as<int>(), ctx->cap_full_d, rc, ctx->d_force.as<double>(), energy,
                           term_sink(ctx, t, MBPOL_TERM_DISPERSION));
     }
-    launch_dispersion_ions(ctx->st, nion, ctx->d_disp_ions.as<int>(), nw, t.d_waters.as<int4>(),
+    if (list_phase) return MBPOL_OK;
+    launch_dispersion_ions(ls, nion, ctx->d_disp_ions.as<int>(), nw, t.d_waters.as<int4>(),
                            ctx->d_pos.as<double>(), box, rc, ctx->d_force.as<double>(), energy);
     return MBPOL_OK;
 }
@@ -588,8 +605,11 @@ mbpol_status mbpol_context_create(int num_particles, int device, mbpol_context**
     ctx->device = device;
     MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
     MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st_e, cudaStreamNonBlocking));
+    MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st_a, cudaStreamNonBlocking));
     MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_pos, cudaEventDisableTiming));
     MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_elec, cudaEventDisableTiming));
+    MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_lists, cudaEventDisableTiming));
+    MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_aux, cudaEventDisableTiming));
     MBPOL_CUDA_OK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
     MBPOL_CUDA_OK(ctx->d_pos.ensure(sizeof(double) * 3 * (size_t)num_particles));
     MBPOL_CUDA_OK(ctx->d_force.ensure(sizeof(double) * 3 * (size_t)num_particles));
@@ -608,12 +628,16 @@ mbpol_status mbpol_context_destroy(mbpol_context* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->st);
     if (ctx->st_e) cudaStreamSynchronize(ctx->st_e);
+    if (ctx->st_a) cudaStreamSynchronize(ctx->st_a);
     ctx->elec.reset();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev_pos) cudaEventDestroy(ctx->ev_pos);
     if (ctx->ev_elec) cudaEventDestroy(ctx->ev_elec);
+    if (ctx->ev_lists) cudaEventDestroy(ctx->ev_lists);
+    if (ctx->ev_aux) cudaEventDestroy(ctx->ev_aux);
     if (ctx->st_e) cudaStreamDestroy(ctx->st_e);
+    if (ctx->st_a) cudaStreamDestroy(ctx->st_a);
     cudaStreamDestroy(ctx->st);
     delete ctx;
     return MBPOL_OK;
@@ -748,25 +772,35 @@ mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
     // positions (with M sites) and zeroed outputs are ready here: the
     // electrostatics stream starts from this point, not after the terms below
     MBPOL_CUDA_OK(cudaEventRecord(ctx->ev_pos, ctx->st));
+    MBPOL_CUDA_OK(cudaStreamWaitEvent(ctx->st_a, ctx->ev_pos, 0));
     if ((mask & MBPOL_TERM_BIT(MBPOL_TERM_ONEBODY)) && ctx->t1.on) {
         const bool periodic = ctx->t1.method == MBPOL_ONEBODY_PERIODIC && ctx->box.periodic;
-        launch_onebody(ctx->st, (int)ctx->t1.waters.size(), ctx->t1.d_waters.as<int4>(), ctx->d_pos.as<double>(),
+        launch_onebody(ctx->st_a, (int)ctx->t1.waters.size(), ctx->t1.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                        term_box(ctx, periodic), ctx->d_force.as<double>(), e + MBPOL_TERM_ONEBODY,
                        term_sink(ctx, ctx->t1, MBPOL_TERM_ONEBODY));
     }
+    const bool do2 = (mask & MBPOL_TERM_BIT(MBPOL_TERM_TWOBODY)) && ctx->t2.on;
+    const bool do3 = (mask & MBPOL_TERM_BIT(MBPOL_TERM_THREEBODY)) && ctx->t3.on;
+    const bool dod = (mask & MBPOL_TERM_BIT(MBPOL_TERM_DISPERSION)) && ctx->tdisp.on;
     ctx->shared_lists = false;
     if (!s) s = build_shared_lists(ctx, mask, &ctx->shared_lists);
-    if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_TWOBODY)) && ctx->t2.on) s = run_twobody(ctx, e + MBPOL_TERM_TWOBODY);
-    if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_THREEBODY)) && ctx->t3.on)
-        s = run_threebody(ctx, e + MBPOL_TERM_THREEBODY);
-    if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_DISPERSION)) && ctx->tdisp.on)
-        s = run_dispersion(ctx, e + MBPOL_TERM_DISPERSION);
+    if (!s && do2) s = run_twobody(ctx, e + MBPOL_TERM_TWOBODY, ctx->st, true);
+    if (!s && do3) s = run_threebody(ctx, e + MBPOL_TERM_THREEBODY, ctx->st, true);
+    if (!s && dod) s = run_dispersion(ctx, e + MBPOL_TERM_DISPERSION, ctx->st, true);
+    if (!s) {
+        MBPOL_CUDA_OK(cudaEventRecord(ctx->ev_lists, ctx->st));
+        MBPOL_CUDA_OK(cudaStreamWaitEvent(ctx->st_a, ctx->ev_lists, 0));
+    }
+    if (!s && dod) s = run_dispersion(ctx, e + MBPOL_TERM_DISPERSION, ctx->st_a, false);
+    if (!s && do2) s = run_twobody(ctx, e + MBPOL_TERM_TWOBODY, ctx->st, false);
+    if (!s && do3) s = run_threebody(ctx, e + MBPOL_TERM_THREEBODY, ctx->st, false);
     ctx->shared_lists = false;
+    MBPOL_CUDA_OK(cudaEventRecord(ctx->ev_aux, ctx->st_a));
     if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS)) && ctx->elec) {
-        // the polynomial and dispersion kernels are queued on st; the
-        // electrostatics (whose solver loop waits on the host every
-        // iteration) run on st_e meanwhile, joined before the M-site
-        // projection.  Both accumulate forces with atomics.
+        // the polynomial kernels are queued on st, the one-body term and
+        // the dispersion on st_a; the electrostatics (whose solver loop
+        // waits on the host every iteration) run on st_e meanwhile, joined
+        // before the M-site projection.  All accumulate forces with atomics.
         MBPOL_CUDA_OK(cudaStreamWaitEvent(ctx->st_e, ctx->ev_pos, 0));
         s = ctx->elec->compute(ctx->st_e, ctx->d_pos.as<double>(), ctx->box, ctx->d_force.as<double>(),
                                e + MBPOL_TERM_ELECTROSTATICS);
@@ -776,9 +810,11 @@ mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
         ctx->counts[3] = ctx->elec->iterations();
         ctx->solver_iterations_total += ctx->elec->iterations();
     }
+    MBPOL_CUDA_OK(cudaStreamWaitEvent(ctx->st, ctx->ev_aux, 0));
     if (s) {
         cudaStreamSynchronize(ctx->st);
         cudaStreamSynchronize(ctx->st_e);
+        cudaStreamSynchronize(ctx->st_a);
         return s;
     }
     launch_spread_vsites(ctx->st, nvs, ctx->d_vs_idx.as<int4>(), ctx->d_vs_w.as<double>(), ctx->d_force.as<double>());
