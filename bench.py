@@ -127,7 +127,7 @@ ALGO_FLOP_PER_UNIT = {"poly2b": 31200, "poly3b": 112600}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # each walk on box4096, measured with ncu --set full, and the units that launch
 # processed; the traffic of a launch is scaled by its unit count.
-NCU_TRAFFIC = {"poly3b": (53.160e6 + 2.438e6, 181889), "poly2b": (16.449e6, 65434)}
+NCU_TRAFFIC = {"poly3b": (53.226e6 + 2.685e6, 181889), "poly2b": (16.451e6, 65434)}
 
 
 def fp32_ops_per_unit(name):

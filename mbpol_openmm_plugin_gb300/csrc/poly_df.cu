@@ -32,7 +32,25 @@ namespace mbpol {
 
 namespace {
 
-constexpr int kBlock = 128;
+// Each unit (dimer or trimer) is walked by kParts threads, each taking a
+// contiguous part of the trie; a block holds kUnits units.
+#ifndef MBPOL_WALK_PARTS
+#define MBPOL_WALK_PARTS 3
+#endif
+constexpr int kParts = MBPOL_WALK_PARTS;
+constexpr int kUnits = 64;
+constexpr int kBlock = kParts * kUnits;
+// resident blocks per SM (shared memory: three-body block of
+// 36 * (kUnits + kBlock) * 8 bytes plus static data)
+constexpr int kBlocksPerSm = kParts == 2 ? 4 : (kParts == 3 ? 3 : 1);
+// Blocks left out of the walk's persistent grid, so that the electrostatics
+// stream finds room beside it: with three parts the walk alone is fastest
+// on every SM, but the electrostatics then end the learned-guess MD step.
+// Measured on box4096 (ms per step over 1000 steps): 0 blocks 12.48, 12
+// blocks 12.14, 24 blocks 12.02, 36 blocks 12.19; two parts 12.32.
+#ifndef MBPOL_WALK_RESERVE_BLOCKS
+#define MBPOL_WALK_RESERVE_BLOCKS 24
+#endif
 
 struct DF {
     float h, l;
@@ -81,7 +99,6 @@ __device__ __forceinline__ void leaf_update(const PolyNode& L, float xl, float x
 // Shared-memory strides: the variables are shared by the two threads of a
 // unit ([variable][unit]), each thread has its own gradient pairs
 // ([variable][thread]).
-constexpr int kUnits = kBlock / 2;  // units per block
 constexpr int kXS = kUnits;         // variable plane stride
 constexpr int kGS = kBlock;         // gradient plane stride
 
@@ -119,30 +136,31 @@ __device__ __forceinline__ void leaf_batch(const PolyNode* __restrict__ lv, cons
     childless_batch<U>(L, xv, gv, P3, V3);
 }
 
-// One half of the trie: level-1 nodes [a0, a1), level-2 nodes [c2_0, c2_1)
+// One part of the trie: level-1 nodes [a0, a1), level-2 nodes [c2_0, c2_1)
 // and the level-3 nodes and leaves under them, which start at c3_0 and
-// cl_0.  When the split falls inside the children of a level-1 node, both
-// halves visit that node and the second leaves out its coefficient
-// (skip_coef): E = sum_i x_i V_i and g_i += V_i are linear in V_i.
+// cl_0.  When a cut falls inside the children of a level-1 node, the parts
+// on both sides visit that node and all but the first leave out its
+// coefficient (skip_coef): E = sum_i x_i V_i and g_i += V_i are linear in
+// V_i.
 struct WalkPart {
     int a0, a1, c2_0, c2_1, c3_0, cl_0, skip_coef;
 };
 struct WalkSplit {
-    WalkPart part[2];
+    WalkPart part[kParts];
 };
 
-// Two threads per unit (dimer or trimer), each walking half of the trie:
-// the unit's variables are stored once for both, so a thread needs
-// NV * 12 bytes of shared memory instead of NV * 16, and an SM holds four
-// 128-thread blocks (16 warps) instead of three.  The two halves' energy and
-// gradient pairs are added at the end (double-float, fixed order).
-// Shared memory holds four blocks per SM; the registers are capped as for
-// six (80 per thread) so that a quarter of the register file stays free for
-// the electrostatics kernels of the other stream, which then run beside the
-// walk (4096-water box: 14.0 against 14.2 ms per MD step; a cap of 72 made
-// the walk slower than the overlap gains).
+// kParts threads per unit (dimer or trimer), each walking a part of the
+// trie: the unit's variables are stored once for all of them, so a thread
+// needs NV * (8 + 8 / kParts) bytes of shared memory (its gradient pairs
+// and its share of the variables).  With three parts an SM holds three
+// 192-thread blocks (18 warps; two parts held 16, one part 12).  The parts'
+// energy and gradient pairs are added at the end (double-float, fixed
+// order).  The registers are capped at 80 per thread, so that a quarter of
+// the register file stays free for the electrostatics kernels of the other
+// stream, which then run beside the walk (a cap of 72 made the walk slower
+// than the overlap gains).
 template <int NV>
-__global__ void __launch_bounds__(kBlock, 6) poly_df_kernel(const PolyNode* __restrict__ l1,
+__global__ void __launch_bounds__(kBlock, 768 / kBlock) poly_df_kernel(const PolyNode* __restrict__ l1,
                                                           const PolyNode* __restrict__ l2,
                                                           const PolyNode* __restrict__ l3, int n3,
                                                           const PolyNode* __restrict__ lv, const WalkSplit split,
@@ -151,21 +169,30 @@ __global__ void __launch_bounds__(kBlock, 6) poly_df_kernel(const PolyNode* __re
     extern __shared__ float2 smem2[];
     float2* xv_all = smem2;                  // [NV][kUnits]  variables (hi, lo)
     float2* gv_all = xv_all + NV * kUnits;   // [NV][kBlock]  gradient pairs
-    __shared__ float e_other[2][kUnits];     // the second half's energy pair
+    __shared__ float e_other[kParts - 1][2][kUnits];  // the other parts' energy pairs
     const int t = threadIdx.x;
-    const int half = t / kUnits;             // warp-uniform
+    const int part = t / kUnits;             // warp-uniform
     const int tu = t % kUnits;
-    const WalkPart& P0 = split.part[0];
-    const WalkPart& P1 = split.part[1];
-    const WalkPart W = {half ? P1.a0 : P0.a0,     half ? P1.a1 : P0.a1,     half ? P1.c2_0 : P0.c2_0,
-                        half ? P1.c2_1 : P0.c2_1, half ? P1.c3_0 : P0.c3_0, half ? P1.cl_0 : P0.cl_0,
-                        half ? P1.skip_coef : P0.skip_coef};
+    // this thread's part, selected field by field (no dynamic indexing of
+    // the parameter array)
+    WalkPart W = split.part[0];
+    #pragma unroll
+    for (int k = 1; k < kParts; ++k)
+        if (part == k) {
+            W.a0 = split.part[k].a0;
+            W.a1 = split.part[k].a1;
+            W.c2_0 = split.part[k].c2_0;
+            W.c2_1 = split.part[k].c2_1;
+            W.c3_0 = split.part[k].c3_0;
+            W.cl_0 = split.part[k].cl_0;
+            W.skip_coef = split.part[k].skip_coef;
+        }
     const float2* xv = xv_all + tu;
     float2* gv = gv_all + t;
     for (int base = blockIdx.x * kUnits; base < n; base += gridDim.x * kUnits) {
         const int u = base + tu;
         const bool live = u < n;
-        for (int v = half; v < NV; v += 2)
+        for (int v = part; v < NV; v += kParts)
             xv_all[v * kXS + tu] = live ? make_float2(X[(size_t)v * stride + u], X[(size_t)(NV + v) * stride + u])
                                         : make_float2(0.f, 0.f);
         #pragma unroll
@@ -284,22 +311,27 @@ __global__ void __launch_bounds__(kBlock, 6) poly_df_kernel(const PolyNode* __re
             acc(g, V1.h, V1.l);
             gv[A.var * kGS] = make_float2(g.h, g.l);
         }
-        if (half) {
-            e_other[0][tu] = Ev.h;
-            e_other[1][tu] = Ev.l;
+        if (part) {
+            e_other[part - 1][0][tu] = Ev.h;
+            e_other[part - 1][1][tu] = Ev.l;
         }
         __syncthreads();
         if (live) {
-            // first half's pair + second half's pair, variables split
-            // between the two threads of the unit
-            for (int v = half; v < NV; v += 2) {
-                const float2 g0 = gv_all[v * kGS + tu], g1 = gv_all[v * kGS + kUnits + tu];
+            // the parts' pairs added in order, the variables divided among
+            // the unit's threads
+            for (int v = part; v < NV; v += kParts) {
+                const float2 g0 = gv_all[v * kGS + tu];
                 DF g = {g0.x, g0.y};
-                acc(g, g1.x, g1.y);
+                #pragma unroll
+                for (int k = 1; k < kParts; ++k) {
+                    const float2 gk = gv_all[v * kGS + k * kUnits + tu];
+                    acc(g, gk.x, gk.y);
+                }
                 G[(size_t)v * stride + u] = __fadd_rn(g.h, g.l);
             }
-            if (!half) {
-                acc(Ev, e_other[0][tu], e_other[1][tu]);
+            if (!part) {
+                #pragma unroll
+                for (int k = 0; k < kParts - 1; ++k) acc(Ev, e_other[k][0][tu], e_other[k][1][tu]);
                 E[u] = __fadd_rn(Ev.h, Ev.l);
             }
         }
@@ -307,12 +339,13 @@ __global__ void __launch_bounds__(kBlock, 6) poly_df_kernel(const PolyNode* __re
     }
 }
 
-// Split of a trie at a level-2 node, the first half taking `frac` of the
+// Split of a trie into kParts parts at level-2 nodes: part k ends where the
 // modelled work (level-3 nodes and leaves weighted by their instruction
-// counts).  The model undercounts the second half's per-node overhead: the
-// fastest splits measured on GB300 (box4096, sweeps of frac) give the first
-// half 54% of the three-body and 57% of the two-body modelled work.
-WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, const PolyNode* l3, double frac) {
+// counts) reaches cut[k] of the total.  The model undercounts the per-node
+// overhead of the later parts, so the fastest cuts measured on GB300
+// (box4096, sweeps) give the earlier parts more than an equal share.
+WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, const PolyNode* l3,
+                     const double (&cut)[kParts - 1]) {
     std::vector<double> w(n2);
     double total = 0.0;
     int c3 = 0, cl = 0;
@@ -326,32 +359,54 @@ WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, con
         w[j] = wj;
         total += wj;
     }
-    int m = 0;
+    // m[k]: first level-2 node of part k; every part gets at least one
+    // (n2 >= kParts for both tries)
+    int m[kParts + 1];
+    m[0] = 0;
+    m[kParts] = n2;
+    int j = 0;
     double pre = 0.0;
-    while (m < n2 && pre + w[m] <= frac * total) pre += w[m++];
-    if (m == 0) m = 1;  // both halves non-empty (n2 >= 2 for both tries)
-    int am = 0;
-    while (am < n1 && l1[am].end <= m) ++am;
-    const int first = am == 0 ? 0 : l1[am - 1].end;
-    const int c3m = l2[m - 1].end;
-    const int clm = c3m == 0 ? 0 : l3[c3m - 1].end;
+    for (int k = 1; k < kParts; ++k) {
+        while (j < n2 && pre + w[j] <= cut[k - 1] * total) pre += w[j++];
+        if (j <= m[k - 1]) pre += w[j++];
+        if (j > n2 - (kParts - k)) j = n2 - (kParts - k);
+        m[k] = j;
+    }
+    // a_start[k]: the level-1 node holding level-2 node m[k]; inside[k]:
+    // m[k] is not that node's first child (the node is shared with part k-1)
+    int a_start[kParts + 1], inside[kParts + 1];
+    for (int k = 1; k < kParts; ++k) {
+        int a = 0;
+        while (a < n1 && l1[a].end <= m[k]) ++a;
+        a_start[k] = a;
+        inside[k] = (a == 0 ? 0 : l1[a - 1].end) != m[k];
+    }
     WalkSplit s;
-    if (first == m) {
-        s.part[0] = WalkPart{0, am, 0, m, 0, 0, 0};
-        s.part[1] = WalkPart{am, n1, m, n2, c3m, clm, 0};
-    } else {
-        s.part[0] = WalkPart{0, am + 1, 0, m, 0, 0, 0};
-        s.part[1] = WalkPart{am, n1, m, n2, c3m, clm, 1};
+    for (int k = 0; k < kParts; ++k) {
+        const int a0 = k == 0 ? 0 : a_start[k];
+        const int a1 = k == kParts - 1 ? n1 : a_start[k + 1] + (inside[k + 1] ? 1 : 0);
+        const int c30 = m[k] == 0 ? 0 : l2[m[k] - 1].end;
+        const int cl0 = c30 == 0 ? 0 : l3[c30 - 1].end;
+        s.part[k] = WalkPart{a0, a1, m[k], m[k + 1], c30, cl0, k > 0 && inside[k] ? 1 : 0};
     }
     return s;
 }
 
+#ifndef MBPOL_WALK_CUTS_2B
+#define MBPOL_WALK_CUTS_2B {0.38, 0.71}
+#endif
+#ifndef MBPOL_WALK_CUTS_3B
+#define MBPOL_WALK_CUTS_3B {0.36, 0.69}
+#endif
+
 const WalkSplit& split2() {
-    static const WalkSplit s = make_split(poly2b_l1, POLY2B_N1, poly2b_l2, POLY2B_N2, poly2b_l3, 0.57);
+    static const double cut[kParts - 1] = MBPOL_WALK_CUTS_2B;
+    static const WalkSplit s = make_split(poly2b_l1, POLY2B_N1, poly2b_l2, POLY2B_N2, poly2b_l3, cut);
     return s;
 }
 const WalkSplit& split3() {
-    static const WalkSplit s = make_split(poly3b_l1, POLY3B_N1, poly3b_l2, POLY3B_N2, poly3b_l3, 0.54);
+    static const double cut[kParts - 1] = MBPOL_WALK_CUTS_3B;
+    static const WalkSplit s = make_split(poly3b_l1, POLY3B_N1, poly3b_l2, POLY3B_N2, poly3b_l3, cut);
     return s;
 }
 
@@ -363,7 +418,8 @@ constexpr int walk_smem() {
 template <int NV>
 int walk_blocks(int n, int num_sms) {
     int blocks = (n + kUnits - 1) / kUnits;
-    if (blocks > num_sms * 4) blocks = num_sms * 4;
+    const int cap = num_sms * kBlocksPerSm - MBPOL_WALK_RESERVE_BLOCKS;
+    if (blocks > cap) blocks = cap > num_sms ? cap : num_sms;
     return blocks;
 }
 
