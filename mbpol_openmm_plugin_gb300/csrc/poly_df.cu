@@ -392,6 +392,14 @@ WalkSplit make_split(const PolyNode* l1, int n1, const PolyNode* l2, int n2, con
     return s;
 }
 
+// Cuts.  Sweeps of the walks alone on box4096 (ms per launch): three-body
+// (0.36, 0.69) 10.15, (0.37, 0.72) 9.81, (0.36, 0.76) 9.61, (0.37, 0.76)
+// 9.53, (0.37, 0.80) 10.54; two-body (0.38, 0.71) 1.73, (0.40, 0.75) 1.56,
+// (0.42, 0.75) 1.63.  In the MD step, where the electrostatics stream runs
+// beside the walks and ends the step, the less balanced cuts are faster
+// (ms per step over 1000 steps, same GPU: 12.10 and 12.01 against 12.39 and
+// 12.40): a block's parts that finish early wait at the barrier and leave
+// issue slots to the electrostatics.
 #ifndef MBPOL_WALK_CUTS_2B
 #define MBPOL_WALK_CUTS_2B {0.38, 0.71}
 #endif
