@@ -919,8 +919,11 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
 // so once the iteration is close, the current dipoles become an anchor whose
 // field is stored once (mode 1) and later iterations evaluate only the field
 // of mu - anchor (mode 2), whose rounding noise is smaller by |mu - anchor|/|mu|.
+// PME (one box): 7 blocks per SM (at most 72 registers) hold a 4096-water
+// box's 1024 blocks in one wave (4096 molecules, one warp each); at 6 blocks
+// a second, nearly empty wave made the launch 80 instead of 50 us.
 template <bool PME>
-__global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ damp,
+__global__ void __launch_bounds__(128, PME ? 7 : 6) induced_update_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ damp,
                                       const float* __restrict__ pol, const int* __restrict__ type,
                                       const int* __restrict__ nb, const float* __restrict__ nbd,
                                       const int* __restrict__ nnb, int cap, const float* __restrict__ E0,
@@ -999,11 +1002,45 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
             E[a][1] = warp_sum(E[a][1]);
             E[a][2] = warp_sum(E[a][2]);
         }
-        // one lane per site a of the molecule (the sites' updates are
-        // independent): its intramolecular field, then the split form's
-        // store or the fused update
+        // intramolecular pairs: coefficients of this geometry from the
+        // fixed-field pass
+        const float* pin = intra + (size_t)2 * kMaxIntra * A;
+        if (PME) {
+            // split form (every PME launch passes Edir): the direct and
+            // intramolecular field only; the reciprocal part and the update
+            // follow in induced_finish_kernel.  Lane 0 takes every site
+            // (compile-time pair indices); this instantiation holds no
+            // fused update.
+            if (lane == 0) {
+                #pragma unroll
+                for (int a = 0; a < kMaxK; ++a)
+                    #pragma unroll
+                    for (int b = 0; b < kMaxK; ++b) {
+                        if (a >= K || b >= K || a == b) continue;
+                        const int p = intra_pair(a, b, K);
+                        const float pf1 = pin[2 * p], pf2 = pin[2 * p + 1];
+                        const f3 mub = ld3(mu_in, K * A + b);
+                        const f3 d = offA[b] - offA[a];
+                        const float dur = dot(mub, d) * pf2;
+                        E[a][0] += d.x * dur + mub.x * pf1;
+                        E[a][1] += d.y * dur + mub.y * pf1;
+                        E[a][2] += d.z * dur + mub.z * pf1;
+                    }
+                #pragma unroll
+                for (int a = 0; a < kMaxK; ++a) {
+                    if (a >= K) continue;
+                    const int i = K * A + a;
+                    Edir[3 * i] = E[a][0];
+                    Edir[3 * i + 1] = E[a][1];
+                    Edir[3 * i + 2] = E[a][2];
+                }
+            }
+        }
+        // fused update: one lane per site a of the molecule (the sites'
+        // updates are independent; batched clusters, 4096 clusters: solver
+        // 38.6 against 55.6 ms with lane 0 taking every site)
         const int a = lane;
-        if (a < K) {
+        if (!PME && a < K) {
             float ea[3] = {0.f, 0.f, 0.f};
             f3 offa = mk(0.f, 0.f, 0.f);
             #pragma unroll
@@ -1014,9 +1051,6 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
                     ea[2] = E[aa][2];
                     offa = offA[aa];
                 }
-            // intramolecular pairs: coefficients of this geometry from the
-            // fixed-field pass
-            const float* pin = intra + (size_t)2 * kMaxIntra * A;
             #pragma unroll
             for (int b = 0; b < kMaxK; ++b) {
                 if (b >= K || a == b) continue;
@@ -1030,13 +1064,7 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
                 ea[2] += d.z * dur + mub.z * pf1;
             }
             const int i = K * A + a;
-            if (Edir) {
-                // split form: the direct and intramolecular field only; the
-                // reciprocal part and the update follow in induced_finish_kernel
-                Edir[3 * i] = ea[0];
-                Edir[3 * i + 1] = ea[1];
-                Edir[3 * i + 2] = ea[2];
-            } else {
+            {
                 const f3 mu = ld3(mu_in, i);
                 const double m0 = mu_d[3 * i], m1 = mu_d[3 * i + 1], m2 = mu_d[3 * i + 2];
                 float ex = ea[0], ey = ea[1], ez = ea[2];
@@ -1087,7 +1115,7 @@ __global__ void __launch_bounds__(128, 6) induced_update_kernel(int nmol, const 
             }
         }
     }
-    if (mcl) {
+    if (!PME && mcl) {  // batched clusters are never periodic
         #pragma unroll
         for (int o = 16; o > 0; o >>= 1) d2sum += __shfl_xor_sync(0xffffffffu, d2sum, o);
         if (cA >= 0 && !frozen && lane == 0) atomicAdd(eps2c + cA, d2sum);
