@@ -216,6 +216,16 @@ mbpol_status mbpol_profile_read(int kernel, double* total_ms, long* launches);
 const char* mbpol_status_string(mbpol_status s);
 const char* mbpol_last_error(void);
 
+/* ---- Three-body polynomial evaluator ------------------------------------
+ * No reference counterpart (the reference runs the generated FP64 code of
+ * platforms/reference/src/poly-3b-v2x.cpp).  MBPOL_POLY3B_TENSOR (default):
+ * the polynomial re-expanded about a fixed point and evaluated as a
+ * quadratic form on the tensor cores (fp16 operand pieces, FP32 sums).
+ * MBPOL_POLY3B_WALK: the double-float trie walk on the FP32 pipe (slower,
+ * ~1e-12 relative).  Both are checked against the FP64 reference. */
+enum { MBPOL_POLY3B_TENSOR = 0, MBPOL_POLY3B_WALK = 1 };
+mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind);
+
 /* ---- Batched independent clusters ---------------------------------------
  * No reference counterpart as one call: the reference evaluates each water
  * cluster in its own OpenMM Context.  Here one context holds many clusters

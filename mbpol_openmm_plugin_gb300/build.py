@@ -4,7 +4,9 @@ Steps (independent ones in parallel):
   1. model tables (one-body PES) -> csrc/gen/model_tables.inc, from data/;
   2. nvcc -c for each csrc/*.cu (sm_103a only), then one shared link with cuFFT.
 The polynomial trie tables (csrc/gen/poly*_tables.inc) are generated by
-codegen/gen_poly.py and committed.
+codegen/gen_poly.py and committed; the tensor-core tables of the three-body
+polynomial are generated here by codegen/gen_poly_tc.py (a few seconds,
+numpy) into _build/poly_tc_tables.cpp and compiled by the host compiler.
 Only sm_103a code is produced.
 """
 import os
@@ -67,13 +69,30 @@ def compile_cu(src):
     return obj
 
 
+def gen_tc_tables():
+    """codegen/gen_poly_tc.py -> _build/poly_tc_tables.cpp -> object (g++)."""
+    src = os.path.join(BUILD, "poly_tc_tables.cpp")
+    obj = src + ".o"
+    inputs = [os.path.join(PKG, "codegen", f) for f in ("gen_poly_tc.py", "gen_poly.py")]
+    inputs += [os.path.join(DATA, "poly3b_%s.txt" % k) for k in ("basis", "coeffs", "shift")]
+    inputs.append(os.path.join(CSRC, "poly_tc.h"))
+    if not os.path.exists(obj) or any(os.path.getmtime(obj) < os.path.getmtime(f) for f in inputs):
+        sys.path.insert(0, os.path.dirname(PKG))
+        from mbpol_openmm_plugin_gb300.codegen import gen_poly_tc
+        gen_poly_tc.generate(src)
+        run([os.environ.get("CXX", "g++"), "-std=c++17", "-O1", "-fPIC", "-I", CSRC, "-c", src, "-o", obj])
+    return obj
+
+
 def build(verbose=True):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(OUT, exist_ok=True)
     gen_model_tables()
     srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
     with ThreadPoolExecutor(max_workers=max(4, os.cpu_count() or 4)) as ex:
+        tc = ex.submit(gen_tc_tables)
         objs = list(ex.map(compile_cu, srcs))
+        objs.append(tc.result())
     lib = os.path.join(OUT, LIBNAME)
     tmp = lib + ".tmp"
     run([NVCC, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs + ["-lcufft", "-lcudart"])

@@ -10,6 +10,7 @@
 #include "../../include/mbpol_gb300.h"
 #include "elec.h"
 #include "mbpol_kernels.h"
+#include "poly_tc_dev.h"
 
 // Generated at build time: one-body tables.
 #include "gen/model_tables.inc"
@@ -124,6 +125,12 @@ struct mbpol_context {
     // three-body buffers
     DevBuf lower3, nlower3, count3, offs3, trips3, x3, g3, e3, full3, nfull3;
     int cap_lower3 = 48, cap3 = 0, cap_full3 = 96;
+    // polynomial tables of this device; the three-body evaluator (tensor
+    // cores by default) and its per-block scratch
+    const PolyWalkTables* walk = nullptr;
+    const PolyTCDev* tc3 = nullptr;
+    int poly3b_kind = MBPOL_POLY3B_TENSOR;
+    DevBuf ztc;
     // dispersion buffers
     DevBuf full_d, nfull_d, lower_d, nlower_d;
     int cap_full_d = 0;
@@ -329,7 +336,8 @@ mbpol_status run_twobody(mbpol_context* ctx, double* energy, cudaStream_t ls, bo
     launch_twobody_vars(ls, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
                         ctx->x2.as<float>(), stride);
     prof_begin(ls, K_POLY2B);
-    launch_poly2b(ls, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride, ctx->num_sms);
+    launch_poly2b(ls, ctx->walk, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride,
+                  ctx->num_sms);
     prof_end(ls, K_POLY2B);
     launch_twobody_forces(ls, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
                           ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy,
@@ -422,9 +430,15 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy, cudaStream_t ls, 
                                ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>(), true);
     launch_threebody_vars(ls, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                           box, ctx->x3.as<float>(), stride);
+    if (ctx->poly3b_kind == MBPOL_POLY3B_TENSOR)
+        MBPOL_CUDA_OK(ctx->ztc.ensure(sizeof(float) * poly3b_tc_scratch_floats(ctx->num_sms)));
     prof_begin(ls, K_POLY3B);
-    launch_poly3b(ls, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
-                  ctx->num_sms);
+    if (ctx->poly3b_kind == MBPOL_POLY3B_TENSOR)
+        launch_poly3b_tc(ls, ctx->tc3, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
+                         ctx->num_sms, ctx->ztc.as<float>());
+    else
+        launch_poly3b(ls, ctx->walk, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
+                      ctx->num_sms);
     prof_end(ls, K_POLY3B);
     launch_threebody_forces(ls, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                             box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride, ctx->d_force.as<double>(), energy,
@@ -618,7 +632,8 @@ mbpol_status mbpol_context_create(int num_particles, int device, mbpol_context**
     ctx->h_force.resize(3 * (size_t)num_particles);
     upload_polyterm_constants(kOneBodyCoef, &kOneBodyIdx[0][0]);
     MBPOL_CUDA_OK(cudaGetLastError());
-    MBPOL_CUDA_OK(poly_tables_upload(device));
+    MBPOL_CUDA_OK(poly_tables_upload(device, &ctx->walk));
+    MBPOL_CUDA_OK(poly_tc_setup(device, &ctx->tc3));
     *out = ctx.release();
     return MBPOL_OK;
 }
@@ -1065,6 +1080,14 @@ mbpol_status mbpol_guess_fit_predictor(mbpol_context* ctx, const double* history
 }
 
 // ---- batched independent clusters (no reference counterpart as one call)
+mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (kind != MBPOL_POLY3B_TENSOR && kind != MBPOL_POLY3B_WALK)
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "unknown three-body evaluator");
+    ctx->poly3b_kind = kind;
+    return MBPOL_OK;
+}
+
 mbpol_status mbpol_set_clusters(mbpol_context* ctx, const int* cluster_of_particle, int num_clusters) {
     if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
     if (num_clusters < 0 || (num_clusters > 0 && !cluster_of_particle))

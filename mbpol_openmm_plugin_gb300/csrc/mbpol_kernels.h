@@ -27,10 +27,14 @@ void launch_threebody_forces(cudaStream_t st, int ntrip, const int4* trips, cons
                              const double* pos, Box box, const float* G, const float* E, int stride,
                              double* force, double* energy, ClusterSink cs = ClusterSink());
 
-// poly_df.cu
-cudaError_t poly_tables_upload(int device);
-void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms);
-void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms);
+// poly_df.cu: the double-float trie walks; tables per device (upload with
+// `device` current, once per process; thread-safe)
+struct PolyWalkTables;
+cudaError_t poly_tables_upload(int device, const PolyWalkTables** out);
+void launch_poly2b(cudaStream_t st, const PolyWalkTables* t, const float* X, float* G, float* E, int n, int stride,
+                   int num_sms);
+void launch_poly3b(cudaStream_t st, const PolyWalkTables* t, const float* X, float* G, float* E, int n, int stride,
+                   int num_sms);
 // the two-body kernel on caller-supplied device tables (raise its dynamic
 // shared-memory limit once per device with poly2b_kernel_setup first)
 cudaError_t poly2b_kernel_setup();

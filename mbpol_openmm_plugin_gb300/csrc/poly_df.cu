@@ -14,12 +14,14 @@
 // and TwoSum, errors collected in c; Ogita, Rump & Oishi, SIAM J. Sci.
 // Comput. 26 (2005)), which gives FP64-level results on the FP32 pipe.
 //
-// Two threads per unit (dimer or trimer), each walking half of the trie.
+// kParts threads per unit (dimer or trimer), each walking a part of the trie.
 // The variables x ([variable][unit]) and the gradient ([variable][thread])
 // live in shared memory as (hi, lo) float2 pairs, so every access of a warp
 // is one conflict-free 8-byte load or store; the trie tables are read with
 // warp-uniform addresses.  X: [2][nvars][stride] floats (FP64 variables as
 // hi and lo planes); G: [nvars][stride]; E: [stride].
+#include <memory>
+#include <mutex>
 #include <vector>
 
 #include "mbpol_internal.cuh"
@@ -437,11 +439,6 @@ struct PolyTables {
     int n1 = 0;
 };
 
-PolyTables<31> g_t2;
-PolyTables<36> g_t3;
-int g_dev_uploaded = -1;
-
-template <class T>
 cudaError_t upload(const PolyNode* src, size_t n, PolyNode** dst) {
     cudaError_t e = cudaMalloc(dst, n * sizeof(PolyNode));
     if (e != cudaSuccess) return e;
@@ -450,24 +447,44 @@ cudaError_t upload(const PolyNode* src, size_t n, PolyNode** dst) {
 
 }  // namespace
 
+// The trie tables of one device (uploaded once per device and process).
+struct PolyWalkTables {
+    bool ready = false;
+    PolyTables<31> t2;
+    PolyTables<36> t3;
+};
+
+namespace {
+std::mutex g_walk_mu;
+std::vector<std::unique_ptr<PolyWalkTables>> g_walk;  // by device ordinal
+}  // namespace
+
 cudaError_t poly2b_kernel_setup() {
     return cudaFuncSetAttribute(poly_df_kernel<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, walk_smem<31>());
 }
 
-cudaError_t poly_tables_upload(int device) {
-    if (g_dev_uploaded == device) return cudaSuccess;
-    cudaError_t e;
-    if ((e = upload<int>(poly2b_l1, POLY2B_N1, &g_t2.l1)) || (e = upload<int>(poly2b_l2, POLY2B_N2, &g_t2.l2)) ||
-        (e = upload<int>(poly2b_l3, POLY2B_N3, &g_t2.l3)) || (e = upload<int>(poly2b_leaf, POLY2B_NL, &g_t2.lv)) ||
-        (e = upload<int>(poly3b_l1, POLY3B_N1, &g_t3.l1)) || (e = upload<int>(poly3b_l2, POLY3B_N2, &g_t3.l2)) ||
-        (e = upload<int>(poly3b_l3, POLY3B_N3, &g_t3.l3)) || (e = upload<int>(poly3b_leaf, POLY3B_NL, &g_t3.lv)))
-        return e;
-    g_t2.n1 = POLY2B_N1;
-    g_t3.n1 = POLY3B_N1;
-    if ((e = poly2b_kernel_setup())) return e;
-    if ((e = cudaFuncSetAttribute(poly_df_kernel<36>, cudaFuncAttributeMaxDynamicSharedMemorySize, walk_smem<36>())))
-        return e;
-    g_dev_uploaded = device;
+cudaError_t poly_tables_upload(int device, const PolyWalkTables** out) {
+    std::lock_guard<std::mutex> lock(g_walk_mu);
+    if (device < 0) return cudaErrorInvalidDevice;
+    if ((size_t)device >= g_walk.size()) g_walk.resize((size_t)device + 1);
+    if (!g_walk[(size_t)device]) g_walk[(size_t)device].reset(new PolyWalkTables());
+    PolyWalkTables& w = *g_walk[(size_t)device];
+    if (!w.ready) {
+        cudaError_t e;
+        if ((e = upload(poly2b_l1, POLY2B_N1, &w.t2.l1)) || (e = upload(poly2b_l2, POLY2B_N2, &w.t2.l2)) ||
+            (e = upload(poly2b_l3, POLY2B_N3, &w.t2.l3)) || (e = upload(poly2b_leaf, POLY2B_NL, &w.t2.lv)) ||
+            (e = upload(poly3b_l1, POLY3B_N1, &w.t3.l1)) || (e = upload(poly3b_l2, POLY3B_N2, &w.t3.l2)) ||
+            (e = upload(poly3b_l3, POLY3B_N3, &w.t3.l3)) || (e = upload(poly3b_leaf, POLY3B_NL, &w.t3.lv)))
+            return e;
+        w.t2.n1 = POLY2B_N1;
+        w.t3.n1 = POLY3B_N1;
+        if ((e = poly2b_kernel_setup())) return e;
+        if ((e = cudaFuncSetAttribute(poly_df_kernel<36>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      walk_smem<36>())))
+            return e;
+        w.ready = true;
+    }
+    *out = &w;
     return cudaSuccess;
 }
 
@@ -479,15 +496,17 @@ void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, const PolyNode* l2,
                                                                                      split2(), X, G, E, n, stride);
 }
 
-void launch_poly2b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms) {
-    launch_poly2b_with(st, g_t2.l1, g_t2.l2, g_t2.l3, g_t2.lv, X, G, E, n, stride, num_sms);
+void launch_poly2b(cudaStream_t st, const PolyWalkTables* t, const float* X, float* G, float* E, int n, int stride,
+                   int num_sms) {
+    launch_poly2b_with(st, t->t2.l1, t->t2.l2, t->t2.l3, t->t2.lv, X, G, E, n, stride, num_sms);
 }
 
-void launch_poly3b(cudaStream_t st, const float* X, float* G, float* E, int n, int stride, int num_sms) {
+void launch_poly3b(cudaStream_t st, const PolyWalkTables* t, const float* X, float* G, float* E, int n, int stride,
+                   int num_sms) {
     if (n <= 0) return;
     count_launch();
     poly_df_kernel<36><<<walk_blocks<36>(n, num_sms), kBlock, walk_smem<36>(), st>>>(
-        g_t3.l1, g_t3.l2, g_t3.l3, POLY3B_N3, g_t3.lv, split3(), X, G, E, n, stride);
+        t->t3.l1, t->t3.l2, t->t3.l3, POLY3B_N3, t->t3.lv, split3(), X, G, E, n, stride);
 }
 
 }  // namespace mbpol

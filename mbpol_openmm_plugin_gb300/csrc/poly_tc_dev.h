@@ -1,0 +1,31 @@
+// Device copy of the tensor-core polynomial tables (poly_tc.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace mbpol {
+
+struct PolyTCDev {
+    int nv = 0, ny = 0, npad = 0;
+    const float* x0h = nullptr;
+    const float* x0l = nullptr;
+    const float* inv_bound = nullptr;
+    const unsigned* ymeta = nullptr;
+    const float* rowscale = nullptr;
+    const int* warp_begin = nullptr;
+    const int* rt_id = nullptr;
+    const int* rt_entry = nullptr;
+    const unsigned short* ent_kt = nullptr;
+    const unsigned* frag = nullptr;
+};
+
+// Uploads the three-body tables to `device` (current) once per process and
+// sets the kernel's shared-memory limit there; thread-safe.
+cudaError_t poly_tc_setup(int device, const PolyTCDev** out);
+// scratch of the three-body launch (floats): one slice of z per block
+size_t poly3b_tc_scratch_floats(int num_sms);
+void launch_poly3b_tc(cudaStream_t st, const PolyTCDev* tab, const float* X, float* G, float* E, int n, int stride,
+                      int num_sms, float* zscratch);
+
+}  // namespace mbpol

@@ -122,18 +122,29 @@ class MBPolTwoBodyForce(_CutoffWaterForce):
 
 class MBPolThreeBodyForce(_CutoffWaterForce):
     """openmmapi/include/openmm/MBPolThreeBodyForce.h.  setTrimerRule chooses
-    between the reference's enumeration (default) and the complete one."""
+    between the reference's enumeration (default) and the complete one;
+    setPolynomialEvaluator between the tensor-core evaluation of the
+    polynomial (default) and the double-float walk
+    (mbpol_set_threebody_evaluator)."""
     ReferenceTrimers, CompleteTrimers = 0, 1
+    TensorCores, DoubleFloatWalk = 0, 1
 
     def __init__(self):
         super().__init__(1.0)
         self._rule = 0
+        self._evaluator = 0
 
     def setTrimerRule(self, r):
         self._rule = int(r)
 
     def getTrimerRule(self):
         return self._rule
+
+    def setPolynomialEvaluator(self, kind):
+        self._evaluator = int(kind)
+
+    def getPolynomialEvaluator(self):
+        return self._evaluator
 
 
 class MBPolDispersionForce(_CutoffWaterForce):
@@ -452,6 +463,7 @@ class Context:
                 check(lib.mbpol_add_twobody_force(h, nw, ptr(w), f._method, f._cutoff))
             elif isinstance(f, MBPolThreeBodyForce):
                 check(lib.mbpol_add_threebody_force(h, nw, ptr(w), f._method, f._cutoff, f._rule))
+                check(lib.mbpol_set_threebody_evaluator(h, f._evaluator))
             elif isinstance(f, MBPolDispersionForce):
                 c6 = as_c(f.c6, np.float64)
                 d6 = as_c(f.d6, np.float64)

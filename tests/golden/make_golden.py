@@ -13,7 +13,7 @@ Sources:
 Dispersion has no plugin code in the reference (python/mbpol.xml:37-108 builds
 an OpenMM CustomNonbondedForce); its values come from the C oracle port.
 
-    python tests/golden/make_golden.py [/path/to/reference] [elec|pdb|potential|moments|dispersion]
+    python tests/golden/make_golden.py [/path/to/reference] [elec|pdb|potential|moments|dispersion|box4096]
 """
 import ctypes
 import json
@@ -389,8 +389,45 @@ def main_moments():
         print(name, seed, "moments", np.array2string(out, precision=5))
 
 
+def main_box4096():
+    """One frame of the 4096-water benchmark box (systems.workload("box4096",
+    0): 49.67 A, jittered 16^3 lattice), all five terms at the benchmark's
+    settings: cutoffs 0.65 / 0.45 nm, PME rc 0.9 nm, Ewald tolerance 1e-5
+    (alpha and grid explicit), solver threshold 1e-8 D.  Energies of the
+    one-, two- and three-body and electrostatics terms come from the
+    compiled reference; forces, dipoles and dispersion from the oracle port
+    (the reference's PME forces are not finite, see electrostatics() above),
+    which agrees with the reference's energies to ~1e-13."""
+    L = lib()
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from mbpol_openmm_plugin_gb300.plugin import pme_parameters
+    ws = systems.workload("box4096", 0)
+    pos = place_m(ws.positions)
+    nw = pos.shape[0] // 4
+    waters = np.stack([4 * np.arange(nw), 4 * np.arange(nw) + 1, 4 * np.arange(nw) + 2], 1).astype(np.int32)
+    alpha, grid = pme_parameters(ws.box, 0.9, 1e-5)
+    port = oracle.full_model(pos, ws.box, alpha=alpha, grid=grid, eps=1e-8)
+    print("port: e1 %.6f e2 %.6f e3 %.6f edisp %.6f eelec %.6f it %d" % (
+        port["e1"], port["e2"], port["e3"], port["edisp"], port["eelec"], port["iterations"]), flush=True)
+    r = run_terms(L, pos, waters, ws.box)
+    ee, _, dip, it = electrostatics(L, pos, ws.box, True, alpha=alpha, grid=grid, eps=1e-8)
+    etot = r["e1"] + r["e2"] + r["e3"] + port["edisp"] + ee
+    np.savez_compressed(os.path.join(HERE, "box4096_seed0.npz"), positions=pos, box=ws.box, periodic=True,
+                        alpha=alpha, grid=np.array(grid), e1=r["e1"], e2=r["e2"], e3=r["e3"], edisp=port["edisp"],
+                        eelec=ee, etotal=etot, ftotal=port["ftotal"], dipoles=port["dipoles"],
+                        iterations=it, npairs=r["npairs"], ntrip=r["ntrip"], trip_hash=r["trip_hash"],
+                        port_energies=np.array([port["e1"], port["e2"], port["e3"], port["edisp"], port["eelec"]]),
+                        port_iterations=port["iterations"])
+    print("box4096: reference e1 %.6f e2 %.6f e3 %.6f eelec %.6f (it %d), total %.6f kJ/mol; pairs %d trimers %d" % (
+        r["e1"], r["e2"], r["e3"], ee, it, etot, r["npairs"], r["ntrip"]))
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "elec":
+    if len(sys.argv) > 2 and sys.argv[2] == "box4096":
+        main_box4096()
+    elif len(sys.argv) > 2 and sys.argv[2] == "elec":
         main_elec()
     elif len(sys.argv) > 2 and sys.argv[2] == "potential":
         main_potential()
