@@ -129,7 +129,7 @@ struct mbpol_context {
     // cores by default) and its per-block scratch
     const PolyWalkTables* walk = nullptr;
     const PolyTCDev* tc3 = nullptr;
-    int poly3b_kind = MBPOL_POLY3B_TENSOR;
+    int poly3b_kind = MBPOL_POLY3B_AUTO;
     DevBuf ztc;
     // dispersion buffers
     DevBuf full_d, nfull_d, lower_d, nlower_d;
@@ -430,10 +430,11 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy, cudaStream_t ls, 
                                ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>(), true);
     launch_threebody_vars(ls, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                           box, ctx->x3.as<float>(), stride);
-    if (ctx->poly3b_kind == MBPOL_POLY3B_TENSOR)
-        MBPOL_CUDA_OK(ctx->ztc.ensure(sizeof(float) * poly3b_tc_scratch_floats(ctx->num_sms)));
+    const bool tensor = ctx->poly3b_kind == MBPOL_POLY3B_TENSOR ||
+                        (ctx->poly3b_kind == MBPOL_POLY3B_AUTO && ntrip >= 64 * ctx->num_sms);
+    if (tensor) MBPOL_CUDA_OK(ctx->ztc.ensure(sizeof(float) * poly3b_tc_scratch_floats(ctx->num_sms)));
     prof_begin(ls, K_POLY3B);
-    if (ctx->poly3b_kind == MBPOL_POLY3B_TENSOR)
+    if (tensor)
         launch_poly3b_tc(ls, ctx->tc3, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
                          ctx->num_sms, ctx->ztc.as<float>());
     else
@@ -1082,7 +1083,7 @@ mbpol_status mbpol_guess_fit_predictor(mbpol_context* ctx, const double* history
 // ---- batched independent clusters (no reference counterpart as one call)
 mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind) {
     if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
-    if (kind != MBPOL_POLY3B_TENSOR && kind != MBPOL_POLY3B_WALK)
+    if (kind != MBPOL_POLY3B_TENSOR && kind != MBPOL_POLY3B_WALK && kind != MBPOL_POLY3B_AUTO)
         return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "unknown three-body evaluator");
     ctx->poly3b_kind = kind;
     return MBPOL_OK;

@@ -124,15 +124,15 @@ class MBPolThreeBodyForce(_CutoffWaterForce):
     """openmmapi/include/openmm/MBPolThreeBodyForce.h.  setTrimerRule chooses
     between the reference's enumeration (default) and the complete one;
     setPolynomialEvaluator between the tensor-core evaluation of the
-    polynomial (default) and the double-float walk
-    (mbpol_set_threebody_evaluator)."""
+    polynomial, the double-float walk and the automatic choice by size
+    (default; mbpol_set_threebody_evaluator)."""
     ReferenceTrimers, CompleteTrimers = 0, 1
-    TensorCores, DoubleFloatWalk = 0, 1
+    TensorCores, DoubleFloatWalk, AutomaticEvaluator = 0, 1, 2
 
     def __init__(self):
         super().__init__(1.0)
         self._rule = 0
-        self._evaluator = 0
+        self._evaluator = 2
 
     def setTrimerRule(self, r):
         self._rule = int(r)

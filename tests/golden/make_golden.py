@@ -13,7 +13,7 @@ Sources:
 Dispersion has no plugin code in the reference (python/mbpol.xml:37-108 builds
 an OpenMM CustomNonbondedForce); its values come from the C oracle port.
 
-    python tests/golden/make_golden.py [/path/to/reference] [elec|pdb|potential|moments|dispersion|box4096]
+    python tests/golden/make_golden.py [/path/to/reference] [elec|elec_known|pdb|potential|moments|dispersion|box4096]
 """
 import ctypes
 import json
@@ -389,6 +389,103 @@ def main_moments():
         print(name, seed, "moments", np.array2string(out, precision=5))
 
 
+ELEC_CASES = [
+    # (function, M sites, PME, box nm, cutoff, alpha, grid, eps, redistribution, thole, zero polarity)
+    ("static void testWater3()", False, False, None, 0.7, 0.0, None, 1e-9, False, [0.4] * 5, False),
+    ("static void testWater3PMEHugeBox()", False, True, 50.0, 0.9, 1e-15, [20, 20, 20], 1e-12, False, [0.4] * 5,
+     False),
+    ("static void testWater3VirtualSitePMEHugeBox()", True, True, 50.0, 10.0, 1e-15, [20, 20, 20], 1e-4, True,
+     THOLE, True),
+    ("static void testWater3VirtualSitePMESmallBox()", True, True, 1.8, 0.9, None, None, 1e-12, True, [0.4] * 5,
+     False),
+]
+
+
+def parse_elec_test(path, func):
+    """Positions, expected energy and forces of one electrostatics test, with
+    // comments removed (the small-box test lists its forces by push_back)."""
+    src = open(path).read()
+    i = src.index(func)
+    j = min(k for k in (src.find("\nstatic void ", i + 10), src.find("\nint main", i + 10), len(src)) if k > 0)
+    body = "\n".join(ln.split("//")[0] for ln in src[i:j].splitlines())
+    pos = {}
+    for m in re.finditer(r"positions\[(\d+)\]\s*=\s*" + VEC3, body):
+        pos.setdefault(int(m.group(1)), [float(m.group(k)) for k in (2, 3, 4)])
+    forces = {}
+    for m in re.finditer(r"expectedForces\[(\d+)\]\s*=\s*" + VEC3, body):
+        forces[int(m.group(1))] = [float(m.group(k)) for k in (2, 3, 4)]
+    pushed = [[float(m.group(k)) for k in (1, 2, 3)]
+              for m in re.finditer(r"expectedForces\.push_back\(\s*" + VEC3 + r"\s*\)", body)]
+    e = re.search(r"expectedEnergy\s*=\s*([-+0-9.eE]+)\s*(\*\s*cal2joule\s*)?;", body)
+    tol = re.search(r"double tolerance\s*=\s*([-+0-9.eE]+)\s*;", body)
+    n = len(pos)
+    if pushed:
+        f = pushed[:n]
+    else:
+        f = [forces.get(k, [0.0, 0.0, 0.0]) for k in range(n)]
+    start = src.count("\n", 0, i) + 1
+    return {"positions_A": [pos[k] for k in range(n)], "expected_forces_kcal_A": f,
+            "expected_energy": float(e.group(1)), "energy_in_kcal": bool(e.group(2)),
+            "tolerance": float(tol.group(1)), "source": "platforms/reference/tests/"
+            "TestReferenceMBPolElectrostaticsForce.cpp:%d-%d" % (start, src.count("\n", 0, j) + 1)}
+
+
+def main_elec_known():
+    """The electrostatics known answers of the reference's own tests: water3
+    without M sites (NoCutoff and the PME huge box with alpha -> 0), the PME
+    huge box with M sites, charge redistribution and zero polarisabilities,
+    and the 1.8 nm PME box (alpha and grid from OpenMM's rule at Ewald
+    tolerance 1e-3).  Each with the compiled reference's energy and forces
+    at the same settings."""
+    L = lib()
+    sys.path.insert(0, ROOT)
+    from mbpol_openmm_plugin_gb300.plugin import pme_parameters
+    tests = os.path.join(REF, "platforms", "reference", "tests", "TestReferenceMBPolElectrostaticsForce.cpp")
+    out = {}
+    for func, msite, pme, boxL, cutoff, alpha, grid, eps, redist, thole, zeropol in ELEC_CASES:
+        k = parse_elec_test(tests, func)
+        pos = np.array(k["positions_A"]) * 0.1
+        if msite:
+            pos = place_m(pos)
+        n = pos.shape[0]
+        K = 4 if msite else 3
+        if pme and alpha is None:
+            alpha, grid = pme_parameters(np.array([boxL] * 3), cutoff, 1e-3)
+        typ = np.tile([0, 1, 1, 2][:K], n // K).astype(np.int32)
+        q = np.tile([-5.1966000e-01, 2.5983000e-01, 2.5983000e-01, 0.0][:K], n // K)
+        damp = np.tile([0.001310, 0.000294, 0.000294, 0.001310][:K], n // K)
+        pol = np.zeros(n) if zeropol else np.tile([0.001310, 0.000294, 0.000294, 0.0][:K], n // K)
+        mol = np.repeat(np.arange(n // K), K).astype(np.int32)
+        f = np.zeros((n, 3))
+        e = ctypes.c_double()
+        it = ctypes.c_int()
+        err = ctypes.create_string_buffer(512)
+        b = np.array([boxL] * 3 if pme else [0.0] * 3)
+        rc = L.ref_electrostatics(n, p(np.ascontiguousarray(pos)), p(q), p(mol), p(typ), p(damp), p(pol),
+                                  p(np.array(thole, float)), 1 if pme else 0, cutoff, float(alpha or 0.0),
+                                  p(np.array(grid or [0, 0, 0], np.int32)), p(b), eps, 500, 1 if redist else 0,
+                                  p(f), ctypes.byref(e), None, ctypes.byref(it), err, 512)
+        if rc:
+            raise RuntimeError(err.value.decode())
+        if msite:
+            for w in range(n // 4):
+                fm = f[4 * w + 3].copy()
+                f[4 * w + 3] = 0
+                for c in range(3):
+                    f[4 * w + c] += MW[c] * fm
+        name = func.split()[-1].rstrip("()")
+        k.update({"msite": msite, "pme": pme, "box_nm": boxL, "cutoff_nm": cutoff, "alpha": alpha, "grid": grid,
+                  "target_epsilon": eps, "charge_redistribution": redist, "thole": thole, "zero_polarity": zeropol,
+                  "reference_energy_kJ": e.value, "reference_forces_kJ_nm": f.tolist(),
+                  "reference_iterations": it.value})
+        out[name] = k
+        eexp = k["expected_energy"] * (4.184 if k["energy_in_kcal"] else 1.0)
+        print("%-36s expected %.6f kJ/mol, compiled reference %.6f (alpha %s grid %s)" % (
+            name, eexp, e.value, alpha, grid))
+    with open(os.path.join(HERE, "elec_known_answers.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+
+
 def main_box4096():
     """One frame of the 4096-water benchmark box (systems.workload("box4096",
     0): 49.67 A, jittered 16^3 lattice), all five terms at the benchmark's
@@ -427,6 +524,8 @@ def main_box4096():
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "box4096":
         main_box4096()
+    elif len(sys.argv) > 2 and sys.argv[2] == "elec_known":
+        main_elec_known()
     elif len(sys.argv) > 2 and sys.argv[2] == "elec":
         main_elec()
     elif len(sys.argv) > 2 and sys.argv[2] == "potential":
@@ -444,3 +543,4 @@ if __name__ == "__main__":
         main_potential()
         main_moments()
         main_dispersion()
+        main_elec_known()

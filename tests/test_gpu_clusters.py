@@ -7,9 +7,9 @@ count.
 Tolerances: per-cluster total energy within 1e-6 of the sum of the five
 terms' magnitudes (a small cluster's total is a near-cancellation of terms of
 hundreds of kJ/mol, so the bound is taken on the scale the terms are
-evaluated at); each term within 1e-5 of its magnitude with a 1e-4 kJ/mol
-floor; forces 1e-4 relative RMS over the batch; iterations within 2 of the
-oracle's."""
+evaluated at); each term within 2e-5 of its magnitude with a 1e-4 kJ/mol
+floor (2e-5: the three-body term on the tensor cores); forces 1e-4 relative
+RMS over the batch; iterations within 2 of the oracle's."""
 import numpy as np
 import pytest
 
@@ -23,9 +23,20 @@ oracle = pytest.importorskip("oracle")
 KEYS = ("e1", "e2", "e3", "eelec", "edisp")  # term order of the ABI
 
 
-def test_batched_clusters_match_per_cluster_oracle():
-    ws = systems.batched_clusters(nclusters=12, nmin=2, nmax=16, seed=5)
+@pytest.mark.parametrize("ncl,nmax,evaluator", [
+    (12, 16, mb.MBPolThreeBodyForce.AutomaticEvaluator),
+    (24, 64, mb.MBPolThreeBodyForce.AutomaticEvaluator),
+    (24, 64, mb.MBPolThreeBodyForce.TensorCores)])
+def test_batched_clusters_match_per_cluster_oracle(ncl, nmax, evaluator):
+    """Clusters of 2-16 and of 2-64 waters (the batched configuration's
+    range); the three-body term by the automatic choice and forced onto the
+    tensor cores (whose per-trimer error, ~1e-6 kcal/mol, is held by the
+    bars below like every other term's)."""
+    ws = systems.batched_clusters(nclusters=ncl, nmin=2, nmax=nmax, seed=5)
     sysm = mb.create_mbpol_system(ws, target_epsilon=1e-8)
+    for f in sysm.forces:
+        if isinstance(f, mb.MBPolThreeBodyForce):
+            f.setPolynomialEvaluator(evaluator)
     ctx = mb.Context(sysm)
     ctx.setPositions(ws.positions)
     cl = np.repeat(ws.cluster_of_water, 4)
@@ -48,7 +59,7 @@ def test_batched_clusters_match_per_cluster_oracle():
             " ".join("%.1e" % (E[c, k] - ref[k]) for k in range(5))))
         assert abs(tot - tref) <= 1e-6 * scale
         for k in range(5):
-            assert abs(E[c, k] - ref[k]) <= max(1e-5 * abs(ref[k]), 1e-4), (c, KEYS[k])
+            assert abs(E[c, k] - ref[k]) <= max(2e-5 * abs(ref[k]), 1e-4), (c, KEYS[k])
         assert abs(int(its[c]) - int(r["iterations"])) <= 2
     assert abs(st.getPotentialEnergy() - E.sum()) <= 1e-9 * abs(E.sum())
     ferr = rel_rms(st.getForces(), fref)

@@ -1,0 +1,110 @@
+"""GPU: the electrostatics known answers of the reference's own tests
+(platforms/reference/tests/TestReferenceMBPolElectrostaticsForce.cpp, read
+as text into tests/golden/elec_known_answers.json by make_golden.py
+elec_known, together with the compiled reference's energy and forces at the
+same settings):
+
+  testWater3                       water3 without M, NoCutoff, thole 0.4, 1e-9 D:
+                                   -7.08652 kcal/mol (tolerance 1e-4)
+  testWater3PMEHugeBox             the same in a 50 nm PME box, alpha 1e-15,
+                                   grid 20^3, 1e-12 D: -7.08652 (1e-3)
+  testWater3VirtualSitePMEHugeBox  with M sites and charge redistribution,
+                                   zero polarisabilities, 10 nm cutoff:
+                                   -13.0493 kcal/mol (1e-4)
+  testWater3VirtualSitePMESmallBox 1.8 nm box, 0.9 nm cutoff, alpha and grid
+                                   from OpenMM's rule at tolerance 1e-3:
+                                   -66.7426 kJ/mol stated (1e-2); the compiled
+                                   reference gives -67.484 at this and any
+                                   other alpha or grid (1.1% from the stated
+                                   value), so the GPU is held to the compiled
+                                   reference here and the stated value's gap
+                                   is printed.
+
+Bars: energy within 1e-6 of the compiled reference and, where the
+reference itself meets it, within the test's own tolerance of the stated
+value (relative, as its ASSERT_EQUAL_TOL_MOD).  Forces: within 1e-4
+relative RMS of the compiled reference where its forces are finite (its PME
+reciprocal forces read uninitialised memory and come out NaN), and, where
+the reference meets the stated energy, within the test's tolerance
+(relative per component, floor 1 kcal/mol/A, as its ASSERT_EQUAL_VEC_MOD)
+of the test's finite-difference forces."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_rms
+import mbpol_openmm_plugin_gb300 as mb
+
+pytestmark = pytest.mark.gpu
+KCAL = 4.184
+CASES = json.load(open(os.path.join(GOLDEN, "elec_known_answers.json")))
+MW = (0.573293118, 0.213353441, 0.213353441)
+
+
+def build(k):
+    pos = np.array(k["positions_A"]) * 0.1
+    K = 4 if k["msite"] else 3
+    n = pos.shape[0]
+    s = mb.System()
+    for w in range(n // K):
+        for t in range(K):
+            s.addParticle([15.999, 1.008, 1.008, 0.0][t])
+        if k["msite"]:
+            s.setVirtualSite(K * w + 3, mb.ThreeParticleAverageSite(K * w, K * w + 1, K * w + 2, *MW))
+    f = mb.MBPolElectrostaticsForce()
+    if k["pme"]:
+        s.setDefaultPeriodicBoxVectors((k["box_nm"], 0, 0), (0, k["box_nm"], 0), (0, 0, k["box_nm"]))
+        f.setNonbondedMethod(mb.MBPolElectrostaticsForce.PME)
+        f.setAEwald(k["alpha"])
+        f.setPmeGridDimensions(k["grid"])
+    else:
+        f.setNonbondedMethod(mb.MBPolElectrostaticsForce.NoCutoff)
+    f.setCutoffDistance(k["cutoff_nm"])
+    f.setIncludeChargeRedistribution(k["charge_redistribution"])
+    f.setMutualInducedTargetEpsilon(k["target_epsilon"])
+    f.setMutualInducedMaxIterations(500)
+    f.setTholeParameters(k["thole"])
+    q = [-5.1966000e-01, 2.5983000e-01, 2.5983000e-01, 0.0]
+    damp = [0.001310, 0.000294, 0.000294, 0.001310]
+    pol = [0.001310, 0.000294, 0.000294, 0.0]
+    for w in range(n // K):
+        for t in range(K):
+            f.addElectrostatics(q[t], w, [0, 1, 1, 2][t], damp[t], 0.0 if k["zero_polarity"] else pol[t])
+    s.addForce(f)
+    ctx = mb.Context(s)
+    ctx.setPositions(pos)
+    return ctx
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_electrostatics_known_answer(name):
+    k = CASES[name]
+    ctx = build(k)
+    st = ctx.getState()
+    e = st.getPotentialEnergy()
+    f = np.asarray(st.getForces())
+    eref = k["reference_energy_kJ"]
+    fref = np.array(k["reference_forces_kJ_nm"])
+    stated = k["expected_energy"] * (KCAL if k["energy_in_kcal"] else 1.0)
+    tol = k["tolerance"]
+    ferr = rel_rms(f, fref) if np.isfinite(fref).all() else float("nan")
+    print("%s E %.6f compiled reference %.6f (rel %.1e) stated %.6f (rel %.1e, test tolerance %g) | F relrms %.1e" % (
+        name, e, eref, abs(e - eref) / abs(eref), stated, abs(e - stated) / max(abs(stated), 1.0), tol, ferr))
+    assert abs(e - eref) <= 1e-6 * abs(eref)
+    if np.isfinite(fref).all():
+        assert ferr <= 1e-4
+    meets = abs(eref - stated) <= tol * max(abs(stated), 1.0)   # the reference meets its own bar
+    if meets:
+        assert abs(e - stated) <= tol * max(abs(stated), 1.0)
+    # the test's finite-difference forces (kcal/mol/A), real sites only
+    fexp = np.array(k["expected_forces_kcal_A"])
+    fk = f / (KCAL * 10.0)
+    real = np.abs(fexp).sum(axis=1) > 0
+    if fexp.shape == fk.shape and real.any():
+        scale = np.maximum(np.abs(fexp[real]), 1.0)
+        worst = float(np.max(np.abs(fk[real] - fexp[real]) / scale))
+        print("   finite-difference forces: worst component error %.1e" % worst)
+        if meets:
+            assert worst <= max(tol, 1e-3)

@@ -31,7 +31,7 @@ E_TOL = {"e1": 1e-6, "e2": 2e-6, "e3": 2e-6, "edisp": 2e-6}
 E3_TC_TOL, E3_TC_ABS = 2e-5, 5e-5
 
 
-def run(ws_pos, box, terms, trimer_rule=0, cut2=0.65, cut3=0.45, evaluator=0):
+def run(ws_pos, box, terms, trimer_rule=0, cut2=0.65, cut3=0.45, evaluator=mb.MBPolThreeBodyForce.TensorCores):
     ws = systems.WaterSystem(ws_pos, box, 0, "fixture")
     s = mb.create_mbpol_system(ws, terms=terms, trimer_rule=trimer_rule)
     for f in s.forces:
