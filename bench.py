@@ -130,44 +130,55 @@ ALGO_FLOP_PER_UNIT = {"poly2b": 31200, "poly3b": 112600}
 NCU_TRAFFIC = {"poly3b": (53.226e6 + 2.685e6, 181889), "poly2b": (16.451e6, 65434)}
 
 
-def fp32_ops_per_unit(name):
-    """FP32 operations (add/sub/mul = 1, fma = 2) that the double-float walk
-    executes per dimer/trimer, counted from the trie sizes (csrc/poly_df.cu):
-    a leaf is a double-float multiply-add into V (1 mul + 3 fma + TwoSum 6 +
-    2 adds = 15) and into the gradient (15) = 30; nodes of levels 3/2/1 cost
-    40/33/26 (prefix product, two double-float updates)."""
-    path = os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "csrc", "gen", "%s_tables.inc" % name)
-    sizes = {}
-    for ln in open(path):
-        if ln.startswith("#define"):
-            _, k, v = ln.split()
-            sizes[k.split("_")[-1]] = int(v)
-    return 30 * sizes["NL"] + 40 * sizes["N3"] + 33 * sizes["N2"] + 26 * sizes["N1"]
-
-
 GUESS_MODE = {"plain": 1, "learned": 2, "extrapolation": 3}
 GUESS_WEIGHTS = os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "data", "dipole_guess_%s.npy")
+
+
+def guess_params_source(args):
+    path = GUESS_WEIGHTS % args.workload
+    if not os.path.exists(path) and args.workload.startswith("box"):
+        path = GUESS_WEIGHTS % "box4096"
+    return "committed (%s)" % os.path.relpath(path, ROOT) if os.path.exists(path) else \
+        "trained in this run on 200 NVT frames"
 
 
 def guess_params(args):
     """The learned guess's parameter block: the committed one for the
     workload (trained by mbpol_openmm_plugin_gb300.train_guess on 2000 NVT
-    frames of the same box), else one trained here on a short trajectory."""
+    frames of the same box), else one trained here on a short trajectory.
+    A bulk box without its own block uses the 4096-water box's network (its
+    inputs are per-molecule and local, plus the permanent field)."""
     path = GUESS_WEIGHTS % args.workload
     if not os.path.exists(path) and args.workload.startswith("box"):
-        # a bulk box of the same density: the 4096-water box's network (its
-        # inputs are per-molecule and local, plus the permanent field)
         path = GUESS_WEIGHTS % "box4096"
     if os.path.exists(path):
-        return np.load(path), "committed (%s)" % os.path.relpath(path, ROOT)
+        return np.load(path), guess_params_source(args)
     out = os.path.join("/tmp", "dipole_guess_%s_%d.npy" % (args.workload, os.getpid()))
     from mbpol_openmm_plugin_gb300 import train_guess
     train_guess.main(["--workload", args.workload, "--frames", "200", "--steps", "5000", "--out", out])
     return np.load(out), "trained in this run on 200 NVT frames"
 
 
-def timed_md(args, guess, params=None, profile=False):
-    """Warm-up, then K timed MD steps (CUDA events inside mbpol_md_run)."""
+CORRECTION_WEIGHTS = os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "data", "dipole_correction_%s.npy")
+
+
+def correction_params(args):
+    """The correction network's parameter block for the learned arm (trained
+    by mbpol_openmm_plugin_gb300.train_guess --network correction on NVT
+    frames of the same box), or None."""
+    path = CORRECTION_WEIGHTS % args.workload
+    if not os.path.exists(path) and args.workload.startswith("box"):
+        path = CORRECTION_WEIGHTS % "box4096"
+    return np.load(path) if os.path.exists(path) and not args.no_correction else None
+
+
+def md_context(args, guess, params=None, corr=None):
+    """A context of the workload at the trajectory start every arm shares:
+    the seeded box with Maxwell-Boltzmann velocities, `args.equilibrate`
+    untimed MD steps (the history-based guesses reach their steady state
+    after 12 solves), then the warm-up steps (first force evaluation, buffer
+    growth).  The library is deterministic (fixed-point PME spreading, fixed
+    reduction orders), so two contexts built alike reach the same state."""
     import mbpol_openmm_plugin_gb300 as mb
     from mbpol_openmm_plugin_gb300 import _capi
     lib = _capi.load()
@@ -177,6 +188,10 @@ def timed_md(args, guess, params=None, profile=False):
     ctx._build()
     if params is not None:
         ctx.setDipoleGuessParameters(params)
+    if corr is not None:
+        ctx.selectDipoleGuessNetwork(ctx.CorrectionNetwork)
+        ctx.setDipoleGuessParameters(corr)
+        ctx.selectDipoleGuessNetwork(ctx.ColdStartNetwork)
     h = ctx._h
     box = np.ascontiguousarray(ws.box, np.float64)
     pos = np.ascontiguousarray(ws.positions, np.float64)
@@ -185,132 +200,233 @@ def timed_md(args, guess, params=None, profile=False):
     _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), _capi.ptr(box)))
     _capi.check(lib.mbpol_set_masses(h, _capi.ptr(np.ascontiguousarray(masses))))
     _capi.check(lib.mbpol_set_velocities(h, _capi.ptr(np.ascontiguousarray(vel))))
-    ms = ctypes.c_double()
-    iters = ctypes.c_long()
-    en = np.zeros(6)
-    # trajectory start (every arm alike): the history-based guesses reach
-    # their steady state after 12 solves; then the warm-up (first force
-    # evaluation, buffer growth), untimed
+    ms, iters, en = ctypes.c_double(), ctypes.c_long(), np.zeros(6)
     _capi.check(lib.mbpol_md_run(h, args.equilibrate + args.warmup, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(ms),
                                  _capi.ptr(en), ctypes.byref(iters)))
-    r = {"ctx": ctx, "ws": ws, "sysm": sysm, "alpha": alpha, "grid": grid, "counts": ctx.getCounts(),
-         "box": box, "pos": pos, "masses": masses}
-    sampler = ClockSampler() if profile else None
-    if profile:
-        sampler.start()
-    l0 = lib.mbpol_launch_count()
-    _capi.check(lib.mbpol_md_run(h, args.steps, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(ms), _capi.ptr(en),
+    return {"ctx": ctx, "h": h, "ws": ws, "sysm": sysm, "alpha": alpha, "grid": grid, "box": box,
+            "masses": masses, "n": pos.shape[0]}
+
+
+def md_steps(lib, h, nsteps, seed):
+    """nsteps device-resident MD steps; (seconds per step from CUDA events on
+    the library's stream, solver iterations per step, energies)."""
+    from mbpol_openmm_plugin_gb300 import _capi
+    ms, iters, en = ctypes.c_double(), ctypes.c_long(), np.zeros(6)
+    _capi.check(lib.mbpol_md_run(h, nsteps, DT_PS, 0.0, 0.0, seed, ctypes.byref(ms), _capi.ptr(en),
                                  ctypes.byref(iters)))
-    r["launches"] = int(lib.mbpol_launch_count() - l0)
-    r["step_s"] = ms.value / 1e3 / args.steps
-    r["iterations"] = iters.value / max(args.steps, 1)
-    r["energies"] = en.copy()
-    if profile:
-        r["clocks"] = sampler.stop()
-    if args.avg_steps > 0:
-        # the metric's iteration average: >= 1000 further steps of the same
-        # trajectory (after the equilibration and the timed steps)
-        msl, itl, enl = ctypes.c_double(), ctypes.c_long(), np.zeros(6)
-        _capi.check(lib.mbpol_md_run(h, args.avg_steps, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(msl),
-                                     _capi.ptr(enl), ctypes.byref(itl)))
-        r["long_run"] = {"steps": args.avg_steps, "ms_per_step": msl.value / args.avg_steps,
-                         "ns_per_day": ns_per_day(msl.value / 1e3 / args.avg_steps),
-                         "solver_iterations_per_step": itl.value / args.avg_steps}
-    if profile:
-        # per-kernel CUDA-event timers on K further steps (the events add
-        # launches, so the timed steps above run without them)
-        lib.mbpol_profile_enable(1)
-        ms2, it2, en2 = ctypes.c_double(), ctypes.c_long(), np.zeros(6)
-        _capi.check(lib.mbpol_md_run(h, args.steps, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(ms2), _capi.ptr(en2),
-                                     ctypes.byref(it2)))
-        kern = {}
-        for kid, kname in enumerate(_capi.KERNELS):
-            t = ctypes.c_double()
-            n = ctypes.c_long()
-            lib.mbpol_profile_read(kid, ctypes.byref(t), ctypes.byref(n))
-            kern[kname] = {"total_ms": t.value, "launches": n.value}
-        lib.mbpol_profile_enable(0)
-        r["kern"] = kern
-    return r
+    return ms.value / 1e3 / nsteps, iters.value / nsteps, en
 
 
-def run_ours(args):
+def state(lib, h, n):
+    from mbpol_openmm_plugin_gb300 import _capi
+    pos, vel, f = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+    _capi.check(lib.mbpol_get_state(h, _capi.ptr(pos), _capi.ptr(vel), _capi.ptr(f)))
+    return pos, vel, f
+
+
+def arm(args, guess, params=None, corr=None):
+    """One guess arm: K timed steps, then the metric's iteration average over
+    `args.avg_steps` further steps of the same trajectory."""
     from mbpol_openmm_plugin_gb300 import _capi
     lib = _capi.load()
-    params, params_src = guess_params(args)
-    # comparison arms first (same initial state), the headline arm last
-    others = {}
-    for g in ("plain", "extrapolation", "learned"):
-        if g == args.guess or args.no_comparison:
-            continue
-        rr = timed_md(args, g, params if g == "learned" else None)
-        others[g] = {"ns_per_day": ns_per_day(rr["step_s"]), "ms_per_step": rr["step_s"] * 1e3,
-                     "solver_iterations_per_step": rr["iterations"]}
-        if "long_run" in rr:
-            others[g]["long_run"] = rr["long_run"]
-        del rr
-    r = timed_md(args, args.guess, params, profile=True)
-    ctx, ws, sysm, alpha, grid = r["ctx"], r["ws"], r["sysm"], r["alpha"], r["grid"]
-    h = ctx._h
-    box, pos, masses, counts, kern, clocks = r["box"], r["pos"], r["masses"], r["counts"], r["kern"], r["clocks"]
-    launches = r["launches"]
-    step_s = r["step_s"]
-    value = ns_per_day(step_s)
-    solver_it = r["iterations"]
-    en = r["energies"]
+    c = md_context(args, guess, params, corr)
+    step_s, it, _ = md_steps(lib, c["h"], args.steps, args.seed)
+    out = {"ns_per_day": ns_per_day(step_s), "ms_per_step": step_s * 1e3, "solver_iterations_per_step": it}
+    if args.avg_steps > 0:
+        sl, itl, _ = md_steps(lib, c["h"], args.avg_steps, args.seed)
+        out["long_run"] = {"steps": args.avg_steps, "ms_per_step": sl * 1e3, "ns_per_day": ns_per_day(sl),
+                           "solver_iterations_per_step": itl}
+    del c
+    return out
 
-    # NVE energy conservation after the timed region (device-resident state)
-    drift = nve_drift(lib, h, args.drift_steps, pos.shape[0] // 4) if args.drift_steps > 0 else None
 
-    # e2e: public API with host buffers, host-side velocity Verlet
-    hpos = np.zeros_like(pos)
-    hvel = np.zeros_like(pos)
-    hf = np.zeros_like(pos)
-    _capi.check(lib.mbpol_get_state(h, _capi.ptr(hpos), _capi.ptr(hvel), _capi.ptr(hf)))
+def e2e_steps(lib, c, nsteps):
+    """The same steps through the public API with host buffers, as OpenMM
+    drives the reference plugin: every step copies the positions host->device
+    (mbpol_set_positions), evaluates (mbpol_compute: energies and forces
+    copied device->host) and integrates on the host (velocity Verlet)."""
+    from mbpol_openmm_plugin_gb300 import _capi
+    h, n, box = c["h"], c["n"], c["box"]
+    hpos, hvel, forces = state(lib, h, n)
+    masses = c["masses"]
     invm = np.where(masses > 0, 1.0 / np.where(masses > 0, masses, 1.0), 0.0)[:, None]
     e5 = np.zeros(5)
-    forces = hf.copy()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(nsteps):
         hvel += 0.5 * DT_PS * forces * invm
         hpos += DT_PS * hvel * (invm > 0)
         _capi.check(lib.mbpol_set_positions(h, _capi.ptr(hpos), _capi.ptr(box)))
         forces[:] = 0.0
         _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
         hvel += 0.5 * DT_PS * forces * invm
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    n = pos.shape[0]
+    return (time.perf_counter() - t0) / nsteps, hpos
 
-    # roofline of the dominant kernel: the three-body walk, first in the ncu
-    # launch list (the electrostatics timers span multi-kernel passes that
-    # overlap each other and the walks, so they are not kernel durations)
-    dom = "poly3b"
+
+METRIC = "ns/day @4096 H2O PME, learned-guess vs plain GPU at <=1e-4 rel RMS force err"
+
+
+def run_ours(args):
+    from mbpol_openmm_plugin_gb300 import _capi
+    lib = _capi.load()
+    params, params_src = guess_params(args)
+    corr = correction_params(args)
+    # comparison arms first (each from the same trajectory start); the
+    # learned arm without its correction network shows what the network adds
+    others = {}
+    for g in ("plain", "extrapolation", "learned"):
+        if g != args.guess and not args.no_comparison:
+            others[g] = arm(args, g, params if g == "learned" else None, corr if g == "learned" else None)
+    if args.guess == "learned" and corr is not None and not args.no_comparison:
+        others["learned_predictor_only"] = arm(args, "learned", params, None)
+    # headline arm: context A times K device-resident steps (value), context
+    # B, built and advanced alike, times the same K steps end to end (e2e)
+    gp = params if args.guess == "learned" else None
+    gc = corr if args.guess == "learned" else None
+    ca = md_context(args, args.guess, gp, gc)
+    cb = md_context(args, args.guess, gp, gc)
+    h = ca["h"]
+    pa, va, _ = state(lib, h, ca["n"])
+    pb, vb, _ = state(lib, cb["h"], cb["n"])
+    same_start = float(max(np.abs(pa - pb).max(), np.abs(va - vb).max()))
+    sampler = ClockSampler()
+    sampler.start()
+    l0 = lib.mbpol_launch_count()
+    step_s, solver_it, en = md_steps(lib, h, args.steps, args.seed)
+    launches = int(lib.mbpol_launch_count() - l0)
+    clocks = sampler.stop()
+    e2e_s, pos_e2e = e2e_steps(lib, cb, args.steps)
+    pos_dev, _, _ = state(lib, h, ca["n"])
+    same_end = float(np.abs(pos_dev - pos_e2e).max())
+    counts_timed = ca["ctx"].getCounts()
+    # per-kernel CUDA-event timers on K further steps (the events add
+    # launches, so the timed steps above run without them); unit counts from
+    # those same steps
+    lib.mbpol_profile_enable(1)
+    md_steps(lib, h, args.steps, args.seed)
+    kern = {}
+    for kid, kname in enumerate(_capi.KERNELS):
+        t, nl = ctypes.c_double(), ctypes.c_long()
+        lib.mbpol_profile_read(kid, ctypes.byref(t), ctypes.byref(nl))
+        kern[kname] = {"total_ms": t.value, "launches": nl.value}
+    lib.mbpol_profile_enable(0)
+    counts = ca["ctx"].getCounts()
+    long_run = None
+    if args.avg_steps > 0:
+        sl, itl, _ = md_steps(lib, h, args.avg_steps, args.seed)
+        long_run = {"steps": args.avg_steps, "ms_per_step": sl * 1e3, "ns_per_day": ns_per_day(sl),
+                    "solver_iterations_per_step": itl}
+    drift = nve_drift(lib, h, args.drift_steps, ca["n"] // 4) if args.drift_steps > 0 else None
+    ws, alpha, grid, n = ca["ws"], ca["alpha"], ca["grid"], ca["n"]
+    value = ns_per_day(step_s)
+    head = {"ns_per_day": value, "ms_per_step": step_s * 1e3, "solver_iterations_per_step": solver_it}
+    if long_run:
+        head["long_run"] = long_run
+    arms = dict(others, **{args.guess: head})
+    arms_ms = {g: round(a["ms_per_step"], 3) for g, a in arms.items()}
+    if "plain" in arms:
+        pl, hd = arms["plain"], arms[args.guess]
+        arms_ms["%s_vs_plain" % args.guess] = round(pl["ms_per_step"] / hd["ms_per_step"], 3)
+        if "long_run" in pl and "long_run" in hd:
+            arms_ms["%s_vs_plain_long_run" % args.guess] = round(
+                pl["long_run"]["ms_per_step"] / hd["long_run"]["ms_per_step"], 3)
+    roof, secondary = rooflines(kern, counts, grid, n, clocks)
+    out = {
+        "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step_s * 1e3, "arms_ms_per_step": arms_ms, "higher_is_better": True, "scaling": "replicas",
+        "vs_baseline": None,
+        "dtype": "fp16 tensor-core pieces + fp32 sums (3B), double-float fp32 (2B), fp32 bulk, fp64 accumulation",
+        "data": "synthetic (seeded lattice box)",
+        "config": workload_config(args, ws, alpha, grid, params_src),
+        "e2e": {"value": ns_per_day(e2e_s), "unit": "ns/day", "h2d_bytes_per_step": int(n * 24),
+                "d2h_bytes_per_step": int(n * 24 + 5 * 8),
+                "steps": "the same %d steps as value, from the same state (max |dx| at start %.1e nm, at end %.1e nm)"
+                         % (args.steps, same_start, same_end)},
+        "gpu_launches": launches,
+        "solver_iterations_per_step": solver_it,
+        "guess_comparison": arms,
+        "correction_network": "committed (%s)" % os.path.relpath(CORRECTION_WEIGHTS % "box4096", ROOT)
+        if gc is not None else None,
+        "counts": {"pairs_2b": int(counts[0]), "trimers": int(counts[1]), "elec_site_pairs": int(counts[2]),
+                   "pme_grid_points": int(grid[0] * grid[1] * grid[2]) if grid else 0,
+                   "trimers_in_timed_steps": int(counts_timed[1])},
+        "kernels_ms_per_step": {k: v["total_ms"] / args.steps for k, v in kern.items()},
+        "clocks": clocks,
+        "roofline": roof,
+        "roofline_memory_kernels": secondary,
+        "energies_kJ_mol": {"1b": en[0], "2b": en[1], "3b": en[2], "elec": en[3], "disp": en[4], "kinetic": en[5]},
+    }
+    if drift is not None:
+        out["nve_drift"] = drift
+    del ca, cb
+    if not args.no_accuracy:
+        out["accuracy"] = accuracy_check()
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, sample=True)
+    return out
+
+
+def workload_config(args, ws, alpha, grid, params_src):
+    """The workload as both arms (ours and --impl reference) report it."""
+    return {"workload": args.workload, "waters": int(ws.num_waters), "box_nm": float(ws.box[0]), "pme_alpha": alpha,
+            "pme_grid": grid, "cutoff_nm": 0.9, "ewald_tol": 1e-5, "target_epsilon_D": 1e-8, "dt_fs": 0.2,
+            "guess": args.guess, "guess_parameters": params_src, "seed": args.seed, "model": args.model,
+            "equilibration_steps": args.equilibrate,
+            "l2": "no flush: inputs larger than L2 (per step, the pair and trimer variable/gradient planes and "
+                  "the PME grids exceed the 129 MB L2)"}
+
+
+def tc_flop_per_trimer():
+    """Executed tensor-core work of the three-body kernel per trimer: kept
+    16x16 tiles of S x 8 n-tiles of 8 trimers x 4 mma.m16n8k16 (2*16*8*16
+    flop), per 64-trimer tile."""
+    try:
+        import re
+        src = open(os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "_build", "poly_tc_tables.cpp")).read()
+        nent = int(re.search(r"k_poly3b = \{36, 703, 704, \d+, (\d+),", src).group(1))
+    except (OSError, AttributeError):
+        nent = 839
+    return nent * 8 * 4 * 4096 / 64.0
+
+
+def rooflines(kern, counts, grid, n, clocks):
+    """The dominant polynomial kernel by measured time against the FP32 pipe
+    (algorithmic flop of the reference's operation count), with the
+    tensor-core view of the three-body kernel; the memory-bound
+    electrostatics passes against the measured HBM copy rate (algorithmic
+    bytes as in the reference's operation counts: pair index 4 B + cached
+    pair coefficients 8 B per polarisable site pair within the cutoff, 36 B
+    per polarisable site; PME pass: 125 grid updates of 4 B per site, 8 B per
+    grid point for the FFT input and output, 16 B for the convolution).  The
+    electrostatics timers run concurrently with the polynomial kernels, so
+    their fractions are lower bounds."""
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    per = {}
+    for name, cidx in (("poly3b", 1), ("poly2b", 0)):
+        if kern[name]["launches"]:
+            per[name] = (kern[name]["total_ms"] / kern[name]["launches"], int(counts[cidx]))
     roof = None
-    if kern[dom]["launches"]:
-        units = int(counts[1] if dom == "poly3b" else counts[0])
-        per_launch_ms = kern[dom]["total_ms"] / kern[dom]["launches"]
+    if per:
+        dom = max(per, key=lambda k: per[k][0])
+        ms, units = per[dom]
         algo = ALGO_FLOP_PER_UNIT[dom]
-        achieved = units * algo / (per_launch_ms * 1e-3) / 1e12
-        executed = units * fp32_ops_per_unit(dom) / (per_launch_ms * 1e-3) / 1e12
-        sm_mhz = clocks.get("sm_mhz") or 2070.0
-        peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-        roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak,
-                "traffic": NCU_TRAFFIC[dom][0] * units / NCU_TRAFFIC[dom][1],
-                "traffic_note": "DRAM bytes per launch from one ncu capture on this workload, scaled by units",
+        achieved = units * algo / (ms * 1e-3) / 1e12
+        roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak, "traffic": NCU_TRAFFIC[dom][0] * units / NCU_TRAFFIC[dom][1],
+                "traffic_note": "DRAM bytes per launch from one ncu capture of this kernel (profiles/), scaled by units",
                 "work": "%d units x %d algorithmic flop (reference operation count)" % (units, algo),
-                "executed_fp32_tflops": executed, "executed_frac": executed / peak,
-                "executed_work": "%d FP32 flop per unit in the double-float walk" % fp32_ops_per_unit(dom),
-                "peak_kind": "nominal FP32 FMA rate at the median sampled SM clock (152 SM x 128 lanes x 2); "
-                             "the measured-peaks file has no FP32 figure",
-                "launch_ms": per_launch_ms}
-    # memory-bound electrostatics kernels against the measured HBM copy rate
-    # (algorithmic bytes as in the reference's operation counts: pair index
-    # 4 B + cached pair coefficients 8 B per polarisable site pair within the
-    # cutoff, 36 B per polarisable site; PME pass: 125 grid updates of 4 B per
-    # site, 8 B per grid point for the FFT input and output, 16 B for the
-    # convolution).  Both timers run concurrently with the polynomial walks,
-    # so the fractions are lower bounds.
+                "peak_kind": "nominal FP32 rate at the median sampled SM clock (152 SM x 128 lanes x 2); "
+                             "MEASURED_PEAKS.json has no FP32 figure", "launch_ms": ms,
+                "per_kernel_ms": {k: v[0] for k, v in per.items()}}
+        if "poly3b" in per:
+            ms3, u3 = per["poly3b"]
+            tc = u3 * tc_flop_per_trimer() / (ms3 * 1e-3) / 1e12
+            bf16 = measured_peak("bf16_tflops", 1905.0)
+            roof["poly3b_tensor_view"] = {
+                "bound": "tensor", "achieved": tc, "peak": bf16[0], "unit": "TFLOP/s", "frac": tc / bf16[0],
+                "work": "executed mma.m16n8k16 flop: %.0f per trimer" % tc_flop_per_trimer(),
+                "peak_kind": bf16[1] + " (dense bf16; fp16 runs at the same rate)",
+                "fp32_view_frac": u3 * ALGO_FLOP_PER_UNIT["poly3b"] / (ms3 * 1e-3) / 1e12 / fp32_peak}
     hbm = measured_hbm_gbs()
     nsites = 3 * (n // 4)
     secondary = {}
@@ -329,75 +445,54 @@ def run_ours(args):
             "bound": "hbm", "achieved": b / t / 1e9, "peak": hbm[0], "unit": "GB/s", "frac": b / t / 1e9 / hbm[0],
             "traffic": None, "work": "%d sites x 125 x 4 B + %d grid points x 24 B (spread, cuFFT, gather)" % (nsites, G),
             "launch_ms": t * 1e3, "peak_kind": hbm[1]}
-    out = {
-        "metric": "ns/day @4096 H2O PME, learned-guess vs plain GPU at <=1e-4 rel RMS force err",
-        "value": value, "unit": "ns/day", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "replicas", "vs_baseline": None,
-        "dtype": "fp32+double-float polynomials, fp64 accumulation", "data": "synthetic (seeded lattice box)",
-        "config": {"workload": args.workload, "waters": n // 4, "box_nm": float(ws.box[0]), "pme_alpha": alpha,
-                   "pme_grid": grid, "cutoff_nm": 0.9, "ewald_tol": 1e-5, "target_epsilon_D": 1e-8,
-                   "dt_fs": 0.2, "guess": args.guess, "guess_parameters": params_src, "seed": args.seed,
-                   "model": args.model, "equilibration_steps": args.equilibrate,
-                   "l2": "no flush: inputs larger than L2 (per-step trimer and pair variable/gradient planes "
-                         "%.0f MB, PME grids %.0f MB, against 129 MB of L2)" % (
-                             (int(counts[1]) * 36 * 3 + int(counts[0]) * 31 * 3) * 4 / 1e6,
-                             (grid[0] * grid[1] * grid[2] * 16) / 1e6 if grid else 0.0)},
-        "e2e": {"value": ns_per_day(e2e_s), "unit": "ns/day", "h2d_bytes_per_step": int(pos.nbytes),
-                "d2h_bytes_per_step": int(pos.nbytes + 5 * 8)},
-        "gpu_launches": launches,
-        "solver_iterations_per_step": solver_it,
-        "guess_comparison": dict(others, **{args.guess: dict({"ns_per_day": value, "ms_per_step": step_s * 1e3,
-                                                              "solver_iterations_per_step": solver_it},
-                                                             **({"long_run": r["long_run"]} if "long_run" in r
-                                                                else {}))}),
-        "counts": {"pairs_2b": int(counts[0]), "trimers": int(counts[1]), "elec_site_pairs": int(counts[2]),
-                   "pme_grid_points": int(grid[0] * grid[1] * grid[2]) if grid else 0},
-        "kernels_ms_per_step": {k: v["total_ms"] / args.steps for k, v in kern.items()},
-        "clocks": clocks,
-        "roofline": roof,
-        "roofline_memory_kernels": secondary,
-        "energies_kJ_mol": {"1b": en[0], "2b": en[1], "3b": en[2], "elec": en[3], "disp": en[4], "kinetic": en[5]},
-    }
-    if drift is not None:
-        out["nve_drift"] = drift
-    if not args.no_accuracy:
-        out["accuracy"] = accuracy_check()
-    if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args, sample=True)
-    return out
+    return roof, secondary
 
 
 def accuracy_check():
-    """The acceptance bar of the metric (total forces <= 1e-4 relative RMS,
-    energy <= 1e-6 relative) on the largest reference fixture: the
-    reference's 256-water PME box (python/tests/pdb_files/water256.pdb),
-    whose FP64 energy and forces from the reference's own code are committed
-    under tests/golden.  Same settings as the timed box: PME, 1e-8 D."""
+    """The metric's acceptance bar (total forces <= 1e-4 relative RMS, energy
+    <= 1e-6 relative) on the FP64 reference outputs committed under
+    tests/golden: the reference's 256-water PME box
+    (python/tests/pdb_files/water256.pdb) and one frame of this benchmark's
+    4096-water box (tests/golden/box4096_seed0.npz), at the timed settings
+    (PME, 1e-8 D, the reference's alpha*E start).  The 4096-water frame's
+    total (2711 kJ/mol) cancels terms of up to 1.1e5 kJ/mol, so its energy
+    error is also given against the sum of the terms' magnitudes."""
     import mbpol_openmm_plugin_gb300 as mb
     from mbpol_openmm_plugin_gb300 import systems
-    d = np.load(os.path.join(ROOT, "tests", "golden", "pdb_water256_pme.npz"))
-    ws = systems.WaterSystem(d["positions"], d["box"], 0, "water256_pme")
-    s = mb.create_mbpol_system(ws, target_epsilon=1e-8, ewald_alpha=float(d["alpha"]),
-                               pme_grid=[int(v) for v in d["grid"]])
-    ctx = mb.Context(s)
-    ctx.setPositions(d["positions"])
-    st = ctx.getState()
-    e, eref = st.getPotentialEnergy(), float(d["etotal"])
-    f, fref = np.asarray(st.getForces()), np.asarray(d["ftotal"])
-    ferr = float(np.sqrt(np.sum((f - fref) ** 2) / np.sum(fref ** 2)))
-    return {"workload": "water256 PME (reference fixture, FP64 reference outputs)",
-            "energy_rel": abs(e - eref) / abs(eref), "force_rel_rms": ferr,
-            "passes": bool(abs(e - eref) <= 1e-6 * abs(eref) and ferr <= 1e-4)}
+    out = {}
+    for key, fname in (("water256_pme", "pdb_water256_pme.npz"), ("box4096_seed0", "box4096_seed0.npz")):
+        d = np.load(os.path.join(ROOT, "tests", "golden", fname))
+        ws = systems.WaterSystem(d["positions"], d["box"], 0, key)
+        s = mb.create_mbpol_system(ws, target_epsilon=1e-8, ewald_alpha=float(d["alpha"]),
+                                   pme_grid=[int(v) for v in d["grid"]])
+        ctx = mb.Context(s)
+        ctx.setPositions(d["positions"])
+        st = ctx.getState()
+        e, eref = st.getPotentialEnergy(), float(d["etotal"])
+        f, fref = np.asarray(st.getForces()), np.asarray(d["ftotal"])
+        ferr = float(np.sqrt(np.sum((f - fref) ** 2) / np.sum(fref ** 2)))
+        scale = float(sum(abs(float(d[k])) for k in ("e1", "e2", "e3", "edisp", "eelec")))
+        out[key] = {"energy_rel": abs(e - eref) / abs(eref), "energy_rel_to_term_scale": abs(e - eref) / scale,
+                    "force_rel_rms": ferr,
+                    "passes": bool(abs(e - eref) <= 1e-6 * max(abs(eref), scale) and ferr <= 1e-4)}
+        del ctx
+    out["source"] = "FP64 reference outputs (compiled reference energies; oracle-port forces where the " \
+                    "reference's PME forces are not finite)"
+    return out
+
+
+def measured_peak(key, fallback):
+    """(value, source) of MEASURED_PEAKS.json, else the fallback figure of
+    one earlier GB300 measurement."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)[key]), "measured (MEASURED_PEAKS.json %s)" % key
+    except (OSError, KeyError, ValueError):
+        return fallback, "fallback (one earlier GB300 measurement)"
 
 
 def measured_hbm_gbs():
-    """(GB/s, source): the HBM copy rate of MEASURED_PEAKS.json, else the
-    fallback figure of one earlier GB300 measurement."""
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
-            return float(json.load(fh)["hbm_gbs"]), "measured HBM copy rate (MEASURED_PEAKS.json)"
-    except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback HBM copy rate"
+    return measured_peak("hbm_gbs", 6800.0)
 
 
 def nve_drift(lib, h, nsteps, nwaters, block=10):
@@ -479,7 +574,12 @@ def cpu_baseline(args, sample=True):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     try:
         import oracle
-        return oracle.time_reference_step(args.workload, args.seed, budget_s=args.cpu_budget)
+        its = None
+        fx = os.path.join(ROOT, "tests", "golden", "%s_seed%d.npz" % (args.workload, args.seed))
+        if os.path.exists(fx):
+            # the reference's own iteration count on this frame (alpha*E start)
+            its = int(np.load(fx)["iterations"])
+        return oracle.time_reference_step(args.workload, args.seed, budget_s=args.cpu_budget, solver_iterations=its)
     except Exception as ex:  # the port not built / not available
         return {"value": None, "unit": "ns/day", "cores": 1, "kind": "port", "sample": "unavailable: %s" % ex}
 
@@ -496,6 +596,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-comparison", action="store_true", help="time the --guess arm only")
+    ap.add_argument("--no-correction", action="store_true",
+                    help="learned arm without its correction network (the history predictor alone)")
     ap.add_argument("--drift-steps", type=int, default=0, help="NVE steps after the timed region for the drift")
     ap.add_argument("--avg-steps", type=int, default=1000,
                     help="MD steps after the timed ones over which iterations/step are averaged (0: none)")
@@ -510,9 +612,14 @@ def main():
         if rank != 0:
             return
         cb = cpu_baseline(args)
-        out = {"impl": "reference", "metric": "ns/day @4096 H2O PME, learned-guess vs plain GPU at <=1e-4 rel RMS force err",
+        from mbpol_openmm_plugin_gb300 import systems
+        from mbpol_openmm_plugin_gb300.plugin import pme_parameters
+        ws = systems.workload(args.workload, args.seed)
+        alpha, grid = pme_parameters(ws.box, 0.9, 1e-5)
+        out = {"impl": "reference", "metric": METRIC,
                "value": cb.get("value"), "unit": "ns/day", "n_gpus": args.gpus, "steps": args.steps,
-               "warmup": args.warmup, "higher_is_better": True, "config": {"workload": args.workload, "seed": args.seed},
+               "warmup": args.warmup, "higher_is_better": True,
+               "config": workload_config(args, ws, alpha, grid, guess_params_source(args)),
                "cpu_baseline": cb,
                "e2e": {"value": cb.get("value"), "unit": "ns/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         if cb.get("value") is None:

@@ -274,8 +274,22 @@ mbpol_status mbpol_guess_train(mbpol_context* ctx, int steps, int batch, double 
 mbpol_status mbpol_guess_get_params(mbpol_context* ctx, float* block);
 mbpol_status mbpol_guess_set_params(mbpol_context* ctx, const float* block);
 /* Network inputs [n_waters][64] of the last evaluation (48 descriptors,
- * 9 field components, 7 zeros). */
+ * 9 field components, 7 zeros; for the correction network: 48 descriptors,
+ * the water's unpredicted field change (9), its neighbours' (6), 1 zero). */
 mbpol_status mbpol_guess_descriptors(mbpol_context* ctx, float* out);
+/* Which network the mbpol_guess_* calls act on: 0 the cold-start network
+ * above (default), 1 the correction network.  No reference counterpart.
+ * The correction network has the same shape and parameter block; once it
+ * has parameters, every solve that starts from the history predictor below
+ * adds its output to the predictor's dipoles: mu = P(X) + g dF + N(D), where
+ * dF = F_new - P(F) is the unpredicted change of alpha E0 and D the water's
+ * 48 descriptors, its own dF at O, H1, H2 and the sums of fc(r) dF over the
+ * waters within 0.6 nm (O and H sites), all in the water's frame; N outputs
+ * the O, H1, H2 dipole corrections in units of 1e-7 e nm.  Its training
+ * samples (mbpol_guess_collect with network 1 selected) are the last
+ * solve's inputs with targets mu_converged - (P(X) + g dF); while network 1
+ * is selected the inputs are computed at every predictor start. */
+mbpol_status mbpol_guess_select_network(mbpol_context* ctx, int which);
 /* Loss, gradient [8905] and outputs [n][9] of the current network on host
  * data X [n][64] (raw inputs), T [n][9] (targets), without an update. */
 mbpol_status mbpol_guess_loss_grad(mbpol_context* ctx, const float* X, const float* T, int n, double* loss,

@@ -1032,6 +1032,11 @@ static mbpol_status need_elec(mbpol_context* ctx) {
     return MBPOL_OK;
 }
 
+mbpol_status mbpol_guess_select_network(mbpol_context* ctx, int which) {
+    mbpol_status s = need_elec(ctx);
+    return s ? s : ctx->elec->guess_select(which);
+}
+
 mbpol_status mbpol_guess_collect(mbpol_context* ctx) {
     mbpol_status s = need_elec(ctx);
     return s ? s : ctx->elec->guess_collect(ctx->st);

@@ -1870,8 +1870,15 @@ struct ElecImpl {
     int iterations = 0;
     double epsilon = 0.0;
     bool have_prev = false;
-    // learned guess (guess = 2)
+    // learned guess (guess = 2): the cold-start network and the correction
+    // network applied on top of the history predictor; `sel` picks the one
+    // the mbpol_guess_* calls act on
     GuessNet net;
+    GuessNet cnet{1};
+    int sel = 0;
+    DBuf<float> d_dF, d_mcorr;  // unpredicted field change, correction (lab frame)
+    DBuf<double> d_mubase;      // the predictor's dipoles of the last solve
+    bool cdesc_valid = false;   // cnet's inputs belong to the last solve
     DBuf<float> d_mguess;
     DBuf<float> d_mprev;  // the network's prediction at the previous solve
     bool have_mprev = false;
@@ -2024,6 +2031,9 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
         MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_fit, cudaEventDisableTiming));
     }
     MBPOL_CUDA_OK(I.d_mguess.ensure(3 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_dF.ensure(3 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_mcorr.ensure(3 * (size_t)n));
+    MBPOL_CUDA_OK(I.d_mubase.ensure(3 * (size_t)n));
     MBPOL_CUDA_OK(I.d_hist.ensure(3 * kHist * (size_t)n));
     MBPOL_CUDA_OK(I.d_fhist.ensure(3 * kHist * (size_t)n));
     MBPOL_CUDA_OK(I.d_fnow.ensure(3 * (size_t)n));
@@ -2323,6 +2333,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         MBPOL_CUDA_OK(I.net.predict(st, nmol, I.K, I.d_mguess.p));
     }
     const bool used_net = learned && !extrapolate;
+    I.cdesc_valid = false;
     if (history) MBPOL_CUDA_OK(scaled_field(st, 3 * n, I.d_E0.p, I.d_pol.p, I.d_fnow.p));
     if (predictor) {
         PredictorRing ring{};
@@ -2338,7 +2349,22 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
             MBPOL_CUDA_OK(cudaStreamWaitEvent(st, I.ev_fit, 0));  // fitted after the last solve
         else
             MBPOL_CUDA_OK(predictor_fit(st, 3 * n, ring, I.d_pred.p, coef));
-        MBPOL_CUDA_OK(predictor_apply(st, 3 * n, ring, I.d_fnow.p, coef, I.d_mud.p, I.d_mu0.p));
+        // the correction network: its inputs whenever it is trained or being
+        // trained (selected), its output added when it is trained
+        const bool corr = (I.cnet.ready() || I.sel == 1) && (I.K == 3 || I.K == 4);
+        MBPOL_CUDA_OK(predictor_apply(st, 3 * n, ring, I.d_fnow.p, coef, I.d_mud.p, I.d_mu0.p,
+                                      corr ? I.d_dF.p : nullptr));
+        if (corr) {
+            MBPOL_CUDA_OK(I.cnet.descriptors(st, nmol, I.K, I.d_off.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
+                                             box.L, box.periodic && I.pme, I.d_dF.p));
+            MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_mubase.p, I.d_mud.p, sizeof(double) * 3 * (size_t)n,
+                                          cudaMemcpyDeviceToDevice, st));
+            I.cdesc_valid = true;
+            if (I.cnet.ready()) {
+                MBPOL_CUDA_OK(I.cnet.predict(st, nmol, I.K, I.d_mcorr.p));
+                MBPOL_CUDA_OK(add_correction(st, 3 * n, I.d_mcorr.p, I.d_mud.p, I.d_mu0.p));
+            }
+        }
     } else if (extrapolate) {
         const size_t plane = 3 * (size_t)n;
         HistRing h{};
@@ -2658,14 +2684,27 @@ mbpol_status ElecEngine::guess_fit_predictor(cudaStream_t st, const double* hist
     return MBPOL_OK;
 }
 
+mbpol_status ElecEngine::guess_select(int which) {
+    if (which != 0 && which != 1) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "network 0 (cold start) or 1 (correction)");
+    impl_->sel = which;
+    return MBPOL_OK;
+}
+
 mbpol_status ElecEngine::guess_descriptors(cudaStream_t st, float* host_out) {
     ElecImpl& I = *impl_;
     if (!I.evaluated) return mbpol_fail(MBPOL_ERR_STATE, "no electrostatics evaluation yet");
     if (I.K != 3 && I.K != 4) return mbpol_fail(MBPOL_ERR_STATE, "the learned guess needs water molecules");
-    MBPOL_CUDA_OK(I.net.descriptors(st, I.nmol, I.K, I.d_off.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.last_box.L,
-                                    I.last_box.periodic && I.pme, I.d_E0.p));
+    GuessNet& net = I.sel ? I.cnet : I.net;
+    if (I.sel == 1) {
+        // the correction network's inputs are those of the last solve
+        if (!I.cdesc_valid)
+            return mbpol_fail(MBPOL_ERR_STATE, "the last solve did not start from the history predictor");
+    } else {
+        MBPOL_CUDA_OK(I.net.descriptors(st, I.nmol, I.K, I.d_off.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap,
+                                        I.last_box.L, I.last_box.periodic && I.pme, I.d_E0.p));
+    }
     if (host_out) {
-        MBPOL_CUDA_OK(cudaMemcpyAsync(host_out, I.net.d_desc(), sizeof(float) * guess::kIn * (size_t)I.nmol,
+        MBPOL_CUDA_OK(cudaMemcpyAsync(host_out, net.d_desc(), sizeof(float) * guess::kIn * (size_t)I.nmol,
                                       cudaMemcpyDeviceToHost, st));
         MBPOL_CUDA_OK(cudaStreamSynchronize(st));
     }
@@ -2677,28 +2716,36 @@ mbpol_status ElecEngine::guess_collect(cudaStream_t st) {
     if (!I.converged) return mbpol_fail(MBPOL_ERR_STATE, "the last solve did not converge; nothing to collect");
     mbpol_status s = guess_descriptors(st, nullptr);
     if (s) return s;
-    MBPOL_CUDA_OK(I.net.collect(st, I.nmol, I.K, I.d_mud.p));
+    if (I.sel == 1)
+        MBPOL_CUDA_OK(I.cnet.collect(st, I.nmol, I.K, I.d_mud.p, I.d_mubase.p));
+    else
+        MBPOL_CUDA_OK(I.net.collect(st, I.nmol, I.K, I.d_mud.p));
     return MBPOL_OK;
 }
 
 mbpol_status ElecEngine::guess_train(cudaStream_t st, int steps, int batch, double lr, unsigned long long seed,
                                      double* loss) {
-    ElecImpl& I = *impl_;
-    if (I.net.num_samples() <= 0) return mbpol_fail(MBPOL_ERR_STATE, "no training samples collected");
+    GuessNet& net = impl_->sel ? impl_->cnet : impl_->net;
+    if (net.num_samples() <= 0) return mbpol_fail(MBPOL_ERR_STATE, "no training samples collected");
     if (steps <= 0 || batch <= 0 || !(lr > 0)) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad training arguments");
-    MBPOL_CUDA_OK(I.net.train(st, steps, batch, lr, seed, loss));
+    MBPOL_CUDA_OK(net.train(st, steps, batch, lr, seed, loss));
     return MBPOL_OK;
 }
 
 mbpol_status ElecEngine::guess_get_params(float* block) {
+    GuessNet& net = impl_->sel ? impl_->cnet : impl_->net;
     if (!block) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null parameter block");
-    if (!impl_->net.ready()) return mbpol_fail(MBPOL_ERR_STATE, "the network has no parameters yet");
-    MBPOL_CUDA_OK(impl_->net.get_params(block));
+    if (!net.ready()) return mbpol_fail(MBPOL_ERR_STATE, "the network has no parameters yet");
+    MBPOL_CUDA_OK(net.get_params(block));
     return MBPOL_OK;
 }
 
 mbpol_status ElecEngine::guess_set_params(const float* block) {
     if (!block) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null parameter block");
+    if (impl_->sel == 1) {
+        MBPOL_CUDA_OK(impl_->cnet.set_params(block));
+        return MBPOL_OK;
+    }
     MBPOL_CUDA_OK(impl_->net.set_params(block));
     impl_->hist_levels = 0;
     impl_->have_mprev = false;
@@ -2707,13 +2754,14 @@ mbpol_status ElecEngine::guess_set_params(const float* block) {
 
 mbpol_status ElecEngine::guess_loss_grad(cudaStream_t st, const float* X, const float* T, int n, double* loss,
                                          float* grad, float* Y) {
+    GuessNet& net = impl_->sel ? impl_->cnet : impl_->net;
     if (!X || !T || !loss || !grad || !Y || n <= 0) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad arguments");
-    if (!impl_->net.ready()) return mbpol_fail(MBPOL_ERR_STATE, "the network has no parameters yet");
-    MBPOL_CUDA_OK(impl_->net.loss_grad(st, X, T, n, loss, grad, Y));
+    if (!net.ready()) return mbpol_fail(MBPOL_ERR_STATE, "the network has no parameters yet");
+    MBPOL_CUDA_OK(net.loss_grad(st, X, T, n, loss, grad, Y));
     return MBPOL_OK;
 }
 
-long ElecEngine::guess_num_samples() const { return impl_->net.num_samples(); }
+long ElecEngine::guess_num_samples() const { return (impl_->sel ? impl_->cnet : impl_->net).num_samples(); }
 
 bool ElecEngine::converged() const { return impl_->converged; }
 int ElecEngine::iterations() const { return impl_->iterations; }

@@ -35,6 +35,7 @@ public:
     std::string convergence_message() const;
     // learned initial guess (guess = 2); descriptors and collection refer to
     // the last evaluation's geometry and converged dipoles
+    mbpol_status guess_select(int which);
     mbpol_status guess_descriptors(cudaStream_t st, float* host_out);
     mbpol_status guess_collect(cudaStream_t st);
     mbpol_status guess_train(cudaStream_t st, int steps, int batch, double lr, unsigned long long seed,

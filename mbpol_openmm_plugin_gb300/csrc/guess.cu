@@ -69,7 +69,8 @@ struct GBox {
 
 __global__ void descriptor_kernel(int nmol, int K, const float* __restrict__ off, const int* __restrict__ nb,
                                   const float* __restrict__ nbd, const int* __restrict__ nnb, int cap, GBox box,
-                                  const float* __restrict__ E0, float* __restrict__ D, float* __restrict__ F) {
+                                  const float* __restrict__ E0, float* __restrict__ D, float* __restrict__ F,
+                                  int mode) {
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (A >= nmol) return;
@@ -103,13 +104,34 @@ __global__ void descriptor_kernel(int nmol, int K, const float* __restrict__ off
     e3[2] = e1[0] * e2[1] - e1[1] * e2[0];
 
     float acc[kFeat];
+    float nf[kNbField];  // mode 1: neighbours' field changes (lab frame)
     #pragma unroll
     for (int c = 0; c < kFeat; ++c) acc[c] = 0.f;
+    #pragma unroll
+    for (int c = 0; c < kNbField; ++c) nf[c] = 0.f;
     const int n = min(nnb[A], cap);
     for (int t = lane; t < n; t += 32) {
         const int B = nb[(size_t)A * cap + t];
         const float* dd = nbd + 3 * ((size_t)A * cap + t);
         const float* oB = off + 3 * (size_t)K * B;
+        if (mode == 1) {
+            // O-O vector: the list's FP32 minimum-image vector plus B's O offset
+            float d[3] = {dd[0] + oB[0], dd[1] + oB[1], dd[2] + oB[2]};
+            if (box.periodic) {
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) d[k] -= box.L[k] * rintf(d[k] * box.inv[k]);
+            }
+            const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (r2 < kRC * kRC) {
+                const float fc = 0.5f * (cosf(kPiF * sqrtf(r2) / kRC) + 1.f);
+                const float* fB = E0 + 3 * (size_t)K * B;
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    nf[k] += fc * fB[k];
+                    nf[3 + k] += fc * (fB[3 + k] + fB[6 + k]);
+                }
+            }
+        }
         #pragma unroll
         for (int s = 0; s < 3; ++s) {
             float d[3] = {dd[0] + oB[3 * s], dd[1] + oB[3 * s + 1], dd[2] + oB[3 * s + 2]};
@@ -152,6 +174,26 @@ __global__ void descriptor_kernel(int nmol, int K, const float* __restrict__ off
             D[(size_t)A * kIn + kFeat + 3 * s + 2] = e[0] * e3[0] + e[1] * e3[1] + e[2] * e3[2];
         }
         for (int c = kFeat + kField; c < kIn; ++c) D[(size_t)A * kIn + c] = 0.f;
+    }
+    if (mode == 1) {
+        // neighbour sums in the water's frame (fixed-order warp reduction)
+        #pragma unroll
+        for (int c = 0; c < kNbField; ++c) {
+            #pragma unroll
+            for (int o = 16; o > 0; o >>= 1) nf[c] += __shfl_xor_sync(0xffffffffu, nf[c], o);
+        }
+        if (lane == 0) {
+            #pragma unroll
+            for (int g = 0; g < 2; ++g) {
+                const float* e = nf + 3 * g;
+                float* out = D + (size_t)A * kIn + kFeat + kField + 3 * g;
+                out[0] = e[0] * e1[0] + e[1] * e1[1] + e[2] * e1[2];
+                out[1] = e[0] * e2[0] + e[1] * e2[1] + e[2] * e2[2];
+                out[2] = e[0] * e3[0] + e[1] * e3[1] + e[2] * e3[2];
+            }
+        }
+    }
+    if (lane == 0) {
         #pragma unroll
         for (int k = 0; k < 3; ++k) {
             F[(size_t)A * 9 + k] = e1[k];
@@ -542,9 +584,9 @@ __global__ void adam_kernel(int np, float* __restrict__ p, const float* __restri
     p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
 }
 
-// network outputs (frame components, 1e-3 e nm) -> lab-frame dipoles per site
+// network outputs (frame components, `scale` e nm) -> lab-frame dipoles per site
 __global__ void to_lab_kernel(int nmol, int K, const float* __restrict__ Y, const float* __restrict__ F,
-                              float* __restrict__ m) {
+                              float* __restrict__ m, float scale) {
     const int A = blockIdx.x * blockDim.x + threadIdx.x;
     if (A >= nmol) return;
     for (int s = 0; s < K; ++s)
@@ -552,20 +594,25 @@ __global__ void to_lab_kernel(int nmol, int K, const float* __restrict__ Y, cons
             float v = 0.f;
             if (s < 3)
                 for (int c = 0; c < 3; ++c) v += Y[(size_t)A * kOut + 3 * s + c] * F[(size_t)A * 9 + 3 * c + d];
-            m[3 * ((size_t)K * A + s) + d] = kOutScale * v;
+            m[3 * ((size_t)K * A + s) + d] = scale * v;
         }
 }
 
-// converged FP64 dipoles -> frame components (targets) appended at row0
-__global__ void targets_kernel(int nmol, int K, const double* __restrict__ mu, const float* __restrict__ F,
-                               const float* __restrict__ D, float* __restrict__ X, float* __restrict__ T, long row0) {
+// converged FP64 dipoles (minus mu_base if given) -> frame components in
+// units of `scale` (targets) appended at row0
+__global__ void targets_kernel(int nmol, int K, const double* __restrict__ mu, const double* __restrict__ mu_base,
+                               const float* __restrict__ F, const float* __restrict__ D, float* __restrict__ X,
+                               float* __restrict__ T, long row0, double scale) {
     const int A = blockIdx.x * blockDim.x + threadIdx.x;
     if (A >= nmol) return;
     for (int s = 0; s < 3; ++s)
         for (int c = 0; c < 3; ++c) {
             double v = 0.0;
-            for (int d = 0; d < 3; ++d) v += mu[3 * ((size_t)K * A + s) + d] * (double)F[(size_t)A * 9 + 3 * c + d];
-            T[(row0 + A) * kOut + 3 * s + c] = (float)(v / kOutScale);
+            for (int d = 0; d < 3; ++d) {
+                const size_t i = 3 * ((size_t)K * A + s) + d;
+                v += (mu[i] - (mu_base ? mu_base[i] : 0.0)) * (double)F[(size_t)A * 9 + 3 * c + d];
+            }
+            T[(row0 + A) * kOut + 3 * s + c] = (float)(v / scale);
         }
     for (int c = 0; c < kIn; ++c) X[(row0 + A) * kIn + c] = D[(size_t)A * kIn + c];
 }
@@ -644,7 +691,7 @@ int mlp_blocks(int n) {
 
 }  // namespace
 
-GuessNet::GuessNet() : b_(new GuessBuffers) {}
+GuessNet::GuessNet(int mode) : b_(new GuessBuffers), mode_(mode) {}
 
 GuessNet::~GuessNet() {
     for (void* p : {(void*)b_->params, (void*)b_->adam_m, (void*)b_->adam_v, (void*)b_->grad, (void*)b_->loss,
@@ -659,7 +706,7 @@ const float* GuessNet::d_frames() const { return b_->frames; }
 
 cudaError_t GuessNet::descriptors(cudaStream_t st, int nmol, int K, const float* off, const int* nb,
                                   const float* nbd, const int* nnb, int cap, const double* box, int periodic,
-                                  const float* E0) {
+                                  const float* field) {
     if (nmol > b_->cap_mol) {
         GUESS_OK(grow(&b_->desc, 0, (size_t)nmol * kIn, 0));
         GUESS_OK(grow(&b_->frames, 0, (size_t)nmol * 9, 0));
@@ -673,12 +720,12 @@ cudaError_t GuessNet::descriptors(cudaStream_t st, int nmol, int K, const float*
         gb.inv[k] = periodic ? (float)(1.0 / box[k]) : 0.f;
     }
     count_launch();
-    descriptor_kernel<<<(nmol * 32 + 127) / 128, 128, 0, st>>>(nmol, K, off, nb, nbd, nnb, cap, gb, E0, b_->desc,
-                                                               b_->frames);
+    descriptor_kernel<<<(nmol * 32 + 127) / 128, 128, 0, st>>>(nmol, K, off, nb, nbd, nnb, cap, gb, field,
+                                                               b_->desc, b_->frames, mode_);
     return cudaGetLastError();
 }
 
-cudaError_t GuessNet::collect(cudaStream_t st, int nmol, int K, const double* mu_d) {
+cudaError_t GuessNet::collect(cudaStream_t st, int nmol, int K, const double* mu_d, const double* mu_base) {
     const long need = nsamples_ + nmol;
     if (need > b_->cap_s) {
         const long cap = need + need / 2 + 1024;
@@ -688,8 +735,9 @@ cudaError_t GuessNet::collect(cudaStream_t st, int nmol, int K, const double* mu
         b_->cap_s = cap;
     }
     count_launch();
-    targets_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, K, mu_d, b_->frames, b_->desc, b_->X, b_->T,
-                                                        nsamples_);
+    targets_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, K, mu_d, mode_ == 1 ? mu_base : nullptr, b_->frames,
+                                                        b_->desc, b_->X, b_->T, nsamples_,
+                                                        mode_ == 1 ? (double)kResScale : (double)kOutScale);
     nsamples_ = need;
     return cudaGetLastError();
 }
@@ -700,7 +748,8 @@ cudaError_t GuessNet::predict(cudaStream_t st, int nmol, int K, float* m_out) {
     mlp_kernel<false><<<mlp_blocks(nmol), 32 * kWarps, SmemPlan::bytes(false), st>>>(
         nmol, b_->params, b_->desc, nullptr, nmol, 0ull, 0.f, b_->ybuf, nullptr, nullptr);
     count_launch();
-    to_lab_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, K, b_->ybuf, b_->frames, m_out);
+    to_lab_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, K, b_->ybuf, b_->frames, m_out,
+                                                       mode_ == 1 ? kResScale : kOutScale);
     return cudaGetLastError();
 }
 

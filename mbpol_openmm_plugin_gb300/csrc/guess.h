@@ -6,7 +6,10 @@
 //      prediction), or m_now when there is no previous solve.
 //  (2) Trajectories: a linear predictor over the last solves whose
 //      coefficients are refitted by least squares before every solve
-//      (predictor.cu).
+//      (predictor.cu), plus a second network of the same shape (the
+//      correction network) that maps each water's neighbourhood and the
+//      unpredicted change of the permanent field around it to the
+//      predictor's remaining error.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -31,7 +34,13 @@ constexpr int kParams = kB3 + kOut;  // 8905
 // the parameter block handed across the ABI: kParams weights, then the
 // input standardisation (mean[64], 1/std[64])
 constexpr int kBlockFloats = kParams + 2 * kIn;
-constexpr float kOutScale = 1e-3f;  // e nm per network output unit
+constexpr float kOutScale = 1e-3f;  // e nm per network output unit (cold-start network)
+constexpr float kResScale = 1e-7f;  // e nm per output unit of the correction network
+// correction network inputs: 48 descriptors, the water's own unpredicted
+// field change dF = alpha E0 - P(alpha E0) at O, H1, H2 (9, in its frame), and
+// the sums over neighbouring waters B with O-O distance r < 0.6 nm of
+// fc(r) dF_O(B) and fc(r) (dF_H1(B) + dF_H2(B)) (6, in its frame), one zero
+constexpr int kNbField = 6;
 // learned linear predictor over the history of solves (predictor.cu)
 constexpr int kPredOrder = 7;    // backward differences of the dipoles in the model
 constexpr int kPredRegressors = kPredOrder;  // fitted coefficients
@@ -57,9 +66,13 @@ struct PredictorRing {
 int predictor_partial_blocks();
 cudaError_t predictor_fit(cudaStream_t st, int n3, const PredictorRing& ring, double* d_partials, double* d_coef);
 // Starting dipoles (FP64 state and its FP32 copy) from the history, the
-// coefficients and alpha E0 of the new geometry (f_now).
+// coefficients and alpha E0 of the new geometry (f_now); dF (may be null)
+// receives the unpredicted field change f_now - P(f).
 cudaError_t predictor_apply(cudaStream_t st, int n3, const PredictorRing& ring, const double* f_now,
-                            const double* d_coef, double* mu_d, float* mu_f);
+                            const double* d_coef, double* mu_d, float* mu_f, float* dF = nullptr);
+// mu_d += m, mu_f = float(mu_d) (the correction network's output added to
+// the predictor's dipoles)
+cudaError_t add_correction(cudaStream_t st, int n3, const float* m, double* mu_d, float* mu_f);
 // alpha E0 per dipole component, in FP64 (pol per site, E0 [sites][3]).
 cudaError_t scaled_field(cudaStream_t st, int n3, const float* E0, const float* pol, double* out);
 
@@ -69,7 +82,10 @@ struct GuessBuffers;
 // named h_*.
 class GuessNet {
 public:
-    GuessNet();
+    // mode 0: the cold-start network (field slots: E0; outputs: the dipoles,
+    // kOutScale); mode 1: the correction network (field slots: dF and its
+    // neighbour sums; outputs: the predictor's error, kResScale)
+    explicit GuessNet(int mode = 0);
     ~GuessNet();
     GuessNet(const GuessNet&) = delete;
     GuessNet& operator=(const GuessNet&) = delete;
@@ -78,15 +94,17 @@ public:
     long num_samples() const { return nsamples_; }
 
     // network inputs D [nmol][64] (48 descriptors from the electrostatics
-    // neighbour list, the permanent field E0 [sites][3] at O, H1, H2 in the
-    // water's frame, zeros) and frames F [nmol][9] of the current geometry
+    // neighbour list, then mode 0: the permanent field E0 [sites][3] at O,
+    // H1, H2 in the water's frame; mode 1: dF [sites][3] of the water and of
+    // its neighbours as above; zeros) and frames F [nmol][9]
     cudaError_t descriptors(cudaStream_t st, int nmol, int K, const float* off, const int* nb, const float* nbd,
-                            const int* nnb, int cap, const double* box, int periodic, const float* E0);
+                            const int* nnb, int cap, const double* box, int periodic, const float* field);
     const float* d_desc() const;
     const float* d_frames() const;
     // append the current descriptors with the converged dipoles (FP64,
-    // [nsites][3]) as training targets
-    cudaError_t collect(cudaStream_t st, int nmol, int K, const double* mu_d);
+    // [nsites][3]; mode 1: minus the predictor's dipoles mu_base) as
+    // training targets
+    cudaError_t collect(cudaStream_t st, int nmol, int K, const double* mu_d, const double* mu_base = nullptr);
     // network prediction m [nsites][3] (lab frame, e nm) for the current
     // descriptors
     cudaError_t predict(cudaStream_t st, int nmol, int K, float* m_out);
@@ -99,8 +117,11 @@ public:
     cudaError_t get_params(float* h_block) const;
     cudaError_t set_params(const float* h_block);
 
+    int mode() const { return mode_; }
+
 private:
     GuessBuffers* b_;
+    int mode_ = 0;
     bool ready_ = false;
     long nsamples_ = 0;
 };

@@ -184,7 +184,7 @@ __global__ void predictor_solve_kernel(int nblocks, const double* __restrict__ p
 
 __global__ void predictor_apply_kernel(int n3, const PredictorRing ring, const double* __restrict__ f_now,
                                        const double* __restrict__ coef, double* __restrict__ mu_d,
-                                       float* __restrict__ mu_f) {
+                                       float* __restrict__ mu_f, float* __restrict__ dF) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n3) return;
     double x[kJ + 1], d[kJ], fx[kJ + 1], fd[kJ];
@@ -201,9 +201,11 @@ __global__ void predictor_apply_kernel(int n3, const PredictorRing ring, const d
         v += coef[j] * d[j];
         pf += coef[j] * fd[j];
     }
-    v += guess::kFieldGain * (f_now[e] - pf);
+    const double df = f_now[e] - pf;
+    v += guess::kFieldGain * df;
     mu_d[e] = v;
     mu_f[e] = (float)v;
+    if (dF) dF[e] = (float)df;
 }
 
 __global__ void scaled_field_kernel(int n3, const float* __restrict__ E0, const float* __restrict__ pol,
@@ -228,9 +230,25 @@ cudaError_t predictor_fit(cudaStream_t st, int n3, const PredictorRing& ring, do
 }
 
 cudaError_t predictor_apply(cudaStream_t st, int n3, const PredictorRing& ring, const double* f_now,
-                            const double* d_coef, double* mu_d, float* mu_f) {
+                            const double* d_coef, double* mu_d, float* mu_f, float* dF) {
     count_launch();
-    predictor_apply_kernel<<<(n3 + 255) / 256, 256, 0, st>>>(n3, ring, f_now, d_coef, mu_d, mu_f);
+    predictor_apply_kernel<<<(n3 + 255) / 256, 256, 0, st>>>(n3, ring, f_now, d_coef, mu_d, mu_f, dF);
+    return cudaGetLastError();
+}
+
+// mu_d += m (the correction network's output), mu_f = float(mu_d)
+__global__ void add_correction_kernel(int n3, const float* __restrict__ m, double* __restrict__ mu_d,
+                                      float* __restrict__ mu_f) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n3) return;
+    const double v = mu_d[e] + (double)m[e];
+    mu_d[e] = v;
+    mu_f[e] = (float)v;
+}
+
+cudaError_t add_correction(cudaStream_t st, int n3, const float* m, double* mu_d, float* mu_f) {
+    count_launch();
+    add_correction_kernel<<<(n3 + 255) / 256, 256, 0, st>>>(n3, m, mu_d, mu_f);
     return cudaGetLastError();
 }
 

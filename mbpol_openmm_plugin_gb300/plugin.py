@@ -540,6 +540,16 @@ class Context:
 
     # ---- learned initial guess for the induced dipoles (guess = 2); this
     # library's addition, no reference counterpart
+    ColdStartNetwork, CorrectionNetwork = 0, 1
+
+    def selectDipoleGuessNetwork(self, which):
+        """The network the calls below act on: ColdStartNetwork (default) or
+        CorrectionNetwork (added to the history predictor's dipoles at every
+        solve once it has parameters; mbpol_guess_select_network)."""
+        if self._h is None:
+            self._build()
+        check(_capi.load().mbpol_guess_select_network(self._h, int(which)))
+
     def collectDipoleGuessSample(self):
         """Append the last evaluation's descriptors and converged dipoles
         (one sample per water) to the device-resident training set."""

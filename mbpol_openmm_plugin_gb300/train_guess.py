@@ -2,13 +2,18 @@
 
     python -m mbpol_openmm_plugin_gb300.train_guess --workload box4096 \
         --frames 2000 --steps 20000 --out dipole_guess_box4096.npy
+    python -m mbpol_openmm_plugin_gb300.train_guess --network correction \
+        --seed 1 --frames 2000 --steps 20000 --out dipole_correction_box4096.npy
 
 NVT molecular dynamics (velocity Verlet, Andersen thermostat at 300 K,
-0.2 fs) with the plain solver (previous-step guess, 1e-8 D); after every step
-the water descriptors and the converged dipoles are collected on the device,
-and the network is trained there with the library's own forward/backward
-kernels and Adam.  The parameter block (weights, biases and input
-standardisation; mbpol_guess_get_params) is saved as float32 .npy.
+0.2 fs) at 1e-8 D; after every step the network's inputs and targets are
+collected on the device, and the network is trained there with the
+library's own forward/backward kernels and Adam.  The cold-start network
+learns the converged dipoles from the plain solver's frames (previous-step
+guess); the correction network learns the history predictor's remaining
+error (guess 2, from the 13th frame on, when the predictor runs).  The
+parameter block (weights, biases and input standardisation;
+mbpol_guess_get_params) is saved as float32 .npy.
 """
 import argparse
 import ctypes
@@ -33,15 +38,19 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--collision-rate", type=float, default=1.0, help="Andersen collisions per ps")
+    ap.add_argument("--network", default="cold-start", choices=["cold-start", "correction"])
     ap.add_argument("--out", required=True)
     a = ap.parse_args(argv)
+    correction = a.network == "correction"
 
     ws = workload(a.workload, a.seed)
     alpha, grid = pme_parameters(ws.box, 0.9, 1e-5) if ws.box is not None else (0.0, None)
-    sysm = create_mbpol_system(ws, target_epsilon=1e-8, ewald_alpha=alpha, pme_grid=grid, guess=1)
+    sysm = create_mbpol_system(ws, target_epsilon=1e-8, ewald_alpha=alpha, pme_grid=grid, guess=2 if correction else 1)
     ctx = Context(sysm)
     ctx.setPositions(ws.positions)
     ctx._build()
+    if correction:
+        ctx.selectDipoleGuessNetwork(Context.CorrectionNetwork)
     lib = _capi.load()
     h = ctx._h
     masses = np.ascontiguousarray(sysm.masses, np.float64)
@@ -60,7 +69,8 @@ def main(argv=None):
         _capi.check(lib.mbpol_md_run(h, 1, DT_PS, 300.0, a.collision_rate, a.seed * 1000003 + f, ctypes.byref(ms),
                                      _capi.ptr(en), ctypes.byref(it)))
         iters += it.value
-        ctx.collectDipoleGuessSample()
+        if not correction or f >= 12:   # the predictor needs 12 solves of history
+            ctx.collectDipoleGuessSample()
     t1 = time.time()
     loss = ctx.trainDipoleGuess(a.steps, a.batch, a.lr, a.seed + 1)
     t2 = time.time()

@@ -7,9 +7,10 @@ count.
 Tolerances: per-cluster total energy within 1e-6 of the sum of the five
 terms' magnitudes (a small cluster's total is a near-cancellation of terms of
 hundreds of kJ/mol, so the bound is taken on the scale the terms are
-evaluated at); each term within 2e-5 of its magnitude with a 1e-4 kJ/mol
-floor (2e-5: the three-body term on the tensor cores); forces 1e-4 relative
-RMS over the batch; iterations within 2 of the oracle's."""
+evaluated at); each term within 2e-5 of its magnitude (the three-body term
+on the tensor cores), with a floor of 1e-6 of that scale and 1e-4 kJ/mol (a
+cluster's electrostatic energy can itself be a near-cancellation); forces
+1e-4 relative RMS over the batch; iterations within 2 of the oracle's."""
 import numpy as np
 import pytest
 
@@ -59,7 +60,7 @@ def test_batched_clusters_match_per_cluster_oracle(ncl, nmax, evaluator):
             " ".join("%.1e" % (E[c, k] - ref[k]) for k in range(5))))
         assert abs(tot - tref) <= 1e-6 * scale
         for k in range(5):
-            assert abs(E[c, k] - ref[k]) <= max(2e-5 * abs(ref[k]), 1e-4), (c, KEYS[k])
+            assert abs(E[c, k] - ref[k]) <= max(2e-5 * abs(ref[k]), 1e-6 * scale, 1e-4), (c, KEYS[k])
         assert abs(int(its[c]) - int(r["iterations"])) <= 2
     assert abs(st.getPotentialEnergy() - E.sum()) <= 1e-9 * abs(E.sum())
     ferr = rel_rms(st.getForces(), fref)
