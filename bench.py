@@ -125,9 +125,11 @@ def maxwell_boltzmann(masses, T, seed):
 # switch and chain rule around them): these stay fixed whatever the kernels do.
 ALGO_FLOP_PER_UNIT = {"poly2b": 31200, "poly3b": 112600}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# each walk on box4096, measured with ncu --set full, and the units that launch
-# processed; the traffic of a launch is scaled by its unit count.
-NCU_TRAFFIC = {"poly3b": (53.226e6 + 2.685e6, 181889), "poly2b": (16.451e6, 65434)}
+# each polynomial kernel on box4096, measured with ncu --set full
+# (profiles/poly_tc_kernel_box4096.md, profiles/poly_df_kernel_box4096.md),
+# and the units that launch processed; the traffic of a launch is scaled by
+# its unit count.
+NCU_TRAFFIC = {"poly3b": (54.103e6 + 11.153e6, 182343), "poly2b": (16.451e6, 65434)}
 
 
 GUESS_MODE = {"plain": 1, "learned": 2, "extrapolation": 3}
@@ -177,8 +179,9 @@ def md_context(args, guess, params=None, corr=None):
     the seeded box with Maxwell-Boltzmann velocities, `args.equilibrate`
     untimed MD steps (the history-based guesses reach their steady state
     after 12 solves), then the warm-up steps (first force evaluation, buffer
-    growth).  The library is deterministic (fixed-point PME spreading, fixed
-    reduction orders), so two contexts built alike reach the same state."""
+    growth).  Two contexts built alike reach the same state to ~1e-5 nm after
+    200 steps (the forces are summed with FP64 atomics in no fixed order;
+    e2e reports the difference)."""
     import mbpol_openmm_plugin_gb300 as mb
     from mbpol_openmm_plugin_gb300 import _capi
     lib = _capi.load()
@@ -363,6 +366,34 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, sample=True)
     return out
+
+
+def profile_window(args):
+    """The --guess arm's MD steps bracketed by cudaProfilerStart/Stop, so that
+    a profiler started with --profile-from-start off sees only those steps'
+    kernels (after the trajectory start and warm-up of md_context)."""
+    from mbpol_openmm_plugin_gb300 import _capi
+    lib = _capi.load()
+    params, _ = guess_params(args)
+    corr = correction_params(args) if args.guess == "learned" else None
+    c = md_context(args, args.guess, params if args.guess == "learned" else None, corr)
+    rt = None
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            continue
+    if rt is None:
+        raise RuntimeError("the CUDA runtime library was not found")
+    rt.cudaProfilerStart()
+    l0 = lib.mbpol_launch_count()
+    step_s, it, _ = md_steps(lib, c["h"], args.profile_window, args.seed)
+    launches = int(lib.mbpol_launch_count() - l0)
+    rt.cudaProfilerStop()
+    return {"profile_window_steps": args.profile_window, "guess": args.guess, "ms_per_step": step_s * 1e3,
+            "solver_iterations_per_step": it, "gpu_launches": launches, "counts": [int(v) for v in c["ctx"].getCounts()],
+            "note": "timed under a profiler if one is attached: not a bench value"}
 
 
 def workload_config(args, ws, alpha, grid, params_src):
@@ -596,6 +627,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-comparison", action="store_true", help="time the --guess arm only")
+    ap.add_argument("--profile-window", type=int, default=0,
+                    help="profiling run: the --guess arm's context after equilibration and warm-up, then this many "
+                         "MD steps between cudaProfilerStart and cudaProfilerStop (for ncu --profile-from-start off)")
     ap.add_argument("--no-correction", action="store_true",
                     help="learned arm without its correction network (the history predictor alone)")
     ap.add_argument("--drift-steps", type=int, default=0, help="NVE steps after the timed region for the drift")
@@ -631,7 +665,10 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.gpus > 1:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
-    out = run_clusters(args) if args.workload == "clusters" else run_ours(args)
+    if args.profile_window > 0:
+        out = profile_window(args)
+    else:
+        out = run_clusters(args) if args.workload == "clusters" else run_ours(args)
     if rank == 0:
         print(json.dumps(out))
 
