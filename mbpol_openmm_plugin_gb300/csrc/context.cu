@@ -51,6 +51,8 @@ unsigned long long g_launches = 0;
 void count_launch() { ++g_launches; }
 size_t g_open[K_NUM];
 
+bool prof_on() { return g_prof.on; }
+
 void prof_begin(cudaStream_t st, int id) {
     if (!g_prof.on) return;
     cudaEvent_t e = g_prof.get();

@@ -1131,10 +1131,15 @@ __global__ void __launch_bounds__(128, PME ? 7 : 6) induced_update_kernel(int nm
 // the same dipoles run on another stream while the direct field is summed.
 __global__ void induced_finish_kernel(int n, const float* __restrict__ Edir, const float* __restrict__ phi_mu,
                                       const float* __restrict__ E0, const float* __restrict__ pol,
-                                      const float* __restrict__ mu_in, float* __restrict__ mu_out,
-                                      double* __restrict__ mu_d, double* __restrict__ eps2, int mode,
-                                      float* __restrict__ Ebase, const float* __restrict__ anchor) {
+                                      const float* mu_in, float* mu_out, double* __restrict__ mu_d,
+                                      double* __restrict__ eps2, int mode, float* __restrict__ Ebase,
+                                      const float* anchor, const int* __restrict__ d_mode, float* anchor_store) {
+    // mu_out may be mu_in (the device-controlled loop updates in place: each
+    // site's values are read before they are written); d_mode, when given,
+    // holds this iteration's anchoring stage, and at the anchoring iteration
+    // the dipoles are copied to anchor_store
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d_mode) mode = *d_mode;
     double d2 = 0.0;
     if (i < n) {
         const f3 mu = ld3(mu_in, i);
@@ -1145,6 +1150,11 @@ __global__ void induced_finish_kernel(int n, const float* __restrict__ Edir, con
             Ebase[3 * i] = ex;
             Ebase[3 * i + 1] = ey;
             Ebase[3 * i + 2] = ez;
+            if (anchor_store) {
+                anchor_store[3 * i] = mu.x;
+                anchor_store[3 * i + 1] = mu.y;
+                anchor_store[3 * i + 2] = mu.z;
+            }
         } else if (mode == 2) {
             ex += Ebase[3 * i];
             ey += Ebase[3 * i + 1];
@@ -1165,14 +1175,52 @@ __global__ void induced_finish_kernel(int n, const float* __restrict__ Edir, con
             mu_out[3 * i + 1] = (float)u1;
             mu_out[3 * i + 2] = (float)u2;
         } else {
-            const float* an = mode == 1 ? mu_in : anchor;
-            mu_out[3 * i] = (float)(u0 - (double)an[3 * i]);
-            mu_out[3 * i + 1] = (float)(u1 - (double)an[3 * i + 1]);
-            mu_out[3 * i + 2] = (float)(u2 - (double)an[3 * i + 2]);
+            // the anchor: at the anchoring iteration the input dipoles themselves
+            const float a0 = mode == 1 ? mu.x : anchor[3 * i];
+            const float a1 = mode == 1 ? mu.y : anchor[3 * i + 1];
+            const float a2 = mode == 1 ? mu.z : anchor[3 * i + 2];
+            mu_out[3 * i] = (float)(u0 - (double)a0);
+            mu_out[3 * i + 1] = (float)(u1 - (double)a1);
+            mu_out[3 * i + 2] = (float)(u2 - (double)a2);
         }
         d2 = dx * dx + dy * dy + dz * dz;
     }
     block_sum_atomic<128>(d2, eps2);
+}
+
+// State of one system's device-controlled solve (below).
+struct SolveState {
+    int mode;    // anchoring stage of the next iteration: 0 plain, 1 anchoring, 2 anchored
+    int its;     // iterations done
+    int conv;    // converged
+    int rounds;  // iterations launched (bound on the loop)
+    double cur;  // epsilon of the last iteration
+};
+
+// Convergence control of one system's solve on the device: the host loop's
+// rules (reference convergeInduceDipoles, MBPolReferenceElectrostaticsForce.cpp
+// :557-616) applied to the iteration just finished -- epsilon from the sum
+// of squared changes, stop on convergence, on an increase or at the
+// iteration limit -- then the next iteration's anchoring stage, and the
+// condition of the graph's while loop.  One thread.
+__global__ void solve_control_kernel(double* __restrict__ eps2, double inv_n, SolveState* __restrict__ s,
+                                     double target, int max_it, double switch_eps, cudaGraphConditionalHandle loop) {
+    const double e = kSOR * kDebye * sqrt(*eps2 * inv_n);
+    *eps2 = 0.0;  // the next iteration's sum
+    bool stop = false;
+    if (!isfinite(e)) {
+        stop = true;
+    } else if (e < target) {
+        s->conv = 1;
+        stop = true;
+    } else if (s->cur < e || s->its >= max_it) {
+        stop = true;
+    }
+    s->cur = e;
+    s->its += 1;
+    s->mode = s->mode == 0 ? (e < switch_eps ? 1 : 0) : 2;
+    const int r = ++s->rounds;
+    cudaGraphSetConditional(loop, (!stop && r <= max_it + 2) ? 1u : 0u);
 }
 
 // Double-float (FP32 pair) helpers for the pair energies: FP64 arithmetic
@@ -1906,6 +1954,16 @@ struct ElecImpl {
     DBuf<int> d_cl_nsites, d_cl_its, d_cl_conv, d_rounds;
     DBuf<double> d_cl_cur;
     cudaStream_t st_cap = nullptr;
+    // one system's PME solve as one graph launch (solver_graph): a while
+    // node around one iteration (the PME pass on a forked branch beside the
+    // direct field, the update in place, the control kernel)
+    cudaStream_t st_cap2 = nullptr;
+    cudaEvent_t ev_cfork = nullptr, ev_cjoin = nullptr;
+    cudaGraph_t sv_graph = nullptr;
+    cudaGraphExec_t sv_exec = nullptr;
+    std::vector<uintptr_t> sv_key;
+    DBuf<SolveState> d_sstate;
+    bool sv_disabled = false;  // the graph could not be built here: host loop
     cudaGraph_t cl_graph = nullptr;
     cudaGraphExec_t cl_exec = nullptr;
     std::vector<uintptr_t> cl_graph_key;
@@ -1927,6 +1985,11 @@ struct ElecImpl {
     unsigned long long* h_npair = nullptr;
 
     ~ElecImpl() {
+        if (sv_exec) cudaGraphExecDestroy(sv_exec);
+        if (sv_graph) cudaGraphDestroy(sv_graph);
+        if (st_cap2) cudaStreamDestroy(st_cap2);
+        if (ev_cfork) cudaEventDestroy(ev_cfork);
+        if (ev_cjoin) cudaEventDestroy(ev_cjoin);
         if (cl_exec) cudaGraphExecDestroy(cl_exec);
         if (cl_graph) cudaGraphDestroy(cl_graph);
         if (st_cap) cudaStreamDestroy(st_cap);
@@ -2206,6 +2269,86 @@ mbpol_status cluster_solver_graph(ElecImpl& I, int nmol, int wblocks, float* buf
     return MBPOL_OK;
 }
 
+// One system's PME solve as one graph: a while node whose body is one
+// iteration -- the reciprocal-space pass of the dipoles on a forked branch
+// beside their direct field (induced_update_kernel), the self and
+// reciprocal parts and the SOR update in place (induced_finish_kernel, the
+// anchoring stage read from the device), and solve_control_kernel, which
+// applies the reference's stopping rules and sets the loop's condition.
+// The host reads the state once, after the launch.  Rebuilt when a buffer,
+// size, plan or solver parameter it captured changes.
+mbpol_status solver_graph(ElecImpl& I, int nmol, int wblocks, int n, size_t nreal, float* mu, float* anchor_buf,
+                          double switch_eps, const Box& box) {
+    const std::vector<uintptr_t> key = {
+        (uintptr_t)nmol, (uintptr_t)wblocks, (uintptr_t)n, (uintptr_t)nreal, (uintptr_t)I.cap, (uintptr_t)mu,
+        (uintptr_t)anchor_buf, (uintptr_t)I.d_off.p, (uintptr_t)I.d_damp.p, (uintptr_t)I.d_pol.p,
+        (uintptr_t)I.d_type.p, (uintptr_t)I.d_nb.p, (uintptr_t)I.d_nbd.p, (uintptr_t)I.d_nnb.p, (uintptr_t)I.d_E0.p,
+        (uintptr_t)I.d_phi_mu.p, (uintptr_t)I.d_mud.p, (uintptr_t)I.d_eps2.p, (uintptr_t)I.d_ebase.p,
+        (uintptr_t)I.d_intra.p, (uintptr_t)I.d_pcoef.p, (uintptr_t)I.d_polmask.p, (uintptr_t)I.d_edir.p,
+        (uintptr_t)I.d_q.p, (uintptr_t)I.d_gidx.p, (uintptr_t)I.d_gfrac.p, (uintptr_t)I.d_gridq.p,
+        (uintptr_t)I.d_grid.p, (uintptr_t)I.d_cgrid.p, (uintptr_t)I.d_eterm.p, (uintptr_t)I.plan_f,
+        (uintptr_t)I.plan_b, (uintptr_t)I.d_sstate.p, key_bits(I.prm.target_epsilon),
+        (uintptr_t)I.prm.max_iterations, key_bits(switch_eps)};
+    if (I.sv_exec && key == I.sv_key) return MBPOL_OK;
+    if (I.sv_exec) cudaGraphExecDestroy(I.sv_exec);
+    if (I.sv_graph) cudaGraphDestroy(I.sv_graph);
+    I.sv_exec = nullptr;
+    I.sv_graph = nullptr;
+    I.sv_key.clear();
+    if (!I.st_cap) MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&I.st_cap, cudaStreamNonBlocking));
+    if (!I.st_cap2) MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&I.st_cap2, cudaStreamNonBlocking));
+    if (!I.ev_cfork) MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_cfork, cudaEventDisableTiming));
+    if (!I.ev_cjoin) MBPOL_CUDA_OK(cudaEventCreateWithFlags(&I.ev_cjoin, cudaEventDisableTiming));
+    MBPOL_CUDA_OK(cudaGraphCreate(&I.sv_graph, 0));
+    cudaGraphConditionalHandle loop;
+    MBPOL_CUDA_OK(cudaGraphConditionalHandleCreate(&loop, I.sv_graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    MBPOL_CUDA_OK(cudaGraphAddNode(&node, I.sv_graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t sc = I.st_cap, sc2 = I.st_cap2;
+    MBPOL_CUDA_OK(cudaStreamBeginCaptureToGraph(sc, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    // fork: the PME pass of mu on the second branch
+    cudaError_t ce = cudaEventRecord(I.ev_cfork, sc);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(sc2, I.ev_cfork, 0);
+    mbpol_status ps = MBPOL_OK;
+    if (ce == cudaSuccess) ce = pme_spread(I, sc2, 1, mu, n, nreal);
+    if (ce == cudaSuccess) ps = pme_convolve(I, sc2, box);
+    if (ce == cudaSuccess && ps == MBPOL_OK) {
+        pme_gather_kernel<<<(n * 32 + 127) / 128, 128, 0, sc2>>>(n, 4, I.d_grid.p, I.d_gidx.p, I.d_gfrac.p,
+                                                                I.d_phi_mu.p);
+        ce = cudaEventRecord(I.ev_cjoin, sc2);
+    }
+    if (ce == cudaSuccess && ps == MBPOL_OK) {
+        induced_update_kernel<true><<<wblocks, 128, 0, sc>>>(
+            nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p, I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,
+            I.d_phi_mu.p, mu, mu, I.d_mud.p, I.d_eps2.p, 0, I.d_ebase.p, anchor_buf, I.d_intra.p, I.d_pcoef.p,
+            nullptr, nullptr, nullptr, I.d_polmask.p, nullptr, I.d_edir.p);
+        ce = cudaStreamWaitEvent(sc, I.ev_cjoin, 0);
+    }
+    if (ce == cudaSuccess && ps == MBPOL_OK) {
+        induced_finish_kernel<<<(n + 127) / 128, 128, 0, sc>>>(n, I.d_edir.p, I.d_phi_mu.p, I.d_E0.p, I.d_pol.p,
+                                                               mu, mu, I.d_mud.p, I.d_eps2.p, 0, I.d_ebase.p,
+                                                               anchor_buf, reinterpret_cast<const int*>(I.d_sstate.p),
+                                                               anchor_buf);
+        solve_control_kernel<<<1, 1, 0, sc>>>(I.d_eps2.p, 1.0 / (double)n, I.d_sstate.p, I.prm.target_epsilon,
+                                              I.prm.max_iterations, switch_eps, loop);
+    }
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(sc, &captured);
+    if (ps) return ps;
+    MBPOL_CUDA_OK(ce);
+    MBPOL_CUDA_OK(ee);
+    MBPOL_CUDA_OK(cudaGetLastError());
+    MBPOL_CUDA_OK(cudaGraphInstantiate(&I.sv_exec, I.sv_graph, 0));
+    I.sv_key = key;
+    return MBPOL_OK;
+}
+
 }  // namespace
 
 mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& box, double* force, double* energy) {
@@ -2443,6 +2586,29 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
         }
         done = true;
     }
+    if (!done && I.pme && !prof_on() && !I.sv_disabled) {
+        MBPOL_CUDA_OK(I.d_sstate.ensure(1));
+        if (solver_graph(I, nmol, wblocks, n, nreal, bufs[0], bufs[2], switch_eps, box) != MBPOL_OK) {
+            // a capture this driver does not support: keep the host loop
+            I.sv_disabled = true;
+            cudaGetLastError();
+        }
+    }
+    if (!done && I.pme && !prof_on() && !I.sv_disabled) {
+        // one graph launch; the host reads the solve's state once
+        const SolveState s0 = {0, 0, 0, 0, 1.0e+50};
+        MBPOL_CUDA_OK(cudaMemcpyAsync(I.d_sstate.p, &s0, sizeof s0, cudaMemcpyHostToDevice, st));
+        MBPOL_CUDA_OK(cudaMemsetAsync(I.d_eps2.p, 0, sizeof(double), st));
+        MBPOL_CUDA_OK(cudaGraphLaunch(I.sv_exec, st));
+        SolveState sr{};
+        MBPOL_CUDA_OK(cudaMemcpyAsync(&sr, I.d_sstate.p, sizeof sr, cudaMemcpyDeviceToHost, st));
+        MBPOL_CUDA_OK(cudaStreamSynchronize(st));
+        for (int r = 0; r < 7 * sr.rounds; ++r) count_launch();  // spread, conversion, scale, gather, field, update, control
+        it = sr.its;
+        conv = sr.conv != 0;
+        current = sr.cur;
+        done = true;
+    }
     while (!done) {
         int kmode = mode;
         if (mode == 0 && current < switch_eps) kmode = 1;
@@ -2483,7 +2649,7 @@ mbpol_status ElecEngine::compute(cudaStream_t st, const double* pos, const Box& 
             count_launch();
             induced_finish_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, I.d_edir.p, I.d_phi_mu.p, I.d_E0.p, I.d_pol.p,
                                                                    mu_in, mu_out, I.d_mud.p, I.d_eps2.p, kmode,
-                                                                   I.d_ebase.p, anchor);
+                                                                   I.d_ebase.p, anchor, nullptr, nullptr);
         } else
             induced_update_kernel<false><<<wblocks, 128, 0, st>>>(nmol, I.d_off.p, I.d_damp.p, I.d_pol.p, I.d_type.p,
                                                                    I.d_nb.p, I.d_nbd.p, I.d_nnb.p, I.cap, I.d_E0.p,

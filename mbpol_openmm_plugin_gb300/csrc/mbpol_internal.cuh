@@ -23,6 +23,9 @@ namespace mbpol {
 // the timed kernels.
 enum KernelId { K_POLY2B = 0, K_POLY3B, K_ELEC_FIXED, K_ELEC_INDUCED, K_ELEC_PME, K_ELEC_FORCES, K_ELEC_FIELD, K_NUM };
 void prof_begin(cudaStream_t st, int id);
+// Whether the per-kernel timers are on (the solver then keeps its host loop,
+// whose iterations the timers can bracket).
+bool prof_on();
 // Number of kernels this library has launched (cuFFT's own launches excluded).
 void count_launch();
 void prof_end(cudaStream_t st, int id);

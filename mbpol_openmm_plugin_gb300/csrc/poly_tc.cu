@@ -18,8 +18,9 @@
 // reads z back from a per-block scratch slice, so results do not depend on
 // scheduling.
 //
-// Block: 256 threads (8 warps) and 194 KB of shared memory; one block per
-// SM, persistent over tiles of 64 trimers.  Inputs X [2][36][stride] (the
+// Block: 512 threads (16 warps: each of the tables' 8 row-tile groups taken
+// by two warps, each for 32 of the tile's trimers) and 196 KB of shared
+// memory; one block per SM, persistent over tiles of 64 trimers.  Inputs X [2][36][stride] (the
 // variables as FP32 hi and lo planes), outputs G [36][stride], E [stride].
 #include <cuda_fp16.h>
 
@@ -35,8 +36,10 @@ namespace mbpol {
 namespace {
 
 constexpr int kTU = 64;        // units (trimers) per tile
-constexpr int kTWarps = 8;
+constexpr int kGroups = 8;     // row-tile groups of the tables (codegen/gen_poly_tc.py NWARPS)
+constexpr int kTWarps = 16;    // two warps per group, each for half of the tile's trimers
 constexpr int kTThreads = 32 * kTWarps;
+constexpr int kQ = kTThreads / kTU;  // threads per trimer in the epilogue
 
 template <int NV, int NPAD>
 struct TCShape {
@@ -45,7 +48,7 @@ struct TCShape {
     static constexpr int DS = NV + 2;                     // d row stride: d_nv = 1, d_{nv+1} = 0
     static constexpr size_t Y_BYTES = (size_t)2 * kTU * KS * sizeof(__half);
     static constexpr size_t D_BYTES = (size_t)kTU * DS * sizeof(float);
-    static constexpr size_t SMEM = Y_BYTES + D_BYTES + kTU * sizeof(unsigned) + 4 * kTU * sizeof(float2);
+    static constexpr size_t SMEM = Y_BYTES + D_BYTES + kTU * sizeof(unsigned) + kQ * kTU * sizeof(float2);
     static_assert(NY <= NPAD && NPAD % 16 == 0, "padding");
 };
 
@@ -111,7 +114,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
     __half* ysm = reinterpret_cast<__half*>(smem);                           // [2][kTU][KS]
     float* dsm = reinterpret_cast<float*>(smem + Sh::Y_BYTES);               // [kTU][DS]
     unsigned* umax = reinterpret_cast<unsigned*>(smem + Sh::Y_BYTES + Sh::D_BYTES);  // [kTU]
-    float2* epart = reinterpret_cast<float2*>(umax + kTU);                   // [4][kTU]
+    float2* epart = reinterpret_cast<float2*>(umax + kTU);                   // [kQ][kTU]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float* zs = zscratch + (size_t)blockIdx.x * NPAD * kTU;                  // [NPAD][kTU]
     const int ntiles = (n + kTU - 1) / kTU;
@@ -155,15 +158,19 @@ __global__ void __launch_bounds__(kTThreads, 1)
             *reinterpret_cast<__half2*>(ysm + (size_t)(kTU + t) * KS + k) = __halves2half2(l0, l1);
         }
         __syncthreads();
-        // ---- z = S Y' on the tensor cores: each warp owns whole row tiles
+        // ---- z = S Y' on the tensor cores: each pair of warps owns whole row
+        // tiles (a group of the tables), each warp half of the trimers
         {
             const int g = lane >> 2, q = lane & 3;
+            const int grp = warp >> 1, nh = warp & 1;
             // ldmatrix.x4 row addresses: matrices (units 0-7, k 0-7),
             // (units 0-7, k 8-15), (units 8-15, k 0-7), (units 8-15, k 8-15)
+            // of this warp's 32 trimers
             const int mi = lane >> 3, r = lane & 7;
-            const unsigned yb_hi = smem_u32(ysm) + (unsigned)((((mi >> 1) * 8 + r) * KS + (mi & 1) * 8) * 2);
+            const unsigned yb_hi =
+                smem_u32(ysm) + (unsigned)(((nh * 32 + (mi >> 1) * 8 + r) * KS + (mi & 1) * 8) * 2);
             const unsigned yb_lo = yb_hi + (unsigned)(kTU * KS * 2);
-            const int i0 = tab.warp_begin[warp], i1 = tab.warp_begin[warp + 1];
+            const int i0 = tab.warp_begin[grp], i1 = tab.warp_begin[grp + 1];
             const int e_end = tab.rt_entry[i1];
             int e = tab.rt_entry[i0];
             const uint4* fr = reinterpret_cast<const uint4*>(tab.frag);
@@ -178,9 +185,9 @@ __global__ void __launch_bounds__(kTThreads, 1)
             for (int i = i0; i < i1; ++i) {
                 const int rt = tab.rt_id[i];
                 const int ee = tab.rt_entry[i + 1];
-                float acc[8][4];
+                float acc[4][4];
                 #pragma unroll
-                for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+                for (int j = 0; j < 4; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
                 for (; e < ee; ++e) {
                     // next tile's fragments while this one computes
                     uint4 fn0 = fa0, fn1 = fa1, fn2 = fa2;
@@ -193,23 +200,23 @@ __global__ void __launch_bounds__(kTThreads, 1)
                     }
                     const unsigned koff = (unsigned)(kt * 32);   // 16 halves
                     #pragma unroll
-                    for (int jp = 0; jp < 4; ++jp) {
+                    for (int jp = 0; jp < 2; ++jp) {
                         const unsigned uoff = (unsigned)(jp * 16 * KS * 2);
                         unsigned bh[4], bl[4];
                         ldsm_x4(yb_hi + uoff + koff, bh[0], bh[1], bh[2], bh[3]);
                         ldsm_x4(yb_lo + uoff + koff, bl[0], bl[1], bl[2], bl[3]);
                         #pragma unroll
                         for (int jj = 0; jj < 2; ++jj) {
-                            float d[4] = {0.f, 0.f, 0.f, 0.f};
+                            // two chains of two products each (S0 Y0 + S1 Y0, S0 Y1 + S2 Y0),
+                            // both started from zero in this k-tile
+                            float d[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
                             mma16816(d, fa0, bh[2 * jj], bh[2 * jj + 1]);
-                            mma16816(d, fa0, bl[2 * jj], bl[2 * jj + 1]);
+                            mma16816(c, fa0, bl[2 * jj], bl[2 * jj + 1]);
                             mma16816(d, fa1, bh[2 * jj], bh[2 * jj + 1]);
-                            mma16816(d, fa2, bh[2 * jj], bh[2 * jj + 1]);
+                            mma16816(c, fa2, bh[2 * jj], bh[2 * jj + 1]);
                             float* a = acc[2 * jp + jj];
-                            a[0] = __fadd_rn(a[0], d[0]);
-                            a[1] = __fadd_rn(a[1], d[1]);
-                            a[2] = __fadd_rn(a[2], d[2]);
-                            a[3] = __fadd_rn(a[3], d[3]);
+                            #pragma unroll
+                            for (int k = 0; k < 4; ++k) a[k] = __fadd_rn(__fadd_rn(a[k], d[k]), c[k]);
                         }
                     }
                     fa0 = fn0;
@@ -217,12 +224,12 @@ __global__ void __launch_bounds__(kTThreads, 1)
                     fa2 = fn2;
                     kt = ktn;
                 }
-                // rows rt*16 + g and + 8, units 8j + 2q, 8j + 2q + 1
+                // rows rt*16 + g and + 8, units 32 nh + 8j + 2q, + 1
                 const int m0 = rt * 16 + g, m1 = m0 + 8;
                 const float s0 = tab.rowscale[m0], s1 = tab.rowscale[m1];
                 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int u = 8 * j + 2 * q;
+                for (int j = 0; j < 4; ++j) {
+                    const int u = 32 * nh + 8 * j + 2 * q;
                     *reinterpret_cast<float2*>(zs + (size_t)m0 * kTU + u) =
                         make_float2(acc[j][0] * s0, acc[j][1] * s0);
                     *reinterpret_cast<float2*>(zs + (size_t)m1 * kTU + u) =
@@ -231,20 +238,20 @@ __global__ void __launch_bounds__(kTThreads, 1)
             }
         }
         __syncthreads();
-        // ---- E = y . z and dE/dd_i = 2 sum_m z_m dy_m/dd_i; four threads
-        // per unit, fixed summation order
+        // ---- E = y . z and dE/dd_i = 2 sum_m z_m dy_m/dd_i; kQ threads per
+        // unit, fixed summation order
         {
             const int t = tid % kTU, qd = tid / kTU, u = base + t;
             const float ze = exp2i(unit_exp(__uint_as_float(umax[t])));
             const float* dt = dsm + t * DS;
             float2 es = make_float2(0.f, 0.f);
-            for (int r = qd; r < NY; r += 4) {
+            for (int r = qd; r < NY; r += kQ) {
                 const unsigned meta = tab.ymeta[r];
                 const float y = __fmul_rn(dt[meta & 255], dt[(meta >> 8) & 255]);
                 df_fma(es, y, __fmul_rn(zs[(size_t)r * kTU + t], ze));
             }
             epart[qd * kTU + t] = es;
-            for (int v = qd; v < NV; v += 4) {
+            for (int v = qd; v < NV; v += kQ) {
                 // rows (v) and (min(v,j), max(v,j))
                 float2 gs = make_float2(0.f, 0.f);
                 df_fma(gs, 2.f, zs[(size_t)(1 + v) * kTU + t]);
@@ -261,7 +268,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
         if (tid < kTU && base + tid < n) {
             float2 es = epart[tid];
             #pragma unroll
-            for (int k = 1; k < 4; ++k) df_add(es, epart[k * kTU + tid]);
+            for (int k = 1; k < kQ; ++k) df_add(es, epart[k * kTU + tid]);
             E[base + tid] = __fadd_rn(es.x, es.y);
         }
         __syncthreads();
@@ -298,7 +305,7 @@ cudaError_t upload_tc(const PolyTCTables& h, PolyTCDev* d) {
         (e = upload_array(h.inv_bound, (size_t)h.nv, &d->inv_bound, owned)) ||
         (e = upload_array(h.ymeta, (size_t)h.npad, &d->ymeta, owned)) ||
         (e = upload_array(h.rowscale, (size_t)h.npad, &d->rowscale, owned)) ||
-        (e = upload_array(h.warp_begin, (size_t)kTWarps + 1, &d->warp_begin, owned)) ||
+        (e = upload_array(h.warp_begin, (size_t)kGroups + 1, &d->warp_begin, owned)) ||
         (e = upload_array(h.rt_id, (size_t)h.nrt, &d->rt_id, owned)) ||
         (e = upload_array(h.rt_entry, (size_t)h.nrt + 1, &d->rt_entry, owned)) ||
         (e = upload_array(h.ent_kt, (size_t)h.nent, &d->ent_kt, owned)) ||
@@ -328,6 +335,15 @@ cudaError_t poly_tc_setup(int device, const PolyTCDev** out) {
     return cudaSuccess;
 }
 
+// SMs left out of the persistent grid, so that the electrostatics stream
+// finds room beside the three-body kernel (a block takes a whole SM's
+// registers).  Measured on box4096 (learned arm, ms per step over 300
+// steps): 0 SMs 6.121, 24 6.041, 52 6.015, 76 5.980; the plain arm 9.151
+// (0) and 9.050 (52).  52 keeps the kernel alone at ~2.5 ms.
+#ifndef MBPOL_TC_RESERVE_SMS
+#define MBPOL_TC_RESERVE_SMS 52
+#endif
+
 size_t poly3b_tc_scratch_floats(int num_sms) { return (size_t)num_sms * 704 * kTU; }
 
 void launch_poly3b_tc(cudaStream_t st, const PolyTCDev* tab, const float* X, float* G, float* E, int n, int stride,
@@ -335,7 +351,9 @@ void launch_poly3b_tc(cudaStream_t st, const PolyTCDev* tab, const float* X, flo
     if (n <= 0) return;
     count_launch();
     const int ntiles = (n + kTU - 1) / kTU;
-    const int blocks = ntiles < num_sms ? ntiles : num_sms;
+    int blocks = num_sms - MBPOL_TC_RESERVE_SMS;
+    if (blocks < num_sms / 2) blocks = num_sms / 2;
+    if (blocks > ntiles) blocks = ntiles;
     poly_tc_kernel<36, 704><<<blocks, kTThreads, Shape3::SMEM, st>>>(*tab, X, G, E, n, stride, zscratch);
 }
 

@@ -119,3 +119,32 @@ def test_system_moments_vs_reference(name):
     # the quadrupole is symmetric and traceless
     Q = np.asarray(mom[4:]).reshape(3, 3)
     assert np.allclose(Q, Q.T) and abs(np.trace(Q)) <= 1e-9 * np.max(np.abs(Q))
+
+
+def test_solver_graph_matches_host_loop():
+    """A periodic system's solve runs as one graph launch with its stopping
+    rules on the device; with the per-kernel timers on it runs the host loop
+    instead (one host round trip per iteration).  Both take the reference's
+    rules, so they agree: same iteration count, energies and forces to
+    rounding (the residual sums use FP64 atomics in no fixed order)."""
+    from mbpol_openmm_plugin_gb300 import _capi
+    d = np.load(os.path.join(GOLDEN, "elec_box256_seed0.npz"))
+    s = elec_system(d["positions"], d["box"], float(d["alpha"]), [int(v) for v in d["grid"]])
+    res = []
+    lib = _capi.load()
+    for timers in (0, 1):
+        lib.mbpol_profile_enable(timers)
+        try:
+            ctx = mb.Context(s)
+            ctx.setPositions(d["positions"])
+            st = ctx.getState()
+            dip, it, eps = ctx.getInducedDipoles()
+            res.append((st.getPotentialEnergy(), st.getForces(), it, eps))
+        finally:
+            lib.mbpol_profile_enable(0)
+    (e0, f0, i0, p0), (e1, f1, i1, p1) = res
+    print("graph E %.10f it %d eps %.3e | host loop E %.10f it %d eps %.3e | F relrms %.1e" % (
+        e0, i0, p0, e1, i1, p1, rel_rms(f0, f1)))
+    assert i0 == i1
+    assert abs(e0 - e1) <= 1e-10 * abs(e1)
+    assert rel_rms(f0, f1) <= 1e-9
