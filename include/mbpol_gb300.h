@@ -148,6 +148,21 @@ mbpol_status mbpol_add_dispersion_ions(mbpol_context* ctx, int num_ions, const i
  * or box = NULL for a non-periodic system.  Virtual sites are placed from
  * their parents on the device before each evaluation. */
 mbpol_status mbpol_set_positions(mbpol_context* ctx, const double* xyz, const double* box);
+/* updateParametersInContext / copyParametersToContext
+ * (openmmapi/include/openmm/mbpolKernels.h:83,128,167,206;
+ * MBPolReferenceKernels.cpp:116-126, 306-322, 401-411, 485-495): new
+ * parameters of one term of a live context, which keeps its neighbour
+ * lists, the dipoles of its last solves and its history predictor.
+ * term MBPOL_TERM_ONEBODY / TWOBODY / THREEBODY / DISPERSION: count waters
+ * with their particle indices [count][3] (O, H1, H2), count as at creation;
+ * term MBPOL_TERM_ELECTROSTATICS: count = the particle count, with the
+ * per-particle charge, molecule, atom type, damping and polarity of
+ * mbpol_add_electrostatics_force (the molecule layout may not change).
+ * Unused pointers may be NULL.  A changed count is MBPOL_ERR_INVALID_ARGUMENT
+ * with the reference's message. */
+mbpol_status mbpol_update_parameters(mbpol_context* ctx, unsigned term, int count, const int* waters,
+                                     const double* charge, const int* molecule, const int* atom_type,
+                                     const double* damping, const double* polarity);
 
 /* Evaluate the terms in term_mask (MBPOL_TERM_BIT(...)), i.e. ::execute of each
  * kernel (MBPolReferenceKernels.cpp:120-125, 246-259, 362-399, 451-483).

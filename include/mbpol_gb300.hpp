@@ -33,12 +33,18 @@ inline void mbpol_check(mbpol_status s) {
 
 typedef std::array<double, 3> Vec3;
 
+class Context;
+
 class Force {
 public:
     virtual ~Force() {}
     void setForceGroup(int g) { group_ = g; }
     int getForceGroup() const { return group_; }
     virtual int term() const = 0;
+    /* MBPol*Force::updateParametersInContext (copyParametersToContext,
+     * MBPolReferenceKernels.cpp:116-126, 306-322, 401-411, 485-495): this
+     * force's parameters into a live context (mbpol_update_parameters). */
+    void updateParametersInContext(Context& context) const;
 
 protected:
     int group_ = 0;
@@ -48,6 +54,11 @@ protected:
 class WaterForce : public Force {
 public:
     int getNumMolecules() const { return (int)waters_.size(); }
+    std::vector<int> flatWaters() const {
+        std::vector<int> flat;
+        for (const auto& t : waters_) flat.insert(flat.end(), t.begin(), t.end());
+        return flat;
+    }
     const std::vector<std::array<int, 3>>& waters() const { return waters_; }
 
 protected:
@@ -280,6 +291,19 @@ private:
     Vec3 box_{0, 0, 0};
     bool periodic_ = false;
 };
+
+inline void Force::updateParametersInContext(Context& context) const {
+    if (auto* e = dynamic_cast<const MBPolElectrostaticsForce*>(this)) {
+        mbpol_check(mbpol_update_parameters(context.handle(), MBPOL_TERM_ELECTROSTATICS, e->getNumElectrostatics(),
+                                            nullptr, e->q_.data(), e->mol_.data(), e->type_.data(), e->damp_.data(),
+                                            e->pol_.data()));
+        return;
+    }
+    const auto* w = dynamic_cast<const WaterForce*>(this);
+    const std::vector<int> flat = w->flatWaters();
+    mbpol_check(mbpol_update_parameters(context.handle(), (unsigned)term(), w->getNumMolecules(), flat.data(),
+                                        nullptr, nullptr, nullptr, nullptr, nullptr));
+}
 
 inline void MBPolElectrostaticsForce::getElectrostaticPotential(const std::vector<Vec3>& inputGrid, Context& context,
                                                                 std::vector<double>& outputElectrostaticPotential) const {

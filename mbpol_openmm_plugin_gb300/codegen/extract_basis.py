@@ -285,4 +285,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MBPOL_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: extract_basis.py REFERENCE_CHECKOUT (or set MBPOL_REFERENCE_DIR)")
+    main(ref)

@@ -703,6 +703,39 @@ mbpol_status mbpol_add_dispersion_force(mbpol_context* ctx, int nw, const int* w
     return set_term(ctx, ctx->tdisp, nw, w, method, cutoff, 0);
 }
 
+mbpol_status mbpol_update_parameters(mbpol_context* ctx, unsigned term, int count, const int* waters,
+                                     const double* charge, const int* molecule, const int* atom_type,
+                                     const double* damping, const double* polarity) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    MBPOL_CUDA_OK(cudaSetDevice(ctx->device));
+    // nothing of an earlier evaluation may still read the old parameters
+    MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+    if (ctx->st_e) MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st_e));
+    if (ctx->st_a) MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st_a));
+    if (term == MBPOL_TERM_ELECTROSTATICS) {
+        if (!ctx->elec) return mbpol_fail(MBPOL_ERR_STATE, "no electrostatics force in this context");
+        if (count != ctx->N)
+            return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "updateParametersInContext: The number of multipoles has changed");
+        if (!charge || !molecule || !atom_type || !damping || !polarity)
+            return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null argument");
+        ctx->forces_valid = false;
+        return ctx->elec->update_parameters(charge, molecule, atom_type, damping, polarity);
+    }
+    WaterTerm* t = term == MBPOL_TERM_ONEBODY ? &ctx->t1 : term == MBPOL_TERM_TWOBODY ? &ctx->t2
+                 : term == MBPOL_TERM_THREEBODY ? &ctx->t3 : term == MBPOL_TERM_DISPERSION ? &ctx->tdisp : nullptr;
+    if (!t) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "unknown term");
+    if (!t->on) return mbpol_fail(MBPOL_ERR_STATE, "the term has no force in this context");
+    if (count != (int)t->waters.size())
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, term == MBPOL_TERM_ONEBODY
+                          ? "updateParametersInContext: The number of one-body molecules has changed"
+                          : "updateParametersInContext: The number of particles has changed");
+    mbpol_status s = set_term(ctx, *t, count, waters, t->method, t->cutoff, t->rule);
+    if (s) return s;
+    if (ctx->ncl > 0) ctx->cl_dirty = true;
+    ctx->forces_valid = false;
+    return MBPOL_OK;
+}
+
 mbpol_status mbpol_add_dispersion_ions(mbpol_context* ctx, int num_ions, const int* particles) {
     if (!ctx || num_ions < 0 || (num_ions > 0 && !particles))
         return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad ion list");

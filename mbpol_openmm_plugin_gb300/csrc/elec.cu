@@ -2009,6 +2009,75 @@ struct ElecImpl {
 ElecEngine::ElecEngine() : impl_(new ElecImpl()) {}
 ElecEngine::~ElecEngine() { delete impl_; }
 
+// Per-particle parameters (charges, types, damping, polarisabilities) to the
+// device; the molecule layout (I.K, I.nmol) is set.
+static mbpol_status upload_particle_params(ElecImpl& I, const double* charge, const int* atom_type,
+                                           const double* damping, const double* polarity) {
+    const int n = I.N;
+    I.q_static.resize(n);
+    I.q_static64.resize(n);
+    I.damp.resize(n);
+    I.pol.resize(n);
+    I.type.resize(n);
+    for (int i = 0; i < n; ++i) {
+        I.q_static[i] = (float)charge[i];
+        I.q_static64[i] = charge[i];
+        // sixth root of the damping factor: pair kernels use
+        // (damp_i damp_j)^(1/6) = damp_i^(1/6) damp_j^(1/6)
+        I.damp[i] = (float)std::pow(damping[i], 1.0 / 6.0);
+        I.pol[i] = (float)polarity[i];
+        I.type[i] = atom_type[i];
+    }
+    MBPOL_CUDA_OK(I.d_qs.ensure(n));
+    MBPOL_CUDA_OK(I.d_damp.ensure(n));
+    MBPOL_CUDA_OK(I.d_pol.ensure(n));
+    MBPOL_CUDA_OK(I.d_type.ensure(n));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_qs.p, I.q_static.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_damp.p, I.damp.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_pol.p, I.pol.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    MBPOL_CUDA_OK(cudaMemcpy(I.d_type.p, I.type.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    {
+        std::vector<int> mask(I.nmol, 0);
+        for (int m = 0; m < I.nmol; ++m)
+            for (int s = 0; s < I.K; ++s)
+                if (I.pol[I.K * m + s] != 0.f) mask[m] |= 1 << s;
+        MBPOL_CUDA_OK(I.d_polmask.ensure(I.nmol));
+        MBPOL_CUDA_OK(cudaMemcpy(I.d_polmask.p, mask.data(), sizeof(int) * I.nmol, cudaMemcpyHostToDevice));
+    }
+    return MBPOL_OK;
+}
+
+// Molecules: consecutive blocks of K = 3 (O, H, H) or 4 (O, H, H, M) sites
+// with a common molecule index, different from the previous block's.
+static int molecule_layout(int n, const int* molecule) {
+    int K = 1;
+    while (K < n && molecule[K] == molecule[0]) ++K;
+    if (K != 3 && K != 4) return 0;
+    if (n % K) return 0;
+    for (int i = 0; i < n; ++i)
+        if (molecule[i] != molecule[(i / K) * K]) return 0;
+    for (int m = 1; m < n / K; ++m)
+        if (molecule[m * K] == molecule[(m - 1) * K]) return 0;
+    return K;
+}
+
+mbpol_status ElecEngine::update_parameters(const double* charge, const int* molecule, const int* atom_type,
+                                           const double* damping, const double* polarity) {
+    ElecImpl& I = *impl_;
+    if (molecule_layout(I.N, molecule) != I.K)
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "updateParametersInContext: the molecule layout has changed");
+    if (I.prm.include_charge_redistribution)
+        for (int m = 0; m < I.nmol; ++m)
+            if (atom_type[4 * m] != 0 || atom_type[4 * m + 1] != 1 || atom_type[4 * m + 2] != 1 ||
+                atom_type[4 * m + 3] != 2)
+                return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT,
+                                  "charge redistribution needs O, H1, H2, M order (types 0,1,1,2)");
+    // the neighbour lists, the dipoles of the last solves and the history
+    // predictor stay; the next evaluation recomputes every parameter-dependent
+    // quantity
+    return upload_particle_params(I, charge, atom_type, damping, polarity);
+}
+
 mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const double* charge, const int* molecule,
                               const int* atom_type, const double* damping, const double* polarity) {
     ElecImpl& I = *impl_;
@@ -2041,35 +2110,9 @@ mbpol_status ElecEngine::init(int n, const mbpol_electrostatics_params& p, const
         return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad solver parameters");
     I.K = K;
     I.nmol = n / K;
-    I.q_static.resize(n);
-    I.q_static64.resize(n);
-    I.damp.resize(n);
-    I.pol.resize(n);
-    I.type.resize(n);
-    for (int i = 0; i < n; ++i) {
-        I.q_static[i] = (float)charge[i];
-        I.q_static64[i] = charge[i];
-        // sixth root of the damping factor: pair kernels use
-        // (damp_i damp_j)^(1/6) = damp_i^(1/6) damp_j^(1/6)
-        I.damp[i] = (float)std::pow(damping[i], 1.0 / 6.0);
-        I.pol[i] = (float)polarity[i];
-        I.type[i] = atom_type[i];
-    }
-    MBPOL_CUDA_OK(I.d_qs.ensure(n));
-    MBPOL_CUDA_OK(I.d_damp.ensure(n));
-    MBPOL_CUDA_OK(I.d_pol.ensure(n));
-    MBPOL_CUDA_OK(I.d_type.ensure(n));
-    MBPOL_CUDA_OK(cudaMemcpy(I.d_qs.p, I.q_static.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
-    MBPOL_CUDA_OK(cudaMemcpy(I.d_damp.p, I.damp.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
-    MBPOL_CUDA_OK(cudaMemcpy(I.d_pol.p, I.pol.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
-    MBPOL_CUDA_OK(cudaMemcpy(I.d_type.p, I.type.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     {
-        std::vector<int> mask(I.nmol, 0);
-        for (int m = 0; m < I.nmol; ++m)
-            for (int s = 0; s < I.K; ++s)
-                if (I.pol[I.K * m + s] != 0.f) mask[m] |= 1 << s;
-        MBPOL_CUDA_OK(I.d_polmask.ensure(I.nmol));
-        MBPOL_CUDA_OK(cudaMemcpy(I.d_polmask.p, mask.data(), sizeof(int) * I.nmol, cudaMemcpyHostToDevice));
+        mbpol_status s = upload_particle_params(I, charge, atom_type, damping, polarity);
+        if (s) return s;
     }
     for (auto* b : {&I.d_off, &I.d_E0, &I.d_mu0, &I.d_mu1, &I.d_mu2, &I.d_mu_prev, &I.d_gfrac, &I.d_ebase, &I.d_edir})
         MBPOL_CUDA_OK(b->ensure(3 * (size_t)n));

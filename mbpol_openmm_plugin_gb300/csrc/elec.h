@@ -35,6 +35,9 @@ public:
     std::string convergence_message() const;
     // learned initial guess (guess = 2); descriptors and collection refer to
     // the last evaluation's geometry and converged dipoles
+    // updateParametersInContext: new per-particle parameters, same molecules
+    mbpol_status update_parameters(const double* charge, const int* molecule, const int* atom_type,
+                                   const double* damping, const double* polarity);
     mbpol_status guess_select(int which);
     mbpol_status guess_descriptors(cudaStream_t st, float* host_out);
     mbpol_status guess_collect(cudaStream_t st);

@@ -12,8 +12,11 @@
 // variables as FP32 hi/lo planes, the 31 gradient planes and the per-dimer
 // energies -- lives in file-scope __device__ arrays sized for
 // MBPOL_NOALLOC_MAX_DIMERS dimers, and so do this path's copies of the
-// two-body trie tables.  The arrays are part of this translation unit's
-// module, so a process that never calls this entry point does not load them.
+// two-body trie tables.  The arrays belong to the library's device code, so
+// a device holds them (24.6 MB) from the moment that code is loaded on it:
+// with lazy module loading (CUDA_MODULE_LOADING=LAZY, the default) only once
+// this entry point is first called there; with eager loading as soon as the
+// library initialises the device, context API or not.
 // The kernels are the ones mbpol_compute launches (twobody_vars, the
 // double-float polynomial walk, twobody_forces), with the planes strided by
 // the fixed capacity instead of the context's pair capacity.
@@ -22,7 +25,12 @@
 // array with that device current, one cudaMemcpyToSymbol of the tables, the
 // kernel attribute for its dynamic shared memory and the model constants
 // (cudaMemcpyToSymbol).  None of these allocate, but they are synchronous,
-// so the first call on a device should come before any stream capture.
+// so the first call on a device should come before any stream capture.  The
+// model constants are the process-wide ones the context path uploads too
+// (identical values; they must stay identical between the two paths).  The
+// set-up is remembered for the life of the process: after cudaDeviceReset
+// the symbol addresses, tables and constants are gone, and this entry point
+// must not be called on that device again.
 //
 // Every scratch element a call reads is written earlier in the same call
 // (variables by twobody_vars, gradients and energies by the walk, for each

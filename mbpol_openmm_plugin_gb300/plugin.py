@@ -61,11 +61,20 @@ class _WaterForce:
         return len(self._waters) - 1
 
     def updateParametersInContext(self, context):
-        context._invalidate()
+        """copyParametersToContext (MBPolReferenceKernels.cpp:116-126,
+        401-411, 485-495): the waters' particle indices into a live context
+        (mbpol_update_parameters), which keeps its lists, dipole history and
+        predictor; the number of waters may not change."""
+        if context._h is None:
+            return
+        w = as_c(np.array(self._waters, dtype=np.int32).reshape(-1, 3), np.int32)
+        check(_capi.load().mbpol_update_parameters(context._h, self._term, w.shape[0], ptr(w), None, None, None,
+                                                   None, None))
 
 
 class MBPolOneBodyForce(_WaterForce):
     """openmmapi/include/openmm/MBPolOneBodyForce.h"""
+    _term = 0
     NonPeriodic, Periodic = 0, 1
 
     def addOneBody(self, particleIndices):
@@ -115,6 +124,7 @@ class _CutoffWaterForce(_WaterForce):
 
 class MBPolTwoBodyForce(_CutoffWaterForce):
     """openmmapi/include/openmm/MBPolTwoBodyForce.h"""
+    _term = 1
 
     def __init__(self):
         super().__init__(1.0)
@@ -126,6 +136,7 @@ class MBPolThreeBodyForce(_CutoffWaterForce):
     setPolynomialEvaluator between the tensor-core evaluation of the
     polynomial, the double-float walk and the automatic choice by size
     (default; mbpol_set_threebody_evaluator)."""
+    _term = 2
     ReferenceTrimers, CompleteTrimers = 0, 1
     TensorCores, DoubleFloatWalk, AutomaticEvaluator = 0, 1, 2
 
@@ -150,6 +161,7 @@ class MBPolThreeBodyForce(_CutoffWaterForce):
 class MBPolDispersionForce(_CutoffWaterForce):
     """Dispersion as built by the <Script> of python/mbpol.xml:37-108
     (-C6 tt6/r^6 over O/H pairs of different waters)."""
+    _term = 4
 
     def __init__(self):
         super().__init__(0.9)
@@ -283,7 +295,19 @@ class MBPolElectrostaticsForce:
         return self._group
 
     def updateParametersInContext(self, context):
-        context._invalidate()
+        """copyParametersToContext (MBPolReferenceKernels.cpp:306-322): the
+        per-particle charges, types, damping factors and polarities into a
+        live context (mbpol_update_parameters), which keeps its lists, dipole
+        history and predictor; the particles and molecules may not change."""
+        if context._h is None:
+            return
+        q = as_c([p[0] for p in self._particles], np.float64)
+        mol = as_c([p[1] for p in self._particles], np.int32)
+        typ = as_c([p[2] for p in self._particles], np.int32)
+        dmp = as_c([p[3] for p in self._particles], np.float64)
+        pol = as_c([p[4] for p in self._particles], np.float64)
+        check(_capi.load().mbpol_update_parameters(context._h, 3, len(self._particles), None, ptr(q), ptr(mol),
+                                                   ptr(typ), ptr(dmp), ptr(pol)))
 
     def getElectrostaticPotential(self, inputGrid, context, outputElectrostaticPotential=None):
         """MBPolElectrostaticsForce.h:267: potential (kJ/mol/e) at the points

@@ -1,11 +1,11 @@
 #!/bin/sh
 # Builds oracle/_ref/libmbpol_ref.so: the MB-pol Reference-platform force
 # classes compiled unmodified from the reference sources, plus the shim and
-# the harness.  Needs the reference checkout (default /root/reference).
+# the harness.  Needs the reference checkout: MBPOL_REFERENCE_DIR.
 # The polynomial objects take minutes (poly-3b-v2x.cpp ~12 min at -O2) and
 # are reused when present.  Outputs go to oracle/_ref only.
 set -e
-REF=${MBPOL_REFERENCE_DIR:-/root/reference}
+REF=${MBPOL_REFERENCE_DIR:?set MBPOL_REFERENCE_DIR to the reference checkout}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 SRC="$REF/platforms/reference/src"

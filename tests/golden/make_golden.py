@@ -13,7 +13,8 @@ Sources:
 Dispersion has no plugin code in the reference (python/mbpol.xml:37-108 builds
 an OpenMM CustomNonbondedForce); its values come from the C oracle port.
 
-    python tests/golden/make_golden.py [/path/to/reference] [elec|elec_known|pdb|potential|moments|dispersion|box4096]
+    python tests/golden/make_golden.py REFERENCE_CHECKOUT [elec|elec_known|pdb|potential|moments|dispersion|box4096|mbpol_xml]
+(or "-" for the checkout named by MBPOL_REFERENCE_DIR)
 """
 import ctypes
 import json
@@ -28,7 +29,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from mbpol_openmm_plugin_gb300 import systems  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] != "-" else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] != "-" else os.environ.get("MBPOL_REFERENCE_DIR", "")
 LIB = os.path.join(ROOT, "oracle", "_ref", "libmbpol_ref.so")
 
 VEC3 = r"Vec3\(\s*([-+0-9.eE]+)\s*,\s*([-+0-9.eE]+)\s*,\s*([-+0-9.eE]+)\s*\)"
@@ -521,8 +522,28 @@ def main_box4096():
         r["e1"], r["e2"], r["e3"], ee, it, etot, r["npairs"], r["ntrip"]))
 
 
+def main_mbpol_xml():
+    """The parameters of the reference's python/mbpol.xml as this package's
+    loader reads them (types, masses, the four MBPol elements, the C6/d6
+    tables of the dispersion script, the residue template), so that the CPU
+    tests check the built-in copy against them without the checkout."""
+    sys.path.insert(0, ROOT)
+    import mbpol_openmm_plugin_gb300 as mb
+    ff = mb.ForceField(os.path.join(REF, "python", "mbpol.xml"))
+    out = {"thole": list(ff.thole), "elec": ff.elec, "masses": ff.masses, "cutoff2": ff.cutoff2,
+           "cutoff3": ff.cutoff3, "c6": np.asarray(ff.c6).tolist(), "d6": np.asarray(ff.d6).tolist(),
+           "templates": ff.templates, "elements": ff.elements, "source": "python/mbpol.xml"}
+    with open(os.path.join(HERE, "mbpol_xml_params.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+    print("wrote mbpol_xml_params.json")
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "box4096":
+    if not REF or not os.path.isdir(REF):
+        sys.exit("usage: make_golden.py REFERENCE_CHECKOUT [part] (or '-' with MBPOL_REFERENCE_DIR set)")
+    if len(sys.argv) > 2 and sys.argv[2] == "mbpol_xml":
+        main_mbpol_xml()
+    elif len(sys.argv) > 2 and sys.argv[2] == "box4096":
         main_box4096()
     elif len(sys.argv) > 2 and sys.argv[2] == "elec_known":
         main_elec_known()

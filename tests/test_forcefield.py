@@ -2,6 +2,7 @@
 (mbpol_openmm_plugin_gb300.forcefield), against python/mbpol.py's
 generators and python/mbpol.xml."""
 import io
+import json
 import os
 
 import numpy as np
@@ -12,7 +13,6 @@ import mbpol_openmm_plugin_gb300 as mb
 from mbpol_openmm_plugin_gb300 import systems
 from mbpol_openmm_plugin_gb300.forcefield import water_topology
 
-REF_XML = os.path.join(os.environ.get("MBPOL_REFERENCE_DIR", "/root/reference"), "python", "mbpol.xml")
 
 
 def test_pdb_round_trip():
@@ -30,16 +30,20 @@ def test_pdb_round_trip():
     assert [a.name for a in res[0].atoms()] == ["O", "H1", "H2", "M"]
 
 
-@pytest.mark.skipif(not os.path.exists(REF_XML), reason="the reference's mbpol.xml is not present")
 def test_builtin_parameters_match_reference_xml():
-    a, b = mb.ForceField(REF_XML), mb.ForceField()
-    assert a.thole == b.thole
-    assert a.elec == b.elec
-    assert a.masses == b.masses
-    assert (a.cutoff2, a.cutoff3) == (b.cutoff2, b.cutoff3)
-    assert np.array_equal(a.c6, b.c6) and np.array_equal(a.d6, b.d6)
-    assert a.templates == b.templates
-    assert all(a.elements.values())
+    """The built-in parameters against the reference's python/mbpol.xml as
+    the loader read it (tests/golden/mbpol_xml_params.json, written by
+    make_golden.py mbpol_xml)."""
+    a = json.load(open(os.path.join(GOLDEN, "mbpol_xml_params.json")))
+    b = mb.ForceField()
+    rt = lambda v: json.loads(json.dumps(v))  # tuples as JSON lists
+    assert a["thole"] == b.thole
+    assert a["elec"] == rt(b.elec)
+    assert a["masses"] == rt(b.masses)
+    assert (a["cutoff2"], a["cutoff3"]) == (b.cutoff2, b.cutoff3)
+    assert np.array_equal(a["c6"], b.c6) and np.array_equal(a["d6"], b.d6)
+    assert a["templates"] == rt(b.templates)
+    assert all(a["elements"].values())
 
 
 def _summary(s):
