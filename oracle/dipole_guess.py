@@ -122,6 +122,38 @@ def inputs(pos, E0, box=None):
                            np.zeros((nw, NIN - NFEAT - NFIELD))], axis=1)
 
 
+def neighbour_field_features(dF, pos, box=None):
+    """(nw, 6) the correction network's neighbour features: over waters B
+    whose O lies within RC of A's O, sum fc(r) dF_O(B) and
+    fc(r) (dF_H1(B) + dF_H2(B)), in A's frame (csrc/guess.cu,
+    descriptor_kernel, mode 1)."""
+    pos = np.asarray(pos, np.float64)
+    dF = np.asarray(dF, np.float64)
+    nw = pos.shape[0] // 4
+    E = frames(pos, box)
+    O = pos[0::4]
+    out = np.zeros((nw, 6))
+    for i in range(nw):
+        d = _mi(O - O[i], box)
+        r = np.linalg.norm(d, axis=1)
+        m = (r < RC) & (np.arange(nw) != i)
+        fc = 0.5 * (np.cos(np.pi * r[m] / RC) + 1.0)
+        so = (fc[:, None] * dF[0::4][m]).sum(0)
+        sh = (fc[:, None] * (dF[1::4][m] + dF[2::4][m])).sum(0)
+        out[i, :3] = E[i] @ so
+        out[i, 3:] = E[i] @ sh
+    return out
+
+
+def correction_inputs(pos, dF, box=None):
+    """(nw, 64) inputs of the correction network: descriptors, the water's
+    own unpredicted field change dF at O, H1, H2 in its frame, the neighbour
+    features, one zero."""
+    nw = np.asarray(pos).shape[0] // 4
+    return np.concatenate([descriptors(pos, box), field_features(dF, pos, box),
+                           neighbour_field_features(dF, pos, box), np.zeros((nw, 1))], axis=1)
+
+
 def targets(dipoles, pos, box=None):
     """(nw, 9) solver dipoles of O, H1, H2 in each water's frame / OUT_SCALE."""
     E = frames(pos, box)
