@@ -235,13 +235,16 @@ const char* mbpol_last_error(void);
  * No reference counterpart (the reference runs the generated FP64 code of
  * platforms/reference/src/poly-3b-v2x.cpp).  MBPOL_POLY3B_TENSOR: the
  * polynomial re-expanded about a fixed point and evaluated as a quadratic
- * form on the tensor cores (fp16 operand pieces, FP32 sums; ~1e-5 kcal/mol
- * per compact trimer).  MBPOL_POLY3B_WALK: the double-float trie walk on the
- * FP32 pipe (5x slower, ~1e-12 relative).  MBPOL_POLY3B_AUTO (default): the
- * tensor cores from one full wave of trimer tiles up (64 trimers per SM),
- * the walk below, where a few trimers' errors would be a larger share of
- * the total energy and the tensor kernel would not fill the GPU anyway. */
-enum { MBPOL_POLY3B_TENSOR = 0, MBPOL_POLY3B_WALK = 1, MBPOL_POLY3B_AUTO = 2 };
+ * form on the tcgen05 tensor cores (fp16 operand pieces, FP32 sums; ~1e-5
+ * kcal/mol per compact trimer).  MBPOL_POLY3B_TENSOR_SYNC: the same with
+ * mma.sync (the legacy tensor-core path; kept for comparison).
+ * MBPOL_POLY3B_WALK: the double-float trie walk on the FP32 pipe (~1e-12
+ * relative).  MBPOL_POLY3B_AUTO (default): MBPOL_POLY3B_TENSOR from one full
+ * wave of trimer tiles up (64 trimers per SM), the walk below, where a few
+ * trimers' errors would be a larger share of the total energy and the
+ * tensor kernel would not fill the GPU anyway.  A tcgen05 launch whose
+ * bounded waits give up makes the evaluation return MBPOL_ERR_CUDA. */
+enum { MBPOL_POLY3B_TENSOR = 0, MBPOL_POLY3B_WALK = 1, MBPOL_POLY3B_AUTO = 2, MBPOL_POLY3B_TENSOR_SYNC = 3 };
 mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind);
 
 /* ---- Batched independent clusters ---------------------------------------

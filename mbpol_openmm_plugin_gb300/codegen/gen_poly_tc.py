@@ -50,6 +50,8 @@ sys.path.insert(0, os.path.dirname(PKG))
 from mbpol_openmm_plugin_gb300.codegen import gen_poly  # noqa: E402
 
 NWARPS = 8
+TC5_PARTS = 3     # tcgen05 kernel: K split, rows of S per chunk
+TC5_ROWS = 64
 Y_LOG2_MAX = 12   # |y'_k| <= 2^12 over the sampled inputs
 S_LOG2_MAX = 14   # max |scaled row of S| = 2^14
 
@@ -185,7 +187,65 @@ def build(name):
     t.ent_kt = np.array(ent_kt, np.int32)
     t.frag = np.array(frag, np.uint32).reshape(-1)   # [entry][piece][lane][reg]
     t.nmono = len(smono)
+    tc5_stream(t)
     return t
+
+
+def tc5_stream(t):
+    """The S blocks of the tcgen05 kernel (csrc/poly_tc5.cu), in the order
+    it consumes them: K in TC5_PARTS parts (Y' of one part is held in tensor
+    memory), then chunks of TC5_ROWS rows of S (the N of the MMA), then the
+    part's 16-wide k-tiles with a nonzero entry in the chunk.  A block holds
+    the three fp16 pieces, each TC5_ROWS x 16 in the no-swizzle K-major
+    layout of a shared-memory operand: 8-row x 16-byte core matrices,
+    [k half][row group][row][8 k] (PTX ISA, "Shared memory descriptor",
+    canonical K-major layout without swizzling)."""
+    nkt = t.npad // 16
+    nch = t.npad // TC5_ROWS
+    bounds = tc5_part_bounds(nkt)
+    assert t.npad % TC5_ROWS == 0
+    occ = np.zeros((nch, nkt), bool)
+    for p in t.pieces:
+        occ |= (p.astype(np.float64) != 0).reshape(nch, TC5_ROWS, nkt, 16).any(axis=(1, 3))
+    blocks, kt_local, begin = [], [], [0]
+    for part in range(TC5_PARTS):
+        for c in range(nch):
+            for kt in range(bounds[part], bounds[part + 1]):
+                if not occ[c, kt]:
+                    continue
+                kt_local.append(kt - bounds[part])
+                for p in t.pieces:
+                    sub = p.view(np.uint16)[c * TC5_ROWS:(c + 1) * TC5_ROWS, kt * 16:(kt + 1) * 16]
+                    # [row group][row][k half][8 k] -> [k half][row group][row][8 k]
+                    blocks.append(sub.reshape(TC5_ROWS // 8, 8, 2, 8).transpose(2, 0, 1, 3).reshape(-1))
+            begin.append(len(kt_local))
+    t.tc5_sblk = np.concatenate(blocks).astype(np.uint16)
+    t.tc5_kt = np.array(kt_local, np.uint8)
+    t.tc5_begin = np.array(begin, np.int32)      # [parts * chunks + 1]
+
+
+def tc5_part_bounds(nkt):
+    """First k-tile of each K part (the kernel computes the same)."""
+    return [(p * nkt + TC5_PARTS - 1) // TC5_PARTS for p in range(TC5_PARTS + 1)]
+
+
+def tc5_dense(t):
+    """The scaled S (sum of the pieces, FP64) rebuilt from the tcgen05 block
+    stream: the CPU tests compare it with the pieces."""
+    nch = t.npad // TC5_ROWS
+    bounds = tc5_part_bounds(t.npad // 16)
+    A = np.zeros((t.npad, t.npad))
+    per = 3 * TC5_ROWS * 16
+    for part in range(TC5_PARTS):
+        for c in range(nch):
+            i = part * nch + c
+            for b in range(t.tc5_begin[i], t.tc5_begin[i + 1]):
+                kt = bounds[part] + int(t.tc5_kt[b])
+                for q in range(3):
+                    raw = t.tc5_sblk[b * per + q * TC5_ROWS * 16:b * per + (q + 1) * TC5_ROWS * 16]
+                    sub = raw.reshape(2, TC5_ROWS // 8, 8, 8).transpose(1, 2, 0, 3).reshape(TC5_ROWS, 16)
+                    A[c * TC5_ROWS:(c + 1) * TC5_ROWS, kt * 16:(kt + 1) * 16] += sub.view(np.float16).astype(np.float64)
+    return A
 
 
 def ymeta(t):
@@ -231,9 +291,14 @@ def emit(tables, path):
         arr("int", n + "_rt_entry", t.rt_entry.tolist())
         arr("unsigned short", n + "_ent_kt", t.ent_kt.tolist())
         arr("unsigned int", n + "_frag", ["0x%08x" % v for v in t.frag.tolist()], "%s", 12)
+        arr("unsigned short", n + "_sblk", ["0x%04x" % v for v in t.tc5_sblk.tolist()], "%s", 16)
+        arr("unsigned char", n + "_blk_kt", t.tc5_kt.tolist())
+        arr("int", n + "_blk_begin", t.tc5_begin.tolist())
         lines.append("extern const PolyTCTables k_%s = {%d, %d, %d, %d, %d, %s_x0h, %s_x0l, %s_inv_bound, %s_ymeta,"
-                     " %s_rowscale, %s_warp_begin, %s_rt_id, %s_rt_entry, %s_ent_kt, %s_frag};" % (
-                         n, t.nv, t.ny, t.npad, len(t.rt_id), len(t.ent_kt), n, n, n, n, n, n, n, n, n, n))
+                     " %s_rowscale, %s_warp_begin, %s_rt_id, %s_rt_entry, %s_ent_kt, %s_frag, %d, %d, %d,"
+                     " %s_sblk, %s_blk_kt, %s_blk_begin};" % (
+                         n, t.nv, t.ny, t.npad, len(t.rt_id), len(t.ent_kt), n, n, n, n, n, n, n, n, n, n,
+                         TC5_PARTS, TC5_ROWS, len(t.tc5_kt), n, n, n))
     lines.append("}  // namespace mbpol")
     text = "\n".join(lines) + "\n"
     if not os.path.exists(path) or open(path).read() != text:
@@ -289,9 +354,11 @@ def generate(out_path):
     tabs = [build("poly3b")]
     emit(tabs, out_path)
     for t in tabs:
-        print("%s: %d shifted monomials, NY %d (padded %d), %d of %d tiles kept, per-warp tiles %s" % (
-            t.name, t.nmono, t.ny, t.npad, len(t.ent_kt), (t.npad // 16) ** 2,
-            [int(t.rt_entry[t.warp_begin[w + 1]] - t.rt_entry[t.warp_begin[w]]) for w in range(NWARPS)]))
+        print("%s: %d shifted monomials, NY %d (padded %d), %d of %d tiles kept, per-warp tiles %s; "
+              "tcgen05 stream: %d blocks of %d rows" % (
+                  t.name, t.nmono, t.ny, t.npad, len(t.ent_kt), (t.npad // 16) ** 2,
+                  [int(t.rt_entry[t.warp_begin[w + 1]] - t.rt_entry[t.warp_begin[w]]) for w in range(NWARPS)],
+                  len(t.tc5_kt), TC5_ROWS))
     return tabs
 
 

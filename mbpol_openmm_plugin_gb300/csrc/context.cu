@@ -133,6 +133,7 @@ struct mbpol_context {
     const PolyTCDev* tc3 = nullptr;
     int poly3b_kind = MBPOL_POLY3B_AUTO;
     DevBuf ztc;
+    DevBuf kstatus;  // int: nonzero when a bounded wait of the tcgen05 kernel gave up
     // dispersion buffers
     DevBuf full_d, nfull_d, lower_d, nlower_d;
     int cap_full_d = 0;
@@ -432,11 +433,18 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy, cudaStream_t ls, 
                                ctx->offs3.as<int>(), stride, ctx->trips3.as<int4>(), true);
     launch_threebody_vars(ls, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                           box, ctx->x3.as<float>(), stride);
-    const bool tensor = ctx->poly3b_kind == MBPOL_POLY3B_TENSOR ||
-                        (ctx->poly3b_kind == MBPOL_POLY3B_AUTO && ntrip >= 64 * ctx->num_sms);
-    if (tensor) MBPOL_CUDA_OK(ctx->ztc.ensure(sizeof(float) * poly3b_tc_scratch_floats(ctx->num_sms)));
+    const int kind = ctx->poly3b_kind == MBPOL_POLY3B_AUTO
+                         ? (ntrip >= 64 * ctx->num_sms ? MBPOL_POLY3B_TENSOR : MBPOL_POLY3B_WALK)
+                         : ctx->poly3b_kind;
+    if (kind == MBPOL_POLY3B_TENSOR)
+        MBPOL_CUDA_OK(ctx->ztc.ensure(sizeof(float) * poly3b_tc5_scratch_floats(ctx->num_sms)));
+    if (kind == MBPOL_POLY3B_TENSOR_SYNC)
+        MBPOL_CUDA_OK(ctx->ztc.ensure(sizeof(float) * poly3b_tc_scratch_floats(ctx->num_sms)));
     prof_begin(ls, K_POLY3B);
-    if (tensor)
+    if (kind == MBPOL_POLY3B_TENSOR)
+        launch_poly3b_tc5(ls, ctx->tc3, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip,
+                          stride, ctx->num_sms, ctx->ztc.as<float>(), ctx->kstatus.as<int>());
+    else if (kind == MBPOL_POLY3B_TENSOR_SYNC)
         launch_poly3b_tc(ls, ctx->tc3, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
                          ctx->num_sms, ctx->ztc.as<float>());
     else
@@ -637,6 +645,8 @@ mbpol_status mbpol_context_create(int num_particles, int device, mbpol_context**
     MBPOL_CUDA_OK(cudaGetLastError());
     MBPOL_CUDA_OK(poly_tables_upload(device, &ctx->walk));
     MBPOL_CUDA_OK(poly_tc_setup(device, &ctx->tc3));
+    MBPOL_CUDA_OK(ctx->kstatus.ensure(sizeof(int)));
+    MBPOL_CUDA_OK(cudaMemset(ctx->kstatus.p, 0, sizeof(int)));
     *out = ctx.release();
     return MBPOL_OK;
 }
@@ -791,6 +801,19 @@ mbpol_status mbpol_set_positions(mbpol_context* ctx, const double* xyz, const do
 
 namespace {
 
+// Reads (and clears) the tcgen05 kernel's status word after the stream's
+// work; nonzero means one of its bounded waits gave up and the three-body
+// results of that evaluation are invalid.
+mbpol_status check_kernel_status(mbpol_context* ctx) {
+    int h = 0;
+    MBPOL_CUDA_OK(cudaMemcpyAsync(&h, ctx->kstatus.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+    if (!h) return MBPOL_OK;
+    MBPOL_CUDA_OK(cudaMemsetAsync(ctx->kstatus.p, 0, sizeof(int), ctx->st));
+    return mbpol_fail(MBPOL_ERR_CUDA, "three-body tensor kernel: a bounded wait gave up (site " +
+                                          std::to_string(h) + "); results discarded");
+}
+
 // Evaluate the requested terms; forces and energies stay on the device
 // (d_force, d_energy).  Host synchronisation happens only for list sizes and
 // the solver's convergence test.
@@ -892,6 +915,10 @@ mbpol_status mbpol_compute(mbpol_context* ctx, unsigned mask, double* energies, 
         MBPOL_CUDA_OK(cudaMemcpyAsync(ctx->h_force.data(), ctx->d_force.p, sizeof(double) * 3 * ctx->N,
                                       cudaMemcpyDeviceToHost, ctx->st));
     MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+    {
+        const mbpol_status ks = check_kernel_status(ctx);
+        if (ks) return ks;
+    }
     if (energies)
         for (int k = 0; k < MBPOL_NUM_TERMS; ++k) energies[k] = h_e[k];
     if (forces)
@@ -959,6 +986,10 @@ mbpol_status mbpol_md_run(mbpol_context* ctx, int nsteps, double dt, double temp
     MBPOL_CUDA_OK(cudaMemcpyAsync(h, ctx->d_energy.p, sizeof(double) * MBPOL_NUM_TERMS, cudaMemcpyDeviceToHost, ctx->st));
     MBPOL_CUDA_OK(cudaMemcpyAsync(h + MBPOL_NUM_TERMS, ctx->d_ekin.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
     MBPOL_CUDA_OK(cudaStreamSynchronize(ctx->st));
+    {
+        const mbpol_status ks = check_kernel_status(ctx);
+        if (ks) return ks;
+    }
     float ms = 0.f;
     MBPOL_CUDA_OK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     if (gpu_ms) *gpu_ms = ms;
@@ -1123,7 +1154,8 @@ mbpol_status mbpol_guess_fit_predictor(mbpol_context* ctx, const double* history
 // ---- batched independent clusters (no reference counterpart as one call)
 mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind) {
     if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
-    if (kind != MBPOL_POLY3B_TENSOR && kind != MBPOL_POLY3B_WALK && kind != MBPOL_POLY3B_AUTO)
+    if (kind != MBPOL_POLY3B_TENSOR && kind != MBPOL_POLY3B_WALK && kind != MBPOL_POLY3B_AUTO &&
+        kind != MBPOL_POLY3B_TENSOR_SYNC)
         return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "unknown three-body evaluator");
     ctx->poly3b_kind = kind;
     return MBPOL_OK;

@@ -29,6 +29,7 @@
 
 #include "mbpol_internal.cuh"
 #include "poly_tc.h"
+#include "poly_tc_common.cuh"
 #include "poly_tc_dev.h"
 
 namespace mbpol {
@@ -69,39 +70,6 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint4& a, unsigned
         "{%0,%1,%2,%3};\n"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
-}
-
-// double-float accumulation: (s.x + s.y) += a * b (TwoProd by FMA, TwoSum)
-__device__ __forceinline__ void df_fma(float2& s, float a, float b) {
-    const float p = __fmul_rn(a, b);
-    const float pe = __fmaf_rn(a, b, -p);
-    const float t = __fadd_rn(s.x, p);
-    const float bb = __fsub_rn(t, s.x);
-    const float e = __fadd_rn(__fsub_rn(s.x, __fsub_rn(t, bb)), __fsub_rn(p, bb));
-    s.x = t;
-    s.y = __fadd_rn(s.y, __fadd_rn(e, pe));
-}
-
-__device__ __forceinline__ void df_add(float2& s, float2 v) {
-    const float t = __fadd_rn(s.x, v.x);
-    const float bb = __fsub_rn(t, s.x);
-    const float e = __fadd_rn(__fsub_rn(s.x, __fsub_rn(t, bb)), __fsub_rn(v.x, bb));
-    s.x = t;
-    s.y = __fadd_rn(s.y, __fadd_rn(e, v.y));
-}
-
-// per-unit exponent e: inputs up to m times the sampled bounds give
-// |y'| <= 2^12 max(1, m)^2; scaled by 2^-e they stay below 2^15
-__device__ __forceinline__ int unit_exp(float m) {
-    if (!(m > 1.f)) return 0;
-    if (!(m < 1e30f)) return 100;
-    return max(0, 2 * ilogbf(m) - 1);
-}
-
-// 2^k as a float for k in [-126, 127]
-__device__ __forceinline__ float exp2i(int k) {
-    k = max(-126, min(127, k));
-    return __int_as_float((k + 127) << 23);
 }
 
 template <int NV, int NPAD>
@@ -300,6 +268,9 @@ cudaError_t upload_tc(const PolyTCTables& h, PolyTCDev* d) {
     d->nv = h.nv;
     d->ny = h.ny;
     d->npad = h.npad;
+    d->parts5 = h.parts5;
+    d->rows5 = h.rows5;
+    d->nblk5 = h.nblk5;
     if ((e = upload_array(h.x0h, (size_t)h.nv, &d->x0h, owned)) ||
         (e = upload_array(h.x0l, (size_t)h.nv, &d->x0l, owned)) ||
         (e = upload_array(h.inv_bound, (size_t)h.nv, &d->inv_bound, owned)) ||
@@ -309,7 +280,10 @@ cudaError_t upload_tc(const PolyTCTables& h, PolyTCDev* d) {
         (e = upload_array(h.rt_id, (size_t)h.nrt, &d->rt_id, owned)) ||
         (e = upload_array(h.rt_entry, (size_t)h.nrt + 1, &d->rt_entry, owned)) ||
         (e = upload_array(h.ent_kt, (size_t)h.nent, &d->ent_kt, owned)) ||
-        (e = upload_array(h.frag, (size_t)h.nent * 3 * 32 * 4, &d->frag, owned))) {
+        (e = upload_array(h.frag, (size_t)h.nent * 3 * 32 * 4, &d->frag, owned)) ||
+        (e = upload_array(h.sblk, (size_t)h.nblk5 * 3 * h.rows5 * 16, &d->sblk, owned)) ||
+        (e = upload_array(h.blk_kt, (size_t)h.nblk5, &d->blk_kt, owned)) ||
+        (e = upload_array(h.blk_begin, (size_t)h.parts5 * (h.npad / h.rows5) + 1, &d->blk_begin, owned))) {
         for (void* p : owned) cudaFree(p);
         return e;
     }
@@ -327,7 +301,9 @@ cudaError_t poly_tc_setup(int device, const PolyTCDev** out) {
         cudaError_t e = cudaFuncSetAttribute(poly_tc_kernel<36, 704>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Shape3::SMEM);
         if (e != cudaSuccess) return e;
-        if (k_poly3b.nv != 36 || k_poly3b.npad != 704) return cudaErrorInvalidValue;
+        if (k_poly3b.nv != 36 || k_poly3b.npad != 704 || k_poly3b.parts5 != 3 || k_poly3b.rows5 != 64)
+            return cudaErrorInvalidValue;
+        if ((e = poly_tc5_prepare())) return e;
         if ((e = upload_tc(k_poly3b, &c.d3))) return e;
         c.ready = true;
     }

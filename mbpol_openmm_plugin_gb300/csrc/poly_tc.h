@@ -21,6 +21,14 @@ struct PolyTCTables {
     const int* rt_entry;           // [nrt + 1]: tiles of row tile i: ent_kt[rt_entry[i] .. rt_entry[i+1])
     const unsigned short* ent_kt;  // [nent]: k-tile of each kept tile
     const unsigned* frag;          // [nent][3 pieces][32 lanes][4 registers]: fp16 pairs
+    // tcgen05 kernel (poly_tc5.cu): S as a stream of blocks of `rows5` rows x
+    // 16 columns, ordered by K part, row chunk, k-tile
+    int parts5;                    // K parts (Y' of one part in tensor memory)
+    int rows5;                     // rows of S per chunk (N of the MMA)
+    int nblk5;                     // blocks in the stream
+    const unsigned short* sblk;    // [nblk5][3 pieces][2 k halves][rows5 / 8][8 rows][8 k]: fp16
+    const unsigned char* blk_kt;   // [nblk5]: k-tile of each block within its part
+    const int* blk_begin;          // [parts5 * npad / rows5 + 1]: first block of (part, chunk)
 };
 
 extern const PolyTCTables k_poly2b;

@@ -18,6 +18,10 @@ struct PolyTCDev {
     const int* rt_entry = nullptr;
     const unsigned short* ent_kt = nullptr;
     const unsigned* frag = nullptr;
+    int parts5 = 0, rows5 = 0, nblk5 = 0;
+    const unsigned short* sblk = nullptr;
+    const unsigned char* blk_kt = nullptr;
+    const int* blk_begin = nullptr;
 };
 
 // Uploads the three-body tables to `device` (current) once per process and
@@ -27,5 +31,13 @@ cudaError_t poly_tc_setup(int device, const PolyTCDev** out);
 size_t poly3b_tc_scratch_floats(int num_sms);
 void launch_poly3b_tc(cudaStream_t st, const PolyTCDev* tab, const float* X, float* G, float* E, int n, int stride,
                       int num_sms, float* zscratch);
+// The same evaluation with tcgen05.mma (poly_tc5.cu): Y' of 128 trimers in
+// tensor memory as the A operand, S streamed through shared memory as B.
+// `status` (device int, zero before the launch) receives a nonzero code if
+// one of the kernel's bounded waits gave up; the outputs are then invalid.
+cudaError_t poly_tc5_prepare();
+size_t poly3b_tc5_scratch_floats(int num_sms);
+void launch_poly3b_tc5(cudaStream_t st, const PolyTCDev* tab, const float* X, float* G, float* E, int n, int stride,
+                       int num_sms, float* zscratch, int* status);
 
 }  // namespace mbpol

@@ -134,11 +134,12 @@ class MBPolThreeBodyForce(_CutoffWaterForce):
     """openmmapi/include/openmm/MBPolThreeBodyForce.h.  setTrimerRule chooses
     between the reference's enumeration (default) and the complete one;
     setPolynomialEvaluator between the tensor-core evaluation of the
-    polynomial, the double-float walk and the automatic choice by size
-    (default; mbpol_set_threebody_evaluator)."""
+    polynomial (tcgen05; TensorCoresMmaSync for the legacy mma.sync path),
+    the double-float walk and the automatic choice by size (default;
+    mbpol_set_threebody_evaluator)."""
     _term = 2
     ReferenceTrimers, CompleteTrimers = 0, 1
-    TensorCores, DoubleFloatWalk, AutomaticEvaluator = 0, 1, 2
+    TensorCores, DoubleFloatWalk, AutomaticEvaluator, TensorCoresMmaSync = 0, 1, 2, 3
 
     def __init__(self):
         super().__init__(1.0)

@@ -85,20 +85,41 @@ def test_threebody_walk_vs_reference(name):
     assert rel_rms(st.getForces(), d["f3"]) <= FORCE_TOL
 
 
-@pytest.mark.parametrize("name", ["box256_seed0", "pdb_water256_pme"])
-def test_threebody_tensor_vs_walk(name):
-    """The tensor-core evaluation against the double-float walk on the same
-    trimers: energy and forces of the three-body term."""
+@pytest.mark.parametrize("tensor", ["tcgen05", "mma.sync"])
+@pytest.mark.parametrize("name", ["box256_seed0", "pdb_water256_pme", "box4096_seed0"])
+def test_threebody_tensor_vs_walk(name, tensor):
+    """The tensor-core evaluations (tcgen05, and the legacy mma.sync path)
+    against the double-float walk on the same trimers: energy and forces of
+    the three-body term."""
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     box = d["box"] if bool(d["periodic"]) else None
+    T = mb.MBPolThreeBodyForce
     res = []
-    for ev in (mb.MBPolThreeBodyForce.TensorCores, mb.MBPolThreeBodyForce.DoubleFloatWalk):
+    for ev in (T.TensorCores if tensor == "tcgen05" else T.TensorCoresMmaSync, T.DoubleFloatWalk):
         st, ctx = run(d["positions"], box, ("threebody",), evaluator=ev)
         res.append((st.term_energies[2], st.getForces()))
     (e_tc, f_tc), (e_w, f_w) = res
-    print(name, "E3 tensor", e_tc, "walk", e_w, "rel", abs(e_tc - e_w) / abs(e_w), "F relrms", rel_rms(f_tc, f_w))
+    print(name, tensor, "E3", e_tc, "walk", e_w, "rel", abs(e_tc - e_w) / abs(e_w), "F relrms", rel_rms(f_tc, f_w))
     assert abs(e_tc - e_w) <= E3_TC_TOL * abs(e_w) + E3_TC_ABS
     assert rel_rms(f_tc, f_w) <= 2e-5
+
+
+def test_threebody_tcgen05_repeatable_and_ragged():
+    """The tcgen05 kernel on a trimer count that leaves a ragged last tile
+    and more tiles than blocks (box4096 fixture): repeated evaluations and a
+    second context agree to the FP64 atomics' summation order (the kernel's
+    own per-trimer sums have a fixed order)."""
+    d = np.load(os.path.join(GOLDEN, "box4096_seed0.npz"))
+    T = mb.MBPolThreeBodyForce
+    st1, ctx = run(d["positions"], d["box"], ("threebody",), evaluator=T.TensorCores)
+    assert ctx.getCounts()[1] % 128 != 0
+    ctx.setPositions(d["positions"])
+    st2 = ctx.getState()
+    st3, _ = run(d["positions"], d["box"], ("threebody",), evaluator=T.TensorCores)
+    e1 = st1.term_energies[2]
+    for st in (st2, st3):
+        assert abs(st.term_energies[2] - e1) <= 1e-12 * abs(e1)
+        assert rel_rms(st.getForces(), st1.getForces()) <= 1e-12
 
 
 def _known(key):
