@@ -407,16 +407,16 @@ def workload_config(args, ws, alpha, grid, params_src):
 
 
 def tc_flop_per_trimer():
-    """Executed tensor-core work of the three-body kernel per trimer: kept
-    16x16 tiles of S x 8 n-tiles of 8 trimers x 4 mma.m16n8k16 (2*16*8*16
-    flop), per 64-trimer tile."""
+    """Executed tensor-core work of the three-body kernel (tcgen05) per
+    trimer: blocks of S in the stream x 4 MMAs of M = 128 trimers, N = 64
+    rows, K = 16 (2 flop per multiply-add), per 128-trimer tile."""
     try:
         import re
         src = open(os.path.join(ROOT, "mbpol_openmm_plugin_gb300", "_build", "poly_tc_tables.cpp")).read()
-        nent = int(re.search(r"k_poly3b = \{36, 703, 704, \d+, (\d+),", src).group(1))
+        nblk = int(re.search(r"poly3b_frag, \d+, \d+, (\d+),", src).group(1))
     except (OSError, AttributeError):
-        nent = 839
-    return nent * 8 * 4 * 4096 / 64.0
+        nblk = 239
+    return nblk * 4 * 2 * 128 * 64 * 16 / 128.0
 
 
 def rooflines(kern, counts, grid, n, clocks):
@@ -455,7 +455,7 @@ def rooflines(kern, counts, grid, n, clocks):
             bf16 = measured_peak("bf16_tflops", 1905.0)
             roof["poly3b_tensor_view"] = {
                 "bound": "tensor", "achieved": tc, "peak": bf16[0], "unit": "TFLOP/s", "frac": tc / bf16[0],
-                "work": "executed mma.m16n8k16 flop: %.0f per trimer" % tc_flop_per_trimer(),
+                "work": "executed tcgen05.mma (M128 N64 K16) flop: %.0f per trimer" % tc_flop_per_trimer(),
                 "peak_kind": bf16[1] + " (dense bf16; fp16 runs at the same rate)",
                 "fp32_view_frac": u3 * ALGO_FLOP_PER_UNIT["poly3b"] / (ms3 * 1e-3) / 1e12 / fp32_peak}
     hbm = measured_hbm_gbs()

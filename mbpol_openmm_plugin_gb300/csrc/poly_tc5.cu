@@ -12,7 +12,7 @@
 //   - B operand: S in blocks of 64 rows x 16 columns (three fp16 pieces,
 //     6 KB), only blocks with a nonzero entry, streamed from global memory
 //     (L2) by bulk copies through a 28-stage shared-memory ring.
-//   - D: per block, Y0.S0 + Y0.S1 + Y1.S0 + Y0.S2 started from zero
+//   - D: per block, Y0.S0 + Y1.S0 + Y0.S1 + Y0.S2 started from zero
 //     (M = 128, N = 64, K = 16), so the tensor cores' own accumulation
 //     rounding stays relative to one k-tile.  The blocks of a part go in
 //     pairs, each block into its own buffer of 64 columns; two pair slots
@@ -209,9 +209,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                             const uint32_t sa = s_stage + st * kBlkBytes;
                             const uint32_t dt = tb + kAccCol + (2 * slot + q) * kRows;
                             const uint32_t y0 = tb + 8 * j, y1 = y0 + kYCols;
+                            // S0 twice in a row: its operand fetch is shared
                             mma_ts(dt, y0, sdesc(sa, 1024, 128), idesc, 0);
-                            mma_ts(dt, y0, sdesc(sa + 2048, 1024, 128), idesc, 1);
                             mma_ts(dt, y1, sdesc(sa, 1024, 128), idesc, 1);
+                            mma_ts(dt, y0, sdesc(sa + 2048, 1024, 128), idesc, 1);
                             mma_ts(dt, y0, sdesc(sa + 4096, 1024, 128), idesc, 1);
                             mma_commit(b_empty + 8 * st);
                         }

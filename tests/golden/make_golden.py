@@ -487,7 +487,7 @@ def main_elec_known():
         json.dump(out, fh, indent=1)
 
 
-def main_box4096():
+def main_box4096(frame=None):
     """One frame of the 4096-water benchmark box (systems.workload("box4096",
     0): 49.67 A, jittered 16^3 lattice), all five terms at the benchmark's
     settings: cutoffs 0.65 / 0.45 nm, PME rc 0.9 nm, Ewald tolerance 1e-5
@@ -495,13 +495,23 @@ def main_box4096():
     one-, two- and three-body and electrostatics terms come from the
     compiled reference; forces, dipoles and dispersion from the oracle port
     (the reference's PME forces are not finite, see electrostatics() above),
-    which agrees with the reference's energies to ~1e-13."""
+    which agrees with the reference's energies to ~1e-13.
+
+    `frame`: an .npz with `positions` (and `steps`) of the same box after MD
+    (written by the GPU MD driver from the lattice, NVE from 300 K
+    Maxwell-Boltzmann velocities); the fixture is then box4096_md<steps>.npz.
+    Its total energy does not nearly cancel as the lattice frame's does."""
     L = lib()
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from mbpol_openmm_plugin_gb300.plugin import pme_parameters
     ws = systems.workload("box4096", 0)
+    out_name = "box4096_seed0.npz"
+    if frame is not None:
+        fr = np.load(frame)
+        ws.positions = np.asarray(fr["positions"], np.float64)
+        out_name = "box4096_md%d.npz" % int(fr["steps"])
     pos = place_m(ws.positions)
     nw = pos.shape[0] // 4
     waters = np.stack([4 * np.arange(nw), 4 * np.arange(nw) + 1, 4 * np.arange(nw) + 2], 1).astype(np.int32)
@@ -512,14 +522,14 @@ def main_box4096():
     r = run_terms(L, pos, waters, ws.box)
     ee, _, dip, it = electrostatics(L, pos, ws.box, True, alpha=alpha, grid=grid, eps=1e-8)
     etot = r["e1"] + r["e2"] + r["e3"] + port["edisp"] + ee
-    np.savez_compressed(os.path.join(HERE, "box4096_seed0.npz"), positions=pos, box=ws.box, periodic=True,
+    np.savez_compressed(os.path.join(HERE, out_name), positions=pos, box=ws.box, periodic=True,
                         alpha=alpha, grid=np.array(grid), e1=r["e1"], e2=r["e2"], e3=r["e3"], edisp=port["edisp"],
                         eelec=ee, etotal=etot, ftotal=port["ftotal"], dipoles=port["dipoles"],
                         iterations=it, npairs=r["npairs"], ntrip=r["ntrip"], trip_hash=r["trip_hash"],
                         port_energies=np.array([port["e1"], port["e2"], port["e3"], port["edisp"], port["eelec"]]),
                         port_iterations=port["iterations"])
-    print("box4096: reference e1 %.6f e2 %.6f e3 %.6f eelec %.6f (it %d), total %.6f kJ/mol; pairs %d trimers %d" % (
-        r["e1"], r["e2"], r["e3"], ee, it, etot, r["npairs"], r["ntrip"]))
+    print("%s: reference e1 %.6f e2 %.6f e3 %.6f eelec %.6f (it %d), total %.6f kJ/mol; pairs %d trimers %d" % (
+        out_name, r["e1"], r["e2"], r["e3"], ee, it, etot, r["npairs"], r["ntrip"]))
 
 
 def main_mbpol_xml():
@@ -544,7 +554,7 @@ if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "mbpol_xml":
         main_mbpol_xml()
     elif len(sys.argv) > 2 and sys.argv[2] == "box4096":
-        main_box4096()
+        main_box4096(sys.argv[3] if len(sys.argv) > 3 else None)
     elif len(sys.argv) > 2 and sys.argv[2] == "elec_known":
         main_elec_known()
     elif len(sys.argv) > 2 and sys.argv[2] == "elec":
