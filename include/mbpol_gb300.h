@@ -247,6 +247,23 @@ const char* mbpol_last_error(void);
 enum { MBPOL_POLY3B_TENSOR = 0, MBPOL_POLY3B_WALK = 1, MBPOL_POLY3B_AUTO = 2, MBPOL_POLY3B_TENSOR_SYNC = 3 };
 mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind);
 
+/* ---- White-box probes ------------------------------------------------------
+ * The reference tests two protected functions of its electrostatics directly
+ * (platforms/reference/tests/TestReferenceMBPolElectrostaticsForce.cpp):
+ * getAndScaleInverseRs (:80-131, src/MBPolReferenceElectrostaticsForce.cpp:261-333)
+ * and computeWaterCharge (:326-417, src/...:2793-3096).  These run the device
+ * functions the field kernels use, one thread on the current device, no
+ * context needed.
+ * mbpol_probe_thole_inverse_rs: rr[0..3] = Thole-scaled 1/r, 1/r^3, 3/r^5,
+ *   15/r^7 (nm^-k) for site damping factors damp_i, damp_j and Thole
+ *   parameter `thole` (FP32 as in the kernels).
+ * mbpol_probe_water_charges: positions_nm = O, H1, H2 (9 doubles);
+ *   charges[4] = O, H1, H2, M (e); derivatives[27] = [particle O, H1, H2]
+ *   [charge of H1, H2, M][xyz] (e/nm), i.e. the reference's
+ *   particle.chargeDerivatives[vsH1f | vsH2f | vsMf]. */
+mbpol_status mbpol_probe_thole_inverse_rs(double r_nm, double damp_i, double damp_j, double thole, double rr[4]);
+mbpol_status mbpol_probe_water_charges(const double positions_nm[9], double charges[4], double derivatives[27]);
+
 /* ---- Batched independent clusters ---------------------------------------
  * No reference counterpart as one call: the reference evaluates each water
  * cluster in its own OpenMM Context.  Here one context holds many clusters

@@ -10,3 +10,8 @@ from ._capi import MBPolError  # noqa: F401
 from .forcefield import (  # noqa: F401
     ForceField, PDBFile, CMMotionRemover, NoCutoff, CutoffNonPeriodic, CutoffPeriodic, PME,
 )
+from .simulation import (  # noqa: F401
+    VerletIntegrator, AndersenThermostat, MonteCarloBarostat, Simulation, StateDataReporter, PDBReporter,
+    LocalEnergyMinimizer,
+)
+

@@ -1161,6 +1161,22 @@ mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind) {
     return MBPOL_OK;
 }
 
+mbpol_status mbpol_probe_thole_inverse_rs(double r_nm, double damp_i, double damp_j, double thole, double rr[4]) {
+    if (!rr || !(r_nm > 0) || damp_i < 0 || damp_j < 0 || thole < 0)
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad probe arguments");
+    return probe_thole(r_nm, damp_i, damp_j, thole, rr);
+}
+
+mbpol_status mbpol_probe_water_charges(const double positions_nm[9], double charges[4], double derivatives[27]) {
+    if (!positions_nm || !charges || !derivatives) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null probe buffer");
+    double out[31];
+    const mbpol_status s = probe_water_charges(positions_nm, out);
+    if (s) return s;
+    for (int k = 0; k < 4; ++k) charges[k] = out[k];
+    for (int k = 0; k < 27; ++k) derivatives[k] = out[4 + k];
+    return MBPOL_OK;
+}
+
 mbpol_status mbpol_set_clusters(mbpol_context* ctx, const int* cluster_of_particle, int num_clusters) {
     if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
     if (num_clusters < 0 || (num_clusters > 0 && !cluster_of_particle))

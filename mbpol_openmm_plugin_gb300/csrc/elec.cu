@@ -2061,6 +2061,54 @@ static int molecule_layout(int n, const int* molecule) {
     return K;
 }
 
+// ---- white-box probes of the device functions above (one thread each),
+// for the reference's white-box tests: getAndScaleInverseRs
+// (platforms/reference/tests/TestReferenceMBPolElectrostaticsForce.cpp:80-131)
+// and computeWaterCharge (:326-417)
+namespace {
+__global__ void probe_thole_kernel(float r, float d6prod, float gamma, double* out) {
+    const Thole th = thole(r, d6prod, gamma);
+    const float rI = 1.f / r, r2I = rI * rI;
+    out[0] = (double)(s1_of(th, gamma) * rI);
+    out[1] = (double)(s3_of(th) * rI * r2I);
+    out[2] = (double)(s5_of(th) * 3.f * rI * r2I * r2I);
+    out[3] = (double)(s7_of(th, gamma) * 15.f * rI * r2I * r2I * r2I);
+}
+
+__global__ void probe_water_charges_kernel(const double* pos, double* out) {
+    double q[4], dq[4][3][3];
+    water_charges(make_double3(pos[0], pos[1], pos[2]), make_double3(pos[3], pos[4], pos[5]),
+                  make_double3(pos[6], pos[7], pos[8]), q, dq);
+    for (int s = 0; s < 4; ++s) out[s] = q[s];
+    for (int x = 0; x < 3; ++x)
+        for (int o = 0; o < 3; ++o)
+            for (int k = 0; k < 3; ++k) out[4 + 9 * x + 3 * o + k] = dq[x][o][k];
+}
+}  // namespace
+
+mbpol_status probe_thole(double r, double damp_i, double damp_j, double gamma, double* rr) {
+    DBuf<double> d;
+    MBPOL_CUDA_OK(d.ensure(4));
+    // the sites' sixth roots of the damping factors, as the field kernels store them
+    const float d6 = (float)(std::pow(damp_i, 1.0 / 6.0)) * (float)(std::pow(damp_j, 1.0 / 6.0));
+    probe_thole_kernel<<<1, 1>>>((float)r, d6, (float)gamma, d.p);
+    MBPOL_CUDA_OK(cudaGetLastError());
+    MBPOL_CUDA_OK(cudaMemcpy(rr, d.p, 4 * sizeof(double), cudaMemcpyDeviceToHost));
+    return MBPOL_OK;
+}
+
+mbpol_status probe_water_charges(const double* pos9, double* out31) {
+    DBuf<double> d;
+    MBPOL_CUDA_OK(d.ensure(9 + 31));
+    MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms, kDmsCoef, sizeof(kDmsCoef)));
+    MBPOL_CUDA_OK(cudaMemcpyToSymbol(c_dms_idx, kDmsIdx, sizeof(kDmsIdx)));
+    MBPOL_CUDA_OK(cudaMemcpy(d.p, pos9, 9 * sizeof(double), cudaMemcpyHostToDevice));
+    probe_water_charges_kernel<<<1, 1>>>(d.p, d.p + 9);
+    MBPOL_CUDA_OK(cudaGetLastError());
+    MBPOL_CUDA_OK(cudaMemcpy(out31, d.p + 9, 31 * sizeof(double), cudaMemcpyDeviceToHost));
+    return MBPOL_OK;
+}
+
 mbpol_status ElecEngine::update_parameters(const double* charge, const int* molecule, const int* atom_type,
                                            const double* damping, const double* polarity) {
     ElecImpl& I = *impl_;

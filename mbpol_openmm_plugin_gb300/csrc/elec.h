@@ -14,6 +14,12 @@ namespace mbpol {
 
 struct ElecImpl;
 
+// white-box probes (one thread on the current device): the Thole-scaled
+// inverse distances of orders 1, 3, 5, 7 as the field kernels evaluate them
+// (FP32), and one water's charges and charge derivatives (FP64)
+mbpol_status probe_thole(double r, double damp_i, double damp_j, double gamma, double* rr4);
+mbpol_status probe_water_charges(const double* pos9, double* out31);
+
 class ElecEngine {
 public:
     ElecEngine();

@@ -440,6 +440,7 @@ class Context:
         self.device = device
         self._h = None
         self._pos = None
+        self._pos_dirty = False
         self._box = None if system.box is None else np.array(system.box, float)
 
     def _invalidate(self):
@@ -501,6 +502,7 @@ class Context:
 
     def setPositions(self, positions):
         self._pos = as_c(np.asarray(positions, float).reshape(-1, 3), np.float64)
+        self._pos_dirty = True
 
     def setPeriodicBoxVectors(self, a, b, c):
         self._box = np.array([a[0], b[1], c[2]], float)

@@ -699,3 +699,39 @@ int orc_electrostatics(int n, const double* pos, const double* box, int pme, dou
     }
     return conv ? 0 : 1;
 }
+
+/* White-box probes for the reference's own white-box tests
+ * (platforms/reference/tests/TestReferenceMBPolElectrostaticsForce.cpp):
+ * getAndScaleInverseRs (:80-131) as rr[0..3] = scale_k / r^k times the
+ * reference's factors 1, 1, 3, 15 (orders 1, 3, 5, 7; thole parameter index
+ * TCC with every parameter equal to `thole`), and computeWaterCharge
+ * (:326-417): charges O, H1, H2, M and derivatives [particle O, H1, H2]
+ * [charge of H1, H2, M][xyz] in e/nm. */
+void orc_probe_thole(double r, double damp_i, double damp_j, double thole, double* rr) {
+    OCtx C;
+    memset(&C, 0, sizeof C);
+    for (int k = 0; k < 5; ++k) C.thole[k] = thole;
+    OSite a, b;
+    memset(&a, 0, sizeof a);
+    memset(&b, 0, sizeof b);
+    a.damp = damp_i;
+    b.damp = damp_j;
+    b.mol = 1;
+    const double rI = 1.0 / r, r2I = rI * rI;
+    rr[0] = o_scale(&C, &a, &b, r, 1, TCC) * rI;
+    rr[1] = o_scale(&C, &a, &b, r, 3, TCC) * rI * r2I;
+    rr[2] = o_scale(&C, &a, &b, r, 5, TCC) * 3.0 * rI * r2I * r2I;
+    rr[3] = o_scale(&C, &a, &b, r, 7, TCC) * 15.0 * rI * r2I * r2I * r2I;
+}
+
+void orc_probe_water_charges(const double* pos9, double* q4, double* d27) {
+    OSite s[4];
+    memset(s, 0, sizeof s);
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) s[i].r[k] = pos9[3 * i + k];
+    o_water_charge(&s[0], &s[1], &s[2], &s[3]);
+    for (int i = 0; i < 4; ++i) q4[i] = s[i].q;
+    for (int i = 0; i < 3; ++i)
+        for (int o = 0; o < 3; ++o)
+            for (int k = 0; k < 3; ++k) d27[9 * i + 3 * o + k] = s[i].dq[o][k];
+}

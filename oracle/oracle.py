@@ -112,6 +112,10 @@ def port():
     L.orc_system_moments.argtypes = [P, P]
     L.orc_set_pme_fixed_field.restype = None
     L.orc_set_pme_fixed_field.argtypes = [I]
+    L.orc_probe_thole.restype = None
+    L.orc_probe_thole.argtypes = [D, D, D, D, P]
+    L.orc_probe_water_charges.restype = None
+    L.orc_probe_water_charges.argtypes = [P, P, P]
     import numpy as np
     rows = [ln.split() for ln in open(os.path.join(os.path.dirname(HERE), "mbpol_openmm_plugin_gb300", "data",
                                                  "onebody_tables.txt")) if not ln.startswith(("#", "n "))]
@@ -401,3 +405,24 @@ def _estimate_step(workload, seed, solver_iterations):
               % (workload, seed, k2, np_.value, k3, nt.value, R, R, grid, solver_iterations, wall + t["onebody"]))
     return {"value": 0.0002e-3 * 86400.0 / step, "unit": "ns/day", "cores": 1, "kind": "port",
             "sample": sample, "seconds_per_step": step, "per_term_s": t}
+
+
+def probe_thole(r, damp_i, damp_j, thole):
+    """Thole-scaled inverse distances of orders 1, 3, 5, 7 (the reference's
+    getAndScaleInverseRs with its factors 1, 1, 3, 15), FP64."""
+    import numpy as np
+    L = port()
+    out = np.zeros(4)
+    L.orc_probe_thole(r, damp_i, damp_j, thole, _p(out))
+    return out
+
+
+def probe_water_charges(pos_nm):
+    """One water's charges (O, H1, H2, M) and charge derivatives
+    [particle O, H1, H2][charge of H1, H2, M][xyz] (e/nm), FP64."""
+    import numpy as np
+    L = port()
+    q, d = np.zeros(4), np.zeros(27)
+    L.orc_probe_water_charges(_p(np.ascontiguousarray(pos_nm, np.float64).reshape(-1)), _p(q), _p(d))
+    return q, d.reshape(3, 3, 3)
+

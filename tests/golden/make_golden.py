@@ -431,6 +431,70 @@ def parse_elec_test(path, func):
             "TestReferenceMBPolElectrostaticsForce.cpp:%d-%d" % (start, src.count("\n", 0, j) + 1)}
 
 
+def main_elec_whitebox():
+    """The white-box known answers of the reference's electrostatics test:
+    getAndScaleInverseRs (testGetAndScaleInverseRs, the intramolecular
+    O-H case, and testGetAndScaleInverseRsInterMulecolar) and
+    computeWaterCharge (testComputeWaterCharge: charges and charge
+    derivatives), read from the test source as text.  In both Thole cases
+    the test's last argument selects the Thole parameter by index and every
+    parameter is 0.4 (the same value for any index).  Expected values use the
+    test's own scalings: rrI[5] carries the factor 3, positions and
+    derivatives are converted from Angstrom."""
+    path = os.path.join(REF, "platforms", "reference", "tests", "TestReferenceMBPolElectrostaticsForce.cpp")
+    src = open(path).read()
+    num = r"([-+0-9.eE]+(?:\s*\*\s*[0-9.eE+-]+)*)"
+
+    def ev(expr):
+        v = 1.0
+        for f in expr.split("*"):
+            v *= float(f.strip().rstrip("."))
+        return v
+
+    def body_of(func):
+        i = src.index("static void " + func + "(") if ("static void " + func + "(") in src else src.index(func)
+        j = src.find("\nstatic void ", i + 10)
+        j2 = src.find("\nclass ", i + 10)
+        j = min(k for k in (j, j2, len(src)) if k > 0)
+        return i, j, "\n".join(ln.split("//")[0] for ln in src[i:j].splitlines())
+
+    out = {}
+    for func in ("testGetAndScaleInverseRs", "testGetAndScaleInverseRsInterMulecolar"):
+        i, j, b = body_of(func)
+        damp = re.search(r"RealOpenMM damp\s*=\s*([-+0-9.eE]+)", b)
+        dampO = re.search(r"RealOpenMM dampO\s*=\s*([-+0-9.eE]+)", b).group(1)
+        dampH = re.search(r"RealOpenMM dampH\s*=\s*([-+0-9.eE]+)", b)
+        r = re.search(r"RealOpenMM r\s*=\s*" + num + ";", b).group(1)
+        call = re.search(r"wrapGetAndScaleInverseRs\(\s*(\w+),\s*(\w+),", b)
+        vals = {"dampO": float(dampO), "dampH": float(dampH.group(1)) if dampH else None}
+        exp = {int(m.group(2)): ev(m.group(1))
+               for m in re.finditer(r"ASSERT_EQUAL_TOL_MOD\(\s*" + num + r"\s*,\s*rrI\[(\d)\]", b)}
+        thole = float(re.search(r"tholes\.push_back\(([0-9.]+)\)", b).group(1))
+        out[func] = {"r_nm": ev(r), "damp_i": vals[call.group(1)], "damp_j": vals[call.group(2)], "thole": thole,
+                     "expected_rr": [exp[k] for k in (1, 3, 5, 7)], "tolerance": 1e-5,
+                     "source": "platforms/reference/tests/TestReferenceMBPolElectrostaticsForce.cpp:%d-%d" % (
+                         src.count("\n", 0, i) + 1, src.count("\n", 0, j) + 1)}
+    i, j, b = body_of("testComputeWaterCharge")
+    pos = [[float(m.group(k)) for k in (2, 3, 4)] for m in re.finditer(r"positions\[(\d+)\]\s*=\s*" + VEC3, b)]
+    q = {m.group(2): float(m.group(1)) for m in re.finditer(
+        r"ASSERT_EQUAL_TOL_MOD\(\s*([-+0-9.eE]+)\s*,\s*particle(\w+)\.charge", b)}
+    der = {int(m.group(1)): [float(m.group(k)) for k in (2, 3, 4)] for m in re.finditer(
+        r"expectedChargeDerivatives\[(\d+)\]\s*=\s*" + VEC3, b)}
+    out["testComputeWaterCharge"] = {
+        "positions_nm": [[0.1 * v for v in p] for p in pos[:3]],
+        "charges": [q["O"], q["H1"], q["H2"], q["M"]], "charge_tolerance": 1e-5,
+        # rows: particle H1 (0-2), H2 (3-5), O (6-8); each the charge of H1, H2, M; x10 to e/nm
+        "derivatives_by_particle": {"H1": [[10 * v for v in der[k]] for k in range(0, 3)],
+                                    "H2": [[10 * v for v in der[k]] for k in range(3, 6)],
+                                    "O": [[10 * v for v in der[k]] for k in range(6, 9)]},
+        "derivative_tolerance": 1e-6,
+        "source": "platforms/reference/tests/TestReferenceMBPolElectrostaticsForce.cpp:%d-%d" % (
+            src.count("\n", 0, i) + 1, src.count("\n", 0, j) + 1)}
+    with open(os.path.join(HERE, "elec_whitebox.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+    print(json.dumps(out, indent=1)[:1500])
+
+
 def main_elec_known():
     """The electrostatics known answers of the reference's own tests: water3
     without M sites (NoCutoff and the PME huge box with alpha -> 0), the PME
@@ -557,6 +621,8 @@ if __name__ == "__main__":
         main_box4096(sys.argv[3] if len(sys.argv) > 3 else None)
     elif len(sys.argv) > 2 and sys.argv[2] == "elec_known":
         main_elec_known()
+    elif len(sys.argv) > 2 and sys.argv[2] == "elec_whitebox":
+        main_elec_whitebox()
     elif len(sys.argv) > 2 and sys.argv[2] == "elec":
         main_elec()
     elif len(sys.argv) > 2 and sys.argv[2] == "potential":
