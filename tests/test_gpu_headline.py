@@ -12,7 +12,13 @@ This frame's total (2711 kJ/mol) is a near-cancellation of terms of up to
 taken against the sum of the terms' magnitudes (231,552 kJ/mol), the scale
 at which each term is evaluated; the error against the total itself is
 printed.  Pair and trimer counts equal the reference's; the three-body term
-runs on the tensor cores here (181,901 trimers)."""
+runs on the tensor cores here (181,901 trimers).
+
+A second frame (tests/golden/box4096_md3000.npz: the same box after 3000 NVE
+MD steps of 0.2 fs from 300 K Maxwell-Boltzmann velocities, run by this
+package's MD driver; energies of the compiled reference, forces and dipoles
+of the oracle port) has a total of -72,836 kJ/mol, so the metric's energy bar
+applies to the total itself: 1e-6 of |E|."""
 import os
 
 import numpy as np
@@ -64,3 +70,26 @@ def test_box4096_induced_dipoles(frame):
     print("box4096 dipoles relrms %.2e, iterations %d (reference %d)" % (err, it, int(d["iterations"])))
     assert err <= 1e-4
     assert abs(it - int(d["iterations"])) <= 2
+
+
+def test_box4096_md_frame_total_energy():
+    d = np.load(os.path.join(GOLDEN, "box4096_md3000.npz"))
+    ws = systems.WaterSystem(d["positions"], d["box"], 0, "box4096")
+    s = mb.create_mbpol_system(ws, target_epsilon=1e-8, ewald_alpha=float(d["alpha"]),
+                               pme_grid=[int(v) for v in d["grid"]], ewald_tol=1e-5)
+    ctx = mb.Context(s)
+    ctx.setPositions(d["positions"])
+    st = ctx.getState()
+    e = np.array(st.term_energies)
+    ref = np.array([float(d[k]) for k in KEYS])
+    for k, v, r in zip(KEYS, e, ref):
+        print("  %-5s %.6f ref %.6f rel %.2e" % (k, v, r, abs(v - r) / abs(r)))
+    tot, tref = e.sum(), float(d["etotal"])
+    ferr = rel_rms(st.getForces(), d["ftotal"])
+    print("box4096 MD frame E %.6f ref %.6f | err/|E| %.2e | F relrms %.2e" % (tot, tref, abs(tot - tref) / abs(tref),
+                                                                          ferr))
+    assert abs(tot - tref) <= 1e-6 * abs(tref)
+    assert ferr <= 1e-4
+    c = ctx.getCounts()
+    assert c[0] == int(d["npairs"]) and c[1] == int(d["ntrip"])
+
