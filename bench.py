@@ -203,11 +203,21 @@ def md_context(args, guess, params=None, corr=None):
     _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), _capi.ptr(box)))
     _capi.check(lib.mbpol_set_masses(h, _capi.ptr(np.ascontiguousarray(masses))))
     _capi.check(lib.mbpol_set_velocities(h, _capi.ptr(np.ascontiguousarray(vel))))
+    # the autotuner measures its 12 candidate launch shapes (3 steps each)
+    # during the untimed equilibration steps
+    _capi.check(lib.mbpol_set_autotune(h, 3 if getattr(args, "autotune", True) and args.equilibrate >= 36 else 0))
     ms, iters, en = ctypes.c_double(), ctypes.c_long(), np.zeros(6)
     _capi.check(lib.mbpol_md_run(h, args.equilibrate + args.warmup, DT_PS, 0.0, 0.0, args.seed, ctypes.byref(ms),
                                  _capi.ptr(en), ctypes.byref(iters)))
     return {"ctx": ctx, "h": h, "ws": ws, "sysm": sysm, "alpha": alpha, "grid": grid, "box": box,
             "masses": masses, "n": pos.shape[0]}
+
+
+def launch_shape(lib, h):
+    """The polynomial kernels' launch shape in use (mbpol_get_launch_shape)."""
+    a, b, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib.mbpol_get_launch_shape(h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(t))
+    return {"tensor_kernel_free_sms": a.value, "walk_free_blocks": b.value, "autotuned": bool(t.value)}
 
 
 def md_steps(lib, h, nsteps, seed):
@@ -234,7 +244,8 @@ def arm(args, guess, params=None, corr=None):
     lib = _capi.load()
     c = md_context(args, guess, params, corr)
     step_s, it, _ = md_steps(lib, c["h"], args.steps, args.seed)
-    out = {"ns_per_day": ns_per_day(step_s), "ms_per_step": step_s * 1e3, "solver_iterations_per_step": it}
+    out = {"ns_per_day": ns_per_day(step_s), "ms_per_step": step_s * 1e3, "solver_iterations_per_step": it,
+           "launch_shape": launch_shape(lib, c["h"])}
     if args.avg_steps > 0:
         sl, itl, _ = md_steps(lib, c["h"], args.avg_steps, args.seed)
         out["long_run"] = {"steps": args.avg_steps, "ms_per_step": sl * 1e3, "ns_per_day": ns_per_day(sl),
@@ -288,6 +299,9 @@ def run_ours(args):
     ca = md_context(args, args.guess, gp, gc)
     cb = md_context(args, args.guess, gp, gc)
     h = ca["h"]
+    # both contexts run the shape the autotuner chose for the first
+    shape = launch_shape(lib, h)
+    _capi.check(lib.mbpol_set_launch_shape(cb["h"], shape["tensor_kernel_free_sms"], shape["walk_free_blocks"]))
     pa, va, _ = state(lib, h, ca["n"])
     pb, vb, _ = state(lib, cb["h"], cb["n"])
     same_start = float(max(np.abs(pa - pb).max(), np.abs(va - vb).max()))
@@ -345,6 +359,7 @@ def run_ours(args):
                 "steps": "the same %d steps as value, from the same state (max |dx| at start %.1e nm, at end %.1e nm)"
                          % (args.steps, same_start, same_end)},
         "gpu_launches": launches,
+        "launch_shape": shape,
         "solver_iterations_per_step": solver_it,
         "guess_comparison": arms,
         "correction_network": "committed (%s)" % os.path.relpath(CORRECTION_WEIGHTS % "box4096", ROOT)
@@ -575,17 +590,25 @@ def run_clusters(args):
     pos = np.ascontiguousarray(ws.positions, np.float64)
     e5 = np.zeros(5)
     forces = np.zeros((n, 3))
-    for _ in range(args.warmup):
+    # untimed: warm-up, then the autotuner's 12 candidate launch shapes (one
+    # evaluation each)
+    _capi.check(lib.mbpol_set_autotune(h, 1 if args.autotune else 0))
+    for _ in range(args.warmup + (12 if args.autotune else 0)):
         _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), None))
         _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
+    shape = launch_shape(lib, h)
     ts = []
-    lib.mbpol_profile_enable(1)
     for _ in range(args.steps):
         forces[:] = 0.0
         t0 = time.perf_counter()
         _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), None))
         _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
         ts.append(time.perf_counter() - t0)
+    # per-kernel event timers on further evaluations (they add launches)
+    lib.mbpol_profile_enable(1)
+    for _ in range(args.steps):
+        _capi.check(lib.mbpol_set_positions(h, _capi.ptr(pos), None))
+        _capi.check(lib.mbpol_compute(h, _capi.ALL_TERMS, _capi.ptr(e5), _capi.ptr(forces)))
     kern = {}
     for kid, kname in enumerate(_capi.KERNELS):
         t = ctypes.c_double()
@@ -602,7 +625,7 @@ def run_clusters(args):
             "dtype": "fp32+double-float polynomials, fp64 accumulation", "data": "synthetic (seeded clusters)",
             "config": {"workload": "clusters", "clusters": ncl, "waters": int(ws.num_waters),
                        "target_epsilon_D": 1e-8, "guess": "alpha*E (reference)" if args.guess == "learned" else args.guess,
-                       "seed": args.seed},
+                       "seed": args.seed, "launch_shape": shape},
             "e2e": {"value": ncl / step_s, "unit": "clusters/s", "h2d_bytes_per_step": int(n * 24),
                     "d2h_bytes_per_step": int(n * 24 + 40)},
             "solver_iterations": {"mean": float(its.mean()), "max": int(its.max())},
@@ -641,6 +664,8 @@ def main():
     ap.add_argument("--profile-window", type=int, default=0,
                     help="profiling run: the --guess arm's context after equilibration and warm-up, then this many "
                          "MD steps between cudaProfilerStart and cudaProfilerStop (for ncu --profile-from-start off)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="fixed default launch shapes instead of the autotuner's choice")
     ap.add_argument("--no-correction", action="store_true",
                     help="learned arm without its correction network (the history predictor alone)")
     ap.add_argument("--drift-steps", type=int, default=0, help="NVE steps after the timed region for the drift")

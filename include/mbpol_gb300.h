@@ -247,6 +247,24 @@ const char* mbpol_last_error(void);
 enum { MBPOL_POLY3B_TENSOR = 0, MBPOL_POLY3B_WALK = 1, MBPOL_POLY3B_AUTO = 2, MBPOL_POLY3B_TENSOR_SYNC = 3 };
 mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind);
 
+/* ---- Launch shapes and the autotuner -------------------------------------
+ * No reference counterpart.  The persistent polynomial kernels leave part of
+ * the GPU to the other streams (the electrostatics run beside them): the
+ * three-body tensor kernel `tc_reserve_sms` SMs (default 52), the
+ * double-float walks `walk_reserve_blocks` blocks of their grids (default
+ * 24).  Results do not depend on these shapes (each unit's arithmetic is the
+ * same on any grid); timing does, with the workload.
+ * mbpol_set_autotune(ctx, n): the next 12 n force evaluations (MD steps
+ *   included) time the candidate shapes (reserves 0/26/52/76 SMs x 0/24/48
+ *   blocks), n evaluations each, with CUDA events on the context's stream,
+ *   and keep the shape of the smallest median time; 0 turns tuning off.
+ * mbpol_set_launch_shape: a fixed shape (negative values: the defaults);
+ *   stops tuning.
+ * mbpol_get_launch_shape: the shape in use; *tuned = 1 once tuning ended. */
+mbpol_status mbpol_set_autotune(mbpol_context* ctx, int evaluations_per_shape);
+mbpol_status mbpol_set_launch_shape(mbpol_context* ctx, int tc_reserve_sms, int walk_reserve_blocks);
+mbpol_status mbpol_get_launch_shape(mbpol_context* ctx, int* tc_reserve_sms, int* walk_reserve_blocks, int* tuned);
+
 /* ---- White-box probes ------------------------------------------------------
  * The reference tests two protected functions of its electrostatics directly
  * (platforms/reference/tests/TestReferenceMBPolElectrostaticsForce.cpp):

@@ -33,7 +33,8 @@ EXPORTED = [
     "mbpol_guess_collect", "mbpol_guess_num_samples", "mbpol_guess_train", "mbpol_guess_get_params",
     "mbpol_guess_set_params", "mbpol_guess_descriptors", "mbpol_guess_loss_grad", "mbpol_guess_fit_predictor",
     "mbpol_set_clusters", "mbpol_get_cluster_results", "mbpol_set_threebody_evaluator",
-    "mbpol_probe_thole_inverse_rs", "mbpol_probe_water_charges",
+    "mbpol_probe_thole_inverse_rs", "mbpol_probe_water_charges", "mbpol_set_autotune", "mbpol_set_launch_shape",
+    "mbpol_get_launch_shape",
     "mbpol_guess_select_network", "mbpol_update_parameters",
 ]
 GUESS_BLOCK_FLOATS = 9033  # MBPOL_GUESS_BLOCK_FLOATS
@@ -121,6 +122,9 @@ def load(path=None):
         "mbpol_set_threebody_evaluator": (I, [P, I]),
         "mbpol_probe_thole_inverse_rs": (I, [D, D, D, D, P]),
         "mbpol_probe_water_charges": (I, [P, P, P]),
+        "mbpol_set_autotune": (I, [P, I]),
+        "mbpol_set_launch_shape": (I, [P, I, I]),
+        "mbpol_get_launch_shape": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]),
         "mbpol_guess_select_network": (I, [P, I]),
         "mbpol_update_parameters": (I, [P, ctypes.c_uint, I, P, P, P, P, P, P]),
         "mbpol_get_cluster_results": (I, [P, P, P]),

@@ -1,5 +1,6 @@
 // C-ABI implementation: context, buffers, orchestration of the MB-pol
 // kernels on one CUDA stream.  See include/mbpol_gb300.h for the contract.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -107,6 +108,30 @@ struct WaterTerm {
 
 using namespace mbpol;
 
+// Launch shape of the persistent polynomial kernels: SMs the three-body
+// tensor kernel leaves to the other streams, blocks the double-float walks
+// leave out of their grids.  Every unit's arithmetic is independent of the
+// grid, so the shape changes timing only.
+struct LaunchShape {
+    int tc_reserve = -1;    // negative: the kernel's default (52 SMs)
+    int walk_reserve = -1;  // negative: the walk's default (24 blocks)
+};
+
+// Project-written autotuner: over the next evaluations (each force
+// evaluation, inside MD steps too) it cycles through candidate launch
+// shapes, `reps` evaluations each, times each evaluation with CUDA events on
+// the context's stream (which joins every other stream), and keeps the
+// shape with the smallest median time.
+struct Autotuner {
+    int reps = 0;                        // 0: off
+    bool done = false;
+    size_t cand = 0;
+    std::vector<LaunchShape> cands;
+    std::vector<std::vector<float>> ms;  // [candidate][repetition]
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    bool timing = false;
+};
+
 struct mbpol_context {
     int N = 0;
     int device = 0;
@@ -134,6 +159,10 @@ struct mbpol_context {
     int poly3b_kind = MBPOL_POLY3B_AUTO;
     DevBuf ztc;
     DevBuf kstatus;  // int: nonzero when a bounded wait of the tcgen05 kernel gave up
+    // launch shapes of the persistent polynomial kernels (results do not
+    // depend on them) and the autotuner that picks them
+    LaunchShape shape;
+    Autotuner tuner;
     // dispersion buffers
     DevBuf full_d, nfull_d, lower_d, nlower_d;
     int cap_full_d = 0;
@@ -340,7 +369,7 @@ mbpol_status run_twobody(mbpol_context* ctx, double* energy, cudaStream_t ls, bo
                         ctx->x2.as<float>(), stride);
     prof_begin(ls, K_POLY2B);
     launch_poly2b(ls, ctx->walk, ctx->x2.as<float>(), ctx->g2.as<float>(), ctx->e2.as<float>(), np, stride,
-                  ctx->num_sms);
+                  ctx->num_sms, ctx->shape.walk_reserve);
     prof_end(ls, K_POLY2B);
     launch_twobody_forces(ls, np, ctx->p2.as<int2>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(), box,
                           ctx->g2.as<float>(), ctx->e2.as<float>(), stride, ctx->d_force.as<double>(), energy,
@@ -443,13 +472,13 @@ mbpol_status run_threebody(mbpol_context* ctx, double* energy, cudaStream_t ls, 
     prof_begin(ls, K_POLY3B);
     if (kind == MBPOL_POLY3B_TENSOR)
         launch_poly3b_tc5(ls, ctx->tc3, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip,
-                          stride, ctx->num_sms, ctx->ztc.as<float>(), ctx->kstatus.as<int>());
+                          stride, ctx->num_sms, ctx->ztc.as<float>(), ctx->kstatus.as<int>(), ctx->shape.tc_reserve);
     else if (kind == MBPOL_POLY3B_TENSOR_SYNC)
         launch_poly3b_tc(ls, ctx->tc3, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
-                         ctx->num_sms, ctx->ztc.as<float>());
+                         ctx->num_sms, ctx->ztc.as<float>(), ctx->shape.tc_reserve);
     else
         launch_poly3b(ls, ctx->walk, ctx->x3.as<float>(), ctx->g3.as<float>(), ctx->e3.as<float>(), ntrip, stride,
-                      ctx->num_sms);
+                      ctx->num_sms, ctx->shape.walk_reserve);
     prof_end(ls, K_POLY3B);
     launch_threebody_forces(ls, ntrip, ctx->trips3.as<int4>(), t.d_waters.as<int4>(), ctx->d_pos.as<double>(),
                             box, ctx->g3.as<float>(), ctx->e3.as<float>(), stride, ctx->d_force.as<double>(), energy,
@@ -631,6 +660,8 @@ mbpol_status mbpol_context_create(int num_particles, int device, mbpol_context**
     MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
     MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st_e, cudaStreamNonBlocking));
     MBPOL_CUDA_OK(cudaStreamCreateWithFlags(&ctx->st_a, cudaStreamNonBlocking));
+    MBPOL_CUDA_OK(cudaEventCreate(&ctx->tuner.t0));
+    MBPOL_CUDA_OK(cudaEventCreate(&ctx->tuner.t1));
     MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_pos, cudaEventDisableTiming));
     MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_elec, cudaEventDisableTiming));
     MBPOL_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_lists, cudaEventDisableTiming));
@@ -661,6 +692,8 @@ mbpol_status mbpol_context_destroy(mbpol_context* ctx) {
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev_pos) cudaEventDestroy(ctx->ev_pos);
+    if (ctx->tuner.t0) cudaEventDestroy(ctx->tuner.t0);
+    if (ctx->tuner.t1) cudaEventDestroy(ctx->tuner.t1);
     if (ctx->ev_elec) cudaEventDestroy(ctx->ev_elec);
     if (ctx->ev_lists) cudaEventDestroy(ctx->ev_lists);
     if (ctx->ev_aux) cudaEventDestroy(ctx->ev_aux);
@@ -817,7 +850,43 @@ mbpol_status check_kernel_status(mbpol_context* ctx) {
 // Evaluate the requested terms; forces and energies stay on the device
 // (d_force, d_energy).  Host synchronisation happens only for list sizes and
 // the solver's convergence test.
+mbpol_status compute_device_inner(mbpol_context* ctx, unsigned mask);
+
+// One evaluation, with the autotuner's bookkeeping while it measures.
 mbpol_status compute_device(mbpol_context* ctx, unsigned mask) {
+    Autotuner& T = ctx->tuner;
+    const bool tune = T.reps > 0 && !T.done && !T.cands.empty();
+    if (tune) {
+        ctx->shape = T.cands[T.cand];
+        MBPOL_CUDA_OK(cudaEventRecord(T.t0, ctx->st));
+    }
+    const mbpol_status s = compute_device_inner(ctx, mask);
+    if (tune && s == MBPOL_OK) {
+        MBPOL_CUDA_OK(cudaEventRecord(T.t1, ctx->st));
+        MBPOL_CUDA_OK(cudaEventSynchronize(T.t1));
+        float ms = 0.f;
+        MBPOL_CUDA_OK(cudaEventElapsedTime(&ms, T.t0, T.t1));
+        T.ms[T.cand].push_back(ms);
+        if ((int)T.ms[T.cand].size() >= T.reps && ++T.cand == T.cands.size()) {
+            size_t best = 0;
+            float best_ms = 0.f;
+            for (size_t c = 0; c < T.cands.size(); ++c) {
+                std::vector<float> v = T.ms[c];
+                std::sort(v.begin(), v.end());
+                const float med = v[v.size() / 2];
+                if (c == 0 || med < best_ms) {
+                    best = c;
+                    best_ms = med;
+                }
+            }
+            ctx->shape = T.cands[best];
+            T.done = true;
+        }
+    }
+    return s;
+}
+
+mbpol_status compute_device_inner(mbpol_context* ctx, unsigned mask) {
     if (ctx->vs_dirty) {
         MBPOL_CUDA_OK(ctx->d_vs_idx.ensure(sizeof(int4) * ctx->vs_idx.size()));
         MBPOL_CUDA_OK(ctx->d_vs_w.ensure(sizeof(double) * ctx->vs_w.size()));
@@ -1158,6 +1227,47 @@ mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind) {
         kind != MBPOL_POLY3B_TENSOR_SYNC)
         return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "unknown three-body evaluator");
     ctx->poly3b_kind = kind;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_set_autotune(mbpol_context* ctx, int evaluations_per_shape) {
+    if (!ctx || evaluations_per_shape < 0) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "bad autotune arguments");
+    Autotuner& T = ctx->tuner;
+    T.reps = evaluations_per_shape;
+    T.done = false;
+    T.cand = 0;
+    T.cands.clear();
+    T.ms.clear();
+    if (T.reps > 0) {
+        for (int tc : {0, 26, 52, 76})
+            for (int walk : {0, 24, 48}) {
+                LaunchShape sh;
+                sh.tc_reserve = tc;
+                sh.walk_reserve = walk;
+                T.cands.push_back(sh);
+            }
+        T.ms.resize(T.cands.size());
+    }
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_set_launch_shape(mbpol_context* ctx, int tc_reserve_sms, int walk_reserve_blocks) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (tc_reserve_sms >= ctx->num_sms || walk_reserve_blocks >= 3 * ctx->num_sms)
+        return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "reserve larger than the device");
+    ctx->tuner.reps = 0;
+    ctx->tuner.done = false;
+    ctx->shape.tc_reserve = tc_reserve_sms;
+    ctx->shape.walk_reserve = walk_reserve_blocks;
+    return MBPOL_OK;
+}
+
+mbpol_status mbpol_get_launch_shape(mbpol_context* ctx, int* tc_reserve_sms, int* walk_reserve_blocks, int* tuned) {
+    if (!ctx) return mbpol_fail(MBPOL_ERR_INVALID_ARGUMENT, "null context");
+    if (tc_reserve_sms) *tc_reserve_sms = ctx->shape.tc_reserve < 0 ? tc5_default_reserve() : ctx->shape.tc_reserve;
+    if (walk_reserve_blocks)
+        *walk_reserve_blocks = ctx->shape.walk_reserve < 0 ? walk_default_reserve() : ctx->shape.walk_reserve;
+    if (tuned) *tuned = ctx->tuner.done ? 1 : 0;
     return MBPOL_OK;
 }
 

@@ -31,15 +31,19 @@ void launch_threebody_forces(cudaStream_t st, int ntrip, const int4* trips, cons
 // `device` current, once per process; thread-safe)
 struct PolyWalkTables;
 cudaError_t poly_tables_upload(int device, const PolyWalkTables** out);
+// reserve_blocks: blocks left out of the persistent grid for the other
+// streams (negative: the default, walk_default_reserve())
+int walk_default_reserve();
 void launch_poly2b(cudaStream_t st, const PolyWalkTables* t, const float* X, float* G, float* E, int n, int stride,
-                   int num_sms);
+                   int num_sms, int reserve_blocks = -1);
 void launch_poly3b(cudaStream_t st, const PolyWalkTables* t, const float* X, float* G, float* E, int n, int stride,
-                   int num_sms);
+                   int num_sms, int reserve_blocks = -1);
 // the two-body kernel on caller-supplied device tables (raise its dynamic
 // shared-memory limit once per device with poly2b_kernel_setup first)
 cudaError_t poly2b_kernel_setup();
 void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, const PolyNode* l2, const PolyNode* l3,
-                        const PolyNode* lv, const float* X, float* G, float* E, int n, int stride, int num_sms);
+                        const PolyNode* lv, const float* X, float* G, float* E, int n, int stride, int num_sms,
+                        int reserve_blocks = -1);
 
 // neighbor.cu
 // opos: scratch of nw float4 (FP32 O positions for the distance prefilter)

@@ -426,9 +426,9 @@ constexpr int walk_smem() {
 }
 
 template <int NV>
-int walk_blocks(int n, int num_sms) {
+int walk_blocks(int n, int num_sms, int reserve_blocks) {
     int blocks = (n + kUnits - 1) / kUnits;
-    const int cap = num_sms * kBlocksPerSm - MBPOL_WALK_RESERVE_BLOCKS;
+    const int cap = num_sms * kBlocksPerSm - (reserve_blocks < 0 ? MBPOL_WALK_RESERVE_BLOCKS : reserve_blocks);
     if (blocks > cap) blocks = cap > num_sms ? cap : num_sms;
     return blocks;
 }
@@ -488,24 +488,27 @@ cudaError_t poly_tables_upload(int device, const PolyWalkTables** out) {
     return cudaSuccess;
 }
 
+int walk_default_reserve() { return MBPOL_WALK_RESERVE_BLOCKS; }
+
 void launch_poly2b_with(cudaStream_t st, const PolyNode* l1, const PolyNode* l2, const PolyNode* l3,
-                        const PolyNode* lv, const float* X, float* G, float* E, int n, int stride, int num_sms) {
+                        const PolyNode* lv, const float* X, float* G, float* E, int n, int stride, int num_sms,
+                        int reserve_blocks) {
     if (n <= 0) return;
     count_launch();
-    poly_df_kernel<31><<<walk_blocks<31>(n, num_sms), kBlock, walk_smem<31>(), st>>>(l1, l2, l3, POLY2B_N3, lv,
-                                                                                     split2(), X, G, E, n, stride);
+    poly_df_kernel<31><<<walk_blocks<31>(n, num_sms, reserve_blocks), kBlock, walk_smem<31>(), st>>>(
+        l1, l2, l3, POLY2B_N3, lv, split2(), X, G, E, n, stride);
 }
 
 void launch_poly2b(cudaStream_t st, const PolyWalkTables* t, const float* X, float* G, float* E, int n, int stride,
-                   int num_sms) {
-    launch_poly2b_with(st, t->t2.l1, t->t2.l2, t->t2.l3, t->t2.lv, X, G, E, n, stride, num_sms);
+                   int num_sms, int reserve_blocks) {
+    launch_poly2b_with(st, t->t2.l1, t->t2.l2, t->t2.l3, t->t2.lv, X, G, E, n, stride, num_sms, reserve_blocks);
 }
 
 void launch_poly3b(cudaStream_t st, const PolyWalkTables* t, const float* X, float* G, float* E, int n, int stride,
-                   int num_sms) {
+                   int num_sms, int reserve_blocks) {
     if (n <= 0) return;
     count_launch();
-    poly_df_kernel<36><<<walk_blocks<36>(n, num_sms), kBlock, walk_smem<36>(), st>>>(
+    poly_df_kernel<36><<<walk_blocks<36>(n, num_sms, reserve_blocks), kBlock, walk_smem<36>(), st>>>(
         t->t3.l1, t->t3.l2, t->t3.l3, POLY3B_N3, t->t3.lv, split3(), X, G, E, n, stride);
 }
 

@@ -323,11 +323,11 @@ cudaError_t poly_tc_setup(int device, const PolyTCDev** out) {
 size_t poly3b_tc_scratch_floats(int num_sms) { return (size_t)num_sms * 704 * kTU; }
 
 void launch_poly3b_tc(cudaStream_t st, const PolyTCDev* tab, const float* X, float* G, float* E, int n, int stride,
-                      int num_sms, float* zscratch) {
+                      int num_sms, float* zscratch, int reserve_sms) {
     if (n <= 0) return;
     count_launch();
     const int ntiles = (n + kTU - 1) / kTU;
-    int blocks = num_sms - MBPOL_TC_RESERVE_SMS;
+    int blocks = num_sms - (reserve_sms < 0 ? MBPOL_TC_RESERVE_SMS : reserve_sms);
     if (blocks < num_sms / 2) blocks = num_sms / 2;
     if (blocks > ntiles) blocks = ntiles;
     poly_tc_kernel<36, 704><<<blocks, kTThreads, Shape3::SMEM, st>>>(*tab, X, G, E, n, stride, zscratch);

@@ -478,12 +478,14 @@ size_t poly3b_tc5_scratch_floats(int num_sms) { return (size_t)num_sms * 2 * kNp
 #define MBPOL_TC5_RESERVE_SMS 52
 #endif
 
+int tc5_default_reserve() { return MBPOL_TC5_RESERVE_SMS; }
+
 void launch_poly3b_tc5(cudaStream_t st, const PolyTCDev* tab, const float* X, float* G, float* E, int n, int stride,
-                       int num_sms, float* zscratch, int* status) {
+                       int num_sms, float* zscratch, int* status, int reserve_sms) {
     if (n <= 0) return;
     count_launch();
     const int ntiles = (n + kU - 1) / kU;
-    int blocks = num_sms - MBPOL_TC5_RESERVE_SMS;
+    int blocks = num_sms - (reserve_sms < 0 ? MBPOL_TC5_RESERVE_SMS : reserve_sms);
     if (blocks < num_sms / 2) blocks = num_sms / 2;
     if (blocks > ntiles) blocks = ntiles;
     poly_tc5_kernel<<<blocks, kThreads, kSmem, st>>>(*tab, X, G, E, n, stride, zscratch, status);

@@ -29,15 +29,18 @@ struct PolyTCDev {
 cudaError_t poly_tc_setup(int device, const PolyTCDev** out);
 // scratch of the three-body launch (floats): one slice of z per block
 size_t poly3b_tc_scratch_floats(int num_sms);
+// reserve_sms: SMs left out of the persistent grid for the other streams
+// (negative: the default of each kernel)
 void launch_poly3b_tc(cudaStream_t st, const PolyTCDev* tab, const float* X, float* G, float* E, int n, int stride,
-                      int num_sms, float* zscratch);
+                      int num_sms, float* zscratch, int reserve_sms = -1);
 // The same evaluation with tcgen05.mma (poly_tc5.cu): Y' of 128 trimers in
 // tensor memory as the A operand, S streamed through shared memory as B.
 // `status` (device int, zero before the launch) receives a nonzero code if
 // one of the kernel's bounded waits gave up; the outputs are then invalid.
 cudaError_t poly_tc5_prepare();
 size_t poly3b_tc5_scratch_floats(int num_sms);
+int tc5_default_reserve();
 void launch_poly3b_tc5(cudaStream_t st, const PolyTCDev* tab, const float* X, float* G, float* E, int n, int stride,
-                       int num_sms, float* zscratch, int* status);
+                       int num_sms, float* zscratch, int* status, int reserve_sms = -1);
 
 }  // namespace mbpol

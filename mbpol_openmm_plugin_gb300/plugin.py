@@ -538,6 +538,29 @@ class Context:
         check(_capi.load().mbpol_get_counts(self._h, ptr(c)))
         return c
 
+    # ---- launch shapes of the polynomial kernels (this library's addition)
+    def setAutotune(self, evaluations_per_shape=3):
+        """Time the candidate launch shapes over the next 12 x n force
+        evaluations (MD steps included) and keep the fastest
+        (mbpol_set_autotune); 0 stops tuning."""
+        if self._h is None:
+            self._build()
+        check(_capi.load().mbpol_set_autotune(self._h, int(evaluations_per_shape)))
+
+    def setLaunchShape(self, tc_reserve_sms=-1, walk_reserve_blocks=-1):
+        if self._h is None:
+            self._build()
+        check(_capi.load().mbpol_set_launch_shape(self._h, int(tc_reserve_sms), int(walk_reserve_blocks)))
+
+    def getLaunchShape(self):
+        """(SMs the three-body tensor kernel leaves free, blocks the walks
+        leave out, whether the autotuner has finished)."""
+        if self._h is None:
+            self._build()
+        a, b, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(_capi.load().mbpol_get_launch_shape(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(t)))
+        return a.value, b.value, bool(t.value)
+
     # ---- batched independent clusters (this library's addition): one
     # context evaluates many water clusters that do not interact
     def setClusters(self, cluster_of_particle):
