@@ -1500,13 +1500,12 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                     }
                 }
             }
+            // atomics: the polynomial, one-body and dispersion kernels add to
+            // the same force array from other streams at the same time
             #pragma unroll
             for (int a = 0; a < kMaxK; ++a) {
                 if (a >= K) continue;
-                const int i = K * A + a;
-                force[3 * i] += (double)F[a][0] * f;
-                force[3 * i + 1] += (double)F[a][1] * f;
-                force[3 * i + 2] += (double)F[a][2] * f;
+                add_force(force, K * A + a, (double)F[a][0] * f, (double)F[a][1] * f, (double)F[a][2] * f);
             }
             e_out = e * kElectric;
             cluster_energy(cs, A, e_out);
