@@ -107,10 +107,18 @@ class MBPolThreeBodyForce : public CutoffWaterForce {
 public:
     void setTrimerRule(int r) { rule_ = r; }
     int getTrimerRule() const { return rule_; }
+    /* tensor cores (tcgen05; MBPOL_POLY3B_TENSOR_SYNC: mma.sync), the
+     * double-float walk, or the automatic choice by size (default); no
+     * reference counterpart (mbpol_set_threebody_evaluator) */
+    enum Evaluator { TensorCores = MBPOL_POLY3B_TENSOR, DoubleFloatWalk = MBPOL_POLY3B_WALK,
+                     AutomaticEvaluator = MBPOL_POLY3B_AUTO, TensorCoresMmaSync = MBPOL_POLY3B_TENSOR_SYNC };
+    void setPolynomialEvaluator(int kind) { evaluator_ = kind; }
+    int getPolynomialEvaluator() const { return evaluator_; }
     int term() const override { return MBPOL_TERM_THREEBODY; }
 
 private:
     int rule_ = MBPOL_TRIMER_REFERENCE;
+    int evaluator_ = MBPOL_POLY3B_AUTO;
 };
 
 class MBPolDispersionForce : public CutoffWaterForce {
@@ -260,6 +268,14 @@ public:
     }
     mbpol_context* handle() { return h_; }
     const System& getSystem() const { return sys_; }
+    /* launch shapes of the polynomial kernels: tune over the next 12 n
+     * evaluations, or read the shape in use (no reference counterpart) */
+    void setAutotune(int evaluationsPerShape) { mbpol_check(mbpol_set_autotune(h_, evaluationsPerShape)); }
+    void getLaunchShape(int& tcReserveSms, int& walkReserveBlocks, bool& tuned) {
+        int t = 0;
+        mbpol_check(mbpol_get_launch_shape(h_, &tcReserveSms, &walkReserveBlocks, &t));
+        tuned = t != 0;
+    }
 
 private:
     void add(const Force& f) {
@@ -279,9 +295,11 @@ private:
             mbpol_check(mbpol_add_onebody_force(h_, nw, flat.data(), o->getNonbondedMethod()));
         else if (auto* t2 = dynamic_cast<const MBPolTwoBodyForce*>(&f))
             mbpol_check(mbpol_add_twobody_force(h_, nw, flat.data(), t2->getNonbondedMethod(), t2->getCutoff()));
-        else if (auto* t3 = dynamic_cast<const MBPolThreeBodyForce*>(&f))
+        else if (auto* t3 = dynamic_cast<const MBPolThreeBodyForce*>(&f)) {
             mbpol_check(mbpol_add_threebody_force(h_, nw, flat.data(), t3->getNonbondedMethod(), t3->getCutoff(),
                                                   t3->getTrimerRule()));
+            mbpol_check(mbpol_set_threebody_evaluator(h_, t3->getPolynomialEvaluator()));
+        }
         else if (auto* d = dynamic_cast<const MBPolDispersionForce*>(&f))
             mbpol_check(mbpol_add_dispersion_force(h_, nw, flat.data(), d->getNonbondedMethod(), d->getCutoff(),
                                                    d->c6_.data(), d->d6_.data()));
