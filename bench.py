@@ -313,7 +313,10 @@ def run_ours(args):
     clocks = sampler.stop()
     e2e_s, pos_e2e = e2e_steps(lib, cb, args.steps)
     pos_dev, _, _ = state(lib, h, ca["n"])
-    same_end = float(np.abs(pos_dev - pos_e2e).max())
+    # atoms only: the host loop does not move the M sites, which the library
+    # places from their waters at every evaluation
+    atoms = ca["masses"] > 0
+    same_end = float(np.abs(pos_dev[atoms] - pos_e2e[atoms]).max())
     counts_timed = ca["ctx"].getCounts()
     # per-kernel CUDA-event timers on K further steps (the events add
     # launches, so the timed steps above run without them); unit counts from
@@ -356,7 +359,8 @@ def run_ours(args):
         "config": workload_config(args, ws, alpha, grid, params_src),
         "e2e": {"value": ns_per_day(e2e_s), "unit": "ns/day", "h2d_bytes_per_step": int(n * 24),
                 "d2h_bytes_per_step": int(n * 24 + 5 * 8),
-                "steps": "the same %d steps as value, from the same state (max |dx| at start %.1e nm, at end %.1e nm)"
+                "steps": "the same %d steps as value, from the same state (max |dx| at start %.1e nm, "
+                         "of the atoms at the end %.1e nm)"
                          % (args.steps, same_start, same_end)},
         "gpu_launches": launches,
         "launch_shape": shape,

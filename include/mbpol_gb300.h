@@ -255,7 +255,7 @@ mbpol_status mbpol_set_threebody_evaluator(mbpol_context* ctx, int kind);
  * 24).  Results do not depend on these shapes (each unit's arithmetic is the
  * same on any grid); timing does, with the workload.
  * mbpol_set_autotune(ctx, n): the next 12 n force evaluations (MD steps
- *   included) time the candidate shapes (reserves 0/26/52/76 SMs x 0/24/48
+ *   included) time the candidate shapes (reserves 0/26/52/76 SMs x 0/48/96
  *   blocks), n evaluations each, with CUDA events on the context's stream,
  *   and keep the shape of the smallest median time; 0 turns tuning off.
  * mbpol_set_launch_shape: a fixed shape (negative values: the defaults);

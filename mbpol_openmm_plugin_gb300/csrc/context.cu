@@ -935,8 +935,13 @@ mbpol_status compute_device_inner(mbpol_context* ctx, unsigned mask) {
         MBPOL_CUDA_OK(cudaStreamWaitEvent(ctx->st_a, ctx->ev_lists, 0));
     }
     if (!s && dod) s = run_dispersion(ctx, e + MBPOL_TERM_DISPERSION, ctx->st_a, false);
-    if (!s && do2) s = run_twobody(ctx, e + MBPOL_TERM_TWOBODY, ctx->st, false);
+    // the three-body term first: its tensor kernel holds one block on each of
+    // a fixed number of SMs and leaves whole SMs to the electrostatics, whose
+    // charges, neighbour list and fixed field then run beside it and reach
+    // the solver early; the two-body walk (blocks on every SM, minus the
+    // tuned reserve) follows and shares the GPU with the solver iterations
     if (!s && do3) s = run_threebody(ctx, e + MBPOL_TERM_THREEBODY, ctx->st, false);
+    if (!s && do2) s = run_twobody(ctx, e + MBPOL_TERM_TWOBODY, ctx->st, false);
     ctx->shared_lists = false;
     MBPOL_CUDA_OK(cudaEventRecord(ctx->ev_aux, ctx->st_a));
     if (!s && (mask & MBPOL_TERM_BIT(MBPOL_TERM_ELECTROSTATICS)) && ctx->elec) {
@@ -1240,7 +1245,7 @@ mbpol_status mbpol_set_autotune(mbpol_context* ctx, int evaluations_per_shape) {
     T.ms.clear();
     if (T.reps > 0) {
         for (int tc : {0, 26, 52, 76})
-            for (int walk : {0, 24, 48}) {
+            for (int walk : {0, 48, 96}) {
                 LaunchShape sh;
                 sh.tc_reserve = tc;
                 sh.walk_reserve = walk;

@@ -6,9 +6,15 @@
 // as an OpenMM CustomNonbondedForce (truncated at the nonbonded cutoff under
 // PME, no switching, no long-range correction).
 //
-// One thread per (water i, neighbour slot); only j > i is evaluated so each
-// water pair is visited once.  Chloride ions: dispersion_ions_kernel.  FP32 pair arithmetic from FP64 minimum-image
-// differences; FP64 force atomics and energy reduction.
+// One warp per water i: the lanes take i's listed neighbours j > i in turn
+// (each water pair once), keep i's forces in registers, summed over the warp
+// at the end, and add j's with atomics.  Site positions are taken relative to
+// each water's O (each H imaged next to its O in FP64, the O-O difference
+// minimum-imaged in FP64), so a site pair's difference is an FP32 sum of
+// three small vectors; a final FP32 minimum image makes it the per-site
+// minimum image of the force field's nonbonded force in any box of at least
+// twice the cutoff.  FP32 pair arithmetic; FP64 force atomics and energy
+// sums.  Chloride ions: dispersion_ions_kernel.
 #include "mbpol_internal.cuh"
 #include "mbpol_kernels.h"
 
@@ -17,71 +23,109 @@ namespace mbpol {
 __constant__ float c_disp_c6[16];  // [class_i * 4 + class_j], kJ/mol nm^6
 __constant__ float c_disp_d6[16];  // nm^-1
 
-__global__ void dispersion_kernel(int nw, const int4* __restrict__ waters, const double* __restrict__ pos, Box box,
-                                  const int* __restrict__ full, const int* __restrict__ nfull, int cap_full,
-                                  float rc2, double* __restrict__ force, double* __restrict__ energy,
-                                  ClusterSink cs) {
-    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = gid / cap_full, slot = gid - i * cap_full;
+constexpr int kDispBlock = 128;
+
+// r_h - r_o with h imaged next to o (FP64 difference, then FP32).
+__device__ __forceinline__ f3 site_offset(const double3 o, const double3 h, const Box& box) {
+    double dx = h.x - o.x, dy = h.y - o.y, dz = h.z - o.z;
+    if (box.periodic) {
+        dx = min_image(dx, box.L[0], box.inv[0]);
+        dy = min_image(dy, box.L[1], box.inv[1]);
+        dz = min_image(dz, box.L[2], box.inv[2]);
+    }
+    return mk((float)dx, (float)dy, (float)dz);
+}
+
+__device__ __forceinline__ float lane_sum(float v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float min_image_f(float d, float L, float invL) {
+    return d - L * floorf(d * invL + 0.5f);
+}
+
+__global__ void __launch_bounds__(kDispBlock) dispersion_kernel(
+    int nw, const int4* __restrict__ waters, const double* __restrict__ pos, Box box,
+    const int* __restrict__ full, const int* __restrict__ nfull, int cap_full, float rc2,
+    double* __restrict__ force, double* __restrict__ energy, ClusterSink cs) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     double e_out = 0.0;
-    if (i < nw && slot < min(nfull[i], cap_full)) {
-        const int j = full[(size_t)i * cap_full + slot];
-        if (j > i) {
-            const int4 wi = waters[i], wj = waters[j];
-            const int ai[3] = {wi.x, wi.y, wi.z}, aj[3] = {wj.x, wj.y, wj.z};
-            double3 pi[3], pj[3];
+    if (i < nw) {  // uniform over the warp
+        const float Lf[3] = {(float)box.L[0], (float)box.L[1], (float)box.L[2]};
+        const float iLf[3] = {(float)box.inv[0], (float)box.inv[1], (float)box.inv[2]};
+        const int4 wi = waters[i];
+        const int ai[3] = {wi.x, wi.y, wi.z};
+        const double3 oi = load_pos(pos, wi.x);
+        const f3 si[3] = {mk(0.f, 0.f, 0.f), site_offset(oi, load_pos(pos, wi.y), box),
+                          site_offset(oi, load_pos(pos, wi.z), box)};
+        f3 fi[3];
+        #pragma unroll
+        for (int a = 0; a < 3; ++a) fi[a] = mk(0.f, 0.f, 0.f);
+        const int n = min(nfull[i], cap_full);
+        for (int t = lane; t < n; t += 32) {
+            const int j = full[(size_t)i * cap_full + t];
+            if (j <= i) continue;
+            const int4 wj = waters[j];
+            const int aj[3] = {wj.x, wj.y, wj.z};
+            const double3 oj = load_pos(pos, wj.x);
+            const f3 dO = site_offset(oi, oj, box);
+            const f3 sj[3] = {mk(0.f, 0.f, 0.f), site_offset(oj, load_pos(pos, wj.y), box),
+                              site_offset(oj, load_pos(pos, wj.z), box)};
+            f3 fj[3];
             #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                pi[a] = load_pos(pos, ai[a]);
-                pj[a] = load_pos(pos, aj[a]);
-            }
-            f3 fi[3], fj[3];
-            #pragma unroll
-            for (int a = 0; a < 3; ++a) fi[a] = fj[a] = mk(0.f, 0.f, 0.f);
+            for (int b = 0; b < 3; ++b) fj[b] = mk(0.f, 0.f, 0.f);
             float e = 0.f;
             #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 #pragma unroll
                 for (int b = 0; b < 3; ++b) {
-                    double dx = pj[b].x - pi[a].x, dy = pj[b].y - pi[a].y, dz = pj[b].z - pi[a].z;
+                    f3 d = dO + sj[b] - si[a];  // r_jb - r_ia
                     if (box.periodic) {
-                        dx = min_image(dx, box.L[0], box.inv[0]);
-                        dy = min_image(dy, box.L[1], box.inv[1]);
-                        dz = min_image(dz, box.L[2], box.inv[2]);
+                        d.x = min_image_f(d.x, Lf[0], iLf[0]);
+                        d.y = min_image_f(d.y, Lf[1], iLf[1]);
+                        d.z = min_image_f(d.z, Lf[2], iLf[2]);
                     }
-                    f3 d = mk((float)dx, (float)dy, (float)dz);
-                    float r2 = dot(d, d);
+                    const float r2 = dot(d, d);
                     if (r2 > rc2) continue;
                     const int cls = (a == 0 ? 0 : 1) * 4 + (b == 0 ? 0 : 1);
                     const float c6 = c_disp_c6[cls], d6 = c_disp_d6[cls];
-                    float r = sqrtf(r2);
-                    float x = d6 * r;
-                    float ex = expf(-x);
+                    const float r = sqrtf(r2);
+                    const float x = d6 * r;
+                    const float ex = expf(-x);
                     // sum_{n<=6} x^n/n! by Horner
-                    float s6 = 1.f + x * (1.f + x * (0.5f + x * (1.f / 6.f + x * (1.f / 24.f + x * (1.f / 120.f + x * (1.f / 720.f))))));
-                    float tt = 1.f - ex * s6;
+                    const float s6 = 1.f + x * (1.f + x * (0.5f + x * (1.f / 6.f + x * (1.f / 24.f + x * (1.f / 120.f + x * (1.f / 720.f))))));
+                    const float tt = 1.f - ex * s6;
                     float x6 = x * x * x;
                     x6 *= x6;
-                    float dtt = d6 * ex * x6 * (1.f / 720.f);  // d tt6 / dr
-                    float ir2 = 1.f / r2, ir6 = ir2 * ir2 * ir2;
+                    const float dtt = d6 * ex * x6 * (1.f / 720.f);  // d tt6 / dr
+                    const float ir2 = 1.f / r2, ir6 = ir2 * ir2 * ir2;
                     e += -c6 * tt * ir6;
                     // dE/dr = -c6 (dtt r^-6 - 6 tt r^-7); force on j = -dE/dr * d/r
-                    float dEdr = -c6 * (dtt * ir6 - 6.f * tt * ir6 / r);
-                    f3 f = d * (-dEdr / r);
+                    const float dEdr = -c6 * (dtt * ir6 - 6.f * tt * ir6 / r);
+                    const f3 f = d * (-dEdr / r);
                     fj[b] += f;
                     fi[a] -= f;
                 }
             }
             #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                add_force(force, ai[a], fi[a].x, fi[a].y, fi[a].z);
-                add_force(force, aj[a], fj[a].x, fj[a].y, fj[a].z);
-            }
-            e_out = e;
-            cluster_energy(cs, i, e_out);
+            for (int b = 0; b < 3; ++b) add_force(force, aj[b], fj[b].x, fj[b].y, fj[b].z);
+            e_out += (double)e;
         }
+        #pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            fi[a].x = lane_sum(fi[a].x);
+            fi[a].y = lane_sum(fi[a].y);
+            fi[a].z = lane_sum(fi[a].z);
+        }
+        if (lane == 0)
+            #pragma unroll
+            for (int a = 0; a < 3; ++a) add_force(force, ai[a], fi[a].x, fi[a].y, fi[a].z);
+        cluster_energy(cs, i, e_out);
     }
-    block_sum_atomic<128>(e_out, energy);
+    block_sum_atomic<kDispBlock>(e_out, energy);
 }
 
 // Chloride ions (class CL = 3 of the tables, python/mbpol.xml:52-83): one
@@ -163,11 +207,11 @@ void launch_dispersion(cudaStream_t st, int nw, const int4* waters, const double
                        const int* nfull, int cap_full, double rc, double* force, double* energy,
                        ClusterSink cs) {
     if (nw <= 0 || cap_full <= 0) return;
-    const long total = (long)nw * cap_full;
     const float rc2 = rc > 1e15 ? 3.0e38f : (float)(rc * rc);
+    const int per_block = kDispBlock / 32;
     count_launch();
-    dispersion_kernel<<<(int)((total + 127) / 128), 128, 0, st>>>(nw, waters, pos, box, full, nfull, cap_full, rc2,
-                                                                   force, energy, cs);
+    dispersion_kernel<<<(nw + per_block - 1) / per_block, kDispBlock, 0, st>>>(nw, waters, pos, box, full, nfull,
+                                                                               cap_full, rc2, force, energy, cs);
 }
 
 }  // namespace mbpol
