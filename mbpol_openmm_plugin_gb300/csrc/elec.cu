@@ -1282,6 +1282,8 @@ __device__ __forceinline__ DFe dfe_rinv(const f3& d) {
 // list (force on A's sites, half the pair energy), intramolecular pairs, the
 // reciprocal and self parts, and the charge-derivative forces through the
 // total potential at A's H1, H2, M sites.
+constexpr int kEFWarps = 4;  // energy_force_kernel: 128 threads, one warp per molecule
+static_assert(kMaxK == 4, "energy_force_kernel packs site indices in two bits");
 template <bool PME>
 __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ q,
                                     const float* __restrict__ dq, const float* __restrict__ damp,
@@ -1290,26 +1292,29 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
                                     const float* __restrict__ mu, const float* __restrict__ phi_fix,
                                     const float* __restrict__ phi_mu, int redist, double* __restrict__ force,
                                     double* __restrict__ energy, ClusterSink cs) {
+    // per warp: the queue of site pairs within the cutoff of the current 32
+    // neighbours (source lane << 4 | a << 2 | b), those neighbours' index and
+    // O-O vector, and A's sites
+    __shared__ unsigned short s_item[kEFWarps][32 * kMaxK * kMaxK];
+    __shared__ int s_nbB[kEFWarps][32];
+    __shared__ float s_nbd[kEFWarps][32][3];
+    __shared__ float s_site[kEFWarps][kMaxK][8];  // off xyz, mu xyz, q, damp
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     double e_out = 0.0;
     if (A < nmol) {
         const int K = c_el.K;
         const float f = (float)kElectric;
-        f3 offA[kMaxK], muA[kMaxK];
-        float qA[kMaxK], dA[kMaxK];
-        int tA[kMaxK];
-        #pragma unroll
-        for (int a = 0; a < kMaxK; ++a) {
-            if (a < K) {
-                const int i = K * A + a;
-                offA[a] = ld3(off, i);
-                muA[a] = ld3(mu, i);
-                qA[a] = q[i];
-                dA[a] = damp[i];
-                tA[a] = type[i];
-            }
+        if (lane < K) {
+            const int i = K * A + lane;
+            const f3 o = ld3(off, i), m = ld3(mu, i);
+            float* sa = s_site[wid][lane];
+            sa[0] = o.x; sa[1] = o.y; sa[2] = o.z;
+            sa[3] = m.x; sa[4] = m.y; sa[5] = m.z;
+            sa[6] = q[i];
+            sa[7] = damp[i];
         }
+        __syncwarp();
         float F[kMaxK][3], P[kMaxK];  // force on A's sites (before * f), potential (for dq terms)
         #pragma unroll
         for (int a = 0; a < kMaxK; ++a) F[a][0] = F[a][1] = F[a][2] = P[a] = 0.f;
@@ -1318,88 +1323,133 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
         DFe el = {0.f, 0.f};
         const int n = min(nnb[A], cap);
         const float gcc = c_el.thole[0], gcd = c_el.thole[1], gdd = c_el.thole[2];
-        for (int t = lane; t < n; t += 32) {
-            const int B = nb[(size_t)A * cap + t];
-            const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
+        for (int t0 = 0; t0 < n; t0 += 32) {
+            // 1. each lane tests the site pairs of its neighbour against the
+            //    cutoff and queues those inside it
+            const int t = t0 + lane;
+            unsigned msk = 0;
+            if (t < n) {
+                const int B = nb[(size_t)A * cap + t];
+                const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
+                s_nbB[wid][lane] = B;
+                s_nbd[wid][lane][0] = dAB.x;
+                s_nbd[wid][lane][1] = dAB.y;
+                s_nbd[wid][lane][2] = dAB.z;
+                #pragma unroll
+                for (int b = 0; b < kMaxK; ++b) {
+                    if (b >= K) continue;
+                    const f3 offb = ld3(off, K * B + b);
+                    #pragma unroll
+                    for (int a = 0; a < kMaxK; ++a) {
+                        if (a >= K) continue;
+                        const f3 offa = mk(s_site[wid][a][0], s_site[wid][a][1], s_site[wid][a][2]);
+                        const f3 d = site_delta(dAB, offb, offa);
+                        if (!PME || dot(d, d) <= c_el.rc2) msk |= 1u << (a * kMaxK + b);
+                    }
+                }
+            }
+            const int cnt = __popc(msk);
+            int incl = cnt;
             #pragma unroll
-            for (int b = 0; b < kMaxK; ++b) {
-                if (b >= K) continue;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            int pos = incl - cnt;
+            while (msk) {
+                const int bit = __ffs(msk) - 1;
+                msk &= msk - 1;
+                s_item[wid][pos++] = (unsigned short)((lane << 4) | bit);
+            }
+            __syncwarp();
+            // 2. the warp evaluates the queued pairs, 32 at a time
+            for (int g = lane; g < total; g += 32) {
+                const unsigned item = s_item[wid][g];
+                const int src = item >> 4, a = (item >> 2) & 3, b = item & 3;
+                const int B = s_nbB[wid][src];
+                const f3 dAB = mk(s_nbd[wid][src][0], s_nbd[wid][src][1], s_nbd[wid][src][2]);
+                const float* sa = s_site[wid][a];
+                const f3 offa = mk(sa[0], sa[1], sa[2]), mua = mk(sa[3], sa[4], sa[5]);
+                const float qa = sa[6], da = sa[7];
                 const int jb = K * B + b;
                 const f3 offb = ld3(off, jb), mub = ld3(mu, jb);
                 const float qb = q[jb], db = damp[jb];
-                #pragma unroll
-                for (int a = 0; a < kMaxK; ++a) {
-                    if (a >= K) continue;
-                    const f3 d = site_delta(dAB, offb, offA[a]);  // r_b - r_a  (A = i, B = j)
-                    const float r2 = dot(d, d);
-                    if (PME && r2 > c_el.rc2) continue;
-                    const float r = sqrtf(r2);
-                    const float rr1 = 1.f / r, rr3 = rr1 / r2, rr5 = 3.f * rr3 / r2, rr7 = 5.f * rr5 / r2;
-                    const float dprod = dA[a] * db;
-                    const float sci3 = dot(muA[a], d), sci4 = dot(mub, d), mumu = dot(muA[a], mub);
-                    const float gl0 = qA[a] * qb;
-                    const float gli = qb * sci3 - qA[a] * sci4;
-                    const Thole tCC = thole(r, dprod, gcc), tCD = thole(r, dprod, gcd), tDD = thole(r, dprod, gdd);
-                    f3 fo;
-                    if (PME) {
-                        const Bn bn = ewald_bn(r, r2);
-                        const float s1CC = gl0 != 0.f || qb != 0.f ? s1_of(tCC, gcc) : 1.f;
-                        const float s3CD = s3_of(tCD);
-                        {
-                            // bn0 and bn1 are FP32 (~1e-7), which bounds each term; the
-                            // terms are formed in FP32 and summed in double-float
-                            const float pe = 0.5f * (bn.b0 * gl0 + 0.5f * bn.b1 * gli -
-                                                     rr1 * gl0 * (1.f - s1CC) - 0.5f * rr3 * gli * (1.f - s3CD));
-                            dfe_acc(el, pe, 0.f);
-                        }
-                        P[a] += qb * (bn.b0 - rr1 * (1.f - s1CC)) - sci4 * (bn.b1 - rr3 * (1.f - s3CD));
-                        const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
-                        const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
-                        const float gf1 = bn.b1 * gl0, gfr1 = (1.f - s3CC) * rr3 * gl0;
-                        const float gfi1 = bn.b2 * (gli + mumu) - bn.b3 * sci3 * sci4;
-                        const float gfri1 = rr5 * (gli * (1.f - s5CD) + mumu * (1.f - s5DD)) -
-                                            rr7 * sci3 * sci4 * (1.f - s7DD);
-                        const float c_d = gf1 - gfr1 + gfi1 - gfri1;
-                        const float c_i = -qb * bn.b1 - (-qb) * rr3 * (1.f - s3CD);  // mu_i coefficient
-                        const float c_j = qA[a] * bn.b1 - qA[a] * rr3 * (1.f - s3CD);
-                        const float c_dd = bn.b2 - rr5 * (1.f - s5DD);
-                        fo = d * c_d + muA[a] * (c_i + sci4 * c_dd) + mub * (c_j + sci3 * c_dd);
-                    } else {
-                        const float s1CC = s1_of(tCC, gcc), s3CD = s3_of(tCD);
-                        {
-                            // no cutoff: the charge-charge and charge-dipole terms of a
-                            // pair of neutral waters cancel to ~1e-3 of their size, so
-                            // 1/r, the products and the dot products are double-float
-                            const DFe r1 = dfe_rinv(d);
-                            const DFe r3 = dfe_mul(dfe_mul(r1, r1), r1);
-                            const DFe cc = dfe_mulf(dfe_mul(dfe_prod(qA[a], qb), r1), 0.5f * s1CC);
-                            DFe glid = dfe_mulf(dfe_dot(muA[a], d), qb);
-                            const DFe t2 = dfe_mulf(dfe_dot(mub, d), -qA[a]);
-                            dfe_acc(glid, t2.h, t2.l);
-                            const DFe cd = dfe_mulf(dfe_mul(glid, r3), 0.25f * s3CD);
-                            dfe_acc(el, cc.h, cc.l);
-                            dfe_acc(el, cd.h, cd.l);
-                        }
-                        const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
-                        const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
-                        const float gf0 = rr3 * gl0 * s3CC;
-                        const float gfi0 = rr5 * gli * s5CD + rr5 * mumu * s5DD - rr7 * sci3 * sci4 * s7DD;
-                        fo = d * (gf0 + gfi0) + (muA[a] * sci4 + mub * sci3) * (rr5 * s5DD) +
-                             (mub * qA[a] - muA[a] * qb) * (rr3 * s3CD);
-                        if (redist) {
-                            // potential at A's site from B's site, TCC scaling for both
-                            // terms (reference :808-827)
-                            const float sc3 = s3_of(tCC);
-                            const float sc1 = s1_of(tCC, gcc);
-                            P[a] += qb * sc1 * rr1 - sc3 * sci4 * rr3;
-                        }
+                const f3 d = site_delta(dAB, offb, offa);  // r_b - r_a  (A = i, B = j)
+                const float r2 = dot(d, d);
+                const float r = sqrtf(r2);
+                const float rr1 = 1.f / r, rr3 = rr1 / r2, rr5 = 3.f * rr3 / r2, rr7 = 5.f * rr5 / r2;
+                const float dprod = da * db;
+                const float sci3 = dot(mua, d), sci4 = dot(mub, d), mumu = dot(mua, mub);
+                const float gl0 = qa * qb;
+                const float gli = qb * sci3 - qa * sci4;
+                const Thole tCC = thole(r, dprod, gcc), tCD = thole(r, dprod, gcd), tDD = thole(r, dprod, gdd);
+                f3 fo;
+                float pa = 0.f;  // potential at site a from site b (charge-derivative forces)
+                if (PME) {
+                    const Bn bn = ewald_bn(r, r2);
+                    const float s1CC = gl0 != 0.f || qb != 0.f ? s1_of(tCC, gcc) : 1.f;
+                    const float s3CD = s3_of(tCD);
+                    {
+                        // bn0 and bn1 are FP32 (~1e-7), which bounds each term; the
+                        // terms are formed in FP32 and summed in double-float
+                        const float pe = 0.5f * (bn.b0 * gl0 + 0.5f * bn.b1 * gli -
+                                                 rr1 * gl0 * (1.f - s1CC) - 0.5f * rr3 * gli * (1.f - s3CD));
+                        dfe_acc(el, pe, 0.f);
                     }
-                    // force on site a of A: -force(i, j)
-                    F[a][0] -= fo.x;
-                    F[a][1] -= fo.y;
-                    F[a][2] -= fo.z;
+                    pa = qb * (bn.b0 - rr1 * (1.f - s1CC)) - sci4 * (bn.b1 - rr3 * (1.f - s3CD));
+                    const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
+                    const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
+                    const float gf1 = bn.b1 * gl0, gfr1 = (1.f - s3CC) * rr3 * gl0;
+                    const float gfi1 = bn.b2 * (gli + mumu) - bn.b3 * sci3 * sci4;
+                    const float gfri1 = rr5 * (gli * (1.f - s5CD) + mumu * (1.f - s5DD)) -
+                                        rr7 * sci3 * sci4 * (1.f - s7DD);
+                    const float c_d = gf1 - gfr1 + gfi1 - gfri1;
+                    const float c_i = -qb * bn.b1 - (-qb) * rr3 * (1.f - s3CD);  // mu_i coefficient
+                    const float c_j = qa * bn.b1 - qa * rr3 * (1.f - s3CD);
+                    const float c_dd = bn.b2 - rr5 * (1.f - s5DD);
+                    fo = d * c_d + mua * (c_i + sci4 * c_dd) + mub * (c_j + sci3 * c_dd);
+                } else {
+                    const float s1CC = s1_of(tCC, gcc), s3CD = s3_of(tCD);
+                    {
+                        // no cutoff: the charge-charge and charge-dipole terms of a
+                        // pair of neutral waters cancel to ~1e-3 of their size, so
+                        // 1/r, the products and the dot products are double-float
+                        const DFe r1 = dfe_rinv(d);
+                        const DFe r3 = dfe_mul(dfe_mul(r1, r1), r1);
+                        const DFe cc = dfe_mulf(dfe_mul(dfe_prod(qa, qb), r1), 0.5f * s1CC);
+                        DFe glid = dfe_mulf(dfe_dot(mua, d), qb);
+                        const DFe t2 = dfe_mulf(dfe_dot(mub, d), -qa);
+                        dfe_acc(glid, t2.h, t2.l);
+                        const DFe cd = dfe_mulf(dfe_mul(glid, r3), 0.25f * s3CD);
+                        dfe_acc(el, cc.h, cc.l);
+                        dfe_acc(el, cd.h, cd.l);
+                    }
+                    const float s3CC = s3_of(tCC), s5CD = s5_of(tCD);
+                    const float s5DD = s5_of(tDD), s7DD = s7_of(tDD, gdd);
+                    const float gf0 = rr3 * gl0 * s3CC;
+                    const float gfi0 = rr5 * gli * s5CD + rr5 * mumu * s5DD - rr7 * sci3 * sci4 * s7DD;
+                    fo = d * (gf0 + gfi0) + (mua * sci4 + mub * sci3) * (rr5 * s5DD) +
+                         (mub * qa - mua * qb) * (rr3 * s3CD);
+                    if (redist) {
+                        // potential at A's site from B's site, TCC scaling for both
+                        // terms (reference :808-827)
+                        const float sc3 = s3_of(tCC);
+                        const float sc1 = s1_of(tCC, gcc);
+                        pa = qb * sc1 * rr1 - sc3 * sci4 * rr3;
+                    }
                 }
+                // force on site a of A: -force(i, j)
+                #pragma unroll
+                for (int k = 0; k < kMaxK; ++k)
+                    if (k == a) {
+                        F[k][0] -= fo.x;
+                        F[k][1] -= fo.y;
+                        F[k][2] -= fo.z;
+                        P[k] += pa;
+                    }
             }
+            __syncwarp();
         }
         double e = (double)el.h + (double)el.l;
         #pragma unroll
@@ -1412,6 +1462,20 @@ __global__ void energy_force_kernel(int nmol, const float* __restrict__ off, con
             P[a] = warp_sum(P[a]);
         }
         if (lane == 0) {
+            f3 offA[kMaxK], muA[kMaxK];
+            float qA[kMaxK], dA[kMaxK];
+            int tA[kMaxK];
+            #pragma unroll
+            for (int a = 0; a < kMaxK; ++a) {
+                if (a < K) {
+                    const int i = K * A + a;
+                    offA[a] = ld3(off, i);
+                    muA[a] = ld3(mu, i);
+                    qA[a] = q[i];
+                    dA[a] = damp[i];
+                    tA[a] = type[i];
+                }
+            }
             // intramolecular pairs, a < b (both sites are A's)
             #pragma unroll
             for (int a = 0; a < kMaxK; ++a)
