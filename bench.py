@@ -439,10 +439,10 @@ def tc_flop_per_trimer():
 
 
 def rooflines(kern, counts, grid, n, clocks):
-    """The dominant polynomial kernel by measured time: the three-body
-    kernel against the measured tensor-core rate (executed tcgen05 work),
+    """The top kernel of the step's launch list, the three-body tensor
+    kernel, against the measured tensor-core rate (executed tcgen05 work),
     with the FP32 view of the reference's operation count beside it; the
-    two-body walk against the FP32 pipe.  The memory-bound
+    two-body walk (nested) against the FP32 pipe.  The memory-bound
     electrostatics passes against the measured HBM copy rate (algorithmic
     bytes as in the reference's operation counts: pair index 4 B + cached
     pair coefficients 8 B per polarisable site pair within the cutoff, 36 B
@@ -456,36 +456,46 @@ def rooflines(kern, counts, grid, n, clocks):
     for name, cidx in (("poly3b", 1), ("poly2b", 0)):
         if kern[name]["launches"]:
             per[name] = (kern[name]["total_ms"] / kern[name]["launches"], int(counts[cidx]))
-    roof = None
-    if per:
-        dom = max(per, key=lambda k: per[k][0])
-        ms, units = per[dom]
-        algo = ALGO_FLOP_PER_UNIT[dom]
+
+    def poly_roof(name):
+        ms, units = per[name]
+        algo = ALGO_FLOP_PER_UNIT[name]
         fp32_view = {"achieved": units * algo / (ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": units * algo / (ms * 1e-3) / 1e12 / fp32_peak,
                      "work": "%d units x %d algorithmic flop (reference operation count)" % (units, algo),
                      "peak_kind": "nominal FP32 rate at the median sampled SM clock (152 SM x 128 lanes x 2); "
                                   "MEASURED_PEAKS.json has no FP32 figure"}
-        common = {"kernel": dom, "traffic": NCU_TRAFFIC[dom][0] * units / NCU_TRAFFIC[dom][1],
+        common = {"kernel": name, "traffic": NCU_TRAFFIC[name][0] * units / NCU_TRAFFIC[name][1],
                   "traffic_note": "DRAM bytes per launch from one ncu capture of this kernel (profiles/), scaled by "
                                   "units", "launch_ms": ms, "per_kernel_ms": {k: v[0] for k, v in per.items()}}
-        if dom == "poly3b":
+        if name == "poly3b":
             # the three-body kernel runs on the tensor cores: executed tcgen05
             # work against the measured dense fp16/bf16 rate
             tc = units * tc_flop_per_trimer() / (ms * 1e-3) / 1e12
             bf16 = measured_peak("bf16_tflops", 1905.0)
-            roof = {"bound": "tensor", "achieved": tc, "peak": bf16[0], "unit": "TFLOP/s", "frac": tc / bf16[0],
-                    "work": "executed tcgen05.mma (M128 N64 K16) flop: %.0f per trimer x %d trimers" % (
-                        tc_flop_per_trimer(), units),
-                    "peak_kind": bf16[1] + " (dense bf16; fp16 runs at the same rate)",
-                    "fp32_algorithmic_view": fp32_view}
+            r = {"bound": "tensor", "achieved": tc, "peak": bf16[0], "unit": "TFLOP/s", "frac": tc / bf16[0],
+                 "work": "executed tcgen05.mma (M128 N64 K16) flop: %.0f per trimer x %d trimers" % (
+                     tc_flop_per_trimer(), units),
+                 "peak_kind": bf16[1] + " (dense bf16; fp16 runs at the same rate)",
+                 "fp32_algorithmic_view": fp32_view}
         else:
             # the two-body double-float walk runs on the FP32 pipe
-            roof = dict(fp32_view, bound="fp32")
-        roof.update(common)
+            r = dict(fp32_view, bound="fp32")
+        r.update(common)
+        return r
+
+    roof = None
+    secondary = {}
+    if per:
+        # the top kernel of the step's ncu launch list (the three-body tensor
+        # kernel on box4096); inside the step the walk's event time can be the
+        # longer of the two, because the solver iterations share its SMs
+        dom = "poly3b" if "poly3b" in per else "poly2b"
+        roof = poly_roof(dom)
+        if dom == "poly3b" and "poly2b" in per:
+            roof["two_body_walk"] = poly_roof("poly2b")
     hbm = measured_hbm_gbs()
     nsites = 3 * (n // 4)
-    secondary = {}
     if kern["elec_direct_field"]["launches"] and counts[2] > 0:
         t = kern["elec_direct_field"]["total_ms"] / kern["elec_direct_field"]["launches"] * 1e-3
         b = 12 * int(counts[2]) + 36 * nsites

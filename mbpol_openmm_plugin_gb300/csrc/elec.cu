@@ -757,6 +757,7 @@ __device__ __forceinline__ int intra_pair(int a, int b, int K) {
 // Thole parameters; with PME the reciprocal-space part is taken out and
 // pairs beyond the cutoff get zeros).  They are used by every solver
 // iteration, so the Thole and Ewald functions of these pairs run once.
+constexpr int kFFWarps = 4;  // fixed_field_kernel: 128 threads, one warp per molecule
 template <bool PME>
 __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, const float* __restrict__ q,
                                    const float* __restrict__ damp, const float* __restrict__ pol,
@@ -765,12 +766,30 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
                                    const float* __restrict__ phi_fix, float* __restrict__ E0,
                                    float* __restrict__ mu_out, float* __restrict__ intra,
                                    float* __restrict__ pcoef, unsigned long long* __restrict__ npair) {
+    // per warp: the queue of the current 32 neighbours' site pairs within the
+    // cutoff (source lane << 5 | kind << 4 | a << 2 | b; kind 0: both sites
+    // polarisable, dipole-field coefficients; kind 1: charge field), the
+    // neighbours' index and O-O vector, and A's site offsets and damping
+    __shared__ unsigned short s_item[kFFWarps][32 * 2 * kMaxK * kMaxK];
+    __shared__ int s_nbB[kFFWarps][32];
+    __shared__ float s_nbd[kFFWarps][32][3];
+    __shared__ float s_site[kFFWarps][kMaxK][8];  // off xyz, damp, pol
     const int A = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (A >= nmol) return;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (A >= nmol) return;  // uniform over the warp
     const int K = c_el.K;
     MolSites MA;
     load_mol(A, off, q, damp, pol, type, MA);
+    if (lane < K) {
+        const int i = K * A + lane;
+        const f3 o = ld3(off, i);
+        s_site[wid][lane][0] = o.x;
+        s_site[wid][lane][1] = o.y;
+        s_site[wid][lane][2] = o.z;
+        s_site[wid][lane][3] = damp[i];
+        s_site[wid][lane][4] = pol[i];
+    }
+    __syncwarp();
     #pragma unroll
     for (int a = 0; a < kMaxK; ++a)
     #pragma unroll
@@ -800,55 +819,107 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
     #pragma unroll
     for (int a = 0; a < kMaxK; ++a) E[a][0] = E[a][1] = E[a][2] = 0.f;
     const int n = min(nnb[A], cap);
-    const float gcc = c_el.thole[0];
+    const float gcc = c_el.thole[0], gdd = c_el.thole[2];
     unsigned npol = 0;  // polarisable site pairs within the cutoff
-    for (int t = lane; t < n; t += 32) {
-        const int B = nb[(size_t)A * cap + t];
-        const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
-        MolSites MB;
-        load_mol(B, off, q, damp, pol, type, MB);
-        // dipole-dipole field coefficients of this geometry for the solver
-        // iterations (layout of pair_coef_index); pairs with an unpolarizable
-        // site are never read and not written
-        #pragma unroll
-        for (int a = 0; a < kMaxK; ++a) {
-            if (a >= K || MA.pol[a] == 0.f) continue;
+    for (int t0 = 0; t0 < n; t0 += 32) {
+        // 1. each lane tests the site pairs of its neighbour: polarisable
+        //    pairs within the cutoff and charge pairs within the cutoff are
+        //    queued; polarisable pairs beyond it get zero coefficients (pairs
+        //    with an unpolarisable site are never read and not written)
+        const int t = t0 + lane;
+        unsigned mpol = 0, mq = 0;
+        if (t < n) {
+            const int B = nb[(size_t)A * cap + t];
+            const f3 dAB = ld3(nbd, (int)((size_t)A * cap + t));
+            s_nbB[wid][lane] = B;
+            s_nbd[wid][lane][0] = dAB.x;
+            s_nbd[wid][lane][1] = dAB.y;
+            s_nbd[wid][lane][2] = dAB.z;
             #pragma unroll
             for (int b = 0; b < kMaxK; ++b) {
-                if (b >= K || MB.pol[b] == 0.f) continue;
-                const f3 d = site_delta(dAB, MB.off[b], MA.off[a]);
-                const float r2 = dot(d, d);
-                float pf1 = 0.f, pf2 = 0.f;
-                if (!PME || r2 <= c_el.rc2) {
-                    ++npol;
-                    const float r = sqrtf(r2);
-                    const Thole th = thole(r, MA.damp[a] * MB.damp[b], c_el.thole[2]);
-                    if (PME) {
-                        const Bn bn = ewald_bn(r, r2);
-                        const float rr3 = (1.f - s3_of(th)) / (r2 * r);
-                        const float rr5 = 3.f * (1.f - s5_of(th)) / (r2 * r2 * r);
-                        pf1 = rr3 - bn.b1;
-                        pf2 = bn.b2 - rr5;
-                    } else {
-                        pf1 = -s3_of(th) / (r2 * r);
-                        pf2 = 3.f * s5_of(th) / (r2 * r2 * r);
+                if (b >= K) continue;
+                const int jb = K * B + b;
+                const f3 offb = ld3(off, jb);
+                const bool polb = pol[jb] != 0.f, qb = q[jb] != 0.f;
+                #pragma unroll
+                for (int a = 0; a < kMaxK; ++a) {
+                    if (a >= K) continue;
+                    const f3 offa = mk(s_site[wid][a][0], s_site[wid][a][1], s_site[wid][a][2]);
+                    const f3 d = site_delta(dAB, offb, offa);
+                    const bool in = !PME || dot(d, d) <= c_el.rc2;
+                    if (polb && s_site[wid][a][4] != 0.f) {
+                        if (in) {
+                            mpol |= 1u << (a * kMaxK + b);
+                        } else {
+                            pcoef[pair_coef_index(A, a, b, 0, t, cap)] = 0.f;
+                            pcoef[pair_coef_index(A, a, b, 1, t, cap)] = 0.f;
+                        }
                     }
+                    if (qb && in) mq |= 1u << (a * kMaxK + b);
                 }
-                pcoef[pair_coef_index(A, a, b, 0, t, cap)] = pf1;
-                pcoef[pair_coef_index(A, a, b, 1, t, cap)] = pf2;
             }
         }
+        // polarisable items first, then charge items, so that at most one
+        // round of the evaluation mixes the two kinds
+        const int cp = __popc(mpol), cq = __popc(mq);
+        int ip = cp, iq = cq;
         #pragma unroll
-        for (int a = 0; a < kMaxK; ++a) {
-            if (a >= K) continue;
-            #pragma unroll
-            for (int b = 0; b < kMaxK; ++b) {
-                if (b >= K || MB.q[b] == 0.f) continue;
-                const f3 d = site_delta(dAB, MB.off[b], MA.off[a]);  // r_b - r_a
-                const float r2 = dot(d, d);
-                if (PME && r2 > c_el.rc2) continue;
-                const float r = sqrtf(r2);
-                const Thole th = thole(r, MA.damp[a] * MB.damp[b], gcc);
+        for (int o = 1; o < 32; o <<= 1) {
+            const int vp = __shfl_up_sync(0xffffffffu, ip, o);
+            const int vq = __shfl_up_sync(0xffffffffu, iq, o);
+            if (lane >= o) {
+                ip += vp;
+                iq += vq;
+            }
+        }
+        const int tp = __shfl_sync(0xffffffffu, ip, 31), tq = __shfl_sync(0xffffffffu, iq, 31);
+        int pos = ip - cp;
+        while (mpol) {
+            const int bit = __ffs(mpol) - 1;
+            mpol &= mpol - 1;
+            s_item[wid][pos++] = (unsigned short)((lane << 5) | bit);
+        }
+        pos = tp + iq - cq;
+        while (mq) {
+            const int bit = __ffs(mq) - 1;
+            mq &= mq - 1;
+            s_item[wid][pos++] = (unsigned short)((lane << 5) | 16 | bit);
+        }
+        __syncwarp();
+        // 2. the warp evaluates the queued pairs, 32 at a time
+        for (int g = lane; g < tp + tq; g += 32) {
+            const unsigned item = s_item[wid][g];
+            const int src = item >> 5, a = (item >> 2) & 3, b = item & 3;
+            const int B = s_nbB[wid][src];
+            const f3 dAB = mk(s_nbd[wid][src][0], s_nbd[wid][src][1], s_nbd[wid][src][2]);
+            const f3 offa = mk(s_site[wid][a][0], s_site[wid][a][1], s_site[wid][a][2]);
+            const float da = s_site[wid][a][3];
+            const int jb = K * B + b;
+            const f3 d = site_delta(dAB, ld3(off, jb), offa);  // r_b - r_a
+            const float r2 = dot(d, d);
+            const float r = sqrtf(r2);
+            const float dprod = da * damp[jb];
+            if (!(item & 16)) {
+                // dipole-dipole field coefficients of this geometry for the
+                // solver iterations (layout of pair_coef_index)
+                ++npol;
+                const Thole th = thole(r, dprod, gdd);
+                float pf1, pf2;
+                if (PME) {
+                    const Bn bn = ewald_bn(r, r2);
+                    const float rr3 = (1.f - s3_of(th)) / (r2 * r);
+                    const float rr5 = 3.f * (1.f - s5_of(th)) / (r2 * r2 * r);
+                    pf1 = rr3 - bn.b1;
+                    pf2 = bn.b2 - rr5;
+                } else {
+                    pf1 = -s3_of(th) / (r2 * r);
+                    pf2 = 3.f * s5_of(th) / (r2 * r2 * r);
+                }
+                const int t = t0 + src;
+                pcoef[pair_coef_index(A, a, b, 0, t, cap)] = pf1;
+                pcoef[pair_coef_index(A, a, b, 1, t, cap)] = pf2;
+            } else {
+                const Thole th = thole(r, dprod, gcc);
                 float fac;
                 if (PME) {
                     const Bn bn = ewald_bn(r, r2);
@@ -859,12 +930,17 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
                 } else {
                     fac = s3_of(th) / (r2 * r);
                 }
-                const float c = -MB.q[b] * fac;
-                E[a][0] += d.x * c;
-                E[a][1] += d.y * c;
-                E[a][2] += d.z * c;
+                const float c = -q[jb] * fac;
+                #pragma unroll
+                for (int k = 0; k < kMaxK; ++k)
+                    if (k == a) {
+                        E[k][0] += d.x * c;
+                        E[k][1] += d.y * c;
+                        E[k][2] += d.z * c;
+                    }
             }
         }
+        __syncwarp();
     }
     #pragma unroll
     for (int a = 0; a < kMaxK; ++a) {
@@ -875,6 +951,7 @@ __global__ void fixed_field_kernel(int nmol, const float* __restrict__ off, cons
     npol = __reduce_add_sync(0xffffffffu, npol);
     if (lane == 0 && npair) atomicAdd(npair, (unsigned long long)npol);
     if (lane == 0) {
+        load_mol(A, off, q, damp, pol, type, MA);
         if (PME) {
             // intramolecular pairs: s3 = 2 (reference :1381-1384), within the cutoff
             #pragma unroll
@@ -1084,16 +1161,21 @@ __global__ void __launch_bounds__(128, PME ? 7 : 6) induced_update_kernel(int nm
                         anchor_store[3 * i + 1] = mu_in[3 * i + 1];
                         anchor_store[3 * i + 2] = mu_in[3 * i + 2];
                     }
-                } else if (mode == 2) {
-                    ex += Ebase[3 * i];
-                    ey += Ebase[3 * i + 1];
-                    ez += Ebase[3 * i + 2];
+                }
+                // the anchor's field is added in FP64: an FP32 sum would round
+                // the small field of mu - anchor to the anchor field's ulp,
+                // a floor of ~1e-9 D under the convergence measure
+                double bx = 0.0, by = 0.0, bz = 0.0;
+                if (mode == 2) {
+                    bx = Ebase[3 * i];
+                    by = Ebase[3 * i + 1];
+                    bz = Ebase[3 * i + 2];
                 }
                 const float al = pol[i];
                 // reference updateInducedDipole (:516-531); E0 is unscaled here
-                const double nx = (double)al * ((double)E0[3 * i] + ex);
-                const double ny = (double)al * ((double)E0[3 * i + 1] + ey);
-                const double nz = (double)al * ((double)E0[3 * i + 2] + ez);
+                const double nx = (double)al * ((double)E0[3 * i] + bx + ex);
+                const double ny = (double)al * ((double)E0[3 * i + 1] + by + ey);
+                const double nz = (double)al * ((double)E0[3 * i + 2] + bz + ez);
                 // the dipole state is FP64: FP32 storage alone would put a
                 // floor of ~1e-8 D under the convergence measure
                 const double dx = nx - m0, dy = ny - m1, dz = nz - m2;
@@ -1155,16 +1237,19 @@ __global__ void induced_finish_kernel(int n, const float* __restrict__ Edir, con
                 anchor_store[3 * i + 1] = mu.y;
                 anchor_store[3 * i + 2] = mu.z;
             }
-        } else if (mode == 2) {
-            ex += Ebase[3 * i];
-            ey += Ebase[3 * i + 1];
-            ez += Ebase[3 * i + 2];
+        }
+        // the anchor's field in FP64, as in induced_update_kernel
+        double bx = 0.0, by = 0.0, bz = 0.0;
+        if (mode == 2) {
+            bx = Ebase[3 * i];
+            by = Ebase[3 * i + 1];
+            bz = Ebase[3 * i + 2];
         }
         const double m0 = mu_d[3 * i], m1 = mu_d[3 * i + 1], m2 = mu_d[3 * i + 2];
         const float al = pol[i];
-        const double nx = (double)al * ((double)E0[3 * i] + ex);
-        const double ny = (double)al * ((double)E0[3 * i + 1] + ey);
-        const double nz = (double)al * ((double)E0[3 * i + 2] + ez);
+        const double nx = (double)al * ((double)E0[3 * i] + bx + ex);
+        const double ny = (double)al * ((double)E0[3 * i + 1] + by + ey);
+        const double nz = (double)al * ((double)E0[3 * i + 2] + bz + ez);
         const double dx = nx - m0, dy = ny - m1, dz = nz - m2;
         const double u0 = m0 + kSOR * dx, u1 = m1 + kSOR * dy, u2 = m2 + kSOR * dz;
         mu_d[3 * i] = u0;
