@@ -343,8 +343,9 @@ mbpol_status mbpol_guess_descriptors(mbpol_context* ctx, float* out);
  * solve's inputs with targets mu_converged - (P(X) + g dF); while network 1
  * is selected the inputs are computed at every predictor start. */
 mbpol_status mbpol_guess_select_network(mbpol_context* ctx, int which);
-/* Loss, gradient [8905] and outputs [n][9] of the current network on host
- * data X [n][64] (raw inputs), T [n][9] (targets), without an update. */
+/* Loss, gradient [8905] (the training kernel) and outputs [n][9] (the
+ * prediction kernel the solves use) of the current network on host data
+ * X [n][64] (raw inputs), T [n][9] (targets), without an update. */
 mbpol_status mbpol_guess_loss_grad(mbpol_context* ctx, const float* X, const float* T, int n, double* loss,
                                    float* grad, float* Y);
 /* The learned linear predictor used by guess 2 once MBPOL_GUESS_HISTORY

@@ -14,14 +14,17 @@
 // long-range electrostatics a 0.6 nm descriptor cannot see), 7 zeros.
 // Network: x = bf16((in - mean)/std), h1 = SiLU(W1 x + b1), h2 = SiLU(W2 h1 +
 // b2), y = W3 h2 + b3 (64-64-64-9), the O, H1, H2 dipoles in the frame in
-// units of 1e-3 e nm.  Every product runs on the tensor cores as
+// units of 1e-3 e nm.  Prediction (every solve that uses a network) runs on
+// the fifth-generation tensor cores, tcgen05.mma with the activations in
+// tensor memory (mlp_tc5_kernel).  Training runs every product as
 // mma.sync.m16n8k16 with BF16 operands and FP32 accumulation, one warp per
 // 16 samples; each layer's accumulator fragments are re-packed in registers
-// as the next layer's A fragments.  Training recomputes the forward pass,
+// as the next layer's A fragments; it recomputes the forward pass,
 // back-propagates with the same instruction (the transposed operands of the
 // weight gradients go through per-warp shared-memory tiles), sums the
 // gradients in shared memory per block and updates with Adam.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cmath>
 #include <cstring>
@@ -29,6 +32,7 @@
 
 #include "guess.h"
 #include "mbpol_internal.cuh"
+#include "umma.cuh"
 
 namespace mbpol {
 
@@ -52,6 +56,7 @@ struct GuessBuffers {
     float* ht = nullptr;
     float* hy = nullptr;
     int cap_h = 0;
+    int* status = nullptr;    // set by the tcgen05 inference kernel when a wait gives up
     int adam_t = 0;
     bool stats_set = false;
 };
@@ -572,6 +577,196 @@ __global__ void __launch_bounds__(32 * kWarps) mlp_kernel(int n, const float* __
     }
 }
 
+// ------------------------------------------------ inference on tcgen05
+// The forward pass for prediction (not training) on the fifth-generation
+// tensor cores: a block of 128 threads takes tiles of 128 samples (M = 128,
+// thread t owns sample row t, which is tensor-memory lane t).  Each layer is
+// four tcgen05.mma.kind::f16 (K = 16 each) issued by one thread: A, the
+// layer's input activations, in tensor memory (two fp16 per 32-bit column,
+// column 8 j + c of k-tile j holding inputs 16 j + 2c and 16 j + 2c + 1); B,
+// the layer's weights [out][in], in shared memory as no-swizzle K-major core
+// matrices (per k-tile [k half][row group][row][8 k]); D, FP32 in tensor
+// memory (lane = sample, column = output).  Between layers each thread reads
+// its row of D, adds the bias, applies SiLU and writes the fp16 activations
+// back as the next layer's A.  fp16 operands (the products are rounded less
+// than by the training kernel's bf16; the weights and activations of this
+// network are far inside fp16's range), FP32 accumulation.
+//
+// Tensor memory: 128 columns (X, later H2, at 0-31; H1 at 32-63; D at
+// 64-127).  The block's ~19.5 KB of shared memory keeps it off the SMs that
+// run the three-body tensor kernel (which holds all 512 columns and ~218 KB
+// of shared memory), so its allocation never waits on that kernel.  Every
+// wait is bounded; a block that gives up writes NaN outputs for its tiles
+// and records the failure in *status.
+constexpr int kTcRows = 128;   // samples per tile
+constexpr int kTcCols = 128;   // tensor-memory columns
+constexpr int kColA0 = 0, kColA1 = 32, kColD = 64;
+constexpr int kW3Rows = 16;    // layer 3's N (outputs padded to 16)
+
+// element index of weight (n, k) in the shared-memory B operand of N rows
+__host__ __device__ constexpr int bmat_index(int n, int k, int N) {
+    return (k >> 4) * (N * 16) + ((k & 15) >> 3) * (N * 8) + (n >> 3) * 64 + (n & 7) * 8 + (k & 7);
+}
+
+__device__ __forceinline__ uint32_t pack_f16(float lo, float hi) {
+    const __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+__device__ __forceinline__ bool mlp_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* status) {
+    return umma::mbar_wait(bar, parity, abort_flag, status, 1);
+}
+
+__global__ void __launch_bounds__(kTcRows) mlp_tc5_kernel(int n, const float* __restrict__ params,
+                                                         const float* __restrict__ X, float* __restrict__ Y,
+                                                         int* __restrict__ status) {
+    using namespace umma;
+    __shared__ __align__(128) __half sW1[kHidden * kIn];
+    __shared__ __align__(128) __half sW2[kHidden * kHidden];
+    __shared__ __align__(128) __half sW3[kW3Rows * kHidden];
+    __shared__ float sB1[kHidden], sB2[kHidden], sB3[kW3Rows], sMean[kIn], sInv[kIn];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < kHidden * kIn; i += kTcRows) {
+        const int o = i / kIn, k = i % kIn;
+        sW1[bmat_index(o, k, kHidden)] = __float2half_rn(params[kW1 + i]);
+    }
+    for (int i = tid; i < kHidden * kHidden; i += kTcRows) {
+        const int o = i / kHidden, k = i % kHidden;
+        sW2[bmat_index(o, k, kHidden)] = __float2half_rn(params[kW2 + i]);
+    }
+    for (int i = tid; i < kW3Rows * kHidden; i += kTcRows) {
+        const int o = i / kHidden, k = i % kHidden;
+        sW3[bmat_index(o, k, kW3Rows)] = __float2half_rn(o < kOut ? params[kW3 + i] : 0.f);
+    }
+    if (tid < kHidden) {
+        sB1[tid] = params[kB1 + tid];
+        sB2[tid] = params[kB2 + tid];
+        sMean[tid] = params[kParams + tid];
+        sInv[tid] = params[kParams + kIn + tid];
+    }
+    if (tid < kW3Rows) sB3[tid] = tid < kOut ? params[kB3 + tid] : 0.f;
+    const uint32_t bar = smem_addr(&s_bar);
+    if (warp == 0) {
+        tmem_alloc(smem_addr(&s_tmem), kTcCols);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        s_abort = 0;
+        mbar_init(bar, 1);
+        fence_barrier_init();
+    }
+    fence_proxy_async();  // the weights, written by generic stores, are read by the tensor cores
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tb = s_tmem;
+    const uint32_t lb = tb + ((uint32_t)(32 * warp) << 16);  // this warp's lane quadrant
+    const uint32_t w1 = smem_addr(sW1), w2 = smem_addr(sW2), w3 = smem_addr(sW3);
+    const int ntiles = (n + kTcRows - 1) / kTcRows;
+    uint32_t phase = 0;
+    bool ok = true;
+    int tile = blockIdx.x;
+    for (; tile < ntiles && ok; tile += gridDim.x) {
+        const int row = tile * kTcRows + tid;
+        const bool valid = row < n;
+        // standardised inputs -> A (columns 0-31)
+        #pragma unroll
+        for (int kt = 0; kt < kIn / 16; ++kt) {
+            uint32_t v[8];
+            #pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const int k = 16 * kt + 2 * c;
+                const float x0 = valid ? (X[(size_t)row * kIn + k] - sMean[k]) * sInv[k] : 0.f;
+                const float x1 = valid ? (X[(size_t)row * kIn + k + 1] - sMean[k + 1]) * sInv[k + 1] : 0.f;
+                v[c] = pack_f16(x0, x1);
+            }
+            tmem_st8(lb + kColA0 + 8 * kt, v);
+        }
+        tmem_wait_st();
+        tc_fence_before();
+        __syncthreads();
+        float out[kW3Rows];
+        #pragma unroll 1
+        for (int layer = 0; layer < 3 && ok; ++layer) {
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t a_col = layer == 1 ? kColA1 : kColA0;
+                const uint32_t wb = layer == 0 ? w1 : (layer == 1 ? w2 : w3);
+                const int N = layer == 2 ? kW3Rows : kHidden;
+                const uint32_t idesc = idesc_f16(kTcRows, N);
+                #pragma unroll
+                for (int kt = 0; kt < kHidden / 16; ++kt)
+                    mma_ts(tb + kColD, tb + a_col + 8 * kt,
+                           sdesc(wb + (uint32_t)(kt * N * 16 * 2), (uint32_t)(N * 16), 128u), idesc, kt > 0);
+                mma_commit(bar);
+            }
+            ok = mlp_wait(bar, phase, reinterpret_cast<volatile int*>(&s_abort), status);
+            phase ^= 1;
+            ok = __syncthreads_and(ok);
+            if (!ok) break;
+            tc_fence_after();
+            if (layer < 2) {
+                // bias + SiLU -> fp16 -> the next layer's A (H1 at 32-63, H2 at 0-31)
+                const float* bias = layer == 0 ? sB1 : sB2;
+                const uint32_t dst = layer == 0 ? kColA1 : kColA0;
+                #pragma unroll
+                for (int half = 0; half < 2; ++half) {
+                    float z[32];
+                    tmem_ld32(lb + kColD + 32 * half, z);
+                    tmem_wait_ld();
+                    #pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        uint32_t v[8];
+                        #pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            const int o = 32 * half + 16 * q + 2 * c;
+                            v[c] = pack_f16(silu(z[16 * q + 2 * c] + bias[o]), silu(z[16 * q + 2 * c + 1] + bias[o + 1]));
+                        }
+                        tmem_st8(lb + dst + 8 * (2 * half + q), v);
+                    }
+                }
+                tmem_wait_st();
+                tc_fence_before();
+                __syncthreads();
+            } else {
+                float z[16];
+                tmem_ld16(lb + kColD, z);
+                tmem_wait_ld();
+                #pragma unroll
+                for (int o = 0; o < kW3Rows; ++o) out[o] = z[o] + sB3[o];
+            }
+        }
+        if (!ok) break;
+        if (valid)
+            #pragma unroll
+            for (int o = 0; o < kOut; ++o) Y[(size_t)row * kOut + o] = out[o];
+        // D and A are rewritten by the next tile only after every thread's loads
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    if (!ok) {
+        // a wait gave up: NaN outputs for this block's remaining tiles (the
+        // solver then fails loudly), and one more bounded wait for the
+        // outstanding commit before the tensor memory is freed
+        for (int t = tile; t < ntiles; t += gridDim.x) {
+            const int row = t * kTcRows + tid;
+            if (row < n)
+                for (int o = 0; o < kOut; ++o) Y[(size_t)row * kOut + o] = __int_as_float(0x7fc00000);
+        }
+        const long long t0 = clock64();
+        while (!mbar_try_wait(bar, phase ^ 1) && clock64() - t0 < kWaitCycles) {
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tb, kTcCols);
+}
+
 __global__ void adam_kernel(int np, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                             float* __restrict__ v, float lr, float b1, float b2, float c1, float c2, float eps) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -663,9 +858,6 @@ cudaError_t mlp_attributes() {
     if ((e = cudaFuncSetAttribute(mlp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)SmemPlan::bytes(true))))
         return e;
-    if ((e = cudaFuncSetAttribute(mlp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)SmemPlan::bytes(false))))
-        return e;
     done = dev;
     return cudaSuccess;
 }
@@ -675,6 +867,11 @@ unsigned long long mix64_host(unsigned long long z) {
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
+}
+
+int mlp_tc5_blocks(int n) {
+    const int tiles = (n + kTcRows - 1) / kTcRows;
+    return tiles < 1 ? 1 : (tiles > 1024 ? 1024 : tiles);
 }
 
 int mlp_blocks(int n) {
@@ -696,7 +893,7 @@ GuessNet::GuessNet(int mode) : b_(new GuessBuffers), mode_(mode) {}
 GuessNet::~GuessNet() {
     for (void* p : {(void*)b_->params, (void*)b_->adam_m, (void*)b_->adam_v, (void*)b_->grad, (void*)b_->loss,
                     (void*)b_->stats, (void*)b_->desc, (void*)b_->frames, (void*)b_->ybuf, (void*)b_->X,
-                    (void*)b_->T, (void*)b_->hx, (void*)b_->ht, (void*)b_->hy})
+                    (void*)b_->T, (void*)b_->hx, (void*)b_->ht, (void*)b_->hy, (void*)b_->status})
         if (p) cudaFree(p);
     delete b_;
 }
@@ -743,10 +940,12 @@ cudaError_t GuessNet::collect(cudaStream_t st, int nmol, int K, const double* mu
 }
 
 cudaError_t GuessNet::predict(cudaStream_t st, int nmol, int K, float* m_out) {
-    GUESS_OK(mlp_attributes());
+    if (!b_->status) {
+        GUESS_OK(cudaMalloc(&b_->status, sizeof(int)));
+        GUESS_OK(cudaMemset(b_->status, 0, sizeof(int)));
+    }
     count_launch();
-    mlp_kernel<false><<<mlp_blocks(nmol), 32 * kWarps, SmemPlan::bytes(false), st>>>(
-        nmol, b_->params, b_->desc, nullptr, nmol, 0ull, 0.f, b_->ybuf, nullptr, nullptr);
+    mlp_tc5_kernel<<<mlp_tc5_blocks(nmol), kTcRows, 0, st>>>(nmol, b_->params, b_->desc, b_->ybuf, b_->status);
     count_launch();
     to_lab_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, K, b_->ybuf, b_->frames, m_out,
                                                        mode_ == 1 ? kResScale : kOutScale);
@@ -872,14 +1071,25 @@ cudaError_t GuessNet::loss_grad(cudaStream_t st, const float* h_X, const float* 
     GUESS_OK(cudaMemcpyAsync(b_->ht, h_T, sizeof(float) * (size_t)n * kOut, cudaMemcpyHostToDevice, st));
     GUESS_OK(cudaMemsetAsync(b_->grad, 0, sizeof(float) * kParams, st));
     GUESS_OK(cudaMemsetAsync(b_->loss, 0, sizeof(double), st));
+    if (!b_->status) {
+        GUESS_OK(cudaMalloc(&b_->status, sizeof(int)));
+        GUESS_OK(cudaMemset(b_->status, 0, sizeof(int)));
+    }
     count_launch();
     mlp_kernel<true><<<mlp_blocks(n), 32 * kWarps, SmemPlan::bytes(true), st>>>(
         n, b_->params, b_->hx, b_->ht, n, 0ull, 1.f / (float)n, b_->hy, b_->grad, b_->loss);
     GUESS_OK(cudaGetLastError());
+    // the outputs by the inference kernel (the one the solver's guess uses)
+    count_launch();
+    mlp_tc5_kernel<<<mlp_tc5_blocks(n), kTcRows, 0, st>>>(n, b_->params, b_->hx, b_->hy, b_->status);
+    GUESS_OK(cudaGetLastError());
     GUESS_OK(cudaMemcpyAsync(loss, b_->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
     GUESS_OK(cudaMemcpyAsync(h_grad, b_->grad, sizeof(float) * kParams, cudaMemcpyDeviceToHost, st));
     GUESS_OK(cudaMemcpyAsync(h_Y, b_->hy, sizeof(float) * (size_t)n * kOut, cudaMemcpyDeviceToHost, st));
-    return cudaStreamSynchronize(st);
+    int kst = 0;
+    GUESS_OK(cudaMemcpyAsync(&kst, b_->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GUESS_OK(cudaStreamSynchronize(st));
+    return kst ? cudaErrorTimeout : cudaSuccess;
 }
 
 }  // namespace mbpol
