@@ -57,6 +57,7 @@ struct GuessBuffers {
     float* hy = nullptr;
     int cap_h = 0;
     int* status = nullptr;    // set by the tcgen05 inference kernel when a wait gives up
+    __half* wpack = nullptr;  // fp16 operand image of the weights (pack_weights_kernel)
     int adam_t = 0;
     bool stats_set = false;
 };
@@ -617,7 +618,25 @@ __device__ __forceinline__ bool mlp_wait(uint32_t bar, uint32_t parity, volatile
     return umma::mbar_wait(bar, parity, abort_flag, status, 1);
 }
 
+// The fp16 operand image of W1, W2, W3 (W3 padded to 16 rows) in the
+// shared-memory B layout, made once per parameter change.
+constexpr int kPackW1 = 0, kPackW2 = kHidden * kIn, kPackW3 = kPackW2 + kHidden * kHidden;
+constexpr int kPackHalves = kPackW3 + kW3Rows * kHidden;
+__global__ void pack_weights_kernel(const float* __restrict__ params, __half* __restrict__ wpack) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kPackW2) {
+        wpack[kPackW1 + bmat_index(i / kIn, i % kIn, kHidden)] = __float2half_rn(params[kW1 + i]);
+    } else if (i < kPackW3) {
+        const int j = i - kPackW2;
+        wpack[kPackW2 + bmat_index(j / kHidden, j % kHidden, kHidden)] = __float2half_rn(params[kW2 + j]);
+    } else if (i < kPackHalves) {
+        const int j = i - kPackW3, o = j / kHidden;
+        wpack[kPackW3 + bmat_index(o, j % kHidden, kW3Rows)] = __float2half_rn(o < kOut ? params[kW3 + j] : 0.f);
+    }
+}
+
 __global__ void __launch_bounds__(kTcRows) mlp_tc5_kernel(int n, const float* __restrict__ params,
+                                                         const __half* __restrict__ wpack,
                                                          const float* __restrict__ X, float* __restrict__ Y,
                                                          int* __restrict__ status) {
     using namespace umma;
@@ -629,17 +648,14 @@ __global__ void __launch_bounds__(kTcRows) mlp_tc5_kernel(int n, const float* __
     __shared__ uint32_t s_tmem;
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5;
-    for (int i = tid; i < kHidden * kIn; i += kTcRows) {
-        const int o = i / kIn, k = i % kIn;
-        sW1[bmat_index(o, k, kHidden)] = __float2half_rn(params[kW1 + i]);
-    }
-    for (int i = tid; i < kHidden * kHidden; i += kTcRows) {
-        const int o = i / kHidden, k = i % kHidden;
-        sW2[bmat_index(o, k, kHidden)] = __float2half_rn(params[kW2 + i]);
-    }
-    for (int i = tid; i < kW3Rows * kHidden; i += kTcRows) {
-        const int o = i / kHidden, k = i % kHidden;
-        sW3[bmat_index(o, k, kW3Rows)] = __float2half_rn(o < kOut ? params[kW3 + i] : 0.f);
+    {
+        // the packed weights, 16 bytes per thread and copy
+        const uint4* src = reinterpret_cast<const uint4*>(wpack);
+        for (int i = tid; i < kPackW2 / 8; i += kTcRows) reinterpret_cast<uint4*>(sW1)[i] = src[kPackW1 / 8 + i];
+        for (int i = tid; i < (kPackW3 - kPackW2) / 8; i += kTcRows)
+            reinterpret_cast<uint4*>(sW2)[i] = src[kPackW2 / 8 + i];
+        for (int i = tid; i < (kPackHalves - kPackW3) / 8; i += kTcRows)
+            reinterpret_cast<uint4*>(sW3)[i] = src[kPackW3 / 8 + i];
     }
     if (tid < kHidden) {
         sB1[tid] = params[kB1 + tid];
@@ -675,12 +691,22 @@ __global__ void __launch_bounds__(kTcRows) mlp_tc5_kernel(int n, const float* __
         // standardised inputs -> A (columns 0-31)
         #pragma unroll
         for (int kt = 0; kt < kIn / 16; ++kt) {
+            float x[16];
+            #pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 f = valid ? reinterpret_cast<const float4*>(X + (size_t)row * kIn)[4 * kt + q]
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+                x[4 * q] = f.x;
+                x[4 * q + 1] = f.y;
+                x[4 * q + 2] = f.z;
+                x[4 * q + 3] = f.w;
+            }
             uint32_t v[8];
             #pragma unroll
             for (int c = 0; c < 8; ++c) {
                 const int k = 16 * kt + 2 * c;
-                const float x0 = valid ? (X[(size_t)row * kIn + k] - sMean[k]) * sInv[k] : 0.f;
-                const float x1 = valid ? (X[(size_t)row * kIn + k + 1] - sMean[k + 1]) * sInv[k + 1] : 0.f;
+                const float x0 = valid ? (x[2 * c] - sMean[k]) * sInv[k] : 0.f;
+                const float x1 = valid ? (x[2 * c + 1] - sMean[k + 1]) * sInv[k + 1] : 0.f;
                 v[c] = pack_f16(x0, x1);
             }
             tmem_st8(lb + kColA0 + 8 * kt, v);
@@ -886,6 +912,19 @@ int mlp_blocks(int n) {
         if (e_ != cudaSuccess) return e_;       \
     } while (0)
 
+// the weights changed: make the fp16 operand image the prediction kernel copies
+cudaError_t repack_weights(GuessBuffers* b, cudaStream_t st) {
+    if (!b->wpack) GUESS_OK(cudaMalloc(&b->wpack, sizeof(__half) * kPackHalves));
+    if (!b->status) {
+        GUESS_OK(cudaMalloc(&b->status, sizeof(int)));
+        GUESS_OK(cudaMemset(b->status, 0, sizeof(int)));
+    }
+    count_launch();
+    pack_weights_kernel<<<(kPackHalves + 255) / 256, 256, 0, st>>>(b->params, b->wpack);
+    return cudaGetLastError();
+}
+
+
 }  // namespace
 
 GuessNet::GuessNet(int mode) : b_(new GuessBuffers), mode_(mode) {}
@@ -893,7 +932,7 @@ GuessNet::GuessNet(int mode) : b_(new GuessBuffers), mode_(mode) {}
 GuessNet::~GuessNet() {
     for (void* p : {(void*)b_->params, (void*)b_->adam_m, (void*)b_->adam_v, (void*)b_->grad, (void*)b_->loss,
                     (void*)b_->stats, (void*)b_->desc, (void*)b_->frames, (void*)b_->ybuf, (void*)b_->X,
-                    (void*)b_->T, (void*)b_->hx, (void*)b_->ht, (void*)b_->hy, (void*)b_->status})
+                    (void*)b_->T, (void*)b_->hx, (void*)b_->ht, (void*)b_->hy, (void*)b_->status, (void*)b_->wpack})
         if (p) cudaFree(p);
     delete b_;
 }
@@ -940,12 +979,10 @@ cudaError_t GuessNet::collect(cudaStream_t st, int nmol, int K, const double* mu
 }
 
 cudaError_t GuessNet::predict(cudaStream_t st, int nmol, int K, float* m_out) {
-    if (!b_->status) {
-        GUESS_OK(cudaMalloc(&b_->status, sizeof(int)));
-        GUESS_OK(cudaMemset(b_->status, 0, sizeof(int)));
-    }
+    if (!b_->wpack) return cudaErrorInvalidValue;  // set_params or train make the image
     count_launch();
-    mlp_tc5_kernel<<<mlp_tc5_blocks(nmol), kTcRows, 0, st>>>(nmol, b_->params, b_->desc, b_->ybuf, b_->status);
+    mlp_tc5_kernel<<<mlp_tc5_blocks(nmol), kTcRows, 0, st>>>(nmol, b_->params, b_->wpack, b_->desc, b_->ybuf,
+                                                             b_->status);
     count_launch();
     to_lab_kernel<<<(nmol + 127) / 128, 128, 0, st>>>(nmol, K, b_->ybuf, b_->frames, m_out,
                                                        mode_ == 1 ? kResScale : kOutScale);
@@ -981,6 +1018,8 @@ cudaError_t GuessNet::set_params(const float* h_block) {
         GUESS_OK(cudaMemset(b_->adam_m, 0, sizeof(float) * kParams));
         GUESS_OK(cudaMemset(b_->adam_v, 0, sizeof(float) * kParams));
     }
+    GUESS_OK(repack_weights(b_, 0));
+    GUESS_OK(cudaStreamSynchronize(0));
     ready_ = true;
     return cudaSuccess;
 }
@@ -1047,6 +1086,7 @@ cudaError_t GuessNet::train(cudaStream_t st, int steps, int batch, double lr, un
         adam_kernel<<<(kParams + 255) / 256, 256, 0, st>>>(kParams, b_->params, b_->grad, b_->adam_m, b_->adam_v,
                                                             lr_s, b1, b2, c1, c2, 1e-8f);
     }
+    GUESS_OK(repack_weights(b_, st));
     double hl[2] = {0, 0};
     GUESS_OK(cudaMemcpyAsync(hl, b_->loss, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
     GUESS_OK(cudaStreamSynchronize(st));
@@ -1071,17 +1111,14 @@ cudaError_t GuessNet::loss_grad(cudaStream_t st, const float* h_X, const float* 
     GUESS_OK(cudaMemcpyAsync(b_->ht, h_T, sizeof(float) * (size_t)n * kOut, cudaMemcpyHostToDevice, st));
     GUESS_OK(cudaMemsetAsync(b_->grad, 0, sizeof(float) * kParams, st));
     GUESS_OK(cudaMemsetAsync(b_->loss, 0, sizeof(double), st));
-    if (!b_->status) {
-        GUESS_OK(cudaMalloc(&b_->status, sizeof(int)));
-        GUESS_OK(cudaMemset(b_->status, 0, sizeof(int)));
-    }
+    if (!b_->wpack) GUESS_OK(repack_weights(b_, st));
     count_launch();
     mlp_kernel<true><<<mlp_blocks(n), 32 * kWarps, SmemPlan::bytes(true), st>>>(
         n, b_->params, b_->hx, b_->ht, n, 0ull, 1.f / (float)n, b_->hy, b_->grad, b_->loss);
     GUESS_OK(cudaGetLastError());
     // the outputs by the inference kernel (the one the solver's guess uses)
     count_launch();
-    mlp_tc5_kernel<<<mlp_tc5_blocks(n), kTcRows, 0, st>>>(n, b_->params, b_->hx, b_->hy, b_->status);
+    mlp_tc5_kernel<<<mlp_tc5_blocks(n), kTcRows, 0, st>>>(n, b_->params, b_->wpack, b_->hx, b_->hy, b_->status);
     GUESS_OK(cudaGetLastError());
     GUESS_OK(cudaMemcpyAsync(loss, b_->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
     GUESS_OK(cudaMemcpyAsync(h_grad, b_->grad, sizeof(float) * kParams, cudaMemcpyDeviceToHost, st));
